@@ -1,0 +1,125 @@
+"""ctypes binding of the CPU restatement (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module, as the checker.  It builds
+``oracle/liboracle.so`` from ``bertha_oracle.cpp`` on first use.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        src = os.path.join(_HERE, "bertha_oracle.cpp")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            build()
+        L = ctypes.CDLL(path)
+        d, i, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+        L.orc_boys.argtypes = [d, i, P]
+        L.orc_rints.argtypes = [P, d, i, P]
+        L.orc_cart_index.argtypes = [i, i, i]
+        L.orc_eq_pair.argtypes = [i, i, d, P, i, i, d, P, i, P]
+        L.orc_fock_layout.argtypes = [i, P, P, P, P, i, i, i, P, P]
+        L.orc_clmfast.argtypes = [i, P, P, P, P, i, i, i, i, i, i, P, i, P, P, i]
+        L.orc_eri_quartet.argtypes = [P, P, P, i, i, P]
+        _LIB = L
+    return _LIB
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def ntuv(L):
+    return (L + 1) * (L + 2) * (L + 3) // 6
+
+
+def boys(T, lam):
+    F = np.zeros(lam + 1)
+    lib().orc_boys(float(T), int(lam), _p(F))
+    return F
+
+
+def rints(qp, alpha, lam):
+    R = np.zeros(ntuv(lam))
+    q = np.ascontiguousarray(qp, dtype=np.float64)
+    lib().orc_rints(_p(q), float(alpha), int(lam), _p(R))
+    return R
+
+
+def cart_index(t, u, v):
+    return lib().orc_cart_index(t, u, v)
+
+
+def eq_pair(ka, mqa, ea, A, kb, mqb, eb, B, small):
+    """E-coefficients of one primitive spinor pair; mqa, mqb are signed 2m."""
+    la = -ka - 1 if ka < 0 else ka
+    lb = -kb - 1 if kb < 0 else kb
+    out = np.zeros(2 * ntuv(la + lb + 2 + 2))
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    n = lib().orc_eq_pair(ka, mqa, ea, _p(A), kb, mqb, eb, _p(B), int(small), _p(out))
+    return out[: 2 * n].view(np.complex128).copy()
+
+
+def eri_quartet(xyz4, l4, ex4, t1, t2):
+    """All spinor integrals of one primitive quartet.
+
+    Returns an array [lab_a, lab_b, lab_c, lab_d, 16] (complex), labels in the
+    order kappa=l (|m| ascending) then kappa=-l-1 (|m| ascending); the last
+    index is 8*sa+4*sb+2*sc+sd with s=1 for m>0.
+    """
+    xyz4 = np.ascontiguousarray(xyz4, dtype=np.float64)
+    l4 = np.ascontiguousarray(l4, dtype=np.int32)
+    ex4 = np.ascontiguousarray(ex4, dtype=np.float64)
+    nl = [2 * l + 1 for l in l4]
+    out = np.zeros(2 * 16 * int(np.prod(nl)))
+    n = lib().orc_eri_quartet(_p(xyz4), _p(l4), _p(ex4), int(t1), int(t2), _p(out))
+    assert n == 16 * int(np.prod(nl))
+    return out.view(np.complex128).reshape(nl + [16])
+
+
+def _basis_arrays(basis):
+    xyz = np.ascontiguousarray(basis.xyz, dtype=np.float64)
+    lmax = np.ascontiguousarray(basis.lmax, dtype=np.int32)
+    nfn = np.ascontiguousarray(basis.nfn, dtype=np.int32)
+    ex = np.ascontiguousarray(basis.ex, dtype=np.float64)
+    return xyz, lmax, nfn, ex
+
+
+def fock_layout(basis):
+    xyz, lmax, nfn, ex = _basis_arrays(basis)
+    maxl1, maxbs = ex.shape[1], ex.shape[2]
+    nk = 2 * (maxl1 - 1) + 2
+    lrge = np.full((basis.ncnt, nk, 28), -1, dtype=np.int32)
+    nskp = ctypes.c_int(0)
+    ndim = lib().orc_fock_layout(basis.ncnt, _p(xyz), _p(lmax), _p(nfn), _p(ex),
+                                 maxl1, maxbs, int(basis.hmlt == 0), _p(lrge),
+                                 ctypes.byref(nskp))
+    return ndim, nskp.value, lrge
+
+
+def clmfast(basis, dent, ilev, racah1=True):
+    """Multi-centre Coulomb Fock build (INTSYM off): returns (GDIR, GXCH)."""
+    xyz, lmax, nfn, ex = _basis_arrays(basis)
+    maxl1, maxbs = ex.shape[1], ex.shape[2]
+    nd = dent.shape[0]
+    D = np.asfortranarray(dent, dtype=np.complex128)
+    gd = np.zeros((nd, nd), dtype=np.complex128, order="F")
+    gx = np.zeros((nd, nd), dtype=np.complex128, order="F")
+    lib().orc_clmfast(basis.ncnt, _p(xyz), _p(lmax), _p(nfn), _p(ex), maxl1, maxbs,
+                      int(basis.hmlt), int(basis.isym), int(ilev), int(racah1),
+                      _p(D), nd, _p(gd), _p(gx), nd)
+    return gd, gx
