@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Dirac-Coulomb Fock build.
+
+Workload (the configuration the headline metric is quoted on): the seeded
+ERI-kernel microbenchmark, 2^20 random primitive shell quartets with
+l_a..l_d uniform on {0..3}, exponents log-uniform on [0.05, 1e6], centres
+uniform in a 10-bohr cube with 20% overlapping pairs, split evenly over the
+LL|LL, LL|SS, SS|LL and SS|SS component classes.  One step digests every
+quartet into the Coulomb (J) and exchange (K) matrices of the shell pool
+(CLMMTG batch types 1 and 5), FP64.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  --impl reference times the CPU
+restatement of the reference (the Fortran reference cannot be compiled
+here: no Fortran compiler on either machine) on all host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "bertha-program_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Fock-build ERI quartets/s (FP64)"
+UNIT = "quartets/s"
+WORKLOAD = "eri-microbench: 2^20 random shell quartets, l<=3, LL/SS classes"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--quartets", type=int, default=1 << 20)
+    p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    return p.parse_args()
+
+
+def config(args, extra=None):
+    c = {"workload": WORKLOAD, "quartets_per_step": args.quartets, "seed": args.seed,
+         "pool": "32 centres x 4 l x 2 exponents (256 shells, NDIM 4096)",
+         "l2": "flushed between timed steps (256 MiB write)",
+         "parallelism": f"replicas x{args.gpus}"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------------------
+# CPU timing of the restatement (oracle) on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_rate(basis, quarts, dent, seconds, nthreads):
+    from oracle import oracle as orc
+    O = orc.QuartetOracle(basis)
+    n = basis.ndim
+    gd = np.zeros((n, n), complex, order="F")
+    gx = np.zeros((n, n), complex, order="F")
+    # probe the rate on a small sample, then size the sample to `seconds`
+    probe = 256
+    t_probe = 0.0
+    for cls, q in quarts.items():
+        O.prepare(q[:probe], *cls)
+        t0 = time.perf_counter()
+        O.digest(q[:probe], *cls, dent, gd, gx, nthreads=nthreads)
+        t_probe += time.perf_counter() - t0
+    rate = 4 * probe / max(t_probe, 1e-9)
+    per = int(max(probe, min(len(next(iter(quarts.values()))), rate * seconds / 4)))
+    tot, nq = 0.0, 0
+    for cls, q in quarts.items():
+        s = q[:per]
+        O.prepare(s, *cls)
+        t0 = time.perf_counter()
+        O.digest(s, *cls, dent, gd, gx, nthreads=nthreads)
+        tot += time.perf_counter() - t0
+        nq += len(s)
+    O.close()
+    return nq / tot, nq, tot
+
+
+def run_reference(args):
+    from berthagpu import deck, workloads
+    basis = workloads.microbench_pool(seed=args.seed)
+    quarts = workloads.microbench_quartets(basis, args.quartets, seed=args.seed)
+    dent = deck.density(basis, seed=args.seed)
+    cores = os.cpu_count() or 1
+    rates = []
+    per_step = max(2.0, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
+    for i in range(args.warmup + args.steps):
+        r, nq, t = cpu_rate(basis, quarts, dent, per_step, cores)
+        if i >= args.warmup:
+            rates.append((r, nq, t))
+    value = float(np.mean([r for r, _, _ in rates]))
+    sample = (f"{rates[-1][1]} quartets per step (equal per component class) of the "
+              f"{args.quartets}-quartet workload, {rates[-1][2]:.1f} s")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * args.quartets / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config(args), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) == 6:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if r[2 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def read_traffic():
+    """DRAM bytes per k_quartet launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_quartet_eri_microbench.md")
+    try:
+        for ln in open(path):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def fp64_peak(torch):
+    """FP64 peak of this GPU measured now: cuBLAS DGEMM, 4096^3, best of 5."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    a @ b
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        e.synchronize()
+        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    import berthagpu
+    from berthagpu import deck, workloads
+    from berthagpu.build import build as build_lib
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if rank == 0:
+        build_lib()
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.barrier()
+        build_lib()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    basis = workloads.microbench_pool(seed=args.seed)
+    quarts = workloads.microbench_quartets(basis, args.quartets, seed=args.seed)
+    dent = deck.density(basis, seed=args.seed)
+    flops = {cls: workloads.quartet_flops(basis, q, *cls) for cls, q in quarts.items()}
+    fb = berthagpu.FockBuilder(basis)
+    n = fb.ndim
+    # complex matrices as interleaved doubles; the column-major (n x n) array
+    # is the row-major transpose, which torch holds as [n, 2n]
+    dent_rows = np.ascontiguousarray(dent.T).view(np.float64).reshape(n, 2 * n)
+    D = torch.from_numpy(dent_rows).to(dev)
+    GD = torch.zeros(n, 2 * n, dtype=torch.float64, device=dev)
+    GX = torch.zeros_like(GD)
+    dq = {cls: torch.from_numpy(q).to(dev) for cls, q in quarts.items()}
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step(events=None):
+        launches = 0
+        for k, (cls, q) in enumerate(dq.items()):
+            if events is not None:
+                events[k][0].record(stream)
+            fb.quartets(q.data_ptr(), q.shape[0], cls[0], cls[1], D.data_ptr(),
+                        GD.data_ptr(), GX.data_ptr(), n, sp)
+            launches += fb.launches()
+            if events is not None:
+                events[k][1].record(stream)
+        return launches
+
+    peak64 = fp64_peak(torch)
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+
+    ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in dq]
+          for _ in range(args.steps)]
+    launches = 0
+    with ClockSampler(local) as clk:
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for s in range(args.steps):
+            flush.zero_()
+            launches += step(ev[s])
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+    kern_ms = np.array([[ev[s][k][0].elapsed_time(ev[s][k][1]) for k in range(len(dq))]
+                        for s in range(args.steps)])
+    step_ms = float(kern_ms.sum(1).max() if args.steps else 0.0)
+    step_ms_mean = float(kern_ms.sum(1).mean())
+    ms = torch.tensor([step_ms_mean], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(ms, op=dist.ReduceOp.MAX)
+    ms_per_step = float(ms.item())
+    value = args.quartets * world / (ms_per_step * 1e-3)
+
+    # end to end through the C ABI: host density and quartet lists in pinned
+    # memory copied in, J/K copied back, every step
+    hD = torch.from_numpy(dent_rows).pin_memory()
+    hq = {cls: torch.from_numpy(q).pin_memory() for cls, q in quarts.items()}
+    hGD = torch.empty(GD.shape, dtype=torch.float64).pin_memory()
+    hGX = torch.empty(GX.shape, dtype=torch.float64).pin_memory()
+    h2d = hD.numel() * 8 + sum(v.numel() * 4 for v in hq.values())
+    d2h = 2 * hGD.numel() * 8
+    e_ms = []
+    for s in range(max(1, min(args.steps, 3))):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        D.copy_(hD, non_blocking=True)
+        for cls in dq:
+            dq[cls].copy_(hq[cls], non_blocking=True)
+        GD.zero_()
+        GX.zero_()
+        step()
+        hGD.copy_(GD, non_blocking=True)
+        hGX.copy_(GX, non_blocking=True)
+        b.record(stream)
+        b.synchronize()
+        e_ms.append(a.elapsed_time(b))
+    e2e_value = args.quartets / (float(np.mean(e_ms)) * 1e-3)
+
+    tot_flops = sum(flops.values())
+    kern_mean = kern_ms.mean(0)
+    achieved = tot_flops / (kern_mean.sum() * 1e-3) / 1e12
+    per_class = {f"{'LS'[c[0]]}{'LS'[c[0]]}|{'LS'[c[1]]}{'LS'[c[1]]}":
+                 {"ms": float(kern_mean[k]), "quartets_per_s": float(quarts[c].shape[0] / (kern_mean[k] * 1e-3)),
+                  "tflops": float(flops[c] / (kern_mean[k] * 1e-3) / 1e12)}
+                 for k, c in enumerate(dq)}
+    traffic = read_traffic()
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if world == 1:
+            r, nq, t = cpu_rate(basis, quarts, dent, args.cpu_seconds, os.cpu_count() or 1)
+            cpu = {"value": r, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                   "sample": f"{nq} quartets (equal per class) of the same workload, {t:.1f} s, "
+                             "C++ restatement of bertha-scf.f ERIFAST/CLMMTG"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": config(args, {"per_class": per_class, "step_ms_max": step_ms}),
+            "roofline": {"bound": "fp64", "kernel": "k_quartet", "achieved": achieved,
+                         "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
+                                        "(MEASURED_PEAKS.json has no FP64 entry)",
+                         "traffic": traffic,
+                         "flops_per_step": tot_flops},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    fb.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", 0)) != 0:
+            return
+        run_reference(args)
+        return
+    run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

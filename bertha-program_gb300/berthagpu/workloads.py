@@ -1,0 +1,80 @@
+"""Seeded synthetic workloads.
+
+ERI microbenchmark: random shell quartets over a pool of primitive shells.
+Angular momenta l_a..l_d are uniform on {0,1,2,3}; exponents are
+log-uniform on [0.05, 1e6]; centres are uniform in a 10-bohr cube, and the
+second shell of a pair sits on the first one's centre in 20% of pairs.  The
+quartets are split evenly over the four component classes LL|LL, LL|SS,
+SS|LL and SS|SS (the SS partners carry l+1 through kinetic balance).
+"""
+import numpy as np
+
+from .deck import make_basis
+
+CLASSES = ((0, 0), (0, 1), (1, 0), (1, 1))
+
+
+def microbench_pool(seed=2024, ncentres=32, nexp=2, lmax=3, cube=10.0,
+                    emin=0.05, emax=1.0e6):
+    rng = np.random.default_rng(seed)
+    cents = []
+    for _ in range(ncentres):
+        pos = rng.uniform(0.0, cube, 3)
+        d = {l: list(np.exp(rng.uniform(np.log(emin), np.log(emax), nexp)))
+             for l in range(lmax + 1)}
+        cents.append((pos, d))
+    return make_basis(cents, hmlt="DHFR", isym=0, name="eri-pool")
+
+
+def shell_index(basis):
+    """shell id of (centre, l, i) in the library's order"""
+    idx = {}
+    for s, (c, l, i, _) in enumerate(basis.shells()):
+        idx[(c, l, i)] = s
+    return idx
+
+
+def microbench_quartets(basis, nquart, seed=2024, overlap=0.2):
+    """Returns {(t1,t2): int32 array [n,4]} with nquart quartets in total."""
+    rng = np.random.default_rng(seed + 1)
+    idx = shell_index(basis)
+    nc = basis.ncnt
+    out = {}
+    per = nquart // len(CLASSES)
+    for k, cls in enumerate(CLASSES):
+        n = per if k < len(CLASSES) - 1 else nquart - per * (len(CLASSES) - 1)
+        ls = rng.integers(0, 4, size=(n, 4))
+        ca = rng.integers(0, nc, size=n)
+        cc = rng.integers(0, nc, size=n)
+        cb = np.where(rng.random(n) < overlap, ca, (ca + rng.integers(1, nc, size=n)) % nc)
+        cd = np.where(rng.random(n) < overlap, cc, (cc + rng.integers(1, nc, size=n)) % nc)
+        cen = np.stack([ca, cb, cc, cd], 1)
+        q = np.empty((n, 4), np.int32)
+        for j in range(4):
+            ii = rng.integers(0, basis.nfn[0, 0], size=n)
+            q[:, j] = [idx[(int(c), int(l), int(i))] for c, l, i in zip(cen[:, j], ls[:, j], ii)]
+        out[cls] = q
+    return out
+
+
+def quartet_flops(basis, quart, t1, t2):
+    """Algorithmic FP64 flops of a quartet list: Boys+R recursion
+    (6 per R entry up to the class order), first contraction
+    2*(4P_ab)*N_ab*N_cd and second contraction 2*(4P_ab)*(4P_cd)*N_cd."""
+    sh = basis.shells()
+    l = np.array([s[1] for s in sh])
+    la, lb, lc, ld = (l[quart[:, j]] for j in range(4))
+
+    def nt(L):
+        return (L + 1) * (L + 2) * (L + 3) // 6
+
+    degab = la + lb + 2 * t1
+    degcd = lc + ld + 2 * t2
+    lam = degab + degcd
+    pab = (2 * la + 1) * (2 * lb + 1)
+    pcd = (2 * lc + 1) * (2 * ld + 1)
+    fr = 6 * sum(nt(k) for k in range(0, 1))  # placeholder, replaced below
+    fr = 6 * np.array([sum(nt(k) for k in range(int(L) + 1)) for L in lam])
+    f1 = 2 * (4 * pab) * nt(degab) * nt(degcd)
+    f2 = 2 * (4 * pab) * (4 * pcd) * nt(degcd)
+    return float(np.sum(fr + f1 + f2))

@@ -29,6 +29,9 @@
 #include <cstring>
 #include <deque>
 #include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 typedef std::complex<double> cplx;
 
@@ -835,6 +838,102 @@ int orc_fock_layout(int ncnt, const double *xyz, const int *lmax,
   return b.ndim;
 }
 
+// Oracle context for explicit shell-quartet lists (the ERI microbenchmark):
+// shells in the order centre, l, exponent; E-coefficients prepared once.
+struct OrcCtx {
+  Basis b;
+  struct Sh { int c, l, i; };
+  std::vector<Sh> sh;
+  std::vector<std::vector<HVec>> eq;  // [pair*2+comp][lab_a][lab_b][set] flattened
+  std::vector<char> have;
+};
+
+// One shell quartet: all label pairs, 16 m-signs, batch types 1 and 5.
+void orc_one_quartet(const OrcCtx &o, const int *q, int t1, int t2, const Mat &D,
+                     Mat &GD, Mat &GX, bool atomic) {
+  const Cart &C = cart();
+  const OrcCtx::Sh &A = o.sh[q[0]], &B = o.sh[q[1]], &Cc = o.sh[q[2]], &Dd = o.sh[q[3]];
+  const Basis &b = o.b;
+  size_t ns = o.sh.size();
+  const std::vector<HVec> &Eab = o.eq[((size_t)q[0] * ns + q[1]) * 2 + t1];
+  const std::vector<HVec> &Ecd = o.eq[((size_t)q[2] * ns + q[3]) * 2 + t2];
+  std::vector<Label> la = labels_for(A.l), lb = labels_for(B.l);
+  std::vector<Label> lc = labels_for(Cc.l), ld = labels_for(Dd.l);
+  int degab = A.l + B.l + 2 * t1, degcd = Cc.l + Dd.l + 2 * t2, lam = degab + degcd;
+  int nab = ntuv(degab), ncd = ntuv(degcd);
+  double ei = b.ex[A.c][A.l][A.i], ej = b.ex[B.c][B.l][B.i];
+  double ek = b.ex[Cc.c][Cc.l][Cc.i], el = b.ex[Dd.c][Dd.l][Dd.i];
+  double eij = ei + ej, ekl = ek + el, qp[3];
+  for (int x = 0; x < 3; ++x)
+    qp[x] = (b.xyz[3 * Cc.c + x] * ek + b.xyz[3 * Dd.c + x] * el) / ekl -
+            (b.xyz[3 * A.c + x] * ei + b.xyz[3 * B.c + x] * ej) / eij;
+  std::vector<double> R(ntuv(lam));
+  rints(qp, eij * ekl / (eij + ekl), lam, R.data());
+  double pre = 2.0 * PI52 / (std::sqrt(eij + ekl) * eij * ekl);
+  for (double &r : R) r *= pre;
+  int oab = t1 ? b.nskp : 0, ocd = t2 ? b.nskp : 0;
+  std::vector<cplx> g11(ncd), g21(ncd);
+  for (size_t ia = 0; ia < la.size(); ++ia)
+  for (size_t ib = 0; ib < lb.size(); ++ib) {
+    const HVec &e11 = Eab[(ia * lb.size() + ib) * 2], &e21 = Eab[(ia * lb.size() + ib) * 2 + 1];
+    for (int qq = 0; qq < ncd; ++qq) {
+      cplx x(0), y(0);
+      for (int s = 0; s < nab; ++s) {
+        double rv = R[C.idx[C.t[s] + C.t[qq]][C.u[s] + C.u[qq]][C.v[s] + C.v[qq]]];
+        x += e11[s] * rv;
+        y += e21[s] * rv;
+      }
+      g11[qq] = x;
+      g21[qq] = y;
+    }
+    int na[2] = {b.lrge[A.c][la[ia].ka][2 * la[ia].ma - 2] + oab + A.i,
+                 b.lrge[A.c][la[ia].ka][2 * la[ia].ma - 1] + oab + A.i};
+    int nb[2] = {b.lrge[B.c][lb[ib].ka][2 * lb[ib].ma - 2] + oab + B.i,
+                 b.lrge[B.c][lb[ib].ka][2 * lb[ib].ma - 1] + oab + B.i};
+    for (size_t ic = 0; ic < lc.size(); ++ic)
+    for (size_t id = 0; id < ld.size(); ++id) {
+      Eri16 rr;
+      double pab = phase_pair(la[ia].kq, la[ia].ma, lb[ib].kq, lb[ib].ma);
+      double pcd = phase_pair(lc[ic].kq, lc[ic].ma, ld[id].kq, ld[id].ma);
+      const HVec &f11 = Ecd[(ic * ld.size() + id) * 2], &f21 = Ecd[(ic * ld.size() + id) * 2 + 1];
+      second_contraction(g11.data(), g21.data(), f11.data(), f21.data(), ncd, pab, pcd, rr);
+      int nc[2] = {b.lrge[Cc.c][lc[ic].ka][2 * lc[ic].ma - 2] + ocd + Cc.i,
+                   b.lrge[Cc.c][lc[ic].ka][2 * lc[ic].ma - 1] + ocd + Cc.i};
+      int nd[2] = {b.lrge[Dd.c][ld[id].ka][2 * ld[id].ma - 2] + ocd + Dd.i,
+                   b.lrge[Dd.c][ld[id].ka][2 * ld[id].ma - 1] + ocd + Dd.i};
+      if (!atomic) {
+        digest(rr, na, nb, nc, nd, D, GD, GX, 0);
+      } else {
+        for (int sa = 0; sa < 2; ++sa)
+        for (int sb = 0; sb < 2; ++sb)
+        for (int sc = 0; sc < 2; ++sc)
+        for (int sd = 0; sd < 2; ++sd) {
+          cplx v = rr.v[8 * sa + 4 * sb + 2 * sc + sd];
+          cplx j = v * D(nc[sc], nd[sd]), k = v * D(nc[sc], nb[sb]);
+          double *pj = reinterpret_cast<double *>(&GD(na[sa], nb[sb]));
+          double *pk = reinterpret_cast<double *>(&GX(na[sa], nd[sd]));
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+          pj[0] += j.real();
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+          pj[1] += j.imag();
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+          pk[0] += k.real();
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+          pk[1] += k.imag();
+        }
+      }
+    }
+  }
+}
+
 // All spinor integrals of one primitive quartet: shells given by centre,
 // l and exponent; t1/t2 select LL (0) or SS (1) for the ab and cd pairs.
 // out: [lab_a][lab_b][lab_c][lab_d][16] complex with labels ordered as
@@ -895,6 +994,85 @@ int orc_eri_quartet(const double *xyz4, const int *l4, const double *ex4,
     }
   }
   return n;
+}
+
+void *orc_ctx_new(int ncnt, const double *xyz, const int *lmax, const int *nfn,
+                  const double *ex, int maxl1, int maxbs, int hmlt) {
+  OrcCtx *o = new OrcCtx();
+  o->b = make_basis(ncnt, xyz, lmax, nfn, ex, maxl1, maxbs, hmlt == 0);
+  for (int c = 0; c < ncnt; ++c)
+    for (int l = 0; l <= o->b.lmax[c]; ++l)
+      for (int i = 0; i < (int)o->b.ex[c][l].size(); ++i) o->sh.push_back({c, l, i});
+  size_t ns = o->sh.size();
+  o->eq.assign(ns * ns * 2, {});
+  o->have.assign(ns * ns * 2, 0);
+  return o;
+}
+
+void orc_ctx_free(void *h) { delete (OrcCtx *)h; }
+
+// Prepare E-coefficients of every shell pair used by the quartet list.
+int orc_ctx_prepare(void *h, const int *quart, long long n, int t1, int t2) {
+  OrcCtx &o = *(OrcCtx *)h;
+  std::vector<std::pair<int, int>> need;
+  size_t ns = o.sh.size();
+  std::vector<char> mark(ns * ns * 2, 0);
+  for (long long i = 0; i < n; ++i) {
+    size_t k1 = ((size_t)quart[4 * i] * ns + quart[4 * i + 1]) * 2 + t1;
+    size_t k2 = ((size_t)quart[4 * i + 2] * ns + quart[4 * i + 3]) * 2 + t2;
+    if (!mark[k1] && !o.have[k1]) { mark[k1] = 1; need.push_back({(int)(k1 / 2), t1}); }
+    if (!mark[k2] && !o.have[k2]) { mark[k2] = 1; need.push_back({(int)(k2 / 2), t2}); }
+  }
+  std::vector<std::vector<HVec>> tmp(need.size());
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic)
+#endif
+  for (long long i = 0; i < (long long)need.size(); ++i) {
+    int pr = need[i].first;
+    const OrcCtx::Sh &A = o.sh[pr / ns], &B = o.sh[pr % ns];
+    std::vector<Label> la = labels_for(A.l), lb = labels_for(B.l);
+    for (size_t ia = 0; ia < la.size(); ++ia)
+      for (size_t ib = 0; ib < lb.size(); ++ib)
+        for (int set = 0; set < 2; ++set) {
+          int mqa = (set == 0 ? -1 : 1) * (2 * la[ia].ma - 1);
+          int mqb = -(2 * lb[ib].ma - 1);
+          tmp[i].push_back(eq_pair(la[ia].kq, mqa, o.b.ex[A.c][A.l][A.i], &o.b.xyz[3 * A.c],
+                                   lb[ib].kq, mqb, o.b.ex[B.c][B.l][B.i],
+                                   &o.b.xyz[3 * B.c], need[i].second != 0));
+        }
+  }
+  for (size_t i = 0; i < need.size(); ++i) {
+    size_t key = (size_t)need[i].first * 2 + need[i].second;
+    o.eq[key] = std::move(tmp[i]);
+    o.have[key] = 1;
+  }
+  return (int)need.size();
+}
+
+// Digest an explicit quartet list (adds into gd/gx, batch types 1 and 5),
+// with nthreads OpenMP threads (atomic accumulation when > 1).
+int orc_ctx_quartets(void *h, const int *quart, long long n, int t1, int t2,
+                     const double *dent, int ldd, double *gd, double *gx, int ldf,
+                     int nthreads) {
+  OrcCtx &o = *(OrcCtx *)h;
+  orc_ctx_prepare(h, quart, n, t1, t2);
+  Mat D{(cplx *)dent, ldd}, GD{(cplx *)gd, ldf}, GX{(cplx *)gx, ldf};
+  bool atomic = nthreads > 1;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+#endif
+  for (long long i = 0; i < n; ++i) {
+    Mat gdl = GD, gxl = GX;
+    orc_one_quartet(o, &quart[4 * i], t1, t2, D, gdl, gxl, atomic);
+  }
+  return 0;
+}
+
+int orc_ndim(void *h, int *nskp) {
+  OrcCtx &o = *(OrcCtx *)h;
+  *nskp = o.b.nskp;
+  return o.b.ndim;
 }
 
 // Full-mode multi-centre Coulomb Fock build (CLMFAST with INTSYM=.FALSE.).

@@ -123,3 +123,46 @@ def clmfast(basis, dent, ilev, racah1=True):
                       int(basis.hmlt), int(basis.isym), int(ilev), int(racah1),
                       _p(D), nd, _p(gd), _p(gx), nd)
     return gd, gx
+
+
+class QuartetOracle:
+    """Oracle digestion of explicit shell-quartet lists (batch types 1, 5)."""
+
+    def __init__(self, basis):
+        L = lib()
+        P, i, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong
+        L.orc_ctx_new.argtypes = [i, P, P, P, P, i, i, i]
+        L.orc_ctx_new.restype = P
+        L.orc_ctx_free.argtypes = [P]
+        L.orc_ctx_prepare.argtypes = [P, P, ll, i, i]
+        L.orc_ctx_quartets.argtypes = [P, P, ll, i, i, P, i, P, P, i, i]
+        L.orc_ndim.argtypes = [P, P]
+        xyz, lmax, nfn, ex = _basis_arrays(basis)
+        self._keep = (xyz, lmax, nfn, ex)
+        self.h = L.orc_ctx_new(basis.ncnt, _p(xyz), _p(lmax), _p(nfn), _p(ex),
+                               ex.shape[1], ex.shape[2], int(basis.hmlt == 0))
+        ns = ctypes.c_int()
+        self.ndim = L.orc_ndim(self.h, ctypes.byref(ns))
+        self.nskp = ns.value
+
+    def prepare(self, quart, t1, t2):
+        q = np.ascontiguousarray(quart, dtype=np.int32)
+        return lib().orc_ctx_prepare(self.h, _p(q), q.shape[0], int(t1), int(t2))
+
+    def digest(self, quart, t1, t2, dent, gd, gx, nthreads=1):
+        q = np.ascontiguousarray(quart, dtype=np.int32)
+        assert gd.flags.f_contiguous and gx.flags.f_contiguous
+        D = np.asfortranarray(dent, dtype=np.complex128)
+        lib().orc_ctx_quartets(self.h, _p(q), q.shape[0], int(t1), int(t2), _p(D),
+                               D.shape[0], _p(gd), _p(gx), gd.shape[0], int(nthreads))
+
+    def close(self):
+        if self.h:
+            lib().orc_ctx_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
