@@ -12,7 +12,6 @@
 //               digestion of CLMMTG/CLMMTZ batch types 1 and 5 into shared
 //               accumulators flushed with one atomic per element.
 //   k_zero      clears the outputs (CLMFAST zeroes GDIR/GXCH, :11592).
-//   k_hermfix   nothing to do in full mode (kept out).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -333,30 +332,34 @@ __global__ void k_eqgen(const Shell *sh, int ns, const PairE *pe, int ncomp,
 }
 
 // ---------------------------------------------------------------------------
-// Boys function in the reference's four regimes (FUNFM, bertha-scf.f:32465)
+// Boys function in the reference's four regimes (FUNFM, bertha-scf.f:32465).
+// The power series multiplies by tabulated reciprocals 1/(2n+1) instead of
+// dividing (the FP64 pipe is the scarce resource on this part).
 // ---------------------------------------------------------------------------
+constexpr int NRINV = 2 * (MAXLAM + 2) + 2 * 60 + 4;
+__constant__ double c_rinv[NRINV];  // c_rinv[n] = 1/(2n+1)
+
 __device__ void boys_ref(double T, int lam, double *F) {
   const double A0 = 4.994501191201870e-1, B0 = 4.551838436668326e-1;
   const double PI12 = 1.7724538509055160;
   if (T <= 1.0e-11) {
-    for (int m = 0; m <= lam; ++m) F[m] = 1.0 / double(2 * m + 1);
+    for (int m = 0; m <= lam; ++m) F[m] = c_rinv[m];
   } else if (T <= 17.0) {
     double txp = exp(-T), tt2 = 2.0 * T, term = 1.0, s = 1.0;
     for (int k = 1; k <= 60; ++k) {
-      term = term * tt2 / double(2 * lam + 2 * k + 1);
+      term = term * tt2 * c_rinv[lam + k];
       s += term;
     }
-    F[lam] = s * txp / double(2 * lam + 1);
-    for (int m = lam - 1; m >= 0; --m)
-      F[m] = (tt2 * F[m + 1] + txp) / double(2 * m + 1);
+    F[lam] = s * txp * c_rinv[lam];
+    for (int m = lam - 1; m >= 0; --m) F[m] = (tt2 * F[m + 1] + txp) * c_rinv[m];
   } else if (T <= 30.0) {
-    double txp = exp(-T), tt2 = 2.0 * T;
+    double txp = exp(-T), tt2 = 2.0 * T, r2 = 1.0 / tt2;
     F[0] = 0.5 * PI12 / sqrt(T) - txp * (A0 / (B0 + T));
-    for (int m = 0; m < lam; ++m) F[m + 1] = (double(2 * m + 1) * F[m] - txp) / tt2;
+    for (int m = 0; m < lam; ++m) F[m + 1] = (double(2 * m + 1) * F[m] - txp) * r2;
   } else {
-    double tt2 = 2.0 * T;
+    double r2 = 0.5 / T;
     F[0] = 0.5 * PI12 / sqrt(T);
-    for (int m = 0; m < lam; ++m) F[m + 1] = double(2 * m + 1) * F[m] / tt2;
+    for (int m = 0; m < lam; ++m) F[m + 1] = double(2 * m + 1) * F[m] * r2;
   }
 }
 
@@ -371,6 +374,14 @@ struct QArgs {
   double *GD, *GX;
   int ns, ldd, ldf, nskp, isym, racah1;
 };
+
+constexpr unsigned long long SGN = 0x8000000000000000ULL;
+
+// x * (+-1) through the sign bit, without an FP64 instruction
+__device__ inline double flip(double x, unsigned long long m) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)m);
+}
+__device__ inline unsigned long long smask(double p) { return p < 0.0 ? SGN : 0ULL; }
 
 __device__ inline double pair_phase(int kqa, int ma, int kqb, int mb) {
   double s = ((kqa > 0) == (kqb > 0)) ? 1.0 : -1.0;
@@ -426,15 +437,25 @@ __device__ inline void satomic(double2 *p, double2 v) {
   atomicAdd(&p->y, v.y);
 }
 
-__global__ void __launch_bounds__(QTHREADS)
+// FP64 multiply-adds of the two contraction orders of one quartet class:
+// ERIFAST's order contracts the ab E-coefficients against R first.
+__host__ __device__ inline long long contraction_cost(int pab, int nab, int pcd, int ncd) {
+  return 4LL * pab * nab * ncd + 16LL * pab * pcd * ncd;
+}
+
+// One CTA per ordered shell quartet.  The pair whose E-coefficients enter
+// the first contraction is the "left" pair; it is ab (the reference's order,
+// ERIFAST :12676) unless the other order needs fewer multiply-adds, in which
+// case (cd|ab) = (ab|cd) is evaluated and the m-sign index is remapped.
+__global__ void __launch_bounds__(QTHREADS, 2)
 k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
   extern __shared__ double smem[];
-  double *R = smem;                    // NTR
-  double *R2 = R + NTR;                // NTR
-  double *F = R2 + NTR;                // MAXLAM+2
+  double *R = smem;                          // NTR
+  double *R2 = R + NTR;                      // NTR
+  double *F = R2 + NTR;                      // MAXLAM+2
   double2 *G = (double2 *)(F + MAXLAM + 2);  // CHUNK*2*NTE
-  double2 *Jl = G + CHUNK * 2 * NTE;   // MAXSP*MAXSP
-  double2 *Kl = Jl + MAXSP * MAXSP;    // MAXSP*MAXSP
+  double2 *Jl = G + CHUNK * 2 * NTE;         // MAXSP*MAXSP
+  double2 *Kl = Jl + MAXSP * MAXSP;          // MAXSP*MAXSP
   __shared__ double sgeo[8];
 
   for (long long qi = blockIdx.x; qi < nq; qi += gridDim.x) {
@@ -443,7 +464,10 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
     int la = A.l, lb = B.l, lc = C.l, ld = Dd.l;
     int degab = la + lb + 2 * t1, degcd = lc + ld + 2 * t2;
     int lam = degab + degcd;
+    int nla = 2 * la + 1, nlb = 2 * lb + 1, nlc = 2 * lc + 1, nld = 2 * ld + 1;
+    int nlab = nla * nlb, nlcd = nlc * nld;
     int nab = ntuv(degab), ncd = ntuv(degcd);
+    bool swp = contraction_cost(nlcd, ncd, nlab, nab) < contraction_cost(nlab, nab, nlcd, ncd);
     int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
     if (threadIdx.x == 0) {
       double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
@@ -456,7 +480,9 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
       double aph = p * qq / (p + qq);
       double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
       boys_ref(T, lam, F);
-      sgeo[0] = Px - Qx; sgeo[1] = Py - Qy; sgeo[2] = Pz - Qz;
+      // R is built for the left pair's centre minus the right pair's centre
+      double sg = swp ? -1.0 : 1.0;
+      sgeo[0] = sg * (Px - Qx); sgeo[1] = sg * (Py - Qy); sgeo[2] = sg * (Pz - Qz);
       sgeo[3] = -2.0 * aph;
       sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
     }
@@ -466,8 +492,7 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
       double X = sgeo[0], Y = sgeo[1], Z = sgeo[2], m2a = sgeo[3];
       double *cur = R, *nxt = R2;
       for (int n = lam; n >= 0; --n) {
-        int top = lam - n;
-        int cnt = ntuv(top);
+        int cnt = ntuv(lam - n);
         for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
           double val;
           if (k == 0) {
@@ -492,45 +517,52 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         __syncthreads();
         double *tmp = cur; cur = nxt; nxt = tmp;
       }
-      // cur holds R^(0); scale by the ERI prefactor into R
       double pre = sgeo[4];
       int nt = ntuv(lam);
-      for (int k = threadIdx.x; k < nt; k += blockDim.x) R[k] = (cur == R ? R[k] : cur[k]) * pre;
-      __syncthreads();
+      if (cur != R)
+        for (int k = threadIdx.x; k < nt; k += blockDim.x) R[k] = cur[k] * pre;
+      else
+        for (int k = threadIdx.x; k < nt; k += blockDim.x) R[k] *= pre;
     }
-    int nla = 2 * la + 1, nlb = 2 * lb + 1, nlc = 2 * lc + 1, nld = 2 * ld + 1;
     for (int k = threadIdx.x; k < MAXSP * MAXSP; k += blockDim.x) {
       Jl[k] = make_double2(0.0, 0.0);
       Kl[k] = make_double2(0.0, 0.0);
     }
     const double2 *Eab = q.E + q.pe[Q4.x * q.ns + Q4.y].off[t1];
     const double2 *Ecd = q.E + q.pe[Q4.z * q.ns + Q4.w].off[t2];
-    int nlab = nla * nlb, nlcd = nlc * nld;
+    // left/right roles
+    const double2 *EL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
+    int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
+    int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
+    int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;  // second label count
     int lq[4] = {la, lb, lc, ld};
+    int oab = t1 ? q.nskp : 0, ocd = t2 ? q.nskp : 0;
     __syncthreads();
-    for (int c0 = 0; c0 < nlab; c0 += CHUNK) {
-      int nch = min(CHUNK, nlab - c0);
-      // first contraction: G[lab][set][q] = sum_s E_ab[lab][set][s] R[s+q]
-      for (int w = threadIdx.x; w < nch * 2 * ncd; w += blockDim.x) {
-        int lab = w / (2 * ncd), rem = w % (2 * ncd);
-        int set = rem / ncd, qq = rem % ncd;
-        const double2 *e = Eab + ((long long)(c0 + lab) * 2 + set) * nab;
+    for (int c0 = 0; c0 < nlL; c0 += CHUNK) {
+      int nch = min(CHUNK, nlL - c0);
+      // first contraction: G[lab][set][q] = Z(q) sum_s E_L[lab][set][s] R[s+q]
+      for (int w = threadIdx.x; w < nch * 2 * nR; w += blockDim.x) {
+        int lab = w / (2 * nR), rem = w % (2 * nR);
+        int set = rem / nR, qq = rem % nR;
+        const double2 *e = EL + ((long long)(c0 + lab) * 2 + set) * nL;
         int tq = c_t[qq], uq = c_u[qq], vq = c_v[qq];
-        double2 acc = make_double2(0.0, 0.0);
-        for (int s = 0; s < nab; ++s) {
+        double ax = 0.0, ay = 0.0;
+        for (int s = 0; s < nL; ++s) {
           double rv = R[hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq)];
           double2 ev = e[s];
-          acc.x += ev.x * rv;
-          acc.y += ev.y * rv;
+          ax = fma(ev.x, rv, ax);
+          ay = fma(ev.y, rv, ay);
         }
-        G[(lab * 2 + set) * NTE + qq] = acc;
+        unsigned long long zm = ((tq + uq + vq) & 1) ? SGN : 0ULL;
+        G[(lab * 2 + set) * NTE + qq] = make_double2(flip(ax, zm), flip(ay, zm));
       }
       __syncthreads();
       // second contraction and digestion
-      for (int w = threadIdx.x; w < nch * nlcd; w += blockDim.x) {
-        int lab = w / nlcd, lcd = w % nlcd;
-        int labab = c0 + lab;
-        int ia = labab / nlb, ib = labab % nlb, ic = lcd / nld, id = lcd % nld;
+      for (int w = threadIdx.x; w < nch * nlR; w += blockDim.x) {
+        int lab = w / nlR, lr = w % nlR;
+        int labL = c0 + lab;
+        int l1 = labL / nl2L, l2 = labL % nl2L, r1 = lr / nl2R, r2 = lr % nl2R;
+        int ia = swp ? r1 : l1, ib = swp ? r2 : l2, ic = swp ? l1 : r1, id = swp ? l2 : r2;
         int kq[4], mq[4], mm[4];
         label_of(la, ia, kq[0], mm[0]);
         label_of(lb, ib, kq[1], mm[1]);
@@ -540,74 +572,102 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         if (!label_ok(q, mcnt, kq, mq, lq)) continue;
         double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
         double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
+        double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
         const double2 *g11 = G + (lab * 2 + 0) * NTE, *g21 = G + (lab * 2 + 1) * NTE;
-        const double2 *e11 = Ecd + ((long long)lcd * 2 + 0) * ncd;
-        const double2 *e21 = Ecd + ((long long)lcd * 2 + 1) * ncd;
-        double2 s1 = {0, 0}, s1c = {0, 0}, s2 = {0, 0}, s2c = {0, 0};
-        double2 s3 = {0, 0}, s3c = {0, 0}, s4 = {0, 0}, s4c = {0, 0};
-        for (int k = 0; k < ncd; ++k) {
-          double z = (c_t[k] + c_u[k] + c_v[k]) & 1 ? -1.0 : 1.0;
-          double2 a = cscale(e11[k], z), b = cscale(e21[k], z);
-          double2 x1 = g11[k], x2 = g21[k];
-          s1 = cadd(s1, cmul(a, x1));
-          s1c = cadd(s1c, cmulc(a, x1));
-          s2 = cadd(s2, cmul(b, x1));
-          s2c = cadd(s2c, cmulc(b, x1));
-          s3 = cadd(s3, cmul(a, x2));
-          s3c = cadd(s3c, cmulc(a, x2));
-          s4 = cadd(s4, cmul(b, x2));
-          s4c = cadd(s4c, cmulc(b, x2));
+        const double2 *e11 = ER + ((long long)lr * 2 + 0) * nR;
+        const double2 *e21 = ER + ((long long)lr * 2 + 1) * nR;
+        // four complex products (E_R set) x (G set), kept as real partials
+        double a0 = 0, b0 = 0, c0r = 0, d0 = 0, a1 = 0, b1 = 0, c1 = 0, d1 = 0;
+        double a2 = 0, b2 = 0, c2 = 0, d2 = 0, a3 = 0, b3 = 0, c3 = 0, d3 = 0;
+        for (int k = 0; k < nR; ++k) {
+          double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
+          a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
+          c0r = fma(u1.x, x1.y, c0r); d0 = fma(u1.y, x1.x, d0);
+          a1 = fma(u2.x, x1.x, a1); b1 = fma(u2.y, x1.y, b1);
+          c1 = fma(u2.x, x1.y, c1); d1 = fma(u2.y, x1.x, d1);
+          a2 = fma(u1.x, x2.x, a2); b2 = fma(u1.y, x2.y, b2);
+          c2 = fma(u1.x, x2.y, c2); d2 = fma(u1.y, x2.x, d2);
+          a3 = fma(u2.x, x2.x, a3); b3 = fma(u2.y, x2.y, b3);
+          c3 = fma(u2.x, x2.y, c3); d3 = fma(u2.y, x2.x, d3);
         }
-        double pabcd = pab * pcd;
+        // u*x = (a-b, c+d); u*conj(x) = (a+b, d-c)
+        double2 s1 = {a0 - b0, c0r + d0}, s1c = {a0 + b0, d0 - c0r};
+        double2 s2 = {a1 - b1, c1 + d1}, s2c = {a1 + b1, d1 - c1};
+        double2 s3 = {a2 - b2, c2 + d2}, s3c = {a2 + b2, d2 - c2};
+        double2 s4 = {a3 - b3, c3 + d3}, s4c = {a3 + b3, d3 - c3};
+        // 16 m-sign combinations of (left|right) (ERIFAST :12809-13119);
+        // phases are +-1 and applied through the sign bit
+        unsigned long long ml = smask(pl), mlr = smask(pl * pr);
         double2 r[16];
-        r[0] = s1;  r[12] = cscale(s1c, pab);
-        r[15] = cscale(cconj(r[0]), pabcd);  r[3] = cscale(cconj(r[12]), pabcd);
-        r[2] = s2;  r[14] = cscale(s2c, pab);
-        r[13] = cscale(cconj(r[2]), -pabcd); r[1] = cscale(cconj(r[14]), -pabcd);
-        r[8] = s3;  r[4] = cscale(s3c, -pab);
-        r[7] = cscale(cconj(r[8]), -pabcd);  r[11] = cscale(cconj(r[4]), -pabcd);
-        r[10] = s4; r[6] = cscale(s4c, -pab);
-        r[5] = cscale(cconj(r[10]), pabcd);  r[9] = cscale(cconj(r[6]), pabcd);
-        // Fock indices of the spinors (component offset for S)
-        int oab = t1 ? q.nskp : 0, ocd = t2 ? q.nskp : 0;
+        r[0] = s1;
+        r[12] = make_double2(flip(s1c.x, ml), flip(s1c.y, ml));
+        r[15] = make_double2(flip(r[0].x, mlr), flip(r[0].y, mlr ^ SGN));
+        r[3] = make_double2(flip(r[12].x, mlr), flip(r[12].y, mlr ^ SGN));
+        r[2] = s2;
+        r[14] = make_double2(flip(s2c.x, ml), flip(s2c.y, ml));
+        r[13] = make_double2(flip(r[2].x, mlr ^ SGN), flip(r[2].y, mlr));
+        r[1] = make_double2(flip(r[14].x, mlr ^ SGN), flip(r[14].y, mlr));
+        r[8] = s3;
+        r[4] = make_double2(flip(s3c.x, ml ^ SGN), flip(s3c.y, ml ^ SGN));
+        r[7] = make_double2(flip(r[8].x, mlr ^ SGN), flip(r[8].y, mlr));
+        r[11] = make_double2(flip(r[4].x, mlr ^ SGN), flip(r[4].y, mlr));
+        r[10] = s4;
+        r[6] = make_double2(flip(s4c.x, ml ^ SGN), flip(s4c.y, ml ^ SGN));
+        r[5] = make_double2(flip(r[10].x, mlr), flip(r[10].y, mlr ^ SGN));
+        r[9] = make_double2(flip(r[6].x, mlr), flip(r[6].y, mlr ^ SGN));
+        // (ab|cd) m-sign index from the (left|right) one
+#define RV(sa, sb, sc, sd) (swp ? r[8 * (sc) + 4 * (sd) + 2 * (sa) + (sb)] \
+                                : r[8 * (sa) + 4 * (sb) + 2 * (sc) + (sd)])
         int fb[2] = {B.fock[ib][0] + oab, B.fock[ib][1] + oab};
         int fc[2] = {C.fock[ic][0] + ocd, C.fock[ic][1] + ocd};
         int fd[2] = {Dd.fock[id][0] + ocd, Dd.fock[id][1] + ocd};
         if (q.isym == 0) {
+          double2 Dcd[4], Dcb[4];
+          for (int x = 0; x < 2; ++x)
+            for (int y = 0; y < 2; ++y) {
+              Dcd[2 * x + y] = ldD(q, fc[x], fd[y]);
+              Dcb[2 * x + y] = ldD(q, fc[x], fb[y]);
+            }
           for (int sa = 0; sa < 2; ++sa)
             for (int sb = 0; sb < 2; ++sb) {
-              double2 jacc = {0, 0};
+              double jx = 0.0, jy = 0.0;
               for (int sc = 0; sc < 2; ++sc)
-                for (int sd = 0; sd < 2; ++sd)
-                  jacc = cadd(jacc, cmul(r[8 * sa + 4 * sb + 2 * sc + sd], ldD(q, fc[sc], fd[sd])));
-              satomic(&Jl[(ia * 2 + sa) * MAXSP + ib * 2 + sb], jacc);
+                for (int sd = 0; sd < 2; ++sd) {
+                  double2 v = RV(sa, sb, sc, sd), d = Dcd[2 * sc + sd];
+                  jx = fma(v.x, d.x, fma(-v.y, d.y, jx));
+                  jy = fma(v.x, d.y, fma(v.y, d.x, jy));
+                }
+              satomic(&Jl[(ia * 2 + sa) * MAXSP + ib * 2 + sb], make_double2(jx, jy));
             }
           for (int sa = 0; sa < 2; ++sa)
             for (int sd = 0; sd < 2; ++sd) {
-              double2 kacc = {0, 0};
+              double kx = 0.0, ky = 0.0;
               for (int sb = 0; sb < 2; ++sb)
-                for (int sc = 0; sc < 2; ++sc)
-                  kacc = cadd(kacc, cmul(r[8 * sa + 4 * sb + 2 * sc + sd], ldD(q, fc[sc], fb[sb])));
-              satomic(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], kacc);
+                for (int sc = 0; sc < 2; ++sc) {
+                  double2 v = RV(sa, sb, sc, sd), d = Dcb[2 * sc + sb];
+                  kx = fma(v.x, d.x, fma(-v.y, d.y, kx));
+                  ky = fma(v.x, d.y, fma(v.y, d.x, ky));
+                }
+              satomic(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], make_double2(kx, ky));
             }
         } else {
           // CLMMTZ: real parts, equal-sign direct blocks, crossed exchange
           for (int s = 0; s < 2; ++s) {
             double jv = 0.0, kv = 0.0;
             for (int t = 0; t < 2; ++t) {
-              jv += r[8 * s + 4 * s + 2 * t + t].x * ldD(q, fc[t], fd[t]).x;
-              kv += r[8 * s + 4 * t + 2 * t + s].x * ldD(q, fc[t], fb[t]).x;
+              jv = fma(RV(s, s, t, t).x, ldD(q, fc[t], fd[t]).x, jv);
+              kv = fma(RV(s, t, t, s).x, ldD(q, fc[t], fb[t]).x, kv);
             }
             atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, jv);
             atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
           }
         }
+#undef RV
       }
       __syncthreads();
     }
     // flush shared accumulators
     {
-      int oab = t1 ? q.nskp : 0, ocd = t2 ? q.nskp : 0;
       int nsa = 2 * nla;
       for (int w = threadIdx.x; w < nsa * 2 * nlb; w += blockDim.x) {
         int a = w / (2 * nlb), b = w % (2 * nlb);
@@ -710,6 +770,9 @@ int upload_tables() {
   if (cudaMemcpyToSymbol(c_t, t, sizeof(t)) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(c_u, u, sizeof(u)) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(c_v, v, sizeof(v)) != cudaSuccess) return 1;
+  double rinv[NRINV];
+  for (int k = 0; k < NRINV; ++k) rinv[k] = 1.0 / double(2 * k + 1);
+  if (cudaMemcpyToSymbol(c_rinv, rinv, sizeof(rinv)) != cudaSuccess) return 1;
   done = true;
   return 0;
 }
