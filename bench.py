@@ -30,7 +30,7 @@ for _p in (ROOT, os.path.join(ROOT, "bertha-program_gb300")):
 
 import numpy as np  # noqa: E402
 
-METRIC = "Fock-build ERI quartets/s (FP64)"
+METRIC = "Fock-build ERI quartets/s"
 UNIT = "quartets/s"
 WORKLOAD = "eri-microbench: 2^20 random shell quartets, l<=3, LL/SS classes"
 
@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--quartets", type=int, default=1 << 20)
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--precision", default="df32", choices=["fp64", "df32"],
+                   help="precision of the headline value; the other is timed beside it")
     return p.parse_args()
 
 
@@ -61,29 +63,24 @@ def config(args, extra=None):
 # CPU timing of the restatement (oracle) on a bounded sample
 # ---------------------------------------------------------------------------
 def cpu_rate(basis, quarts, dent, seconds, nthreads):
+    """Quartets/s of the CPU restatement: chunks of 2048 quartets of every
+    component class in turn until `seconds` of digestion time are spent."""
     from oracle import oracle as orc
     O = orc.QuartetOracle(basis)
     n = basis.ndim
     gd = np.zeros((n, n), complex, order="F")
     gx = np.zeros((n, n), complex, order="F")
-    # probe the rate on a small sample, then size the sample to `seconds`
-    probe = 256
-    t_probe = 0.0
-    for cls, q in quarts.items():
-        O.prepare(q[:probe], *cls)
-        t0 = time.perf_counter()
-        O.digest(q[:probe], *cls, dent, gd, gx, nthreads=nthreads)
-        t_probe += time.perf_counter() - t0
-    rate = 4 * probe / max(t_probe, 1e-9)
-    per = int(max(probe, min(len(next(iter(quarts.values()))), rate * seconds / 4)))
-    tot, nq = 0.0, 0
-    for cls, q in quarts.items():
-        s = q[:per]
-        O.prepare(s, *cls)
-        t0 = time.perf_counter()
-        O.digest(s, *cls, dent, gd, gx, nthreads=nthreads)
-        tot += time.perf_counter() - t0
-        nq += len(s)
+    chunk, off, tot, nq = 2048, 0, 0.0, 0
+    nmax = min(len(q) for q in quarts.values())
+    while tot < seconds and off < nmax:
+        for cls, q in quarts.items():
+            s = q[off:off + chunk]
+            O.prepare(s, *cls)
+            t0 = time.perf_counter()
+            O.digest(s, *cls, dent, gd, gx, nthreads=nthreads)
+            tot += time.perf_counter() - t0
+            nq += len(s)
+        off += chunk
     O.close()
     return nq / tot, nq, tot
 
@@ -248,27 +245,63 @@ def run_gpu(args):
                 events[k][1].record(stream)
         return launches
 
-    peak64 = fp64_peak(torch)
-    for _ in range(args.warmup):
-        flush.zero_()
+    def energy_terms():
+        # one clean step; J/K contracted with the density (the two-electron
+        # energy terms 1/2 Re tr(D J), 1/2 Re tr(D K), ENRGIES form)
+        GD.zero_()
+        GX.zero_()
         step()
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()
+        gd = GD.cpu().numpy().view(np.complex128).reshape(n, n).T
+        gx = GX.cpu().numpy().view(np.complex128).reshape(n, n).T
+        return gd, gx
 
-    ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in dq]
-          for _ in range(args.steps)]
-    launches = 0
-    with ClockSampler(local) as clk:
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        for s in range(args.steps):
+    def timed(prec):
+        fb.set_precision(prec)
+        for _ in range(args.warmup):
             flush.zero_()
-            launches += step(ev[s])
+            step()
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-    kern_ms = np.array([[ev[s][k][0].elapsed_time(ev[s][k][1]) for k in range(len(dq))]
-                        for s in range(args.steps)])
+        ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in dq]
+              for _ in range(args.steps)]
+        launches = 0
+        with ClockSampler(local) as clk:
+            if world > 1:
+                dist.barrier()
+            torch.cuda.synchronize()
+            for s in range(args.steps):
+                flush.zero_()
+                launches += step(ev[s])
+            torch.cuda.synchronize()
+            if world > 1:
+                dist.barrier()
+        kern_ms = np.array([[ev[s][k][0].elapsed_time(ev[s][k][1]) for k in range(len(dq))]
+                            for s in range(args.steps)])
+        return kern_ms, launches, clk.summary()
+
+    peak64 = fp64_peak(torch)
+    other = "fp64" if args.precision == "df32" else "df32"
+    kern_other, _, _ = timed(other)
+    kern_ms, launches, clocks = timed(args.precision)
+    fb.set_precision("fp64")
+    gd64, gx64 = energy_terms()
+    fb.set_precision("df32")
+    gdm, gxm = energy_terms()
+    fb.set_precision(args.precision)
+    scale = max(np.abs(gd64).max(), np.abs(gx64).max())
+
+    def e2(gd, gx):
+        return (0.5 * np.sum(dent * gd.T).real, 0.5 * np.sum(dent * gx.T).real)
+
+    ej64, ek64 = e2(gd64, gx64)
+    ejm, ekm = e2(gdm, gxm)
+    accuracy = {"j_max_abs": float(np.abs(gdm - gd64).max()),
+                "k_max_abs": float(np.abs(gxm - gx64).max()),
+                "rel_to_max_element": float(max(np.abs(gdm - gd64).max(),
+                                                np.abs(gxm - gx64).max()) / scale),
+                "energy_j_abs_eh": float(abs(ejm - ej64)),
+                "energy_k_abs_eh": float(abs(ekm - ek64)),
+                "energy_j_eh": float(ej64), "energy_k_eh": float(ek64)}
     step_ms = float(kern_ms.sum(1).max() if args.steps else 0.0)
     step_ms_mean = float(kern_ms.sum(1).mean())
     ms = torch.tensor([step_ms_mean], dtype=torch.float64, device=dev)
@@ -276,6 +309,7 @@ def run_gpu(args):
         dist.all_reduce(ms, op=dist.ReduceOp.MAX)
     ms_per_step = float(ms.item())
     value = args.quartets * world / (ms_per_step * 1e-3)
+    other_value = args.quartets * world / (float(kern_other.sum(1).mean()) * 1e-3)
 
     # end to end through the C ABI: host density and quartet lists in pinned
     # memory copied in, J/K copied back, every step
@@ -307,6 +341,8 @@ def run_gpu(args):
     tot_flops = sum(flops.values())
     kern_mean = kern_ms.mean(0)
     achieved = tot_flops / (kern_mean.sum() * 1e-3) / 1e12
+    kern64 = kern_ms if args.precision == "fp64" else kern_other
+    achieved64 = tot_flops / (kern64.mean(0).sum() * 1e-3) / 1e12
     per_class = {f"{'LS'[c[0]]}{'LS'[c[0]]}|{'LS'[c[1]]}{'LS'[c[1]]}":
                  {"ms": float(kern_mean[k]), "quartets_per_s": float(quarts[c].shape[0] / (kern_mean[k] * 1e-3)),
                   "tflops": float(flops[c] / (kern_mean[k] * 1e-3) / 1e12)}
@@ -325,19 +361,31 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": config(args, {"per_class": per_class, "step_ms_max": step_ms}),
-            "roofline": {"bound": "fp64", "kernel": "k_quartet", "achieved": achieved,
-                         "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
+            "dtype": ("f64" if args.precision == "fp64" else
+                      "f32x2 double-float contractions; f64 Boys, R, J/K sums"),
+            "data": "synthetic",
+            "config": config(args, {"precision": args.precision, "per_class": per_class,
+                                    "step_ms_max": step_ms}),
+            "fp64_path": {"value": value if args.precision == "fp64" else other_value,
+                          "unit": UNIT},
+            "split_precision_path": {"value": value if args.precision == "df32" else other_value,
+                                     "unit": UNIT},
+            "speedup_split_vs_fp64": (value / other_value if args.precision == "df32"
+                                      else other_value / value),
+            "accuracy_split_vs_fp64": accuracy,
+            "roofline": {"bound": "fp64", "kernel": "k_quartet (FP64 path)",
+                         "achieved": achieved64,
+                         "peak": peak64, "unit": "TFLOP/s", "frac": achieved64 / peak64,
                          "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
                                         "(MEASURED_PEAKS.json has no FP64 entry)",
                          "traffic": traffic,
-                         "flops_per_step": tot_flops},
+                         "flops_per_step": tot_flops,
+                         "split_path_effective_tflops": achieved},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
-            "clocks": clk.summary(),
+            "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
     fb.close()

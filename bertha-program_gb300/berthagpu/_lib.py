@@ -12,6 +12,7 @@ BG_OK, BG_ERR_ARG, BG_ERR_CAPACITY, BG_ERR_CUDA, BG_ERR_STATE = 0, 1, 2, 3, 4
 HMLT = {"NORL": 0, "BARE": 1, "DHFR": 2, "DHFP": 3, "DHFB": 4, "DHFQ": 5}
 SHAPE = {"NOSYMM": 0, "PLANAR": 0, "GENERAL": 0, "DIATOM": 1, "LINEAR": 1, "ATOMIC": 2}
 FLAG_NO_RACAH1 = 1
+PREC = {"fp64": 0, "df32": 1}
 MAX_L = 3
 
 _CODES = {1: "invalid argument", 2: "capacity exceeded", 3: "CUDA error", 4: "context unusable"}
@@ -35,6 +36,7 @@ def lib():
         P, i, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong
         L.bertha_gpu_init.argtypes = [ctypes.POINTER(P), i, P, P, P, i, P, i, i, i, i]
         L.bertha_gpu_dims.argtypes = [P, P, P]
+        L.bertha_gpu_set_precision.argtypes = [P, i]
         L.bertha_gpu_clmfast.argtypes = [P, P, i, i, P, P, i]
         L.bertha_gpu_clmfast_device.argtypes = [P, P, i, i, P, P, i, P]
         L.bertha_gpu_quartets.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
@@ -51,7 +53,7 @@ def lib():
 
 
 EXPORTED = [
-    "bertha_gpu_init", "bertha_gpu_dims", "bertha_gpu_clmfast",
+    "bertha_gpu_init", "bertha_gpu_set_precision", "bertha_gpu_dims", "bertha_gpu_clmfast",
     "bertha_gpu_clmfast_device", "bertha_gpu_quartets", "bertha_gpu_shells",
     "bertha_gpu_layout", "bertha_gpu_launches", "bertha_gpu_last_error",
     "bertha_gpu_free",

@@ -36,6 +36,12 @@ class FockBuilder:
         nd, ns = ctypes.c_int(), ctypes.c_int()
         check(lib().bertha_gpu_dims(self._ctx, ctypes.byref(nd), ctypes.byref(ns)), self._ctx)
         self.ndim, self.nskp = nd.value, ns.value
+        self.precision = "fp64"
+
+    def set_precision(self, prec):
+        """'fp64' (drop-in) or 'df32' (split precision on the FP32 pipes)."""
+        check(lib().bertha_gpu_set_precision(self._ctx, _lib.PREC[prec]), self._ctx)
+        self.precision = prec
 
     def close(self):
         if self._ctx:

@@ -54,6 +54,8 @@ struct Shell {
 
 struct PairE {
   long long off[2];  // E offset (complex units) for LL and SS, -1 if absent
+  int kexp;          // power-of-two scale of the double-float copy (see k_econv)
+  int pad;
 };
 
 // complex helpers
@@ -397,11 +399,11 @@ __device__ inline int ncntrs(int a, int b, int c, int d) {
 }
 
 // CLMFAST label-level selection rules (bertha-scf.f:11843-11939)
-__device__ bool label_ok(const QArgs &q, int mcnt, const int *kq, const int *mq,
+__device__ bool label_ok(int isym, int racah1, int mcnt, const int *kq, const int *mq,
                          const int *lq) {
   int jq[4];
   for (int i = 0; i < 4; ++i) jq[i] = 2 * abs(kq[i]) - 1;
-  bool onec = (mcnt == 1 && !q.racah1);
+  bool onec = (mcnt == 1 && !racah1);
   if (onec) {
     int nui = max(abs(jq[0] - jq[1]) / 2, abs(jq[2] - jq[3]) / 2);
     int nuf = min((jq[0] + jq[1]) / 2, (jq[2] + jq[3]) / 2);
@@ -411,7 +413,7 @@ __device__ bool label_ok(const QArgs &q, int mcnt, const int *kq, const int *mq,
       if (((lq[0] + lq[1] + nu) & 1) == 0 && ((lq[2] + lq[3] + nu) & 1) == 0) selk = true;
     if (!selk) return false;
   }
-  if (q.isym == 1 || q.isym == 2) {
+  if (isym == 1 || isym == 2) {
     bool ok = (mq[0] == mq[1] && mq[2] == mq[3]) || (mq[0] == mq[2] && mq[1] == mq[3]) ||
               (mq[0] == mq[3] && mq[1] == mq[2]);
     if (!ok) return false;
@@ -569,7 +571,7 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         label_of(lc, ic, kq[2], mm[2]);
         label_of(ld, id, kq[3], mm[3]);
         for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
-        if (!label_ok(q, mcnt, kq, mq, lq)) continue;
+        if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
         double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
         double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
         double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
@@ -692,6 +694,382 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Split-precision (double-float) path.
+// Every FP64 value v is carried as a pair of FP32 words (h, l), v = h + l,
+// |l| <= ulp(h)/2, about 48 significant bits.  Products are formed exactly
+// with FMA (TwoProd) and sums with TwoSum, so the contractions run on the
+// FP32 pipes at ~2^-44 relative accuracy.  Boys values, the R recursion and
+// the J/K accumulation stay FP64.  FP32's exponent range is kept by exact
+// power-of-two scaling: E-coefficients of a pair with exponent sum p are
+// stored times 2^(k_p*lambda), k_p = floor(log2(2p)/2); a quartet with
+// reduced exponent alpha uses k = floor(log2(2 alpha)/2) <= k_p, k_q and
+// rescales by 2^((k-k_p)lambda) (<= 1), R by 2^(-k lambda).
+// ---------------------------------------------------------------------------
+__host__ __device__ inline int half_floor_log2(double x) {
+  int e = ilogb(x);
+  return e >= 0 ? e / 2 : -((-e + 1) / 2);
+}
+
+__device__ inline void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// (sh, sl) += (ah + al) * (bh + bl)
+__device__ inline void df_fma(float ah, float al, float bh, float bl, float &sh, float &sl) {
+  float p = ah * bh;
+  float pe = fmaf(ah, bh, -p);
+  pe = fmaf(ah, bl, pe);
+  pe = fmaf(al, bh, pe);
+  float s, e;
+  two_sum(sh, p, s, e);
+  sh = s;
+  sl += e + pe;
+}
+
+// (h, l) = (ah + al) + sgn * (bh + bl), renormalised
+__device__ inline void df_add(float ah, float al, float bh, float bl, float &h, float &l) {
+  float s, e;
+  two_sum(ah, bh, s, e);
+  e += al + bl;
+  h = s + e;
+  l = e - (h - s);
+}
+
+__device__ inline void df_split(double v, float &h, float &l) {
+  h = __double2float_rn(v);
+  l = __double2float_rn(v - (double)h);
+}
+
+__device__ inline double df_val(float h, float l) { return (double)h + (double)l; }
+
+// Double-float copy of the E-coefficients, scaled per pair.
+__global__ void k_econv(const double2 *E, float4 *Edf, const PairE *pe, const Shell *sh,
+                        int ns, int ncomp) {
+  long long pair = blockIdx.x;
+  if (pair >= (long long)ns * ns) return;
+  const Shell &A = sh[pair / ns], &B = sh[pair % ns];
+  int k = pe[pair].kexp;
+  int nl = (2 * A.l + 1) * (2 * B.l + 1);
+  for (int comp = 0; comp < ncomp; ++comp) {
+    int nt = ntuv(A.l + B.l + 2 * comp);
+    long long off = pe[pair].off[comp];
+    for (int w = threadIdx.x; w < nl * 2 * nt; w += blockDim.x) {
+      int t = w % nt;
+      int lam = c_t[t] + c_u[t] + c_v[t];
+      double2 v = E[off + w];
+      float4 o;
+      df_split(ldexp(v.x, k * lam), o.x, o.y);
+      df_split(ldexp(v.y, k * lam), o.z, o.w);
+      Edf[off + w] = o;
+    }
+  }
+}
+
+// Double-float copy of the density (column-major, leading dimension ld).
+__global__ void k_dconv(const double2 *D, int ld, int n, float4 *Ddf) {
+  long long tot = (long long)n * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long r = i % n, c = i / n;
+    double2 v = D[r + (long long)ld * c];
+    float4 o;
+    df_split(v.x, o.x, o.y);
+    df_split(v.y, o.z, o.w);
+    Ddf[r + (long long)n * c] = o;
+  }
+}
+
+constexpr int CHDF = 6;  // left labels per first-contraction pass (df path)
+
+struct QArgsDF {
+  const Shell *sh;
+  const PairE *pe;
+  const float4 *E;
+  const float4 *D;  // n x n, leading dimension n
+  double *GD, *GX;
+  int ns, ldd, ldf, nskp, isym, racah1;
+};
+
+// complex double-float product accumulate: (acc) += u * v
+struct cdf { float rh, rl, ih, il; };
+
+__device__ inline void cdf_mac(cdf &acc, float4 u, float4 v) {
+  // re += u.re v.re - u.im v.im ; im += u.re v.im + u.im v.re
+  df_fma(u.x, u.y, v.x, v.y, acc.rh, acc.rl);
+  df_fma(-u.z, -u.w, v.z, v.w, acc.rh, acc.rl);
+  df_fma(u.x, u.y, v.z, v.w, acc.ih, acc.il);
+  df_fma(u.z, u.w, v.x, v.y, acc.ih, acc.il);
+}
+
+__global__ void __launch_bounds__(QTHREADS, 2)
+k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
+  extern __shared__ double smem[];
+  double *R = smem;                            // NTR (FP64)
+  float2 *Rf = (float2 *)(R + NTR);            // NTR (df)
+  double *R2 = (double *)Rf;                   // FP64 recursion buffer (aliases Rf)
+  double *F = R + 2 * NTR;                     // MAXLAM+2
+  float4 *EL = (float4 *)(F + MAXLAM + 2);     // CHDF*2*NTE
+  float4 *G = EL + CHDF * 2 * NTE;             // CHDF*2*NTE
+  double2 *Jl = (double2 *)(G + CHDF * 2 * NTE);  // MAXSP*MAXSP
+  double2 *Kl = Jl + MAXSP * MAXSP;
+  __shared__ double sgeo[8];
+  __shared__ int sk;
+
+  for (long long qi = blockIdx.x; qi < nq; qi += gridDim.x) {
+    int4 Q4 = quart[qi];
+    const Shell &A = q.sh[Q4.x], &B = q.sh[Q4.y], &C = q.sh[Q4.z], &Dd = q.sh[Q4.w];
+    int la = A.l, lb = B.l, lc = C.l, ld = Dd.l;
+    int degab = la + lb + 2 * t1, degcd = lc + ld + 2 * t2;
+    int lam = degab + degcd;
+    int nla = 2 * la + 1, nlb = 2 * lb + 1, nlc = 2 * lc + 1, nld = 2 * ld + 1;
+    int nlab = nla * nlb, nlcd = nlc * nld;
+    int nab = ntuv(degab), ncd = ntuv(degcd);
+    bool swp = contraction_cost(nlcd, ncd, nlab, nab) < contraction_cost(nlab, nab, nlcd, ncd);
+    int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
+    const PairE &pab_e = q.pe[Q4.x * q.ns + Q4.y], &pcd_e = q.pe[Q4.z * q.ns + Q4.w];
+    if (threadIdx.x == 0) {
+      double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
+      double Px = (A.alpha * A.x + B.alpha * B.x) / p;
+      double Py = (A.alpha * A.y + B.alpha * B.y) / p;
+      double Pz = (A.alpha * A.z + B.alpha * B.z) / p;
+      double Qx = (C.alpha * C.x + Dd.alpha * Dd.x) / qq;
+      double Qy = (C.alpha * C.y + Dd.alpha * Dd.y) / qq;
+      double Qz = (C.alpha * C.z + Dd.alpha * Dd.z) / qq;
+      double aph = p * qq / (p + qq);
+      double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
+      boys_ref(T, lam, F);
+      double sg = swp ? -1.0 : 1.0;
+      sgeo[0] = sg * (Px - Qx); sgeo[1] = sg * (Py - Qy); sgeo[2] = sg * (Pz - Qz);
+      sgeo[3] = -2.0 * aph;
+      sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
+      sk = half_floor_log2(2.0 * aph);
+    }
+    __syncthreads();
+    {
+      double X = sgeo[0], Y = sgeo[1], Z = sgeo[2], m2a = sgeo[3];
+      double *cur = R, *nxt = R2;
+      for (int n = lam; n >= 0; --n) {
+        int cnt = ntuv(lam - n);
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+          double val;
+          if (k == 0) {
+            double pw = 1.0;
+            for (int i = 0; i < n; ++i) pw *= m2a;
+            val = pw * F[n];
+          } else {
+            int t = c_t[k], u = c_u[k], v = c_v[k];
+            if (t > 0) {
+              val = X * cur[hidx(t - 1, u, v)];
+              if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
+            } else if (u > 0) {
+              val = Y * cur[hidx(t, u - 1, v)];
+              if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
+            } else {
+              val = Z * cur[hidx(t, u, v - 1)];
+              if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
+            }
+          }
+          nxt[k] = val;
+        }
+        __syncthreads();
+        double *tmp = cur; cur = nxt; nxt = tmp;
+      }
+      // scaled double-float copy of PRE*R (R2 and Rf alias: go through R)
+      double pre = sgeo[4];
+      int nt = ntuv(lam);
+      if (cur != R) {
+        for (int k = threadIdx.x; k < nt; k += blockDim.x) R[k] = cur[k];
+        __syncthreads();
+      }
+      int k = sk;
+      for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        int L = c_t[i] + c_u[i] + c_v[i];
+        float h, l;
+        df_split(ldexp(R[i] * pre, -k * L), h, l);
+        Rf[i] = make_float2(h, l);
+      }
+    }
+    for (int i = threadIdx.x; i < MAXSP * MAXSP; i += blockDim.x) {
+      Jl[i] = make_double2(0.0, 0.0);
+      Kl[i] = make_double2(0.0, 0.0);
+    }
+    const float4 *Eab = q.E + pab_e.off[t1];
+    const float4 *Ecd = q.E + pcd_e.off[t2];
+    const float4 *EGL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
+    int kL = swp ? pcd_e.kexp : pab_e.kexp, kR = swp ? pab_e.kexp : pcd_e.kexp;
+    int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
+    int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
+    int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;
+    int lq[4] = {la, lb, lc, ld};
+    int oab = t1 ? q.nskp : 0, ocd = t2 ? q.nskp : 0;
+    int kq0 = sk;
+    __syncthreads();
+    for (int c0 = 0; c0 < nlL; c0 += CHDF) {
+      int nch = min(CHDF, nlL - c0);
+      // stage the left E-coefficients rescaled to this quartet's exponent
+      for (int w = threadIdx.x; w < nch * 2 * nL; w += blockDim.x) {
+        int s = w % nL;
+        int L = c_t[s] + c_u[s] + c_v[s];
+        float4 v = EGL[(long long)c0 * 2 * nL + w];
+        float f = ldexpf(1.0f, (kq0 - kL) * L);
+        EL[w] = make_float4(v.x * f, v.y * f, v.z * f, v.w * f);
+      }
+      __syncthreads();
+      // first contraction G[lab][set][q] = Z(q) 2^((k-kR)lq) sum_s E_L R'[s+q]
+      for (int w = threadIdx.x; w < nch * 2 * nR; w += blockDim.x) {
+        int ls = w / nR, qq = w % nR;
+        const float4 *e = EL + ls * nL;
+        int tq = c_t[qq], uq = c_u[qq], vq = c_v[qq];
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+        for (int s = 0; s < nL; ++s) {
+          float2 rv = Rf[hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq)];
+          float4 ev = e[s];
+          df_fma(ev.x, ev.y, rv.x, rv.y, rh, rl);
+          df_fma(ev.z, ev.w, rv.x, rv.y, ih, il);
+        }
+        int lq_ = tq + uq + vq;
+        float f = ldexpf((lq_ & 1) ? -1.0f : 1.0f, (kq0 - kR) * lq_);
+        G[ls * NTE + qq] = make_float4(rh * f, rl * f, ih * f, il * f);
+      }
+      __syncthreads();
+      for (int w = threadIdx.x; w < nch * nlR; w += blockDim.x) {
+        int lab = w / nlR, lr = w % nlR;
+        int labL = c0 + lab;
+        int l1 = labL / nl2L, l2 = labL % nl2L, r1 = lr / nl2R, r2 = lr % nl2R;
+        int ia = swp ? r1 : l1, ib = swp ? r2 : l2, ic = swp ? l1 : r1, id = swp ? l2 : r2;
+        int kq[4], mq[4], mm[4];
+        label_of(la, ia, kq[0], mm[0]);
+        label_of(lb, ib, kq[1], mm[1]);
+        label_of(lc, ic, kq[2], mm[2]);
+        label_of(ld, id, kq[3], mm[3]);
+        for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
+        if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
+        double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
+        double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
+        double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
+        const float4 *g11 = G + (lab * 2 + 0) * NTE, *g21 = G + (lab * 2 + 1) * NTE;
+        const float4 *e11 = ER + ((long long)lr * 2 + 0) * nR;
+        const float4 *e21 = ER + ((long long)lr * 2 + 1) * nR;
+        // partial products a=re*re, b=im*im, c=re*im, d=im*re of the four
+        // (E_R set) x (G set) pairs, double-float
+        float acc[16][2];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) { acc[i][0] = 0.f; acc[i][1] = 0.f; }
+        for (int k = 0; k < nR; ++k) {
+          float4 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
+#define P4(o, UU, XX)                                     \
+  df_fma(UU.x, UU.y, XX.x, XX.y, acc[o][0], acc[o][1]);     \
+  df_fma(UU.z, UU.w, XX.z, XX.w, acc[o + 1][0], acc[o + 1][1]); \
+  df_fma(UU.x, UU.y, XX.z, XX.w, acc[o + 2][0], acc[o + 2][1]); \
+  df_fma(UU.z, UU.w, XX.x, XX.y, acc[o + 3][0], acc[o + 3][1]);
+          P4(0, u1, x1) P4(4, u2, x1) P4(8, u1, x2) P4(12, u2, x2)
+#undef P4
+        }
+        // s = u*x = (a-b, c+d) ; sc = u*conj(x) = (a+b, d-c)
+        float4 sv[8];
+        for (int pp = 0; pp < 4; ++pp) {
+          float *a = acc[4 * pp], *b = acc[4 * pp + 1], *c = acc[4 * pp + 2], *d = acc[4 * pp + 3];
+          float4 t, tc;
+          df_add(a[0], a[1], -b[0], -b[1], t.x, t.y);
+          df_add(c[0], c[1], d[0], d[1], t.z, t.w);
+          df_add(a[0], a[1], b[0], b[1], tc.x, tc.y);
+          df_add(d[0], d[1], -c[0], -c[1], tc.z, tc.w);
+          sv[2 * pp] = t;
+          sv[2 * pp + 1] = tc;
+        }
+        // 16 m-sign combinations; phases +-1 through the sign
+        float sl_ = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
+        float4 r[16];
+        auto cj = [](float4 v, float f) { return make_float4(f * v.x, f * v.y, -f * v.z, -f * v.w); };
+        auto sc = [](float4 v, float f) { return make_float4(f * v.x, f * v.y, f * v.z, f * v.w); };
+        r[0] = sv[0];
+        r[12] = sc(sv[1], sl_);
+        r[15] = cj(r[0], slr);
+        r[3] = cj(r[12], slr);
+        r[2] = sv[2];
+        r[14] = sc(sv[3], sl_);
+        r[13] = cj(r[2], -slr);
+        r[1] = cj(r[14], -slr);
+        r[8] = sv[4];
+        r[4] = sc(sv[5], -sl_);
+        r[7] = cj(r[8], -slr);
+        r[11] = cj(r[4], -slr);
+        r[10] = sv[6];
+        r[6] = sc(sv[7], -sl_);
+        r[5] = cj(r[10], slr);
+        r[9] = cj(r[6], slr);
+#define RV(sa, sb, sc_, sd) (swp ? r[8 * (sc_) + 4 * (sd) + 2 * (sa) + (sb)] \
+                                 : r[8 * (sa) + 4 * (sb) + 2 * (sc_) + (sd)])
+        int fb[2] = {B.fock[ib][0] + oab, B.fock[ib][1] + oab};
+        int fc[2] = {C.fock[ic][0] + ocd, C.fock[ic][1] + ocd};
+        int fd[2] = {Dd.fock[id][0] + ocd, Dd.fock[id][1] + ocd};
+        const size_t ld = (size_t)q.ldd;
+        if (q.isym == 0) {
+          for (int sa = 0; sa < 2; ++sa)
+            for (int sb = 0; sb < 2; ++sb) {
+              cdf j = {0.f, 0.f, 0.f, 0.f};
+              for (int sc2 = 0; sc2 < 2; ++sc2)
+                for (int sd = 0; sd < 2; ++sd)
+                  cdf_mac(j, RV(sa, sb, sc2, sd), q.D[fc[sc2] + ld * fd[sd]]);
+              satomic(&Jl[(ia * 2 + sa) * MAXSP + ib * 2 + sb],
+                      make_double2(df_val(j.rh, j.rl), df_val(j.ih, j.il)));
+            }
+          for (int sa = 0; sa < 2; ++sa)
+            for (int sd = 0; sd < 2; ++sd) {
+              cdf kk = {0.f, 0.f, 0.f, 0.f};
+              for (int sb = 0; sb < 2; ++sb)
+                for (int sc2 = 0; sc2 < 2; ++sc2)
+                  cdf_mac(kk, RV(sa, sb, sc2, sd), q.D[fc[sc2] + ld * fb[sb]]);
+              satomic(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd],
+                      make_double2(df_val(kk.rh, kk.rl), df_val(kk.ih, kk.il)));
+            }
+        } else {
+          for (int s2 = 0; s2 < 2; ++s2) {
+            float jh = 0.f, jl = 0.f, kh = 0.f, kl2 = 0.f;
+            for (int t = 0; t < 2; ++t) {
+              float4 vj = RV(s2, s2, t, t), dj = q.D[fc[t] + ld * fd[t]];
+              float4 vk = RV(s2, t, t, s2), dk = q.D[fc[t] + ld * fb[t]];
+              df_fma(vj.x, vj.y, dj.x, dj.y, jh, jl);
+              df_fma(vk.x, vk.y, dk.x, dk.y, kh, kl2);
+            }
+            atomicAdd(&Jl[(ia * 2 + s2) * MAXSP + ib * 2 + s2].x, df_val(jh, jl));
+            atomicAdd(&Kl[(ia * 2 + s2) * MAXSP + id * 2 + s2].x, df_val(kh, kl2));
+          }
+        }
+#undef RV
+      }
+      __syncthreads();
+    }
+    // flush shared accumulators (FP64)
+    {
+      int nsa = 2 * nla;
+      for (int w = threadIdx.x; w < nsa * 2 * nlb; w += blockDim.x) {
+        int a = w / (2 * nlb), b = w % (2 * nlb);
+        double2 v = Jl[a * MAXSP + b];
+        if (v.x == 0.0 && v.y == 0.0) continue;
+        int fa = A.fock[a >> 1][a & 1] + oab, fbb = B.fock[b >> 1][b & 1] + oab;
+        double *dst = q.GD + 2 * ((size_t)fa + (size_t)q.ldf * fbb);
+        atomicAdd(dst, v.x);
+        atomicAdd(dst + 1, v.y);
+      }
+      for (int w = threadIdx.x; w < nsa * 2 * nld; w += blockDim.x) {
+        int a = w / (2 * nld), d = w % (2 * nld);
+        double2 v = Kl[a * MAXSP + d];
+        if (v.x == 0.0 && v.y == 0.0) continue;
+        int fa = A.fock[a >> 1][a & 1] + oab, fdd = Dd.fock[d >> 1][d & 1] + ocd;
+        double *dst = q.GX + 2 * ((size_t)fa + (size_t)q.ldf * fdd);
+        atomicAdd(dst, v.x);
+        atomicAdd(dst + 1, v.y);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_zero2d(double *a, int n, int ld) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   long long tot = (long long)n * n;
@@ -700,6 +1078,11 @@ __global__ void k_zero2d(double *a, int n, int ld) {
     a[2 * (r + (long long)ld * c)] = 0.0;
     a[2 * (r + (long long)ld * c) + 1] = 0.0;
   }
+}
+
+size_t quartet_smem_df() {
+  return sizeof(double) * (2 * NTR + MAXLAM + 2) + sizeof(float4) * (2 * CHDF * 2 * NTE) +
+         sizeof(double2) * (2 * MAXSP * MAXSP);
 }
 
 size_t quartet_smem() {
@@ -726,6 +1109,9 @@ struct bg_ctx {
   long long nquart[4] = {0, 0, 0, 0};
   int quart_ilev = -1;
   double2 *d_D = nullptr, *d_GD = nullptr, *d_GX = nullptr;
+  // split-precision copies
+  float4 *d_Edf = nullptr, *d_Ddf = nullptr;
+  int prec = BG_PREC_FP64;
   long long launches = 0;
   std::string err;
   bool bad = false;
@@ -818,6 +1204,26 @@ int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                     const double2 *d_D, int ldd, double *d_GD, double *d_GX,
                     int ldf, cudaStream_t st) {
   if (nq <= 0) return 0;
+  if (c->prec == BG_PREC_DF32) {
+    static bool attr_df = false;
+    size_t smem = quartet_smem_df();
+    if (!attr_df) {
+      CK(c, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr_df = true;
+    }
+    int n = c->ndim;
+    if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
+    k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, c->d_Ddf);
+    QArgsDF a;
+    a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = c->d_Ddf;
+    a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = n; a.ldf = ldf;
+    a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1;
+    long long grid = std::min<long long>(nq, 152LL * 64);
+    k_quartet_df<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+    CK(c, cudaGetLastError());
+    c->launches += 2;
+    return 0;
+  }
   static bool attr = false;
   size_t smem = quartet_smem();
   if (!attr) {
@@ -922,6 +1328,8 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
     for (int b = 0; b < ns; ++b) {
       PairE &p = pe[(size_t)a * ns + b];
       p.off[0] = p.off[1] = -1;
+      p.kexp = half_floor_log2(2.0 * (c->shells[a].alpha + c->shells[b].alpha));
+      p.pad = 0;
       int la = c->shells[a].l, lb = c->shells[b].l;
       int nl = (2 * la + 1) * (2 * lb + 1);
       for (int comp = 0; comp < ncomp; ++comp) {
@@ -962,7 +1370,28 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
     bertha_gpu_free(c);
     return BG_ERR_CUDA;
   }
+  // double-float copy for the split-precision path
+  if ((e = cudaMalloc(&c->d_Edf, sizeof(float4) * std::max<long long>(off, 1))) != cudaSuccess) {
+    cuda_fail(nullptr, e, "cudaMalloc");
+    bertha_gpu_free(c);
+    return BG_ERR_CUDA;
+  }
+  k_econv<<<(unsigned)((long long)ns * ns), 128>>>(c->d_E, c->d_Edf, c->d_pe, c->d_sh, ns, ncomp);
+  e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    cuda_fail(nullptr, e, "k_econv");
+    bertha_gpu_free(c);
+    return BG_ERR_CUDA;
+  }
   *out = c;
+  return BG_OK;
+}
+
+int bertha_gpu_set_precision(bg_ctx *c, int prec) {
+  if (!c) return BG_ERR_ARG;
+  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32) return BG_ERR_ARG;
+  c->prec = prec;
   return BG_OK;
 }
 
@@ -1078,6 +1507,8 @@ void bertha_gpu_free(bg_ctx *c) {
   cudaFree(c->d_pe);
   cudaFree(c->d_E);
   for (int k = 0; k < 4; ++k) cudaFree(c->d_quart[k]);
+  cudaFree(c->d_Edf);
+  cudaFree(c->d_Ddf);
   cudaFree(c->d_D);
   cudaFree(c->d_GD);
   cudaFree(c->d_GX);

@@ -44,6 +44,11 @@ extern "C" {
 /* init flags */
 #define BG_FLAG_NO_RACAH1 1 /* include one-centre quartets (RACAH1=.FALSE.) */
 
+/* precision of the two-electron contraction */
+#define BG_PREC_FP64 0 /* all FP64: the drop-in path */
+#define BG_PREC_DF32 1 /* split precision: FP32 double-float contractions and
+                          digestion products, FP64 Boys/R and J/K sums */
+
 /* compiled limits */
 #define BG_MAX_L 3 /* highest orbital angular momentum of a basis shell */
 
@@ -62,6 +67,12 @@ int bertha_gpu_init(bg_ctx **ctx, int ncnt, const double *bxyz,
                     const int *nkap, const int *nfnc, int mel,
                     const double *bexl, int mbs, int hmlt, int shape,
                     int flags);
+
+/* Select the contraction precision of later build calls (default FP64).
+ * BG_PREC_DF32 carries every contraction operand as a pair of FP32 words
+ * (about 48 significant bits) on the FP32 pipes.  No counterpart in the
+ * reference, which is FP64 throughout. */
+int bertha_gpu_set_precision(bg_ctx *ctx, int prec);
 
 /* Fock dimension NDIM and small-component offset NSKP (CARDIN :423-430). */
 int bertha_gpu_dims(const bg_ctx *ctx, int *ndim, int *nskp);

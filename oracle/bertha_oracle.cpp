@@ -383,9 +383,9 @@ HVec eq_pair(int ka, int mqa, double ea, const double *A, int kb, int mqb,
   }
   double nrm = rnorm(ea, la, small) * rnorm(eb, lb, small);
   int deg = small ? la + lb + 2 : la + lb;
-  for (int k = 0; k < ntuv(deg); ++k) E[k] *= nrm;
-  E.resize(ntuv(deg));
-  return E;
+  HVec out(E.begin(), E.begin() + ntuv(deg));  // exact size, no scratch capacity
+  for (cplx &v : out) v *= nrm;
+  return out;
 }
 
 // ---------------------------------------------------------------------------

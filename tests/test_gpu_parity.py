@@ -83,5 +83,56 @@ def test_bad_arguments():
     with pytest.raises(berthagpu.BerthaGPUError):
         fb.clmfast(deck.density(b), 7)
     fb.close()
-    big = deck.make_basis([((0, 0, 0), {0: [1.0], 4: [1.0]})]) if False else None
-    assert big is None
+
+
+def test_capacity_error():
+    """An l=4 shell is beyond the compiled limit: BG_ERR_CAPACITY, not a crash."""
+    b = _small()
+    lmax = b.lmax.copy()
+    lmax[0] = 4
+    nfn = np.zeros((b.ncnt, 5), np.int32)
+    nfn[:, :4] = b.nfn
+    nfn[0, 4] = 1
+    ex = np.zeros((b.ncnt, 5, b.ex.shape[2]))
+    ex[:, :4] = b.ex
+    ex[0, 4, 0] = 1.0
+    bad = deck.Basis(xyz=b.xyz, lmax=lmax, nfn=nfn, ex=ex, hmlt=b.hmlt, isym=b.isym)
+    with pytest.raises(berthagpu.BerthaGPUError) as ei:
+        berthagpu.FockBuilder(bad)
+    assert ei.value.code == 2
+
+
+# Split precision: FP32 double-float contractions.  Tolerance 1e-10 of the
+# largest element (about 2^-44 per operation, with cancellation headroom).
+DF_TOL = 1e-10
+
+
+def _cmp_df(b, dent, ilev):
+    fb = berthagpu.FockBuilder(b)
+    fb.set_precision("df32")
+    gd, gx = fb.clmfast(dent, ilev)
+    fb.close()
+    rd, rx = orc.clmfast(b, dent, ilev)
+    scale = max(np.abs(rd).max(), np.abs(rx).max(), 1e-300)
+    assert np.abs(gd - rd).max() <= DF_TOL * scale
+    assert np.abs(gx - rx).max() <= DF_TOL * scale
+
+
+@pytest.mark.parametrize("lmax", [1, 3])
+def test_df32_general(lmax):
+    b = _small(lmax=lmax)
+    _cmp_df(b, deck.density(b, seed=21), 3)
+
+
+def test_df32_linear():
+    b = deck.make_basis([((0, 0, 0), {0: [0.4, 1.9], 1: [0.8], 2: [1.2]}),
+                         ((0, 0, 2.1), {0: [0.6], 1: [0.5]})], hmlt="DHFR")
+    _cmp_df(b, deck.density(b, seed=5, real=True), 3)
+
+
+def test_df32_extreme_exponents():
+    """Exponent ratios up to 1e7 exercise the power-of-two scaling."""
+    b = deck.make_basis([((0, 0, 0), {0: [0.05, 2.0e5], 1: [3.0e4], 2: [0.3]}),
+                         ((0.4, 1.1, -0.7), {0: [1.0e6, 0.08], 1: [0.1]}),
+                         ((1.5, -0.3, 0.9), {0: [0.5], 3: [40.0]})], hmlt="DHFR")
+    _cmp_df(b, deck.density(b, seed=8), 3)
