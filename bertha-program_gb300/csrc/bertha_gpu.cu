@@ -746,6 +746,24 @@ __device__ inline void df_split(double v, float &h, float &l) {
 
 __device__ inline double df_val(float h, float l) { return (double)h + (double)l; }
 
+// Exact float -> double on the integer pipe (the FP64 pipe is the scarce
+// resource).  FP32 zero and subnormals (|f| < 1.2e-38) map to 0.
+__device__ inline double f2d_int(float f) {
+  unsigned int u = __float_as_uint(f);
+  unsigned int e = (u >> 23) & 0xffu;
+  if (e == 0u) return 0.0;
+  unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
+                            ((unsigned long long)(e + 896u) << 52) |
+                            ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// shared-memory accumulate of a double-float value as its two exact parts
+__device__ inline void satomic_df(double *p, float h, float l) {
+  atomicAdd(p, f2d_int(h));
+  atomicAdd(p, f2d_int(l));
+}
+
 // Double-float copy of the E-coefficients, scaled per pair.
 __global__ void k_econv(const double2 *E, float4 *Edf, const PairE *pe, const Shell *sh,
                         int ns, int ncomp) {
@@ -783,7 +801,8 @@ __global__ void k_dconv(const double2 *D, int ld, int n, float4 *Ddf) {
   }
 }
 
-constexpr int CHDF = 6;  // left labels per first-contraction pass (df path)
+constexpr int CHDF = 4;  // left labels per first-contraction pass (df path)
+constexpr int NCB = CHDF * MAXLAB * MAXLAB * 8;  // contribution buffer (float4)
 
 struct QArgsDF {
   const Shell *sh;
@@ -814,7 +833,8 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
   double *F = R + 2 * NTR;                     // MAXLAM+2
   float4 *EL = (float4 *)(F + MAXLAM + 2);     // CHDF*2*NTE
   float4 *G = EL + CHDF * 2 * NTE;             // CHDF*2*NTE
-  double2 *Jl = (double2 *)(G + CHDF * 2 * NTE);  // MAXSP*MAXSP
+  float4 *Cb = G + CHDF * 2 * NTE;             // NCB: J (4) and K (4) per label quartet
+  double2 *Jl = (double2 *)(Cb + NCB);         // MAXSP*MAXSP
   double2 *Kl = Jl + MAXSP * MAXSP;
   __shared__ double sgeo[8];
   __shared__ int sk;
@@ -947,7 +967,11 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
         label_of(lc, ic, kq[2], mm[2]);
         label_of(ld, id, kq[3], mm[3]);
         for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
-        if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
+        float4 *cb = Cb + (size_t)(lab * nlR + lr) * 8;
+        if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) {
+          for (int i = 0; i < 8; ++i) cb[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+          continue;
+        }
         double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
         double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
         double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
@@ -1008,6 +1032,8 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
         int fc[2] = {C.fock[ic][0] + ocd, C.fock[ic][1] + ocd};
         int fd[2] = {Dd.fock[id][0] + ocd, Dd.fock[id][1] + ocd};
         const size_t ld = (size_t)q.ldd;
+        // phase A: this label quartet's J contributions (sa,sb) and K
+        // contributions (sa,sd) into the chunk buffer
         if (q.isym == 0) {
           for (int sa = 0; sa < 2; ++sa)
             for (int sb = 0; sb < 2; ++sb) {
@@ -1015,8 +1041,7 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
               for (int sc2 = 0; sc2 < 2; ++sc2)
                 for (int sd = 0; sd < 2; ++sd)
                   cdf_mac(j, RV(sa, sb, sc2, sd), q.D[fc[sc2] + ld * fd[sd]]);
-              satomic(&Jl[(ia * 2 + sa) * MAXSP + ib * 2 + sb],
-                      make_double2(df_val(j.rh, j.rl), df_val(j.ih, j.il)));
+              cb[2 * sa + sb] = make_float4(j.rh, j.rl, j.ih, j.il);
             }
           for (int sa = 0; sa < 2; ++sa)
             for (int sd = 0; sd < 2; ++sd) {
@@ -1024,10 +1049,11 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
               for (int sb = 0; sb < 2; ++sb)
                 for (int sc2 = 0; sc2 < 2; ++sc2)
                   cdf_mac(kk, RV(sa, sb, sc2, sd), q.D[fc[sc2] + ld * fb[sb]]);
-              satomic(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd],
-                      make_double2(df_val(kk.rh, kk.rl), df_val(kk.ih, kk.il)));
+              cb[4 + 2 * sa + sd] = make_float4(kk.rh, kk.rl, kk.ih, kk.il);
             }
         } else {
+          // CLMMTZ: real parts, equal-sign direct blocks, crossed exchange
+          cb[1] = cb[2] = cb[5] = cb[6] = make_float4(0.f, 0.f, 0.f, 0.f);
           for (int s2 = 0; s2 < 2; ++s2) {
             float jh = 0.f, jl = 0.f, kh = 0.f, kl2 = 0.f;
             for (int t = 0; t < 2; ++t) {
@@ -1036,11 +1062,75 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
               df_fma(vj.x, vj.y, dj.x, dj.y, jh, jl);
               df_fma(vk.x, vk.y, dk.x, dk.y, kh, kl2);
             }
-            atomicAdd(&Jl[(ia * 2 + s2) * MAXSP + ib * 2 + s2].x, df_val(jh, jl));
-            atomicAdd(&Kl[(ia * 2 + s2) * MAXSP + id * 2 + s2].x, df_val(kh, kl2));
+            cb[3 * s2] = make_float4(jh, jl, 0.f, 0.f);
+            cb[4 + 3 * s2] = make_float4(kh, kl2, 0.f, 0.f);
           }
         }
 #undef RV
+      }
+      __syncthreads();
+      // phase B: one thread per J or K target sums the chunk's contributions
+      // in double-float and adds the FP64 value to the shared accumulator
+      {
+        int tj = (swp ? nlR : nch) * 4;
+        int tk = nla * nld * 4;
+        for (int w = threadIdx.x; w < tj + tk; w += blockDim.x) {
+          float sh_r = 0.f, sl_r = 0.f, sh_i = 0.f, sl_i = 0.f;
+          int cnt = 0;
+          double2 *dst;
+          if (w < tj) {
+            int tgt = w >> 2, sig = w & 3;
+            int ia, ib;
+            if (!swp) {
+              int labL = c0 + tgt;
+              ia = labL / nlb; ib = labL % nlb;
+              for (int lr = 0; lr < nlR; ++lr) {
+                float4 v = Cb[(size_t)(tgt * nlR + lr) * 8 + sig];
+                df_add(sh_r, sl_r, v.x, v.y, sh_r, sl_r);
+                df_add(sh_i, sl_i, v.z, v.w, sh_i, sl_i);
+              }
+            } else {
+              ia = tgt / nlb; ib = tgt % nlb;
+              for (int lab = 0; lab < nch; ++lab) {
+                float4 v = Cb[(size_t)(lab * nlR + tgt) * 8 + sig];
+                df_add(sh_r, sl_r, v.x, v.y, sh_r, sl_r);
+                df_add(sh_i, sl_i, v.z, v.w, sh_i, sl_i);
+              }
+            }
+            cnt = 1;
+            dst = &Jl[(ia * 2 + (sig >> 1)) * MAXSP + ib * 2 + (sig & 1)];
+          } else {
+            int u = w - tj, sig = u & 3, tgt = u >> 2;
+            int ia = tgt / nld, id = tgt % nld;
+            if (!swp) {
+              // left labels (ia, ib) in this chunk, right labels (ic, id)
+              int lo = max(c0, ia * nlb), hi = min(c0 + nch, (ia + 1) * nlb);
+              for (int labL = lo; labL < hi; ++labL)
+                for (int ic = 0; ic < nlc; ++ic) {
+                  float4 v = Cb[(size_t)((labL - c0) * nlR + ic * nld + id) * 8 + 4 + sig];
+                  df_add(sh_r, sl_r, v.x, v.y, sh_r, sl_r);
+                  df_add(sh_i, sl_i, v.z, v.w, sh_i, sl_i);
+                  ++cnt;
+                }
+            } else {
+              // left labels (ic, id) in this chunk, right labels (ia, ib)
+              for (int lab = 0; lab < nch; ++lab) {
+                if ((c0 + lab) % nld != id) continue;
+                for (int ib = 0; ib < nlb; ++ib) {
+                  float4 v = Cb[(size_t)(lab * nlR + ia * nlb + ib) * 8 + 4 + sig];
+                  df_add(sh_r, sl_r, v.x, v.y, sh_r, sl_r);
+                  df_add(sh_i, sl_i, v.z, v.w, sh_i, sl_i);
+                  ++cnt;
+                }
+              }
+            }
+            dst = &Kl[(ia * 2 + (sig >> 1)) * MAXSP + id * 2 + (sig & 1)];
+          }
+          if (cnt) {
+            dst->x += df_val(sh_r, sl_r);
+            dst->y += df_val(sh_i, sl_i);
+          }
+        }
       }
       __syncthreads();
     }
@@ -1081,7 +1171,7 @@ __global__ void k_zero2d(double *a, int n, int ld) {
 }
 
 size_t quartet_smem_df() {
-  return sizeof(double) * (2 * NTR + MAXLAM + 2) + sizeof(float4) * (2 * CHDF * 2 * NTE) +
+  return sizeof(double) * (2 * NTR + MAXLAM + 2) + sizeof(float4) * (2 * CHDF * 2 * NTE + NCB) +
          sizeof(double2) * (2 * MAXSP * MAXSP);
 }
 
