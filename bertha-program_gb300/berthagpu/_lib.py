@@ -40,6 +40,7 @@ def lib():
         L.bertha_gpu_clmfast.argtypes = [P, P, i, i, P, P, i]
         L.bertha_gpu_clmfast_device.argtypes = [P, P, i, i, P, P, i, P]
         L.bertha_gpu_quartets.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
+        L.bertha_gpu_quartets_noalloc.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
         L.bertha_gpu_shells.argtypes = [P, P, P, P, P]
         L.bertha_gpu_layout.argtypes = [P, P]
         L.bertha_gpu_launches.argtypes = [P]
@@ -54,7 +55,8 @@ def lib():
 
 EXPORTED = [
     "bertha_gpu_init", "bertha_gpu_set_precision", "bertha_gpu_dims", "bertha_gpu_clmfast",
-    "bertha_gpu_clmfast_device", "bertha_gpu_quartets", "bertha_gpu_shells",
+    "bertha_gpu_clmfast_device", "bertha_gpu_quartets", "bertha_gpu_quartets_noalloc",
+    "bertha_gpu_shells",
     "bertha_gpu_layout", "bertha_gpu_launches", "bertha_gpu_last_error",
     "bertha_gpu_free",
 ]

@@ -39,11 +39,13 @@ def microbench_quartets(basis, nquart, seed=2024, overlap=0.2):
     rng = np.random.default_rng(seed + 1)
     idx = shell_index(basis)
     nc = basis.ncnt
+    lmax = int(basis.lmax.min())
+    nexp = int(basis.nfn[:, : lmax + 1].min())
     out = {}
     per = nquart // len(CLASSES)
     for k, cls in enumerate(CLASSES):
         n = per if k < len(CLASSES) - 1 else nquart - per * (len(CLASSES) - 1)
-        ls = rng.integers(0, 4, size=(n, 4))
+        ls = rng.integers(0, lmax + 1, size=(n, 4))
         ca = rng.integers(0, nc, size=n)
         cc = rng.integers(0, nc, size=n)
         cb = np.where(rng.random(n) < overlap, ca, (ca + rng.integers(1, nc, size=n)) % nc)
@@ -51,7 +53,7 @@ def microbench_quartets(basis, nquart, seed=2024, overlap=0.2):
         cen = np.stack([ca, cb, cc, cd], 1)
         q = np.empty((n, 4), np.int32)
         for j in range(4):
-            ii = rng.integers(0, basis.nfn[0, 0], size=n)
+            ii = rng.integers(0, nexp, size=n)
             q[:, j] = [idx[(int(c), int(l), int(i))] for c, l, i in zip(cen[:, j], ls[:, j], ii)]
         out[cls] = q
     return out

@@ -24,6 +24,14 @@
 
 #include "bertha_gpu.h"
 
+// Scratch of bertha_gpu_quartets_noalloc: the double-float copy of the
+// density, BG_NOALLOC_MAX_NDIM^2 float4 (16 MiB), resident on every GPU that
+// loads the library until the process exits.  Host code must not pass this
+// name to a kernel: it only names a host-side stand-in; the device address
+// comes from cudaGetSymbolAddress (noalloc_scratch below).
+static __device__ __align__(256) float4
+    g_noalloc_density[(size_t)BG_NOALLOC_MAX_NDIM * BG_NOALLOC_MAX_NDIM];
+
 namespace {
 
 __host__ __device__ constexpr int ntuv(int L) { return L < 0 ? 0 : (L + 1) * (L + 2) * (L + 3) / 6; }
@@ -1290,32 +1298,66 @@ std::vector<int> build_quartets(const bg_ctx *c, int t1, int t2, int ilev) {
   return sorted;
 }
 
+// Split-precision launch: density converted into `ddf` (n x n float4), then
+// the quartet kernel.  Allocates nothing.
+int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
+                       const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
+                       cudaStream_t st, float4 *ddf) {
+  if (nq <= 0) return 0;
+  static bool attr_df = false;
+  size_t smem = quartet_smem_df();
+  if (!attr_df) {
+    CK(c, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_df = true;
+  }
+  int n = c->ndim;
+  k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, ddf);
+  QArgsDF a;
+  a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = ddf;
+  a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = n; a.ldf = ldf;
+  a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1;
+  long long grid = std::min<long long>(nq, 152LL * 64);
+  k_quartet_df<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  CK(c, cudaGetLastError());
+  c->launches += 2;
+  return 0;
+}
+
+// Device address of g_noalloc_density for the current device, looked up
+// once per device with that device current (cudaGetSymbolAddress).
+float4 *noalloc_scratch(bg_ctx *c, int *rc) {
+  static float4 *addr[64] = {nullptr};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) {
+    *rc = cuda_fail(c, e == cudaSuccess ? cudaErrorInvalidDevice : e, "cudaGetDevice");
+    return nullptr;
+  }
+  if (!addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_density);
+    if (e != cudaSuccess) {
+      *rc = cuda_fail(c, e, "cudaGetSymbolAddress");
+      return nullptr;
+    }
+    addr[dev] = (float4 *)p;
+  }
+  *rc = 0;
+  return addr[dev];
+}
+
 int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                     const double2 *d_D, int ldd, double *d_GD, double *d_GX,
                     int ldf, cudaStream_t st) {
   if (nq <= 0) return 0;
   if (c->prec == BG_PREC_DF32) {
-    static bool attr_df = false;
-    size_t smem = quartet_smem_df();
-    if (!attr_df) {
-      CK(c, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      attr_df = true;
-    }
     int n = c->ndim;
     if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
-    k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, c->d_Ddf);
-    QArgsDF a;
-    a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = c->d_Ddf;
-    a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = n; a.ldf = ldf;
-    a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1;
-    long long grid = std::min<long long>(nq, 152LL * 64);
-    k_quartet_df<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
-    CK(c, cudaGetLastError());
-    c->launches += 2;
-    return 0;
+    return launch_quartets_df(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, c->d_Ddf);
   }
   static bool attr = false;
   size_t smem = quartet_smem();
+
   if (!attr) {
     CK(c, cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
@@ -1524,6 +1566,26 @@ int bertha_gpu_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   c->launches = 0;
   return launch_quartets(c, d_q, nq, t1, t2, (const double2 *)d_dent, ldd, d_gdir, d_gxch,
                          ldf, (cudaStream_t)stream);
+}
+
+int bertha_gpu_quartets_noalloc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
+                                const double *d_dent, int ldd, double *d_gdir,
+                                double *d_gxch, int ldf, void *stream) {
+  if (!c) return BG_ERR_ARG;
+  if (c->bad) return BG_ERR_STATE;
+  if (t1 < 0 || t1 >= c->ncomp || t2 < 0 || t2 >= c->ncomp || nq < 0 || ldd < c->ndim)
+    return BG_ERR_ARG;
+  if (c->ndim > BG_NOALLOC_MAX_NDIM) {
+    c->err = "bertha_gpu_quartets_noalloc: NDIM " + std::to_string(c->ndim) +
+             " exceeds BG_NOALLOC_MAX_NDIM " + std::to_string(BG_NOALLOC_MAX_NDIM);
+    return BG_ERR_CAPACITY;
+  }
+  int rc = 0;
+  float4 *scratch = noalloc_scratch(c, &rc);
+  if (!scratch) return rc;
+  c->launches = 0;
+  return launch_quartets_df(c, d_q, nq, t1, t2, (const double2 *)d_dent, ldd, d_gdir, d_gxch,
+                            ldf, (cudaStream_t)stream, scratch);
 }
 
 int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev,

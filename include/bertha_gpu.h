@@ -104,6 +104,26 @@ int bertha_gpu_quartets(bg_ctx *ctx, const int *d_quartets, long long nq,
                         int t1, int t2, const double *d_dent, int ldd,
                         double *d_gdir, double *d_gxch, int ldf, void *stream);
 
+/* Largest NDIM bertha_gpu_quartets_noalloc accepts. */
+#define BG_NOALLOC_MAX_NDIM 1024
+
+/* Same digestion as bertha_gpu_quartets in split precision (BG_PREC_DF32),
+ * for callers that cannot allocate device memory: code running inside an
+ * application whose memory pool already owns the GPU's memory, or issuing
+ * work where a cudaMalloc would synchronise the device.  It allocates
+ * nothing: its only scratch, the double-float copy of the density, is a
+ * static device array of BG_NOALLOC_MAX_NDIM^2 x 16 bytes (16 MiB) that every
+ * GPU loading the library holds until exit.  Contexts with NDIM above
+ * BG_NOALLOC_MAX_NDIM get BG_ERR_CAPACITY.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race on it.  The context itself comes from
+ * bertha_gpu_init as usual.  No counterpart in the reference. */
+int bertha_gpu_quartets_noalloc(bg_ctx *ctx, const int *d_quartets,
+                                long long nq, int t1, int t2,
+                                const double *d_dent, int ldd, double *d_gdir,
+                                double *d_gxch, int ldf, void *stream);
+
 /* Number of primitive shells and, per shell (centre, l, index in the
  * exponent list), in the order centre, l, exponent. */
 int bertha_gpu_shells(const bg_ctx *ctx, int *nshell, int *cnt, int *l,
