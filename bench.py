@@ -201,7 +201,7 @@ def run_gpu(args):
     import torch.distributed as dist
 
     import berthagpu
-    from berthagpu import deck, workloads
+    from berthagpu import deck, replicas, workloads
     from berthagpu.build import build as build_lib
 
     rank = int(os.environ.get("RANK", 0))
@@ -304,11 +304,8 @@ def run_gpu(args):
                 "energy_j_eh": float(ej64), "energy_k_eh": float(ek64)}
     step_ms = float(kern_ms.sum(1).max() if args.steps else 0.0)
     step_ms_mean = float(kern_ms.sum(1).mean())
-    ms = torch.tensor([step_ms_mean], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(ms, op=dist.ReduceOp.MAX)
-    ms_per_step = float(ms.item())
-    value = args.quartets * world / (ms_per_step * 1e-3)
+    ms_per_step = replicas.job_step_ms(step_ms_mean, dist if world > 1 else None, dev)
+    value = replicas.job_throughput(args.quartets, world, ms_per_step)
     other_value = args.quartets * world / (float(kern_other.sum(1).mean()) * 1e-3)
 
     # end to end through the C ABI: host density and quartet lists in pinned
