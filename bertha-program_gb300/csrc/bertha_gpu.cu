@@ -809,7 +809,67 @@ __global__ void k_dconv(const double2 *D, int ld, int n, float4 *Ddf) {
   }
 }
 
-constexpr int CHDF = 4;  // left labels per first-contraction pass (df path)
+// Boys table for the split path: F_m(T_i) on T_i = i/32, 0 <= T_i <= 17,
+// m < NBORD; F_m(T) from a 7-term Taylor expansion about the nearest point
+// (|T-T_i| <= 1/64, truncation below 1e-16).  The FP64 path keeps the
+// reference's 60-term series.
+constexpr int NBGRID = 17 * 32 + 1;
+constexpr int NBORD = MAXLAM + 7;
+__device__ double g_boys_tab[NBGRID * NBORD];
+
+__global__ void k_boys_table() {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NBGRID) return;
+  double T = i / 32.0, F[NBORD];
+  int top = NBORD - 1;
+  double txp = exp(-T), tt2 = 2.0 * T, term = 1.0, s = 1.0;
+  for (int k = 1; k <= 120; ++k) {
+    term = term * tt2 / double(2 * top + 2 * k + 1);
+    s += term;
+  }
+  F[top] = s * txp / double(2 * top + 1);
+  for (int m = top - 1; m >= 0; --m) F[m] = (tt2 * F[m + 1] + txp) / double(2 * m + 1);
+  for (int m = 0; m < NBORD; ++m) g_boys_tab[i * NBORD + m] = F[m];
+}
+
+// F_m(T) for m = threadIdx.x <= lam, all threads of the block take part
+// (regimes as in FUNFM: exact at T=0, table below 17, the reference's
+// rational seed up to 30, asymptotic beyond).
+__device__ void boys_block(double T, int lam, double *F) {
+  const double A0 = 4.994501191201870e-1, B0 = 4.551838436668326e-1;
+  const double PI12 = 1.7724538509055160;
+  int m = threadIdx.x;
+  if (T <= 1.0e-11) {
+    if (m <= lam) F[m] = c_rinv[m];
+  } else if (T <= 17.0) {
+    if (m <= lam) {
+      int i = __double2int_rn(T * 32.0);
+      double d = i / 32.0 - T;  // -(T - T_i)
+      const double *f = g_boys_tab + i * NBORD + m;
+      double v = f[6] * (1.0 / 720.0);
+      v = fma(v, d, f[5] * (1.0 / 120.0));
+      v = fma(v, d, f[4] * (1.0 / 24.0));
+      v = fma(v, d, f[3] * (1.0 / 6.0));
+      v = fma(v, d, f[2] * 0.5);
+      v = fma(v, d, f[1]);
+      v = fma(v, d, f[0]);
+      F[m] = v;
+    }
+  } else if (m == 0) {
+    if (T <= 30.0) {
+      double txp = exp(-T), r2 = 0.5 / T;
+      F[0] = 0.5 * PI12 / sqrt(T) - txp * (A0 / (B0 + T));
+      for (int k = 0; k < lam; ++k) F[k + 1] = (double(2 * k + 1) * F[k] - txp) * r2;
+    } else {
+      double r2 = 0.5 / T;
+      F[0] = 0.5 * PI12 / sqrt(T);
+      for (int k = 0; k < lam; ++k) F[k + 1] = double(2 * k + 1) * F[k] * r2;
+    }
+  }
+}
+
+constexpr int CHDF = 2;  // left labels per first-contraction pass (df path)
+constexpr int DFTHREADS = 128;  // 4 quartets in flight per SM
 constexpr int NCB = CHDF * MAXLAB * MAXLAB * 8;  // contribution buffer (float4)
 
 struct QArgsDF {
@@ -832,7 +892,32 @@ __device__ inline void cdf_mac(cdf &acc, float4 u, float4 v) {
   df_fma(u.z, u.w, v.x, v.y, acc.ih, acc.il);
 }
 
-__global__ void __launch_bounds__(QTHREADS, 2)
+// (ab|cd) m-sign combination (sa,sb,sc,sd) of a label quartet from the
+// eight contractions sv[0..7] = s1, s1c, s2, s2c, s3, s3c, s4, s4c of the
+// (left|right) evaluation (ERIFAST :12809-13119): combination index
+// 8a+4b+2c+d of (left|right); odd indices are conjugates; signs from the
+// left pair phase sl and the product phase slr.
+template <bool SWP>
+__device__ inline float4 rv_sign(const float4 (&sv)[8], int sa, int sb, int sc, int sd,
+                                 float sl, float slr) {
+  int idx = SWP ? 8 * sc + 4 * sd + 2 * sa + sb : 8 * sa + 4 * sb + 2 * sc + sd;
+  // source contraction and sign kind per index: kind 0 -> 1, 1 -> sl,
+  // 2 -> slr, 3 -> sl*slr; negative kinds flip the sign
+  const int src[16] = {0, 3, 2, 1, 5, 6, 7, 4, 4, 7, 6, 5, 1, 2, 3, 0};
+  const int kind[16] = {0, -3, 0, 3, -1, 2, -1, -2, 0, -3, 0, 3, 1, -2, 1, 2};
+  int kd = kind[idx];
+  float f = 1.f;
+  int ak = kd < 0 ? -kd : kd;
+  if (ak == 1) f = sl;
+  else if (ak == 2) f = slr;
+  else if (ak == 3) f = sl * slr;
+  if (kd < 0) f = -f;
+  float4 v = sv[src[idx]];
+  if (idx & 1) return make_float4(f * v.x, f * v.y, -f * v.z, -f * v.w);
+  return make_float4(f * v.x, f * v.y, f * v.z, f * v.w);
+}
+
+__global__ void __launch_bounds__(DFTHREADS, 4)
 k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
   extern __shared__ double smem[];
   double *R = smem;                            // NTR (FP64)
@@ -869,13 +954,15 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
       double Qz = (C.alpha * C.z + Dd.alpha * Dd.z) / qq;
       double aph = p * qq / (p + qq);
       double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
-      boys_ref(T, lam, F);
       double sg = swp ? -1.0 : 1.0;
       sgeo[0] = sg * (Px - Qx); sgeo[1] = sg * (Py - Qy); sgeo[2] = sg * (Pz - Qz);
       sgeo[3] = -2.0 * aph;
       sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
+      sgeo[5] = T;
       sk = half_floor_log2(2.0 * aph);
     }
+    __syncthreads();
+    boys_block(sgeo[5], lam, F);
     __syncthreads();
     {
       double X = sgeo[0], Y = sgeo[1], Z = sgeo[2], m2a = sgeo[3];
@@ -964,117 +1051,131 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
         G[ls * NTE + qq] = make_float4(rh * f, rl * f, ih * f, il * f);
       }
       __syncthreads();
-      for (int w = threadIdx.x; w < nch * nlR; w += blockDim.x) {
-        int lab = w / nlR, lr = w % nlR;
-        int labL = c0 + lab;
-        int l1 = labL / nl2L, l2 = labL % nl2L, r1 = lr / nl2R, r2 = lr % nl2R;
-        int ia = swp ? r1 : l1, ib = swp ? r2 : l2, ic = swp ? l1 : r1, id = swp ? l2 : r2;
-        int kq[4], mq[4], mm[4];
-        label_of(la, ia, kq[0], mm[0]);
-        label_of(lb, ib, kq[1], mm[1]);
-        label_of(lc, ic, kq[2], mm[2]);
-        label_of(ld, id, kq[3], mm[3]);
-        for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
-        float4 *cb = Cb + (size_t)(lab * nlR + lr) * 8;
-        if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) {
-          for (int i = 0; i < 8; ++i) cb[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-          continue;
-        }
-        double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
-        double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
-        double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
-        const float4 *g11 = G + (lab * 2 + 0) * NTE, *g21 = G + (lab * 2 + 1) * NTE;
-        const float4 *e11 = ER + ((long long)lr * 2 + 0) * nR;
-        const float4 *e21 = ER + ((long long)lr * 2 + 1) * nR;
-        // partial products a=re*re, b=im*im, c=re*im, d=im*re of the four
-        // (E_R set) x (G set) pairs, double-float
-        float acc[16][2];
+      {
+        // each label quartet's second contraction is split over KS lanes
+        // (more lanes for classes with few label quartets) and summed with a
+        // butterfly of shuffles; the KS lanes then share its 8 J/K targets
+        int items = nch * nlR;
+        int KS = 1;
+        while (KS < 8 && items * KS * 2 <= (int)blockDim.x) KS *= 2;
+        int lanes = items * KS;
+        for (int base = 0; base < lanes; base += blockDim.x) {
+          int t = base + threadIdx.x;
+          bool valid = t < lanes;
+          int item = valid ? t / KS : 0, part = t % KS;
+          int lab = item / nlR, lr = item % nlR;
+          int labL = c0 + lab;
+          int l1 = labL / nl2L, l2 = labL % nl2L, r1 = lr / nl2R, r2 = lr % nl2R;
+          int ia = swp ? r1 : l1, ib = swp ? r2 : l2, ic = swp ? l1 : r1, id = swp ? l2 : r2;
+          int kq[4], mq[4], mm[4];
+          label_of(la, ia, kq[0], mm[0]);
+          label_of(lb, ib, kq[1], mm[1]);
+          label_of(lc, ic, kq[2], mm[2]);
+          label_of(ld, id, kq[3], mm[3]);
+          for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
+          bool active = valid && label_ok(q.isym, q.racah1, mcnt, kq, mq, lq);
+          float acc[16][2];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) { acc[i][0] = 0.f; acc[i][1] = 0.f; }
-        for (int k = 0; k < nR; ++k) {
-          float4 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
-#define P4(o, UU, XX)                                     \
-  df_fma(UU.x, UU.y, XX.x, XX.y, acc[o][0], acc[o][1]);     \
+          for (int i = 0; i < 16; ++i) { acc[i][0] = 0.f; acc[i][1] = 0.f; }
+          if (active) {
+            const float4 *g11 = G + (lab * 2 + 0) * NTE, *g21 = G + (lab * 2 + 1) * NTE;
+            const float4 *e11 = ER + ((long long)lr * 2 + 0) * nR;
+            const float4 *e21 = ER + ((long long)lr * 2 + 1) * nR;
+            // right-side E from L2 with one iteration of register prefetch
+            float4 u1n = make_float4(0.f, 0.f, 0.f, 0.f), u2n = u1n;
+            if (part < nR) { u1n = e11[part]; u2n = e21[part]; }
+            for (int k = part; k < nR; k += KS) {
+              float4 u1 = u1n, u2 = u2n;
+              if (k + KS < nR) { u1n = e11[k + KS]; u2n = e21[k + KS]; }
+              float4 x1 = g11[k], x2 = g21[k];
+#define P4(o, UU, XX)                                           \
+  df_fma(UU.x, UU.y, XX.x, XX.y, acc[o][0], acc[o][1]);         \
   df_fma(UU.z, UU.w, XX.z, XX.w, acc[o + 1][0], acc[o + 1][1]); \
   df_fma(UU.x, UU.y, XX.z, XX.w, acc[o + 2][0], acc[o + 2][1]); \
   df_fma(UU.z, UU.w, XX.x, XX.y, acc[o + 3][0], acc[o + 3][1]);
-          P4(0, u1, x1) P4(4, u2, x1) P4(8, u1, x2) P4(12, u2, x2)
+              P4(0, u1, x1) P4(4, u2, x1) P4(8, u1, x2) P4(12, u2, x2)
 #undef P4
-        }
-        // s = u*x = (a-b, c+d) ; sc = u*conj(x) = (a+b, d-c)
-        float4 sv[8];
-        for (int pp = 0; pp < 4; ++pp) {
-          float *a = acc[4 * pp], *b = acc[4 * pp + 1], *c = acc[4 * pp + 2], *d = acc[4 * pp + 3];
-          float4 t, tc;
-          df_add(a[0], a[1], -b[0], -b[1], t.x, t.y);
-          df_add(c[0], c[1], d[0], d[1], t.z, t.w);
-          df_add(a[0], a[1], b[0], b[1], tc.x, tc.y);
-          df_add(d[0], d[1], -c[0], -c[1], tc.z, tc.w);
-          sv[2 * pp] = t;
-          sv[2 * pp + 1] = tc;
-        }
-        // 16 m-sign combinations; phases +-1 through the sign
-        float sl_ = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
-        float4 r[16];
-        auto cj = [](float4 v, float f) { return make_float4(f * v.x, f * v.y, -f * v.z, -f * v.w); };
-        auto sc = [](float4 v, float f) { return make_float4(f * v.x, f * v.y, f * v.z, f * v.w); };
-        r[0] = sv[0];
-        r[12] = sc(sv[1], sl_);
-        r[15] = cj(r[0], slr);
-        r[3] = cj(r[12], slr);
-        r[2] = sv[2];
-        r[14] = sc(sv[3], sl_);
-        r[13] = cj(r[2], -slr);
-        r[1] = cj(r[14], -slr);
-        r[8] = sv[4];
-        r[4] = sc(sv[5], -sl_);
-        r[7] = cj(r[8], -slr);
-        r[11] = cj(r[4], -slr);
-        r[10] = sv[6];
-        r[6] = sc(sv[7], -sl_);
-        r[5] = cj(r[10], slr);
-        r[9] = cj(r[6], slr);
-#define RV(sa, sb, sc_, sd) (swp ? r[8 * (sc_) + 4 * (sd) + 2 * (sa) + (sb)] \
-                                 : r[8 * (sa) + 4 * (sb) + 2 * (sc_) + (sd)])
-        int fb[2] = {B.fock[ib][0] + oab, B.fock[ib][1] + oab};
-        int fc[2] = {C.fock[ic][0] + ocd, C.fock[ic][1] + ocd};
-        int fd[2] = {Dd.fock[id][0] + ocd, Dd.fock[id][1] + ocd};
-        const size_t ld = (size_t)q.ldd;
-        // phase A: this label quartet's J contributions (sa,sb) and K
-        // contributions (sa,sd) into the chunk buffer
-        if (q.isym == 0) {
-          for (int sa = 0; sa < 2; ++sa)
-            for (int sb = 0; sb < 2; ++sb) {
-              cdf j = {0.f, 0.f, 0.f, 0.f};
-              for (int sc2 = 0; sc2 < 2; ++sc2)
-                for (int sd = 0; sd < 2; ++sd)
-                  cdf_mac(j, RV(sa, sb, sc2, sd), q.D[fc[sc2] + ld * fd[sd]]);
-              cb[2 * sa + sb] = make_float4(j.rh, j.rl, j.ih, j.il);
             }
-          for (int sa = 0; sa < 2; ++sa)
-            for (int sd = 0; sd < 2; ++sd) {
-              cdf kk = {0.f, 0.f, 0.f, 0.f};
-              for (int sb = 0; sb < 2; ++sb)
-                for (int sc2 = 0; sc2 < 2; ++sc2)
-                  cdf_mac(kk, RV(sa, sb, sc2, sd), q.D[fc[sc2] + ld * fb[sb]]);
-              cb[4 + 2 * sa + sd] = make_float4(kk.rh, kk.rl, kk.ih, kk.il);
+          }
+          for (int off = KS >> 1; off > 0; off >>= 1) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              float oh = __shfl_xor_sync(0xffffffffu, acc[i][0], off);
+              float ol = __shfl_xor_sync(0xffffffffu, acc[i][1], off);
+              df_add(acc[i][0], acc[i][1], oh, ol, acc[i][0], acc[i][1]);
             }
-        } else {
-          // CLMMTZ: real parts, equal-sign direct blocks, crossed exchange
-          cb[1] = cb[2] = cb[5] = cb[6] = make_float4(0.f, 0.f, 0.f, 0.f);
-          for (int s2 = 0; s2 < 2; ++s2) {
-            float jh = 0.f, jl = 0.f, kh = 0.f, kl2 = 0.f;
-            for (int t = 0; t < 2; ++t) {
-              float4 vj = RV(s2, s2, t, t), dj = q.D[fc[t] + ld * fd[t]];
-              float4 vk = RV(s2, t, t, s2), dk = q.D[fc[t] + ld * fb[t]];
-              df_fma(vj.x, vj.y, dj.x, dj.y, jh, jl);
-              df_fma(vk.x, vk.y, dk.x, dk.y, kh, kl2);
+          }
+          if (!valid) continue;
+          float4 *cb = Cb + (size_t)(lab * nlR + lr) * 8;
+          if (!active) {
+            for (int tg = part; tg < 8; tg += KS) cb[tg] = make_float4(0.f, 0.f, 0.f, 0.f);
+            continue;
+          }
+          double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
+          double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
+          double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
+          // s = u*x = (a-b, c+d) ; sc = u*conj(x) = (a+b, d-c)
+          float4 sv[8];
+#pragma unroll
+          for (int pp = 0; pp < 4; ++pp) {
+            float *a = acc[4 * pp], *b = acc[4 * pp + 1], *c = acc[4 * pp + 2], *d = acc[4 * pp + 3];
+            float4 tt, tc;
+            df_add(a[0], a[1], -b[0], -b[1], tt.x, tt.y);
+            df_add(c[0], c[1], d[0], d[1], tt.z, tt.w);
+            df_add(a[0], a[1], b[0], b[1], tc.x, tc.y);
+            df_add(d[0], d[1], -c[0], -c[1], tc.z, tc.w);
+            sv[2 * pp] = tt;
+            sv[2 * pp + 1] = tc;
+          }
+          float sl_ = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
+          int fb[2] = {B.fock[ib][0] + oab, B.fock[ib][1] + oab};
+          int fc[2] = {C.fock[ic][0] + ocd, C.fock[ic][1] + ocd};
+          int fd[2] = {Dd.fock[id][0] + ocd, Dd.fock[id][1] + ocd};
+          const size_t ld = (size_t)q.ldd;
+          // phase A: target tg < 4 is J(sa,sb) with sa = tg>>1, sb = tg&1;
+          // tg >= 4 is K(sa,sd) with sa = (tg-4)>>1, sd = (tg-4)&1
+#pragma unroll 1
+          for (int tg = part; tg < 8; tg += KS) {
+            cdf o = {0.f, 0.f, 0.f, 0.f};
+            if (q.isym == 0) {
+#pragma unroll
+              for (int x = 0; x < 2; ++x)
+#pragma unroll
+                for (int y = 0; y < 2; ++y) {
+                  int sa, sb, sc2, sd;
+                  float4 dv;
+                  if (tg < 4) {
+                    sa = tg >> 1; sb = tg & 1; sc2 = x; sd = y;
+                    dv = q.D[fc[sc2] + ld * fd[sd]];
+                  } else {
+                    sa = (tg - 4) >> 1; sd = (tg - 4) & 1; sb = x; sc2 = y;
+                    dv = q.D[fc[sc2] + ld * fb[sb]];
+                  }
+                  float4 v = swp ? rv_sign<true>(sv, sa, sb, sc2, sd, sl_, slr)
+                                 : rv_sign<false>(sv, sa, sb, sc2, sd, sl_, slr);
+                  cdf_mac(o, v, dv);
+                }
+            } else if (tg == 0 || tg == 3 || tg == 4 || tg == 7) {
+              // CLMMTZ: real parts, equal-sign direct blocks, crossed exchange
+              int s2 = (tg == 0 || tg == 4) ? 0 : 1;
+#pragma unroll
+              for (int tt = 0; tt < 2; ++tt) {
+                float4 v, dv;
+                if (tg < 4) {
+                  v = swp ? rv_sign<true>(sv, s2, s2, tt, tt, sl_, slr)
+                          : rv_sign<false>(sv, s2, s2, tt, tt, sl_, slr);
+                  dv = q.D[fc[tt] + ld * fd[tt]];
+                } else {
+                  v = swp ? rv_sign<true>(sv, s2, tt, tt, s2, sl_, slr)
+                          : rv_sign<false>(sv, s2, tt, tt, s2, sl_, slr);
+                  dv = q.D[fc[tt] + ld * fb[tt]];
+                }
+                df_fma(v.x, v.y, dv.x, dv.y, o.rh, o.rl);
+              }
             }
-            cb[3 * s2] = make_float4(jh, jl, 0.f, 0.f);
-            cb[4 + 3 * s2] = make_float4(kh, kl2, 0.f, 0.f);
+            cb[tg] = make_float4(o.rh, o.rl, o.ih, o.il);
           }
         }
-#undef RV
       }
       __syncthreads();
       // phase B: one thread per J or K target sums the chunk's contributions
@@ -1316,8 +1417,8 @@ int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = ddf;
   a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = n; a.ldf = ldf;
   a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1;
-  long long grid = std::min<long long>(nq, 152LL * 64);
-  k_quartet_df<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  long long grid = std::min<long long>(nq, 152LL * 128);
+  k_quartet_df<<<(unsigned)grid, DFTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
   c->launches += 2;
   return 0;
@@ -1451,6 +1552,7 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
     }
   c->ns = (int)c->shells.size();
   if (upload_tables()) { g_init_err = "constant table upload failed"; delete c; return BG_ERR_CUDA; }
+  k_boys_table<<<(NBGRID + 127) / 128, 128>>>();
   // E-coefficient storage for every ordered shell pair and component
   int ns = c->ns, ncomp = c->ncomp;
   std::vector<PairE> pe((size_t)ns * ns);
