@@ -383,6 +383,7 @@ struct QArgs {
   const double2 *D;
   double *GD, *GX;
   int ns, ldd, ldf, nskp, isym, racah1;
+  int sym;  // also digest the swapped quartet (cd|ab) = (ab|cd) when ab != cd
 };
 
 constexpr unsigned long long SGN = 0x8000000000000000ULL;
@@ -464,8 +465,10 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
   double *R2 = R + NTR;                      // NTR
   double *F = R2 + NTR;                      // MAXLAM+2
   double2 *G = (double2 *)(F + MAXLAM + 2);  // CHUNK*2*NTE
-  double2 *Jl = G + CHUNK * 2 * NTE;         // MAXSP*MAXSP
-  double2 *Kl = Jl + MAXSP * MAXSP;          // MAXSP*MAXSP
+  double2 *Jl = G + CHUNK * 2 * NTE;         // MAXSP*MAXSP  J(a,b)
+  double2 *Kl = Jl + MAXSP * MAXSP;          // MAXSP*MAXSP  K(a,d)
+  double2 *J2 = Kl + MAXSP * MAXSP;          // MAXSP*MAXSP  J(c,d) of (cd|ab)
+  double2 *K2 = J2 + MAXSP * MAXSP;          // MAXSP*MAXSP  K(c,b) of (cd|ab)
   __shared__ double sgeo[8];
 
   for (long long qi = blockIdx.x; qi < nq; qi += gridDim.x) {
@@ -537,7 +540,10 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
     for (int k = threadIdx.x; k < MAXSP * MAXSP; k += blockDim.x) {
       Jl[k] = make_double2(0.0, 0.0);
       Kl[k] = make_double2(0.0, 0.0);
+      J2[k] = make_double2(0.0, 0.0);
+      K2[k] = make_double2(0.0, 0.0);
     }
+    bool dual = q.sym && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
     const double2 *Eab = q.E + q.pe[Q4.x * q.ns + Q4.y].off[t1];
     const double2 *Ecd = q.E + q.pe[Q4.z * q.ns + Q4.w].off[t2];
     // left/right roles
@@ -660,6 +666,38 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
                 }
               satomic(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], make_double2(kx, ky));
             }
+          if (dual) {
+            // (cd|ab): J(c,d) += (ab|cd) D(a,b) ; K(c,b) += (ab|cd) D(a,d)
+            int fa[2] = {A.fock[ia][0] + oab, A.fock[ia][1] + oab};
+            double2 Dab[4], Dad[4];
+            for (int x = 0; x < 2; ++x)
+              for (int y = 0; y < 2; ++y) {
+                Dab[2 * x + y] = ldD(q, fa[x], fb[y]);
+                Dad[2 * x + y] = ldD(q, fa[x], fd[y]);
+              }
+            for (int sc = 0; sc < 2; ++sc)
+              for (int sd = 0; sd < 2; ++sd) {
+                double jx = 0.0, jy = 0.0;
+                for (int sa = 0; sa < 2; ++sa)
+                  for (int sb = 0; sb < 2; ++sb) {
+                    double2 v = RV(sa, sb, sc, sd), d = Dab[2 * sa + sb];
+                    jx = fma(v.x, d.x, fma(-v.y, d.y, jx));
+                    jy = fma(v.x, d.y, fma(v.y, d.x, jy));
+                  }
+                satomic(&J2[(ic * 2 + sc) * MAXSP + id * 2 + sd], make_double2(jx, jy));
+              }
+            for (int sc = 0; sc < 2; ++sc)
+              for (int sb = 0; sb < 2; ++sb) {
+                double kx = 0.0, ky = 0.0;
+                for (int sa = 0; sa < 2; ++sa)
+                  for (int sd = 0; sd < 2; ++sd) {
+                    double2 v = RV(sa, sb, sc, sd), d = Dad[2 * sa + sd];
+                    kx = fma(v.x, d.x, fma(-v.y, d.y, kx));
+                    ky = fma(v.x, d.y, fma(v.y, d.x, ky));
+                  }
+                satomic(&K2[(ic * 2 + sc) * MAXSP + ib * 2 + sb], make_double2(kx, ky));
+              }
+          }
         } else {
           // CLMMTZ: real parts, equal-sign direct blocks, crossed exchange
           for (int s = 0; s < 2; ++s) {
@@ -670,6 +708,18 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
             }
             atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, jv);
             atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
+          }
+          if (dual) {
+            int fa[2] = {A.fock[ia][0] + oab, A.fock[ia][1] + oab};
+            for (int s = 0; s < 2; ++s) {
+              double jv = 0.0, kv = 0.0;
+              for (int t = 0; t < 2; ++t) {
+                jv = fma(RV(t, t, s, s).x, ldD(q, fa[t], fb[t]).x, jv);
+                kv = fma(RV(t, s, s, t).x, ldD(q, fa[t], fd[t]).x, kv);
+              }
+              atomicAdd(&J2[(ic * 2 + s) * MAXSP + id * 2 + s].x, jv);
+              atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
+            }
           }
         }
 #undef RV
@@ -696,6 +746,27 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         double *dst = q.GX + 2 * ((size_t)fa + (size_t)q.ldf * fdd);
         atomicAdd(dst, v.x);
         atomicAdd(dst + 1, v.y);
+      }
+      if (dual) {
+        int nsc = 2 * nlc;
+        for (int w = threadIdx.x; w < nsc * 2 * nld; w += blockDim.x) {
+          int c = w / (2 * nld), d = w % (2 * nld);
+          double2 v = J2[c * MAXSP + d];
+          if (v.x == 0.0 && v.y == 0.0) continue;
+          int fcc = C.fock[c >> 1][c & 1] + ocd, fdd = Dd.fock[d >> 1][d & 1] + ocd;
+          double *dst = q.GD + 2 * ((size_t)fcc + (size_t)q.ldf * fdd);
+          atomicAdd(dst, v.x);
+          atomicAdd(dst + 1, v.y);
+        }
+        for (int w = threadIdx.x; w < nsc * 2 * nlb; w += blockDim.x) {
+          int c = w / (2 * nlb), b = w % (2 * nlb);
+          double2 v = K2[c * MAXSP + b];
+          if (v.x == 0.0 && v.y == 0.0) continue;
+          int fcc = C.fock[c >> 1][c & 1] + ocd, fbb = B.fock[b >> 1][b & 1] + oab;
+          double *dst = q.GX + 2 * ((size_t)fcc + (size_t)q.ldf * fbb);
+          atomicAdd(dst, v.x);
+          atomicAdd(dst + 1, v.y);
+        }
       }
     }
     __syncthreads();
@@ -870,7 +941,7 @@ __device__ void boys_block(double T, int lam, double *F) {
 
 constexpr int CHDF = 2;  // left labels per first-contraction pass (df path)
 constexpr int DFTHREADS = 128;  // 4 quartets in flight per SM
-constexpr int NCB = CHDF * MAXLAB * MAXLAB * 8;  // contribution buffer (float4)
+constexpr int NCB = CHDF * MAXLAB * MAXLAB * 16;  // contribution buffer (float4)
 
 struct QArgsDF {
   const Shell *sh;
@@ -879,6 +950,7 @@ struct QArgsDF {
   const float4 *D;  // n x n, leading dimension n
   double *GD, *GX;
   int ns, ldd, ldf, nskp, isym, racah1;
+  int sym;  // also digest the swapped quartet (cd|ab) = (ab|cd) when ab != cd
 };
 
 // complex double-float product accumulate: (acc) += u * v
@@ -926,9 +998,11 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
   double *F = R + 2 * NTR;                     // MAXLAM+2
   float4 *EL = (float4 *)(F + MAXLAM + 2);     // CHDF*2*NTE
   float4 *G = EL + CHDF * 2 * NTE;             // CHDF*2*NTE
-  float4 *Cb = G + CHDF * 2 * NTE;             // NCB: J (4) and K (4) per label quartet
+  float4 *Cb = G + CHDF * 2 * NTE;             // NCB: J, K, J2, K2 (4 each) per label quartet
   double2 *Jl = (double2 *)(Cb + NCB);         // MAXSP*MAXSP
   double2 *Kl = Jl + MAXSP * MAXSP;
+  double2 *J2 = Kl + MAXSP * MAXSP;
+  double2 *K2 = J2 + MAXSP * MAXSP;
   __shared__ double sgeo[8];
   __shared__ int sk;
 
@@ -1011,7 +1085,11 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
     for (int i = threadIdx.x; i < MAXSP * MAXSP; i += blockDim.x) {
       Jl[i] = make_double2(0.0, 0.0);
       Kl[i] = make_double2(0.0, 0.0);
+      J2[i] = make_double2(0.0, 0.0);
+      K2[i] = make_double2(0.0, 0.0);
     }
+    bool dual = q.sym && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
+    int ntg = dual ? 16 : 8;
     const float4 *Eab = q.E + pab_e.off[t1];
     const float4 *Ecd = q.E + pcd_e.off[t2];
     const float4 *EGL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
@@ -1106,9 +1184,9 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
             }
           }
           if (!valid) continue;
-          float4 *cb = Cb + (size_t)(lab * nlR + lr) * 8;
+          float4 *cb = Cb + (size_t)(lab * nlR + lr) * 16;
           if (!active) {
-            for (int tg = part; tg < 8; tg += KS) cb[tg] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int tg = part; tg < ntg; tg += KS) cb[tg] = make_float4(0.f, 0.f, 0.f, 0.f);
             continue;
           }
           double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
@@ -1128,14 +1206,17 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
             sv[2 * pp + 1] = tc;
           }
           float sl_ = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
+          int fa[2] = {A.fock[ia][0] + oab, A.fock[ia][1] + oab};
           int fb[2] = {B.fock[ib][0] + oab, B.fock[ib][1] + oab};
           int fc[2] = {C.fock[ic][0] + ocd, C.fock[ic][1] + ocd};
           int fd[2] = {Dd.fock[id][0] + ocd, Dd.fock[id][1] + ocd};
           const size_t ld = (size_t)q.ldd;
-          // phase A: target tg < 4 is J(sa,sb) with sa = tg>>1, sb = tg&1;
-          // tg >= 4 is K(sa,sd) with sa = (tg-4)>>1, sd = (tg-4)&1
+          // phase A: targets tg = 4*family + sig.  family 0 J(a,b) sig=(sa,sb),
+          // 1 K(a,d) sig=(sa,sd), 2 J(c,d) of (cd|ab) sig=(sc,sd),
+          // 3 K(c,b) of (cd|ab) sig=(sc,sb)
 #pragma unroll 1
-          for (int tg = part; tg < 8; tg += KS) {
+          for (int tg = part; tg < ntg; tg += KS) {
+            int fam = tg >> 2, s1 = (tg >> 1) & 1, s2 = tg & 1;
             cdf o = {0.f, 0.f, 0.f, 0.f};
             if (q.isym == 0) {
 #pragma unroll
@@ -1144,32 +1225,37 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
                 for (int y = 0; y < 2; ++y) {
                   int sa, sb, sc2, sd;
                   float4 dv;
-                  if (tg < 4) {
-                    sa = tg >> 1; sb = tg & 1; sc2 = x; sd = y;
-                    dv = q.D[fc[sc2] + ld * fd[sd]];
+                  if (fam == 0) {
+                    sa = s1; sb = s2; sc2 = x; sd = y; dv = q.D[fc[sc2] + ld * fd[sd]];
+                  } else if (fam == 1) {
+                    sa = s1; sd = s2; sb = x; sc2 = y; dv = q.D[fc[sc2] + ld * fb[sb]];
+                  } else if (fam == 2) {
+                    sc2 = s1; sd = s2; sa = x; sb = y; dv = q.D[fa[sa] + ld * fb[sb]];
                   } else {
-                    sa = (tg - 4) >> 1; sd = (tg - 4) & 1; sb = x; sc2 = y;
-                    dv = q.D[fc[sc2] + ld * fb[sb]];
+                    sc2 = s1; sb = s2; sa = x; sd = y; dv = q.D[fa[sa] + ld * fd[sd]];
                   }
                   float4 v = swp ? rv_sign<true>(sv, sa, sb, sc2, sd, sl_, slr)
                                  : rv_sign<false>(sv, sa, sb, sc2, sd, sl_, slr);
                   cdf_mac(o, v, dv);
                 }
-            } else if (tg == 0 || tg == 3 || tg == 4 || tg == 7) {
+            } else if (s1 == s2) {
               // CLMMTZ: real parts, equal-sign direct blocks, crossed exchange
-              int s2 = (tg == 0 || tg == 4) ? 0 : 1;
+              int sg = s1;
 #pragma unroll
               for (int tt = 0; tt < 2; ++tt) {
-                float4 v, dv;
-                if (tg < 4) {
-                  v = swp ? rv_sign<true>(sv, s2, s2, tt, tt, sl_, slr)
-                          : rv_sign<false>(sv, s2, s2, tt, tt, sl_, slr);
-                  dv = q.D[fc[tt] + ld * fd[tt]];
+                int sa, sb, sc2, sd;
+                float4 dv;
+                if (fam == 0) {
+                  sa = sg; sb = sg; sc2 = tt; sd = tt; dv = q.D[fc[tt] + ld * fd[tt]];
+                } else if (fam == 1) {
+                  sa = sg; sb = tt; sc2 = tt; sd = sg; dv = q.D[fc[tt] + ld * fb[tt]];
+                } else if (fam == 2) {
+                  sa = tt; sb = tt; sc2 = sg; sd = sg; dv = q.D[fa[tt] + ld * fb[tt]];
                 } else {
-                  v = swp ? rv_sign<true>(sv, s2, tt, tt, s2, sl_, slr)
-                          : rv_sign<false>(sv, s2, tt, tt, s2, sl_, slr);
-                  dv = q.D[fc[tt] + ld * fb[tt]];
+                  sa = tt; sb = sg; sc2 = sg; sd = tt; dv = q.D[fa[tt] + ld * fd[tt]];
                 }
+                float4 v = swp ? rv_sign<true>(sv, sa, sb, sc2, sd, sl_, slr)
+                               : rv_sign<false>(sv, sa, sb, sc2, sd, sl_, slr);
                 df_fma(v.x, v.y, dv.x, dv.y, o.rh, o.rl);
               }
             }
@@ -1179,63 +1265,54 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
       }
       __syncthreads();
       // phase B: one thread per J or K target sums the chunk's contributions
-      // in double-float and adds the FP64 value to the shared accumulator
+      // in double-float and adds the FP64 value to the shared accumulator.
+      // Families: 0 J(ia,ib), 1 K(ia,id), 2 J(ic,id), 3 K(ic,ib).
       {
-        int tj = (swp ? nlR : nch) * 4;
-        int tk = nla * nld * 4;
-        for (int w = threadIdx.x; w < tj + tk; w += blockDim.x) {
+        int nfam = dual ? 4 : 2;
+        int nx[4] = {nla, nla, nlc, nlc}, ny[4] = {nlb, nld, nld, nlb};
+        int tot = 0, start[5];
+        for (int f = 0; f < 4; ++f) { start[f] = tot; if (f < nfam) tot += nx[f] * ny[f] * 4; }
+        start[4] = tot;
+        for (int w = threadIdx.x; w < tot; w += blockDim.x) {
+          int f = 0;
+          while (w >= start[f + 1]) ++f;
+          int u = w - start[f], sig = u & 3, tgt = u >> 2;
+          int X = tgt / ny[f], Y = tgt % ny[f];
           float sh_r = 0.f, sl_r = 0.f, sh_i = 0.f, sl_i = 0.f;
           int cnt = 0;
-          double2 *dst;
-          if (w < tj) {
-            int tgt = w >> 2, sig = w & 3;
-            int ia, ib;
-            if (!swp) {
-              int labL = c0 + tgt;
-              ia = labL / nlb; ib = labL % nlb;
-              for (int lr = 0; lr < nlR; ++lr) {
-                float4 v = Cb[(size_t)(tgt * nlR + lr) * 8 + sig];
+          // the left label is (l1,l2) = (ia,ib) or, swapped, (ic,id); the
+          // right label likewise; each family fixes one index on each side
+          // or two on one side
+          for (int lab = 0; lab < nch; ++lab) {
+            int labL = c0 + lab;
+            int l1 = labL / nl2L, l2 = labL % nl2L;
+            int Lia = swp ? -1 : l1, Lib = swp ? -1 : l2, Lic = swp ? l1 : -1, Lid = swp ? l2 : -1;
+            // constraint of this family on the left label
+            bool okL;
+            int fix_a = -1, fix_b = -1, fix_c = -1, fix_d = -1;
+            if (f == 0) { fix_a = X; fix_b = Y; }
+            else if (f == 1) { fix_a = X; fix_d = Y; }
+            else if (f == 2) { fix_c = X; fix_d = Y; }
+            else { fix_c = X; fix_b = Y; }
+            okL = (Lia < 0 || fix_a < 0 || Lia == fix_a) && (Lib < 0 || fix_b < 0 || Lib == fix_b) &&
+                  (Lic < 0 || fix_c < 0 || Lic == fix_c) && (Lid < 0 || fix_d < 0 || Lid == fix_d);
+            if (!okL) continue;
+            // right labels matching the remaining constraints
+            int r1lo = 0, r1hi = nlR / nl2R, r2lo = 0, r2hi = nl2R;
+            int fr1 = swp ? fix_a : fix_c, fr2 = swp ? fix_b : fix_d;
+            if (fr1 >= 0) { r1lo = fr1; r1hi = fr1 + 1; }
+            if (fr2 >= 0) { r2lo = fr2; r2hi = fr2 + 1; }
+            for (int r1 = r1lo; r1 < r1hi; ++r1)
+              for (int r2 = r2lo; r2 < r2hi; ++r2) {
+                float4 v = Cb[(size_t)(lab * nlR + r1 * nl2R + r2) * 16 + 4 * f + sig];
                 df_add(sh_r, sl_r, v.x, v.y, sh_r, sl_r);
                 df_add(sh_i, sl_i, v.z, v.w, sh_i, sl_i);
+                ++cnt;
               }
-            } else {
-              ia = tgt / nlb; ib = tgt % nlb;
-              for (int lab = 0; lab < nch; ++lab) {
-                float4 v = Cb[(size_t)(lab * nlR + tgt) * 8 + sig];
-                df_add(sh_r, sl_r, v.x, v.y, sh_r, sl_r);
-                df_add(sh_i, sl_i, v.z, v.w, sh_i, sl_i);
-              }
-            }
-            cnt = 1;
-            dst = &Jl[(ia * 2 + (sig >> 1)) * MAXSP + ib * 2 + (sig & 1)];
-          } else {
-            int u = w - tj, sig = u & 3, tgt = u >> 2;
-            int ia = tgt / nld, id = tgt % nld;
-            if (!swp) {
-              // left labels (ia, ib) in this chunk, right labels (ic, id)
-              int lo = max(c0, ia * nlb), hi = min(c0 + nch, (ia + 1) * nlb);
-              for (int labL = lo; labL < hi; ++labL)
-                for (int ic = 0; ic < nlc; ++ic) {
-                  float4 v = Cb[(size_t)((labL - c0) * nlR + ic * nld + id) * 8 + 4 + sig];
-                  df_add(sh_r, sl_r, v.x, v.y, sh_r, sl_r);
-                  df_add(sh_i, sl_i, v.z, v.w, sh_i, sl_i);
-                  ++cnt;
-                }
-            } else {
-              // left labels (ic, id) in this chunk, right labels (ia, ib)
-              for (int lab = 0; lab < nch; ++lab) {
-                if ((c0 + lab) % nld != id) continue;
-                for (int ib = 0; ib < nlb; ++ib) {
-                  float4 v = Cb[(size_t)(lab * nlR + ia * nlb + ib) * 8 + 4 + sig];
-                  df_add(sh_r, sl_r, v.x, v.y, sh_r, sl_r);
-                  df_add(sh_i, sl_i, v.z, v.w, sh_i, sl_i);
-                  ++cnt;
-                }
-              }
-            }
-            dst = &Kl[(ia * 2 + (sig >> 1)) * MAXSP + id * 2 + (sig & 1)];
           }
           if (cnt) {
+            double2 *acc2 = f == 0 ? Jl : (f == 1 ? Kl : (f == 2 ? J2 : K2));
+            double2 *dst = &acc2[(X * 2 + (sig >> 1)) * MAXSP + Y * 2 + (sig & 1)];
             dst->x += df_val(sh_r, sl_r);
             dst->y += df_val(sh_i, sl_i);
           }
@@ -1264,6 +1341,27 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
         atomicAdd(dst, v.x);
         atomicAdd(dst + 1, v.y);
       }
+      if (dual) {
+        int nsc = 2 * nlc;
+        for (int w = threadIdx.x; w < nsc * 2 * nld; w += blockDim.x) {
+          int c = w / (2 * nld), d = w % (2 * nld);
+          double2 v = J2[c * MAXSP + d];
+          if (v.x == 0.0 && v.y == 0.0) continue;
+          int fcc = C.fock[c >> 1][c & 1] + ocd, fdd = Dd.fock[d >> 1][d & 1] + ocd;
+          double *dst = q.GD + 2 * ((size_t)fcc + (size_t)q.ldf * fdd);
+          atomicAdd(dst, v.x);
+          atomicAdd(dst + 1, v.y);
+        }
+        for (int w = threadIdx.x; w < nsc * 2 * nlb; w += blockDim.x) {
+          int c = w / (2 * nlb), b = w % (2 * nlb);
+          double2 v = K2[c * MAXSP + b];
+          if (v.x == 0.0 && v.y == 0.0) continue;
+          int fcc = C.fock[c >> 1][c & 1] + ocd, fbb = B.fock[b >> 1][b & 1] + oab;
+          double *dst = q.GX + 2 * ((size_t)fcc + (size_t)q.ldf * fbb);
+          atomicAdd(dst, v.x);
+          atomicAdd(dst + 1, v.y);
+        }
+      }
     }
     __syncthreads();
   }
@@ -1281,11 +1379,11 @@ __global__ void k_zero2d(double *a, int n, int ld) {
 
 size_t quartet_smem_df() {
   return sizeof(double) * (2 * NTR + MAXLAM + 2) + sizeof(float4) * (2 * CHDF * 2 * NTE + NCB) +
-         sizeof(double2) * (2 * MAXSP * MAXSP);
+         sizeof(double2) * (4 * MAXSP * MAXSP);
 }
 
 size_t quartet_smem() {
-  return sizeof(double) * (2 * NTR + MAXLAM + 2) + sizeof(double2) * (CHUNK * 2 * NTE + 2 * MAXSP * MAXSP);
+  return sizeof(double) * (2 * NTR + MAXLAM + 2) + sizeof(double2) * (CHUNK * 2 * NTE + 4 * MAXSP * MAXSP);
 }
 
 }  // namespace
@@ -1365,13 +1463,18 @@ int upload_tables() {
 // Ordered shell quartets of the multi-centre build for one component class,
 // with CLMFAST's centre and stage rules (bertha-scf.f:11672-11677,
 // 12045-12084) and the one-centre parity rule (:11753-11764).
-std::vector<int> build_quartets(const bg_ctx *c, int t1, int t2, int ilev) {
+// With `sym`, (ab|cd) = (cd|ab) is used: only pairs ab >= cd (pair index
+// a*ns+b) are listed for LL|LL and SS|SS, LL|SS lists every ordered pair and
+// SS|LL none; the kernels digest each listed quartet for both orders.
+std::vector<int> build_quartets(const bg_ctx *c, int t1, int t2, int ilev, bool sym) {
   std::vector<int> out;
   int itt = 1 + 2 * t1 + t2;
+  if (sym && t1 == 1 && t2 == 0) return out;
   for (int a = 0; a < c->ns; ++a)
     for (int b = 0; b < c->ns; ++b)
       for (int cc = 0; cc < c->ns; ++cc)
         for (int d = 0; d < c->ns; ++d) {
+          if (sym && t1 == t2 && (long long)a * c->ns + b < (long long)cc * c->ns + d) continue;
           const Shell &A = c->shells[a], &B = c->shells[b], &C = c->shells[cc], &D = c->shells[d];
           int s[4] = {A.cnt, B.cnt, C.cnt, D.cnt};
           std::sort(s, s + 4);
@@ -1403,7 +1506,7 @@ std::vector<int> build_quartets(const bg_ctx *c, int t1, int t2, int ilev) {
 // the quartet kernel.  Allocates nothing.
 int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                        const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
-                       cudaStream_t st, float4 *ddf) {
+                       cudaStream_t st, float4 *ddf, int sym = 0) {
   if (nq <= 0) return 0;
   static bool attr_df = false;
   size_t smem = quartet_smem_df();
@@ -1416,7 +1519,7 @@ int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   QArgsDF a;
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = ddf;
   a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = n; a.ldf = ldf;
-  a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1;
+  a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym;
   long long grid = std::min<long long>(nq, 152LL * 128);
   k_quartet_df<<<(unsigned)grid, DFTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
@@ -1449,12 +1552,12 @@ float4 *noalloc_scratch(bg_ctx *c, int *rc) {
 
 int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                     const double2 *d_D, int ldd, double *d_GD, double *d_GX,
-                    int ldf, cudaStream_t st) {
+                    int ldf, cudaStream_t st, int sym = 0) {
   if (nq <= 0) return 0;
   if (c->prec == BG_PREC_DF32) {
     int n = c->ndim;
     if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
-    return launch_quartets_df(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, c->d_Ddf);
+    return launch_quartets_df(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, c->d_Ddf, sym);
   }
   static bool attr = false;
   size_t smem = quartet_smem();
@@ -1466,7 +1569,7 @@ int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   QArgs a;
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_E; a.D = d_D;
   a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = ldd; a.ldf = ldf;
-  a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1;
+  a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym;
   long long grid = std::min<long long>(nq, 152LL * 64);
   k_quartet<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
@@ -1710,7 +1813,7 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
     }
     for (int t1 = 0; t1 < c->ncomp; ++t1)
       for (int t2 = 0; t2 < c->ncomp; ++t2) {
-        std::vector<int> q = build_quartets(c, t1, t2, ilev);
+        std::vector<int> q = build_quartets(c, t1, t2, ilev, true);
         int k = 2 * t1 + t2;
         c->nquart[k] = (long long)q.size() / 4;
         if (!q.empty()) {
@@ -1724,7 +1827,7 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
     for (int t2 = c->ncomp - 1; t2 >= 0; --t2) {
       int k = 2 * t1 + t2;
       int rc = launch_quartets(c, c->d_quart[k], c->nquart[k], t1, t2, (const double2 *)d_dent,
-                               ldd, d_gdir, d_gxch, ldf, st);
+                               ldd, d_gdir, d_gxch, ldf, st, 1);
       if (rc) return rc;
     }
   return BG_OK;
