@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--quartets", type=int, default=1 << 20)
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-h2o", action="store_true",
+                   help="skip the H2O Fock-build timing reported beside the headline")
     p.add_argument("--precision", default="df32", choices=["fp64", "df32"],
                    help="precision of the headline value; the other is timed beside it")
     return p.parse_args()
@@ -176,6 +178,47 @@ def read_traffic():
     except OSError:
         pass
     return None
+
+
+def h2o_fock_build(torch, with_cpu):
+    """The H2O Dirac-Coulomb configuration: one stage-3 Fock build
+    (CALL CLMFAST) through the C ABI with host arrays, FP64 and split
+    precision, and the CPU restatement on one core for comparison."""
+    import berthagpu
+    from berthagpu import deck
+    b = deck.h2o_basis()
+    dent = deck.density(b, seed=1)
+    out = {"ndim": b.ndim, "shells": len(b.shells()), "ilev": 3,
+           "density": "seeded random Hermitian PSD (DENSTY form)"}
+    res = {}
+    for prec in ("fp64", "df32"):
+        fb = berthagpu.FockBuilder(b)
+        fb.set_precision(prec)
+        fb.clmfast(dent, 3)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            gd, gx = fb.clmfast(dent, 3)
+            ts.append(time.perf_counter() - t0)
+        fb.close()
+        res[prec] = (gd, gx)
+        out[f"{prec}_s"] = float(np.median(ts))
+    e = {}
+    for prec, (gd, gx) in res.items():
+        e[prec] = (0.5 * np.sum(dent * gd.T).real, 0.5 * np.sum(dent * gx.T).real)
+    out["energy_j_eh"], out["energy_k_eh"] = e["fp64"]
+    out["split_energy_err_eh"] = float(max(abs(e["df32"][0] - e["fp64"][0]),
+                                           abs(e["df32"][1] - e["fp64"][1])))
+    if with_cpu:
+        from oracle import oracle as orc
+        t0 = time.perf_counter()
+        rd, rx = orc.clmfast(b, dent, 3)
+        out["cpu_port_1core_s"] = time.perf_counter() - t0
+        scale = max(np.abs(rd).max(), np.abs(rx).max())
+        out["fp64_max_abs_vs_cpu"] = float(max(np.abs(res["fp64"][0] - rd).max(),
+                                               np.abs(res["fp64"][1] - rx).max()))
+        out["fp64_rel_vs_cpu"] = out["fp64_max_abs_vs_cpu"] / scale
+    return out
 
 
 def fp64_peak(torch):
@@ -347,6 +390,9 @@ def run_gpu(args):
     traffic = read_traffic()
 
     line = None
+    h2o = None
+    if rank == 0 and not args.no_h2o:
+        h2o = h2o_fock_build(torch, with_cpu=(world == 1))
     if rank == 0:
         cpu = None
         if world == 1:
@@ -383,6 +429,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
             "clocks": clocks,
+            "fock_build_h2o": h2o,
         }
         print(json.dumps(line), flush=True)
     fb.close()

@@ -37,6 +37,7 @@ def lib():
         L.bertha_gpu_init.argtypes = [ctypes.POINTER(P), i, P, P, P, i, P, i, i, i, i]
         L.bertha_gpu_dims.argtypes = [P, P, P]
         L.bertha_gpu_set_precision.argtypes = [P, i]
+        L.bertha_gpu_set_screening.argtypes = [P, ctypes.c_double]
         L.bertha_gpu_clmfast.argtypes = [P, P, i, i, P, P, i]
         L.bertha_gpu_clmfast_device.argtypes = [P, P, i, i, P, P, i, P]
         L.bertha_gpu_quartets.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
@@ -54,7 +55,8 @@ def lib():
 
 
 EXPORTED = [
-    "bertha_gpu_init", "bertha_gpu_set_precision", "bertha_gpu_dims", "bertha_gpu_clmfast",
+    "bertha_gpu_init", "bertha_gpu_set_screening", "bertha_gpu_set_precision",
+    "bertha_gpu_dims", "bertha_gpu_clmfast",
     "bertha_gpu_clmfast_device", "bertha_gpu_quartets", "bertha_gpu_quartets_noalloc",
     "bertha_gpu_shells",
     "bertha_gpu_layout", "bertha_gpu_launches", "bertha_gpu_last_error",

@@ -43,6 +43,10 @@ class FockBuilder:
         check(lib().bertha_gpu_set_precision(self._ctx, _lib.PREC[prec]), self._ctx)
         self.precision = prec
 
+    def set_screening(self, threshold):
+        """Schwarz threshold on Q_ab*Q_cd (0 = off, the reference default)."""
+        check(lib().bertha_gpu_set_screening(self._ctx, float(threshold)), self._ctx)
+
     def close(self):
         if self._ctx:
             lib().bertha_gpu_free(self._ctx)

@@ -384,6 +384,7 @@ struct QArgs {
   double *GD, *GX;
   int ns, ldd, ldf, nskp, isym, racah1;
   int sym;  // also digest the swapped quartet (cd|ab) = (ab|cd) when ab != cd
+  double *bound;  // non-null: write max |(ab|cd)| per quartet instead of digesting
 };
 
 constexpr unsigned long long SGN = 0x8000000000000000ULL;
@@ -498,6 +499,7 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
       sgeo[0] = sg * (Px - Qx); sgeo[1] = sg * (Py - Qy); sgeo[2] = sg * (Pz - Qz);
       sgeo[3] = -2.0 * aph;
       sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
+      sgeo[6] = 0.0;
     }
     __syncthreads();
     // R recursion: level n = lam..0 ; two buffers
@@ -637,6 +639,14 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         int fb[2] = {B.fock[ib][0] + oab, B.fock[ib][1] + oab};
         int fc[2] = {C.fock[ic][0] + ocd, C.fock[ic][1] + ocd};
         int fd[2] = {Dd.fock[id][0] + ocd, Dd.fock[id][1] + ocd};
+        if (q.bound) {
+          // integral bound mode (Schwarz): largest |(ab|cd)| of the quartet;
+          // non-negative doubles order like their bit patterns
+          double m = 0.0;
+          for (int i = 0; i < 16; ++i) m = fmax(m, fmax(fabs(r[i].x), fabs(r[i].y)));
+          atomicMax((unsigned long long *)&sgeo[6], (unsigned long long)__double_as_longlong(m));
+          continue;
+        }
         if (q.isym == 0) {
           double2 Dcd[4], Dcb[4];
           for (int x = 0; x < 2; ++x)
@@ -725,6 +735,11 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
 #undef RV
       }
       __syncthreads();
+    }
+    if (q.bound) {
+      if (threadIdx.x == 0) q.bound[qi] = sgeo[6];
+      __syncthreads();
+      continue;
     }
     // flush shared accumulators
     {
@@ -1405,6 +1420,8 @@ struct bg_ctx {
   int *d_quart[4] = {nullptr, nullptr, nullptr, nullptr};
   long long nquart[4] = {0, 0, 0, 0};
   int quart_ilev = -1;
+  double screen = 0.0;          // Schwarz threshold on Q_ab*Q_cd, 0 = off
+  std::vector<double> qbound;   // [pair*2+comp] sqrt max |(ab|ab)|
   double2 *d_D = nullptr, *d_GD = nullptr, *d_GX = nullptr;
   // split-precision copies
   float4 *d_Edf = nullptr, *d_Ddf = nullptr;
@@ -1466,44 +1483,77 @@ int upload_tables() {
 // With `sym`, (ab|cd) = (cd|ab) is used: only pairs ab >= cd (pair index
 // a*ns+b) are listed for LL|LL and SS|SS, LL|SS lists every ordered pair and
 // SS|LL none; the kernels digest each listed quartet for both orders.
+// Quartets come out grouped by angular class (l_a,l_b,l_c,l_d), highest
+// first, so neighbouring CTAs carry similar work.  With a Schwarz threshold
+// quartets with Q_ab Q_cd below it are left out (SCHWARZ :37889, at the
+// level of shell pairs).
 std::vector<int> build_quartets(const bg_ctx *c, int t1, int t2, int ilev, bool sym) {
   std::vector<int> out;
   int itt = 1 + 2 * t1 + t2;
   if (sym && t1 == 1 && t2 == 0) return out;
-  for (int a = 0; a < c->ns; ++a)
-    for (int b = 0; b < c->ns; ++b)
-      for (int cc = 0; cc < c->ns; ++cc)
-        for (int d = 0; d < c->ns; ++d) {
-          if (sym && t1 == t2 && (long long)a * c->ns + b < (long long)cc * c->ns + d) continue;
-          const Shell &A = c->shells[a], &B = c->shells[b], &C = c->shells[cc], &D = c->shells[d];
-          int s[4] = {A.cnt, B.cnt, C.cnt, D.cnt};
-          std::sort(s, s + 4);
-          int mcnt = 1;
-          for (int i = 1; i < 4; ++i) mcnt += s[i] != s[i - 1];
-          if (mcnt == 1 && c->racah1) continue;
-          if (ilev == 1 && itt > 1 && mcnt != 1) continue;
-          if (ilev == 2 && itt > 3 && mcnt != 1) continue;
-          if (mcnt == 1 && !c->racah1 && ((A.l + B.l) & 1) != ((C.l + D.l) & 1)) continue;
-          out.push_back(a); out.push_back(b); out.push_back(cc); out.push_back(d);
-        }
-  // order by angular class so that neighbouring CTAs carry similar work
-  size_t n = out.size() / 4;
-  std::vector<size_t> idx(n);
-  for (size_t i = 0; i < n; ++i) idx[i] = i;
-  auto key = [&](size_t i) {
-    const int *q = &out[4 * i];
-    return ((c->shells[q[0]].l * 4 + c->shells[q[1]].l) * 4 + c->shells[q[2]].l) * 4 +
-           c->shells[q[3]].l;
-  };
-  std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return key(x) > key(y); });
-  std::vector<int> sorted(out.size());
-  for (size_t i = 0; i < n; ++i)
-    for (int k = 0; k < 4; ++k) sorted[4 * i + k] = out[4 * idx[i] + k];
-  return sorted;
+  std::vector<int> byl[MAXLB + 1];
+  for (int s = 0; s < c->ns; ++s) byl[c->shells[s].l].push_back(s);
+  bool scr = c->screen > 0.0 && !c->qbound.empty();
+  for (int la = MAXLB; la >= 0; --la)
+  for (int lb = MAXLB; lb >= 0; --lb)
+  for (int lc = MAXLB; lc >= 0; --lc)
+  for (int ld = MAXLB; ld >= 0; --ld) {
+    for (int a : byl[la])
+    for (int b : byl[lb]) {
+      long long pab = (long long)a * c->ns + b;
+      double qab = scr ? c->qbound[pab * 2 + t1] : 0.0;
+      for (int cc : byl[lc])
+      for (int d : byl[ld]) {
+        long long pcd = (long long)cc * c->ns + d;
+        if (sym && t1 == t2 && pab < pcd) continue;
+        const Shell &A = c->shells[a], &B = c->shells[b], &C = c->shells[cc], &D = c->shells[d];
+        int s4[4] = {A.cnt, B.cnt, C.cnt, D.cnt};
+        std::sort(s4, s4 + 4);
+        int mcnt = 1;
+        for (int k = 1; k < 4; ++k) mcnt += s4[k] != s4[k - 1];
+        if (mcnt == 1 && c->racah1) continue;
+        if (ilev == 1 && itt > 1 && mcnt != 1) continue;
+        if (ilev == 2 && itt > 3 && mcnt != 1) continue;
+        if (mcnt == 1 && !c->racah1 && ((la + lb) & 1) != ((lc + ld) & 1)) continue;
+        if (scr && qab * c->qbound[pcd * 2 + t2] < c->screen) continue;
+        out.push_back(a); out.push_back(b); out.push_back(cc); out.push_back(d);
+      }
+    }
+  }
+  return out;
 }
 
-// Split-precision launch: density converted into `ddf` (n x n float4), then
-// the quartet kernel.  Allocates nothing.
+int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
+                    const double2 *d_D, int ldd, double *d_GD, double *d_GX,
+                    int ldf, cudaStream_t st, int sym, double *bound);
+
+// Schwarz bounds Q(ab,T) = sqrt(max |(ab|ab)|) of every shell pair and
+// component, from the FP64 quartet kernel in bound mode (CLMDIAG :38126).
+int compute_bounds(bg_ctx *c, cudaStream_t st) {
+  int ns = c->ns;
+  std::vector<int> diag;
+  for (int a = 0; a < ns; ++a)
+    for (int b = 0; b < ns; ++b) { diag.push_back(a); diag.push_back(b); diag.push_back(a); diag.push_back(b); }
+  long long np = (long long)ns * ns;
+  int *d_q = nullptr;
+  double *d_b = nullptr;
+  CK(c, cudaMalloc(&d_q, sizeof(int) * diag.size()));
+  CK(c, cudaMalloc(&d_b, sizeof(double) * np));
+  CK(c, cudaMemcpyAsync(d_q, diag.data(), sizeof(int) * diag.size(), cudaMemcpyHostToDevice, st));
+  c->qbound.assign(np * 2, 0.0);
+  std::vector<double> hb(np);
+  for (int t = 0; t < c->ncomp; ++t) {
+    int rc = launch_quartets(c, d_q, np, t, t, nullptr, 0, nullptr, nullptr, 0, st, 0, d_b);
+    if (rc) { cudaFree(d_q); cudaFree(d_b); return rc; }
+    CK(c, cudaMemcpyAsync(hb.data(), d_b, sizeof(double) * np, cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    for (long long p = 0; p < np; ++p) c->qbound[p * 2 + t] = sqrt(hb[p]);
+  }
+  cudaFree(d_q);
+  cudaFree(d_b);
+  return 0;
+}
+
 int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                        const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
                        cudaStream_t st, float4 *ddf, int sym = 0) {
@@ -1552,9 +1602,9 @@ float4 *noalloc_scratch(bg_ctx *c, int *rc) {
 
 int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                     const double2 *d_D, int ldd, double *d_GD, double *d_GX,
-                    int ldf, cudaStream_t st, int sym = 0) {
+                    int ldf, cudaStream_t st, int sym = 0, double *bound = nullptr) {
   if (nq <= 0) return 0;
-  if (c->prec == BG_PREC_DF32) {
+  if (c->prec == BG_PREC_DF32 && !bound) {
     int n = c->ndim;
     if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
     return launch_quartets_df(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, c->d_Ddf, sym);
@@ -1570,6 +1620,7 @@ int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_E; a.D = d_D;
   a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = ldd; a.ldf = ldf;
   a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym;
+  a.bound = bound;
   long long grid = std::min<long long>(nq, 152LL * 64);
   k_quartet<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
@@ -1725,6 +1776,13 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
   return BG_OK;
 }
 
+int bertha_gpu_set_screening(bg_ctx *c, double threshold) {
+  if (!c || !(threshold >= 0.0)) return BG_ERR_ARG;
+  if (threshold != c->screen) c->quart_ilev = -1;  // rebuild the lists
+  c->screen = threshold;
+  return BG_OK;
+}
+
 int bertha_gpu_set_precision(bg_ctx *c, int prec) {
   if (!c) return BG_ERR_ARG;
   if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32) return BG_ERR_ARG;
@@ -1805,6 +1863,10 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
   k_zero2d<<<1024, 256, 0, st>>>(d_gxch, c->ndim, ldf);
   CK(c, cudaGetLastError());
   c->launches += 2;
+  if (c->screen > 0.0 && c->qbound.empty()) {
+    int rc = compute_bounds(c, st);
+    if (rc) return rc;
+  }
   if (c->quart_ilev != ilev) {
     for (int k = 0; k < 4; ++k) {
       if (c->d_quart[k]) cudaFree(c->d_quart[k]);

@@ -74,6 +74,12 @@ int bertha_gpu_init(bg_ctx **ctx, int ncnt, const double *bxyz,
  * reference, which is FP64 throughout. */
 int bertha_gpu_set_precision(bg_ctx *ctx, int prec);
 
+/* Schwarz screening of the Fock build (SCHWARZ/CLMDIAG, bertha-scf.f:37889,
+ * :38126; off by default there, SCHWRZ=.FALSE. :5257).  With threshold > 0,
+ * shell quartets whose bound Q_ab Q_cd, Q = sqrt(max |(ab|ab)|) over labels,
+ * m-signs and component, falls below it are skipped; 0 turns it off. */
+int bertha_gpu_set_screening(bg_ctx *ctx, double threshold);
+
 /* Fock dimension NDIM and small-component offset NSKP (CARDIN :423-430). */
 int bertha_gpu_dims(const bg_ctx *ctx, int *ndim, int *nskp);
 

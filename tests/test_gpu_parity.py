@@ -136,3 +136,26 @@ def test_df32_extreme_exponents():
                          ((0.4, 1.1, -0.7), {0: [1.0e6, 0.08], 1: [0.1]}),
                          ((1.5, -0.3, 0.9), {0: [0.5], 3: [40.0]})], hmlt="DHFR")
     _cmp_df(b, deck.density(b, seed=8), 3)
+
+
+def test_schwarz_screening():
+    """Shell-pair Schwarz screening: at 1e-12 the Fock matrices stay within
+    1e-9 (absolute) of the unscreened oracle; a huge threshold removes every
+    quartet (so the screen is really applied)."""
+    b = deck.make_basis([((0, 0, 0), {0: [0.1, 50.0, 5.0e4], 1: [0.3, 2.0e3]}),
+                         ((0, 0, 6.0), {0: [0.2, 8.0e4], 1: [1.0e3]}),
+                         ((5.0, 1.0, 2.0), {0: [0.15, 3.0e4]})], hmlt="DHFR")
+    dent = deck.density(b, seed=13)
+    rd, rx = orc.clmfast(b, dent, 3)
+    fb = berthagpu.FockBuilder(b)
+    fb.set_screening(1e-12)
+    gd, gx = fb.clmfast(dent, 3)
+    assert np.abs(gd - rd).max() <= 1e-9 and np.abs(gx - rx).max() <= 1e-9
+    fb.set_screening(1e3)
+    gd, gx = fb.clmfast(dent, 3)
+    assert np.abs(gd).max() == 0.0 and np.abs(gx).max() == 0.0
+    fb.set_screening(0.0)
+    gd, gx = fb.clmfast(dent, 3)
+    scale = max(np.abs(rd).max(), np.abs(rx).max())
+    assert np.abs(gd - rd).max() <= TOL * scale
+    fb.close()
