@@ -20,6 +20,8 @@
 //   ERIFAST 12269-13132  first/second contraction, 16 m-sign combinations
 //   CLMMTG 13841 / CLMMTZ 13135  J/K digestion (batch types 1 and 5)
 //   CLMFAST 11489-12266  loop structure, selection rules, stage gating
+//   EQLS 34937, EQSL 35433  sigma-coupled LS/SL E-coefficients
+//   BRTFAST 17060, BIIFAST 18337, BRTMTG 19815 / BRTMTZ 19172  Breit exchange
 //   FOCKIND 2582, CARTIND 2651  index layouts
 
 #include <algorithm>
@@ -327,65 +329,76 @@ void cg_pair(int kqn, int mqn, bool small, double &cu, double &cl) {
   }
 }
 
-// Spinor overlap E-coefficients for one primitive pair (EQLL / EQSS with
-// IQ = 0): E^{TT}(kappa_a, m_a; kappa_b, m_b)_{tuv}.  mqa, mqb are signed 2m.
-// small == false gives LL (degree la+lb), true gives SS (degree la+lb+2).
-HVec eq_pair(int ka, int mqa, double ea, const double *A, int kb, int mqb,
-             double eb, const double *B, bool small) {
+// Radial terms of one component of a G-spinor as (coefficient, power of
+// r^2) multiplying r^l' Y_l': large: (1,0); kinetically balanced small:
+// kappa<0 -> (-2a,0) with l'=l+1; kappa>0 -> (2l+1,0), (-2a,1) with l'=l-1
+// (EQSS bertha-scf.f:36010-36029, EQLS :34990-35000).
+struct RTerm { double c; int n; };
+int radial_terms(int kq, double ex, bool small, RTerm *t, int &lp) {
+  int l = lval(kq);
+  if (!small) { lp = l; t[0] = {1.0, 0}; return 1; }
+  if (kq < 0) { lp = l + 1; t[0] = {-2.0 * ex, 0}; return 1; }
+  lp = l - 1;
+  t[0] = {double(2 * l + 1), 0};
+  t[1] = {-2.0 * ex, 1};
+  return 2;
+}
+
+// Spinor overlap E-coefficients psi_a^+ sigma_q psi_b for one primitive pair
+// (EQLL :34649, EQSS :35928, EQLS :34937, EQSL :35433): components small_a,
+// small_b; iq = 0 (unit), 1 (sigma_x), 2 (sigma_y), 3 (sigma_z).  mqa, mqb
+// are signed 2m.  The small component carries the factor i of the
+// reference (LS x i, SL x -i).  Degree l'_a + l'_b + 2(n_a + n_b).
+HVec eq_pair_q(int ka, int mqa, double ea, const double *A, int kb, int mqb, double eb,
+               const double *B, bool sa, bool sb, int iq) {
   const double SENS = 1.0e-14;
   PairGeom g = pair_geom(ea, A, eb, B);
   int la = lval(ka), lb = lval(kb);
   int NT = ntuv(MAXL);
   HVec E(NT, cplx(0.0));
   double cau, cal, cbu, cbl;
-  cg_pair(ka, mqa, small, cau, cal);
-  cg_pair(kb, mqb, small, cbu, cbl);
-  // radial terms (coefficient, r_A^2 power, r_B^2 power) and the orbital
-  // labels of the spherical harmonics they multiply
-  struct Term { double c; int na, nb; };
-  std::vector<Term> terms;
-  int l1 = la, l2 = lb;
-  if (!small) {
-    terms.push_back({1.0, 0, 0});
-  } else {
-    l1 = (ka < 0) ? la + 1 : la - 1;
-    l2 = (kb < 0) ? lb + 1 : lb - 1;
-    double t22 = 4.0 * ea * eb;
-    double t20 = -2.0 * double(2 * lb + 1) * ea;
-    double t02 = -2.0 * double(2 * la + 1) * eb;
-    double t00 = double((2 * la + 1) * (2 * lb + 1));
-    if (ka < 0 && kb < 0) {
-      terms.push_back({t22, 0, 0});
-    } else if (ka < 0 && kb > 0) {
-      terms.push_back({t20, 0, 0});
-      terms.push_back({t22, 0, 1});
-    } else if (ka > 0 && kb < 0) {
-      terms.push_back({t02, 0, 0});
-      terms.push_back({t22, 1, 0});
-    } else {
-      terms.push_back({t00, 0, 0});
-      terms.push_back({t20, 1, 0});
-      terms.push_back({t02, 0, 1});
-      terms.push_back({t22, 1, 1});
-    }
-  }
-  // spin-up (m-1/2) and spin-down (m+1/2) products
+  cg_pair(ka, mqa, sa, cau, cal);
+  cg_pair(kb, mqb, sb, cbu, cbl);
+  RTerm ta[2], tb[2];
+  int l1, l2;
+  int na = radial_terms(ka, ea, sa, ta, l1), nb = radial_terms(kb, eb, sb, tb, l2);
+  // spin products: (A spin, B spin, weight) per Pauli matrix
+  struct SpinTerm { int ua, ub; double w; };
+  SpinTerm st[2];
+  if (iq == 0) { st[0] = {0, 0, 1.0}; st[1] = {1, 1, 1.0}; }
+  else if (iq == 3) { st[0] = {0, 0, 1.0}; st[1] = {1, 1, -1.0}; }
+  else if (iq == 1) { st[0] = {0, 1, 1.0}; st[1] = {1, 0, 1.0}; }
+  else { st[0] = {0, 1, -1.0}; st[1] = {1, 0, 1.0}; }
+  int deg = 0;
   for (int s = 0; s < 2; ++s) {
-    double cab = (s == 0) ? cau * cbu : cal * cbl;
+    double cab = (st[s].ua == 0 ? cau : cal) * (st[s].ub == 0 ? cbu : cbl);
     if (std::fabs(cab) < SENS) continue;
-    int m1 = (s == 0) ? (mqa - 1) / 2 : (mqa + 1) / 2;
-    int m2 = (s == 0) ? (mqb - 1) / 2 : (mqb + 1) / 2;
-    for (const Term &tm : terms) {
-      HVec es = esgtf(l1, m1, l2, m2, tm.na, tm.nb, g);
-      int deg = l1 + l2 + 2 * (tm.na + tm.nb);
-      for (int k = 0; k < ntuv(deg); ++k) E[k] += (cab * tm.c) * es[k];
-    }
+    int m1 = st[s].ua == 0 ? (mqa - 1) / 2 : (mqa + 1) / 2;
+    int m2 = st[s].ub == 0 ? (mqb - 1) / 2 : (mqb + 1) / 2;
+    for (int i = 0; i < na; ++i)
+      for (int j = 0; j < nb; ++j) {
+        HVec es = esgtf(l1, m1, l2, m2, ta[i].n, tb[j].n, g);
+        int d = l1 + l2 + 2 * (ta[i].n + tb[j].n);
+        deg = std::max(deg, d);
+        double c = st[s].w * cab * ta[i].c * tb[j].c;
+        for (int k = 0; k < ntuv(d); ++k) E[k] += c * es[k];
+      }
   }
-  double nrm = rnorm(ea, la, small) * rnorm(eb, lb, small);
-  int deg = small ? la + lb + 2 : la + lb;
-  HVec out(E.begin(), E.begin() + ntuv(deg));  // exact size, no scratch capacity
-  for (cplx &v : out) v *= nrm;
+  double nrm = rnorm(ea, la, sa) * rnorm(eb, lb, sb);
+  cplx ph(1.0, 0.0);
+  if (sa && !sb) ph = cplx(0.0, -1.0);
+  if (!sa && sb) ph = cplx(0.0, 1.0);
+  if (iq == 2) ph *= cplx(0.0, 1.0);
+  int dmax = la + lb + (sa ? 1 : 0) + (sb ? 1 : 0);
+  HVec out(E.begin(), E.begin() + ntuv(dmax));
+  for (cplx &v : out) v *= nrm * ph;
   return out;
+}
+
+// LL / SS E-coefficients (the Coulomb densities)
+HVec eq_pair(int ka, int mqa, double ea, const double *A, int kb, int mqb,
+             double eb, const double *B, bool small) {
+  return eq_pair_q(ka, mqa, ea, A, kb, mqb, eb, B, small, small, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -769,6 +782,255 @@ void fock_full(const Basis &b, const Opts &o, const Mat &D, Mat &GD, Mat &GX) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Breit / Gaunt interaction (BRTFAST :17060, BIIFAST :18337, BRTMTG :19815,
+// BRTMTZ :19172)
+// ---------------------------------------------------------------------------
+
+// Spinor overlap E-coefficients with sigma_x, sigma_y, sigma_z of all labels
+// of a (centre A, l_a; centre B, l_b) block, one component pair: LS (a large,
+// b small, EQLS x i) or SL (a small, b large, EQSL x -i).  Degree
+// l_a + l_b + 1.  Layout [lab_a][lab_b][set][q][ij][nt] (EILSGN :33644 keeps
+// the same 2 sets x 3 Cartesian components per pair).
+struct EBlockQ {
+  int nlab_a, nlab_b, na, nb, nt;
+  std::vector<Label> la, lb;
+  std::vector<cplx> e;
+  const cplx *at(int ia, int ib, int set, int q, int ij) const {
+    return &e[(((((size_t)ia * nlab_b + ib) * 2 + set) * 3 + q) * (na * nb) + ij) * nt];
+  }
+};
+
+EBlockQ make_eblock_q(const Basis &b, int ca, int lA, int cb, int lB, bool a_small) {
+  EBlockQ E;
+  E.la = labels_for(lA);
+  E.lb = labels_for(lB);
+  E.nlab_a = int(E.la.size());
+  E.nlab_b = int(E.lb.size());
+  const std::vector<double> &xa = b.ex[ca][lA], &xb = b.ex[cb][lB];
+  E.na = int(xa.size());
+  E.nb = int(xb.size());
+  E.nt = ntuv(lA + lB + 1);
+  E.e.assign((size_t)E.nlab_a * E.nlab_b * 2 * 3 * E.na * E.nb * E.nt, cplx(0));
+  const double *A = &b.xyz[3 * ca], *B = &b.xyz[3 * cb];
+  for (int ia = 0; ia < E.nlab_a; ++ia)
+    for (int ib = 0; ib < E.nlab_b; ++ib)
+      for (int set = 0; set < 2; ++set)
+        for (int q = 0; q < 3; ++q) {
+          int mqa = (set == 0 ? -1 : 1) * (2 * E.la[ia].ma - 1);
+          int mqb = -(2 * E.lb[ib].ma - 1);
+          for (int i = 0; i < E.na; ++i)
+            for (int j = 0; j < E.nb; ++j) {
+              HVec h = eq_pair_q(E.la[ia].kq, mqa, xa[i], A, E.lb[ib].kq, mqb, xb[j], B,
+                                 a_small, !a_small, q + 1);
+              cplx *dst = const_cast<cplx *>(E.at(ia, ib, set, q, i * E.nb + j));
+              for (int k = 0; k < E.nt; ++k) dst[k] = h[k];
+            }
+        }
+  return E;
+}
+
+// Breit kernel between Cartesian components i (electron 2, cd) and j
+// (electron 1, ab) at Hermite index N = (t,u,v), from PRE*R-integrals of
+// order |N|+2 (BIIFAST first contraction :18650-18800):
+//   W_ij(N) = BFAC * (delta_ij R_N - T_ij(N)),
+//   T_ij(N) = R_{N+e_i+e_j}/(2 alpha) - R_{N+e_i} PQ_j + N_j R_{N+e_i-e_j},
+// PQ = Q - P, BFAC = -1/2.  Gaunt only: W_ij = -delta_ij R_N.
+void breit_kernel(const double *R, const double *pq, double aph, int t, int u, int v,
+                  bool gaunt, double W[3][3]) {
+  const Cart &C = cart();
+  int N[3] = {t, u, v};
+  double rn = R[C.idx[t][u][v]];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      if (gaunt) {
+        W[i][j] = i == j ? -rn : 0.0;
+        continue;
+      }
+      int a[3] = {N[0], N[1], N[2]};
+      a[i] += 1;
+      a[j] += 1;
+      double t1 = R[C.idx[a[0]][a[1]][a[2]]] * 0.5 / aph;
+      a[j] -= 1;
+      double t2 = R[C.idx[a[0]][a[1]][a[2]]] * pq[j];
+      double t3 = 0.0;
+      a[j] -= 1;
+      if (a[j] >= 0) t3 = R[C.idx[a[0]][a[1]][a[2]]] * double(N[j]);
+      W[i][j] = -0.5 * ((i == j ? rn : 0.0) - (t1 - t2 + t3));
+    }
+}
+
+// BIIFAST for one primitive quartet and one ab label pair: the first
+// contraction G_i(cd tuv), i = x, y, z, for sets 11 and 21.
+// g11/g21: [3][ncd].  Wt: [ntuv(degab+degcd)][3][3] kernel table.
+void bii_first(const EBlockQ &Eab, int ia, int ib, int ij, const std::vector<double> &Wt,
+               int ncd, cplx *g11, cplx *g21) {
+  const Cart &C = cart();
+  int nab = Eab.nt;
+  for (int i = 0; i < 3; ++i)
+    for (int q = 0; q < ncd; ++q) {
+      cplx x(0), y(0);
+      for (int j = 0; j < 3; ++j) {
+        const cplx *e11 = Eab.at(ia, ib, 0, j, ij), *e21 = Eab.at(ia, ib, 1, j, ij);
+        for (int s = 0; s < nab; ++s) {
+          int n = C.idx[C.t[s] + C.t[q]][C.u[s] + C.u[q]][C.v[s] + C.v[q]];
+          double w = Wt[(size_t)n * 9 + 3 * i + j];
+          x += e11[s] * w;
+          y += e21[s] * w;
+        }
+      }
+      g11[i * ncd + q] = x;
+      g21[i * ncd + q] = y;
+    }
+}
+
+// Breit phase of a pair: the Coulomb one negated (BRTFAST :17390).
+inline double phase_breit(int kqa, int ma, int kqb, int mb) {
+  return -phase_pair(kqa, ma, kqb, mb);
+}
+
+// Second contraction summed over the Cartesian component (BIIFAST :18870).
+void bii_second(const cplx *g11, const cplx *g21, const EBlockQ &Ecd, int ic, int id,
+                int kl, int ncd, double pab, double pcd, Eri16 &rr) {
+  for (int s = 0; s < 16; ++s) rr.v[s] = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    Eri16 part;
+    second_contraction(g11 + i * ncd, g21 + i * ncd, Ecd.at(ic, id, 0, i, kl),
+                       Ecd.at(ic, id, 1, i, kl), ncd, pab, pcd, part);
+    for (int s = 0; s < 16; ++s) rr.v[s] += part.v[s];
+  }
+}
+
+// Kernel table for one primitive quartet: PRE*R to order degab+degcd+2, then
+// W for every N up to degab+degcd.
+void bii_table(const double *P, double eij, const double *Q, double ekl, int degab,
+               int degcd, bool gaunt, std::vector<double> &Wt) {
+  int lamn = degab + degcd, lam = lamn + (gaunt ? 0 : 2);
+  double qp[3];
+  for (int x = 0; x < 3; ++x) qp[x] = Q[x] - P[x];
+  double aph = eij * ekl / (eij + ekl);
+  double pre = 2.0 * PI52 / (std::sqrt(eij + ekl) * eij * ekl);
+  std::vector<double> R(ntuv(lam));
+  rints(qp, aph, lam, R.data());
+  for (double &r : R) r *= pre;
+  const Cart &C = cart();
+  Wt.assign((size_t)ntuv(lamn) * 9, 0.0);
+  for (int n = 0; n < ntuv(lamn); ++n) {
+    double W[3][3];
+    breit_kernel(R.data(), qp, aph, C.t[n], C.u[n], C.v[n], gaunt, W);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Wt[(size_t)n * 9 + 3 * i + j] = W[i][j];
+  }
+}
+
+// BRTMTG / BRTMTZ batch type 5 (exchange) for one kl element.
+void digest_x(const Eri16 &rr, const int na[2], const int nb[2], const int nc[2],
+              const int nd[2], const Mat &D, Mat &BX, int isym) {
+  if (isym == 0) {
+    for (int sa = 0; sa < 2; ++sa)
+      for (int sb = 0; sb < 2; ++sb)
+        for (int sc = 0; sc < 2; ++sc)
+          for (int sd = 0; sd < 2; ++sd)
+            BX(na[sa], nd[sd]) += rr.v[8 * sa + 4 * sb + 2 * sc + sd] * D(nc[sc], nb[sb]);
+  } else {
+    for (int s = 0; s < 2; ++s)
+      for (int t = 0; t < 2; ++t)
+        BX(na[s], nd[s]) += rr.v[8 * s + 4 * t + 2 * t + s].real() * D(nc[t], nb[t]).real();
+  }
+}
+
+// Closed-shell multi-centre Breit exchange matrix BXCH (BRTFAST with the
+// direct matrix zero, NOPN = 0).  The reference evaluates only (LS|LS)
+// batches and reaches the other component classes through integral
+// permutation symmetry; this restatement evaluates the classes directly:
+// (LS|LS) -> LS block, (LS|SL) -> LL block, (SL|LS) -> SS block, and fills
+// the SL block by the final conjugation of BRTFAST (:17630):
+// BXCH(J,I) = conj(BXCH(I,J)), I large, J small.
+void breit_full(const Basis &b, const Opts &o, bool gaunt, const Mat &D, Mat &BX) {
+  for (int j = 0; j < b.ndim; ++j)
+    for (int i = 0; i < b.ndim; ++i) BX(i, j) = 0.0;
+  std::deque<EBlockQ> ecache;
+  std::vector<int> ekey;
+  auto eblock = [&](int c1, int l1, int c2, int l2, int sm) -> const EBlockQ & {
+    int key = (((c1 * 16 + l1) * 1024 + c2) * 16 + l2) * 2 + sm;
+    for (size_t i = 0; i < ekey.size(); ++i)
+      if (ekey[i] == key) return ecache[i];
+    ekey.push_back(key);
+    ecache.push_back(make_eblock_q(b, c1, l1, c2, l2, sm != 0));
+    return ecache.back();
+  };
+  const int classes[3][2] = {{0, 0}, {0, 1}, {1, 0}};  // 0 = LS, 1 = SL
+  for (int ca = 0; ca < b.ncnt; ++ca)
+  for (int cb = 0; cb < b.ncnt; ++cb)
+  for (int cc = 0; cc < b.ncnt; ++cc)
+  for (int cd = 0; cd < b.ncnt; ++cd) {
+    int mcnt = ncntrs(ca, cb, cc, cd);
+    if (mcnt == 1 && o.racah1) continue;
+    if (mcnt != 1 && o.ilev < 3) continue;
+    for (int lA = 0; lA <= b.lmax[ca]; ++lA)
+    for (int lB = 0; lB <= b.lmax[cb]; ++lB)
+    for (int lC = 0; lC <= b.lmax[cc]; ++lC)
+    for (int lD = 0; lD <= b.lmax[cd]; ++lD) {
+      if (mcnt == 1 && ((lA + lB) % 2) != ((lC + lD) % 2)) continue;
+      int lq[4] = {lA, lB, lC, lD};
+      for (const auto &cl : classes) {
+        int t1 = cl[0], t2 = cl[1];
+        const EBlockQ &Eab = eblock(ca, lA, cb, lB, t1);
+        const EBlockQ &Ecd = eblock(cc, lC, cd, lD, t2);
+        int degab = lA + lB + 1, degcd = lC + lD + 1, ncd = Ecd.nt;
+        const double *A = &b.xyz[3 * ca], *B = &b.xyz[3 * cb];
+        const double *Cc = &b.xyz[3 * cc], *Dd = &b.xyz[3 * cd];
+        // Fock offsets: LS puts a in the large and b in the small block
+        int oa = t1 ? b.nskp : 0, ob = t1 ? 0 : b.nskp;
+        int oc = t2 ? b.nskp : 0, od = t2 ? 0 : b.nskp;
+        std::vector<double> Wt;
+        std::vector<cplx> g11(3 * ncd), g21(3 * ncd);
+        for (int i = 0; i < Eab.na; ++i)
+        for (int j = 0; j < Eab.nb; ++j) {
+          double ei = b.ex[ca][lA][i], ej = b.ex[cb][lB][j], eij = ei + ej;
+          double P[3];
+          for (int x = 0; x < 3; ++x) P[x] = (A[x] * ei + B[x] * ej) / eij;
+          int ij = i * Eab.nb + j;
+          for (int k = 0; k < Ecd.na; ++k)
+          for (int l = 0; l < Ecd.nb; ++l) {
+            double ek = b.ex[cc][lC][k], el = b.ex[cd][lD][l], ekl = ek + el;
+            double Q[3];
+            for (int x = 0; x < 3; ++x) Q[x] = (Cc[x] * ek + Dd[x] * el) / ekl;
+            bii_table(P, eij, Q, ekl, degab, degcd, gaunt, Wt);
+            int kl = k * Ecd.nb + l;
+            for (int ia = 0; ia < Eab.nlab_a; ++ia)
+            for (int ib = 0; ib < Eab.nlab_b; ++ib) {
+              const Label &LA = Eab.la[ia], &LB = Eab.lb[ib];
+              bii_first(Eab, ia, ib, ij, Wt, ncd, g11.data(), g21.data());
+              int na[2] = {b.lrge[ca][LA.ka][2 * LA.ma - 2] + oa + i,
+                           b.lrge[ca][LA.ka][2 * LA.ma - 1] + oa + i};
+              int nb[2] = {b.lrge[cb][LB.ka][2 * LB.ma - 2] + ob + j,
+                           b.lrge[cb][LB.ka][2 * LB.ma - 1] + ob + j};
+              for (int ic = 0; ic < Ecd.nlab_a; ++ic)
+              for (int id = 0; id < Ecd.nlab_b; ++id) {
+                const Label &LC = Ecd.la[ic], &LD = Ecd.lb[id];
+                Label quad[4] = {LA, LB, LC, LD};
+                if (!label_rules(o, mcnt, quad, lq)) continue;
+                double pab = phase_breit(LA.kq, LA.ma, LB.kq, LB.ma);
+                double pcd = phase_breit(LC.kq, LC.ma, LD.kq, LD.ma);
+                Eri16 rr;
+                bii_second(g11.data(), g21.data(), Ecd, ic, id, kl, ncd, pab, pcd, rr);
+                int nc[2] = {b.lrge[cc][LC.ka][2 * LC.ma - 2] + oc + k,
+                             b.lrge[cc][LC.ka][2 * LC.ma - 1] + oc + k};
+                int nd[2] = {b.lrge[cd][LD.ka][2 * LD.ma - 2] + od + l,
+                             b.lrge[cd][LD.ka][2 * LD.ma - 1] + od + l};
+                digest_x(rr, na, nb, nc, nd, D, BX, o.isym);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  for (int i = 0; i < b.nskp; ++i)
+    for (int j = b.nskp; j < b.ndim; ++j) BX(j, i) = std::conj(BX(i, j));
+}
+
 Basis make_basis(int ncnt, const double *xyz, const int *lmax, const int *nfn,
                  const double *ex, int maxl1, int maxbs, bool norl) {
   Basis b;
@@ -1067,6 +1329,88 @@ int orc_ctx_quartets(void *h, const int *quart, long long n, int t1, int t2,
     orc_one_quartet(o, &quart[4 * i], t1, t2, D, gdl, gxl, atomic);
   }
   return 0;
+}
+
+// Spinor overlap E-coefficients psi_a^+ sigma_q psi_b for any component
+// pair (sa, sb: 0 large, 1 small) and q = 0 (unit), 1..3 (x, y, z).
+int orc_eq_pair_q(int ka, int mqa, double ea, const double *A, int kb, int mqb,
+                  double eb, const double *B, int sa, int sb, int iq, double *out) {
+  HVec h = eq_pair_q(ka, mqa, ea, A, kb, mqb, eb, B, sa != 0, sb != 0, iq);
+  for (size_t k = 0; k < h.size(); ++k) {
+    out[2 * k] = h[k].real();
+    out[2 * k + 1] = h[k].imag();
+  }
+  return int(h.size());
+}
+
+// Breit kernel W_ij at Hermite index (t,u,v) for PQ = qp and exponent alpha
+// with PRE = 1 (R-integrals only); out: 3x3 row-major.
+int orc_breit_kernel(const double *qp, double alpha, int t, int u, int v, int gaunt,
+                     double *out) {
+  int lam = t + u + v + 2;
+  std::vector<double> R(ntuv(lam));
+  rints(qp, alpha, lam, R.data());
+  double W[3][3];
+  breit_kernel(R.data(), qp, alpha, t, u, v, gaunt != 0, W);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) out[3 * i + j] = W[i][j];
+  return 0;
+}
+
+// All Breit (or Gaunt) integrals of one primitive quartet; t1/t2 select LS
+// (0) or SL (1) for the ab and cd pairs.  out as orc_eri_quartet.
+int orc_bii_quartet(const double *xyz4, const int *l4, const double *ex4, int t1, int t2,
+                    int gaunt, double *out) {
+  Basis b;
+  b.ncnt = 4;
+  b.xyz.assign(xyz4, xyz4 + 12);
+  b.lmax.assign(4, 0);
+  b.ex.assign(4, {});
+  for (int c = 0; c < 4; ++c) {
+    b.lmax[c] = l4[c];
+    b.ex[c].assign(l4[c] + 1, {});
+    b.ex[c][l4[c]].push_back(ex4[c]);
+  }
+  EBlockQ Eab = make_eblock_q(b, 0, l4[0], 1, l4[1], t1 != 0);
+  EBlockQ Ecd = make_eblock_q(b, 2, l4[2], 3, l4[3], t2 != 0);
+  double P[3], Q[3];
+  for (int x = 0; x < 3; ++x) {
+    P[x] = (xyz4[x] * ex4[0] + xyz4[3 + x] * ex4[1]) / (ex4[0] + ex4[1]);
+    Q[x] = (xyz4[6 + x] * ex4[2] + xyz4[9 + x] * ex4[3]) / (ex4[2] + ex4[3]);
+  }
+  std::vector<double> Wt;
+  bii_table(P, ex4[0] + ex4[1], Q, ex4[2] + ex4[3], l4[0] + l4[1] + 1, l4[2] + l4[3] + 1,
+            gaunt != 0, Wt);
+  int ncd = Ecd.nt, n = 0;
+  std::vector<cplx> g11(3 * ncd), g21(3 * ncd);
+  for (int ia = 0; ia < Eab.nlab_a; ++ia)
+  for (int ib = 0; ib < Eab.nlab_b; ++ib) {
+    bii_first(Eab, ia, ib, 0, Wt, ncd, g11.data(), g21.data());
+    for (int ic = 0; ic < Ecd.nlab_a; ++ic)
+    for (int id = 0; id < Ecd.nlab_b; ++id) {
+      double pab = phase_breit(Eab.la[ia].kq, Eab.la[ia].ma, Eab.lb[ib].kq, Eab.lb[ib].ma);
+      double pcd = phase_breit(Ecd.la[ic].kq, Ecd.la[ic].ma, Ecd.lb[id].kq, Ecd.lb[id].ma);
+      Eri16 rr;
+      bii_second(g11.data(), g21.data(), Ecd, ic, id, 0, ncd, pab, pcd, rr);
+      for (int s = 0; s < 16; ++s) {
+        out[2 * n] = rr.v[s].real();
+        out[2 * n + 1] = rr.v[s].imag();
+        ++n;
+      }
+    }
+  }
+  return n;
+}
+
+// Closed-shell multi-centre Breit exchange matrix (BRTFAST, NOPN = 0).
+int orc_brtfast(int ncnt, const double *xyz, const int *lmax, const int *nfn,
+                const double *ex, int maxl1, int maxbs, int isym, int ilev, int racah1,
+                int gaunt, const double *dent, int ldd, double *bxch, int ldf) {
+  Basis b = make_basis(ncnt, xyz, lmax, nfn, ex, maxl1, maxbs, false);
+  Opts o{ilev, isym, 2, racah1, 0, 0};
+  Mat D{(cplx *)dent, ldd}, BX{(cplx *)bxch, ldf};
+  breit_full(b, o, gaunt != 0, D, BX);
+  return b.ndim;
 }
 
 int orc_ndim(void *h, int *nskp) {

@@ -34,6 +34,10 @@ def lib():
         L.orc_fock_layout.argtypes = [i, P, P, P, P, i, i, i, P, P]
         L.orc_clmfast.argtypes = [i, P, P, P, P, i, i, i, i, i, i, P, i, P, P, i]
         L.orc_eri_quartet.argtypes = [P, P, P, i, i, P]
+        L.orc_eq_pair_q.argtypes = [i, i, d, P, i, i, d, P, i, i, i, P]
+        L.orc_breit_kernel.argtypes = [P, d, i, i, i, i, P]
+        L.orc_bii_quartet.argtypes = [P, P, P, i, i, i, P]
+        L.orc_brtfast.argtypes = [i, P, P, P, P, i, i, i, i, i, i, P, i, P, i]
         _LIB = L
     return _LIB
 
@@ -72,6 +76,41 @@ def eq_pair(ka, mqa, ea, A, kb, mqb, eb, B, small):
     B = np.ascontiguousarray(B, dtype=np.float64)
     n = lib().orc_eq_pair(ka, mqa, ea, _p(A), kb, mqb, eb, _p(B), int(small), _p(out))
     return out[: 2 * n].view(np.complex128).copy()
+
+
+def eq_pair_q(ka, mqa, ea, A, kb, mqb, eb, B, sa, sb, iq):
+    """psi_a^+ sigma_iq psi_b E-coefficients (iq 0 unit, 1..3 x, y, z) for
+    components sa, sb (0 large, 1 small); LS carries i, SL carries -i."""
+    la = -ka - 1 if ka < 0 else ka
+    lb = -kb - 1 if kb < 0 else kb
+    out = np.zeros(2 * ntuv(la + lb + 2 + 2))
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    n = lib().orc_eq_pair_q(ka, mqa, ea, _p(A), kb, mqb, eb, _p(B), int(sa), int(sb),
+                            int(iq), _p(out))
+    return out[: 2 * n].view(np.complex128).copy()
+
+
+def breit_kernel(qp, alpha, t, u, v, gaunt=False):
+    """3x3 Breit kernel W_ij at Hermite index (t,u,v), PRE = 1."""
+    q = np.ascontiguousarray(qp, dtype=np.float64)
+    out = np.zeros(9)
+    lib().orc_breit_kernel(_p(q), float(alpha), int(t), int(u), int(v), int(gaunt), _p(out))
+    return out.reshape(3, 3)
+
+
+def bii_quartet(xyz4, l4, ex4, t1, t2, gaunt=False):
+    """Breit integrals of one primitive quartet (t = 0 LS, 1 SL), shaped as
+    eri_quartet's result."""
+    xyz4 = np.ascontiguousarray(xyz4, dtype=np.float64)
+    l4 = np.ascontiguousarray(l4, dtype=np.int32)
+    ex4 = np.ascontiguousarray(ex4, dtype=np.float64)
+    nl = [2 * l + 1 for l in l4]
+    out = np.zeros(2 * 16 * int(np.prod(nl)))
+    n = lib().orc_bii_quartet(_p(xyz4), _p(l4), _p(ex4), int(t1), int(t2), int(gaunt),
+                              _p(out))
+    assert n == 16 * int(np.prod(nl))
+    return out.view(np.complex128).reshape(nl + [16])
 
 
 def eri_quartet(xyz4, l4, ex4, t1, t2):
@@ -123,6 +162,19 @@ def clmfast(basis, dent, ilev, racah1=True):
                       int(basis.hmlt), int(basis.isym), int(ilev), int(racah1),
                       _p(D), nd, _p(gd), _p(gx), nd)
     return gd, gx
+
+
+def brtfast(basis, dent, ilev, racah1=True, gaunt=False):
+    """Closed-shell multi-centre Breit exchange matrix BXCH."""
+    xyz, lmax, nfn, ex = _basis_arrays(basis)
+    maxl1, maxbs = ex.shape[1], ex.shape[2]
+    nd = dent.shape[0]
+    D = np.asfortranarray(dent, dtype=np.complex128)
+    bx = np.zeros((nd, nd), dtype=np.complex128, order="F")
+    lib().orc_brtfast(basis.ncnt, _p(xyz), _p(lmax), _p(nfn), _p(ex), maxl1, maxbs,
+                      int(basis.isym), int(ilev), int(racah1), int(gaunt), _p(D), nd,
+                      _p(bx), nd)
+    return bx
 
 
 class QuartetOracle:
