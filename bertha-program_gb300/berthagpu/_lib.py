@@ -12,6 +12,7 @@ BG_OK, BG_ERR_ARG, BG_ERR_CAPACITY, BG_ERR_CUDA, BG_ERR_STATE = 0, 1, 2, 3, 4
 HMLT = {"NORL": 0, "BARE": 1, "DHFR": 2, "DHFP": 3, "DHFB": 4, "DHFQ": 5}
 SHAPE = {"NOSYMM": 0, "PLANAR": 0, "GENERAL": 0, "DIATOM": 1, "LINEAR": 1, "ATOMIC": 2}
 FLAG_NO_RACAH1 = 1
+FLAG_GAUNT = 2
 PREC = {"fp64": 0, "df32": 1}
 MAX_L = 3
 
@@ -40,6 +41,8 @@ def lib():
         L.bertha_gpu_set_screening.argtypes = [P, ctypes.c_double]
         L.bertha_gpu_clmfast.argtypes = [P, P, i, i, P, P, i]
         L.bertha_gpu_clmfast_device.argtypes = [P, P, i, i, P, P, i, P]
+        L.bertha_gpu_brtfast.argtypes = [P, P, i, i, P, i]
+        L.bertha_gpu_brtfast_device.argtypes = [P, P, i, i, P, i, P]
         L.bertha_gpu_quartets.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
         L.bertha_gpu_quartets_noalloc.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
         L.bertha_gpu_shells.argtypes = [P, P, P, P, P]
@@ -57,7 +60,8 @@ def lib():
 EXPORTED = [
     "bertha_gpu_init", "bertha_gpu_set_screening", "bertha_gpu_set_precision",
     "bertha_gpu_dims", "bertha_gpu_clmfast",
-    "bertha_gpu_clmfast_device", "bertha_gpu_quartets", "bertha_gpu_quartets_noalloc",
+    "bertha_gpu_clmfast_device", "bertha_gpu_brtfast", "bertha_gpu_brtfast_device",
+    "bertha_gpu_quartets", "bertha_gpu_quartets_noalloc",
     "bertha_gpu_shells",
     "bertha_gpu_layout", "bertha_gpu_launches", "bertha_gpu_last_error",
     "bertha_gpu_free",

@@ -1,8 +1,9 @@
 """Host mirror of the reference's Fock-build interface for this path.
 
-``FockBuilder`` plays the part of EQSAVE + CLMFAST (bertha-scf.f:5287,
-5401): construction uploads the basis and generates the E-coefficients on
-the GPU; ``clmfast(dent, ilev)`` returns (GDIR, GXCH), overwritten as the
+``FockBuilder`` plays the part of EQSAVE + CLMFAST + BRTFAST
+(bertha-scf.f:5287, 5401, 5441): construction uploads the basis and
+generates the E-coefficients on the GPU; ``clmfast(dent, ilev)`` returns
+(GDIR, GXCH) and ``brtfast(dent, ilev)`` returns BXCH, overwritten as the
 reference does.  Errors raise BerthaGPUError (the reference STOPs).
 """
 import ctypes
@@ -18,7 +19,7 @@ def _p(a):
 
 
 class FockBuilder:
-    def __init__(self, basis, racah1=True):
+    def __init__(self, basis, racah1=True, gaunt=False):
         self.basis = basis
         self._ctx = ctypes.c_void_p()
         xyz = np.ascontiguousarray(basis.xyz, dtype=np.float64)
@@ -26,7 +27,7 @@ class FockBuilder:
         nfn = np.ascontiguousarray(basis.nfn, dtype=np.int32)
         ex = np.ascontiguousarray(basis.ex, dtype=np.float64)
         mel, mbs = nfn.shape[1] - 1, ex.shape[2]
-        flags = 0 if racah1 else _lib.FLAG_NO_RACAH1
+        flags = (0 if racah1 else _lib.FLAG_NO_RACAH1) | (_lib.FLAG_GAUNT if gaunt else 0)
         rc = lib().bertha_gpu_init(ctypes.byref(self._ctx), basis.ncnt, _p(xyz), _p(nkap),
                                    _p(nfn), mel, _p(ex), mbs, int(basis.hmlt),
                                    int(basis.isym), flags)
@@ -85,6 +86,21 @@ class FockBuilder:
         check(lib().bertha_gpu_clmfast(self._ctx, _p(D), n, int(ilev), _p(gd), _p(gx), n),
               self._ctx)
         return gd, gx
+
+    def brtfast(self, dent, ilev):
+        """CALL BRTFAST on host arrays: returns BXCH (closed shell)."""
+        n = self.ndim
+        D = np.asfortranarray(dent, dtype=np.complex128)
+        if D.shape != (n, n):
+            raise BerthaGPUError(_lib.BG_ERR_ARG, f"density shape {D.shape} != ({n},{n})")
+        bx = np.zeros((n, n), dtype=np.complex128, order="F")
+        check(lib().bertha_gpu_brtfast(self._ctx, _p(D), n, int(ilev), _p(bx), n), self._ctx)
+        return bx
+
+    def brtfast_device(self, d_dent, d_bxch, ilev, ld, stream=0):
+        check(lib().bertha_gpu_brtfast_device(self._ctx, ctypes.c_void_p(d_dent), ld, int(ilev),
+                                              ctypes.c_void_p(d_bxch), ld,
+                                              ctypes.c_void_p(stream)), self._ctx)
 
     def clmfast_device(self, d_dent, d_gdir, d_gxch, ilev, ld, stream=0):
         """Device-resident build: pointers are integers (e.g. tensor.data_ptr())."""

@@ -67,19 +67,12 @@ struct PairE {
 };
 
 // complex helpers
-__host__ __device__ inline double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__host__ __device__ inline double2 cmulc(double2 a, double2 b) {  // a*conj(b)
-  return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
-}
 __host__ __device__ inline double2 cadd(double2 a, double2 b) {
   return make_double2(a.x + b.x, a.y + b.y);
 }
 __host__ __device__ inline double2 cscale(double2 a, double s) {
   return make_double2(a.x * s, a.y * s);
 }
-__host__ __device__ inline double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
 
 // ---------------------------------------------------------------------------
 // E-coefficient generation (Saunders recursion of EVRS/ESTEPLM/ESTEPL/ESTEPN)
@@ -192,12 +185,14 @@ __device__ double d_fact(int n) {
   return r;
 }
 
-// acc += c * [Y*_{l1 m1}(r_A) Y_{l2 m2}(r_B) (r_A^2)^na (r_B^2)^nb] (ESGTF)
+// acc += c * [Y*_{l1 m1}(r_A) Y_{l2 m2}(r_B) (r_A^2)^na (r_B^2)^nb] (ESGTF);
+// NA: length of the work arrays (>= ntuv of the result degree)
+template <int NA>
 __device__ void e_esgtf_acc(double2 *acc, double c, int l1, int m1, int l2,
                             int m2, int na, int nb, const Geo &g, double2 *cur,
                             double2 *prev, double2 *nx) {
   if (abs(m1) > l1 || abs(m2) > l2) return;
-  e_zero(cur, NTE);
+  e_zero(cur, NA);
   cur[0] = make_double2(g.rkab, 0.0);
   int L = 0;
   L = e_apply_solid(cur, prev, nx, L, l1, -m1, g.PA, g.PA2, g.p);
@@ -333,7 +328,7 @@ __global__ void k_eqgen(const Shell *sh, int ns, const PairE *pe, int ncomp,
     int m1 = s == 0 ? (mqa - 1) / 2 : (mqa + 1) / 2;
     int m2 = s == 0 ? (mqb - 1) / 2 : (mqb + 1) / 2;
     for (int t = 0; t < nterm; ++t)
-      e_esgtf_acc(acc, cab * tc[t], l1, m1, l2, m2, tna[t], tnb[t], g, cur, prev, nx);
+      e_esgtf_acc<NTE>(acc, cab * tc[t], l1, m1, l2, m2, tna[t], tnb[t], g, cur, prev, nx);
   }
   double nrm = rnorm(A.alpha, la, small) * rnorm(B.alpha, lb, small);
   int nt = ntuv(la + lb + (small ? 2 : 0));
@@ -790,6 +785,384 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
 
 
 // ---------------------------------------------------------------------------
+// Breit / Gaunt interaction (BRTFAST :17060, BIIFAST :18337, BRTMTG :19815,
+// BRTMTZ :19172), FP64.
+// ---------------------------------------------------------------------------
+constexpr int NTB = ntuv(2 * MAXLB + 1);  // E terms of an LS/SL pair (120)
+constexpr int NTW = ntuv(4 * MAXLB + 2);  // Breit kernel entries per quartet (680)
+constexpr int BCHUNK = 4;                 // ab labels per first-contraction pass
+
+// sigma-coupled E-coefficients psi_a^+ sigma_q psi_b, q = x, y, z, for the
+// component pairs LS (comp 0: a large, b small, times i; EQLS :34937) and SL
+// (comp 1: a small, b large, times -i; EQSL :35433), sigma_y carrying the
+// extra factor i of both.  One thread per (pair, comp, lab_a, lab_b, set, q);
+// layout per pair and comp: [lab_a][lab_b][set][q][ntuv(la+lb+1)].
+__global__ void k_eqgen_q(const Shell *sh, int ns, const long long *offq, double2 *E,
+                          long long nwork, const long long *wstart) {
+  long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (w >= nwork) return;
+  int lo = 0, hi = ns * ns * 2 - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) / 2;
+    if (wstart[mid] <= w) lo = mid; else hi = mid - 1;
+  }
+  int pc = lo, comp = pc % 2, pair = pc / 2;
+  const Shell &A = sh[pair / ns], &B = sh[pair % ns];
+  int nlb = 2 * B.l + 1;
+  long long r = w - wstart[pc];
+  int q = int(r % 3);
+  int set = int((r / 3) % 2);
+  int ib = int((r / 6) % nlb), ia = int(r / 6 / nlb);
+  if (ia >= 2 * A.l + 1) return;
+  int ka, ma, kb, mb;
+  label_of(A.l, ia, ka, ma);
+  label_of(B.l, ib, kb, mb);
+  int mqa = (set == 0 ? -1 : 1) * (2 * ma - 1), mqb = -(2 * mb - 1);
+  double Ac[3] = {A.x, A.y, A.z}, Bc[3] = {B.x, B.y, B.z};
+  Geo g;
+  g.p = A.alpha + B.alpha;
+  double ab2 = 0.0;
+  for (int x = 0; x < 3; ++x) {
+    double P = (A.alpha * Ac[x] + B.alpha * Bc[x]) / g.p;
+    g.PA[x] = P - Ac[x];
+    g.PB[x] = P - Bc[x];
+    ab2 += (Ac[x] - Bc[x]) * (Ac[x] - Bc[x]);
+  }
+  g.PA2 = g.PA[0] * g.PA[0] + g.PA[1] * g.PA[1] + g.PA[2] * g.PA[2];
+  g.PB2 = g.PB[0] * g.PB[0] + g.PB[1] * g.PB[1] + g.PB[2] * g.PB[2];
+  g.rkab = exp(-(A.alpha * B.alpha * ab2) / g.p);
+  bool sa = comp == 1, sb = comp == 0;
+  double cau, cal, cbu, cbl;
+  cg_pair(ka, mqa, sa, cau, cal);
+  cg_pair(kb, mqb, sb, cbu, cbl);
+  // radial terms (coefficient, power of r^2) of each component
+  double ca[2], cb[2];
+  int na[2], nb[2], nta, ntb, l1, l2;
+  if (!sa) { l1 = A.l; ca[0] = 1.0; na[0] = 0; nta = 1; }
+  else if (ka < 0) { l1 = A.l + 1; ca[0] = -2.0 * A.alpha; na[0] = 0; nta = 1; }
+  else { l1 = A.l - 1; ca[0] = double(2 * A.l + 1); na[0] = 0; ca[1] = -2.0 * A.alpha; na[1] = 1; nta = 2; }
+  if (!sb) { l2 = B.l; cb[0] = 1.0; nb[0] = 0; ntb = 1; }
+  else if (kb < 0) { l2 = B.l + 1; cb[0] = -2.0 * B.alpha; nb[0] = 0; ntb = 1; }
+  else { l2 = B.l - 1; cb[0] = double(2 * B.l + 1); nb[0] = 0; cb[1] = -2.0 * B.alpha; nb[1] = 1; ntb = 2; }
+  // spin terms: (upper/lower of a, upper/lower of b, weight)
+  int ua[2], ub[2];
+  double wt[2];
+  if (q == 0) { ua[0] = 0; ub[0] = 1; wt[0] = 1.0; ua[1] = 1; ub[1] = 0; wt[1] = 1.0; }
+  else if (q == 1) { ua[0] = 0; ub[0] = 1; wt[0] = -1.0; ua[1] = 1; ub[1] = 0; wt[1] = 1.0; }
+  else { ua[0] = 0; ub[0] = 0; wt[0] = 1.0; ua[1] = 1; ub[1] = 1; wt[1] = -1.0; }
+  double2 acc[NTB], cur[NTB], prev[NTB], nx[NTB];
+  e_zero(acc, NTB);
+  for (int st = 0; st < 2; ++st) {
+    double cab = (ua[st] == 0 ? cau : cal) * (ub[st] == 0 ? cbu : cbl);
+    if (fabs(cab) < 1.0e-14) continue;
+    int m1 = ua[st] == 0 ? (mqa - 1) / 2 : (mqa + 1) / 2;
+    int m2 = ub[st] == 0 ? (mqb - 1) / 2 : (mqb + 1) / 2;
+    for (int i = 0; i < nta; ++i)
+      for (int j = 0; j < ntb; ++j)
+        e_esgtf_acc<NTB>(acc, wt[st] * cab * ca[i] * cb[j], l1, m1, l2, m2, na[i], nb[j], g,
+                         cur, prev, nx);
+  }
+  double nrm = rnorm(A.alpha, A.l, sa) * rnorm(B.alpha, B.l, sb);
+  // i (LS) or -i (SL), times i again for sigma_y
+  double ph = sa ? -1.0 : 1.0;
+  int nt = ntuv(A.l + B.l + 1);
+  double2 *dst = E + offq[(size_t)pair * 2 + comp] + (((long long)(ia * nlb + ib) * 2 + set) * 3 + q) * nt;
+  for (int k = 0; k < nt; ++k) {
+    double2 v = cscale(acc[k], nrm * ph);
+    dst[k] = q == 1 ? make_double2(-v.x, -v.y) : make_double2(-v.y, v.x);
+  }
+}
+
+struct BArgs {
+  const Shell *sh;
+  const long long *offq;
+  const double2 *E;
+  const double2 *D;
+  double *BX;
+  int ns, ldd, ldf, nskp, isym, racah1, gaunt;
+  int dual;  // also digest (cd|ab) = (ab|cd): K(c,b) += (ab|cd) D(a,d)
+};
+
+__device__ inline double2 ldDB(const BArgs &q, int i, int j) {
+  return q.D[(size_t)i + (size_t)q.ldd * j];
+}
+
+size_t breit_smem() {
+  return sizeof(double) * NTW * 9 + sizeof(double2) * (BCHUNK * 2 * 3 * NTB + 2 * MAXSP * MAXSP);
+}
+
+// One CTA per shell quartet of component class (t1|t2), t = 0 LS, 1 SL.
+// R-integrals to order degab+degcd+2, the 3x3 Breit kernel table
+//   W_ij(N) = BFAC (delta_ij R_N - T_ij(N)),
+//   T_ij(N) = R_{N+e_i+e_j}/(2 alpha) - R_{N+e_i} PQ_j + N_j R_{N+e_i-e_j}
+// (BIIFAST :18650-18800; Gaunt: W_ij = -delta_ij R_N), the first contraction
+// G_i = sum_j E_j(ab) W_ij for both E sets, the second contraction summed
+// over i, the 16 m-sign combinations with the Breit phases (Coulomb phases
+// negated, :17390) and the exchange digestion of BRTMTG/BRTMTZ batch type 5.
+__global__ void __launch_bounds__(QTHREADS, 2)
+k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
+  extern __shared__ double smem[];
+  double *W = smem;                          // NTW*9
+  double2 *G = (double2 *)(W + NTW * 9);     // BCHUNK*2*3*NTB
+  double *R = (double *)G;                   // R recursion scratch (aliases G)
+  double *R2 = R + NTR;
+  double2 *Kl = G + BCHUNK * 2 * 3 * NTB;    // MAXSP*MAXSP  K(a,d)
+  double2 *K2 = Kl + MAXSP * MAXSP;          // MAXSP*MAXSP  K(c,b) of (cd|ab)
+  __shared__ double sgeo[10];
+  __shared__ double F[MAXLAM + 2];
+  for (long long qi = blockIdx.x; qi < nq; qi += gridDim.x) {
+    int4 Q4 = quart[qi];
+    const Shell &A = q.sh[Q4.x], &B = q.sh[Q4.y], &C = q.sh[Q4.z], &Dd = q.sh[Q4.w];
+    int la = A.l, lb = B.l, lc = C.l, ld = Dd.l;
+    int degab = la + lb + 1, degcd = lc + ld + 1;
+    int lamn = degab + degcd, lam = lamn + (q.gaunt ? 0 : 2);
+    int nla = 2 * la + 1, nlb = 2 * lb + 1, nlc = 2 * lc + 1, nld = 2 * ld + 1;
+    int nlab = nla * nlb, nlcd = nlc * nld;
+    int nab = ntuv(degab), ncd = ntuv(degcd);
+    int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
+    bool dual = q.dual && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
+    if (threadIdx.x == 0) {
+      double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
+      double Px = (A.alpha * A.x + B.alpha * B.x) / p;
+      double Py = (A.alpha * A.y + B.alpha * B.y) / p;
+      double Pz = (A.alpha * A.z + B.alpha * B.z) / p;
+      double Qx = (C.alpha * C.x + Dd.alpha * Dd.x) / qq;
+      double Qy = (C.alpha * C.y + Dd.alpha * Dd.y) / qq;
+      double Qz = (C.alpha * C.z + Dd.alpha * Dd.z) / qq;
+      double aph = p * qq / (p + qq);
+      double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
+      boys_ref(T, lam, F);
+      sgeo[0] = Px - Qx; sgeo[1] = Py - Qy; sgeo[2] = Pz - Qz;
+      sgeo[3] = -2.0 * aph;
+      sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
+      sgeo[5] = 0.5 / aph;
+      sgeo[6] = Qx - Px; sgeo[7] = Qy - Py; sgeo[8] = Qz - Pz;
+    }
+    __syncthreads();
+    {
+      double X = sgeo[0], Y = sgeo[1], Z = sgeo[2], m2a = sgeo[3];
+      double *cur = R, *nxt = R2;
+      for (int n = lam; n >= 0; --n) {
+        int cnt = ntuv(lam - n);
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+          double val;
+          if (k == 0) {
+            double pw = 1.0;
+            for (int i = 0; i < n; ++i) pw *= m2a;
+            val = pw * F[n];
+          } else {
+            int t = c_t[k], u = c_u[k], v = c_v[k];
+            if (t > 0) {
+              val = X * cur[hidx(t - 1, u, v)];
+              if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
+            } else if (u > 0) {
+              val = Y * cur[hidx(t, u - 1, v)];
+              if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
+            } else {
+              val = Z * cur[hidx(t, u, v - 1)];
+              if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
+            }
+          }
+          nxt[k] = val;
+        }
+        __syncthreads();
+        double *tmp = cur; cur = nxt; nxt = tmp;
+      }
+      // kernel table from PRE*R (cur holds R)
+      double pre = sgeo[4], h2a = sgeo[5];
+      double pq[3] = {sgeo[6], sgeo[7], sgeo[8]};
+      double bfac = q.gaunt ? -1.0 : -0.5;
+      int nw = ntuv(lamn);
+      for (int w = threadIdx.x; w < nw * 9; w += blockDim.x) {
+        int n = w / 9, ij = w % 9, i = ij / 3, j = ij % 3;
+        int N[3] = {c_t[n], c_u[n], c_v[n]};
+        double rn = cur[n] * pre;
+        double val;
+        if (q.gaunt) {
+          val = i == j ? -rn : 0.0;
+        } else {
+          int a[3] = {N[0], N[1], N[2]};
+          a[i] += 1;
+          a[j] += 1;
+          double tt = cur[hidx(a[0], a[1], a[2])] * h2a;
+          a[j] -= 1;
+          tt -= cur[hidx(a[0], a[1], a[2])] * pq[j];
+          a[j] -= 1;
+          if (a[j] >= 0) tt += cur[hidx(a[0], a[1], a[2])] * double(N[j]);
+          val = bfac * ((i == j ? rn : 0.0) - tt * pre);
+        }
+        W[w] = val;
+      }
+    }
+    for (int k = threadIdx.x; k < MAXSP * MAXSP; k += blockDim.x) {
+      Kl[k] = make_double2(0.0, 0.0);
+      K2[k] = make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    const double2 *Eab = q.E + q.offq[((size_t)Q4.x * q.ns + Q4.y) * 2 + t1];
+    const double2 *Ecd = q.E + q.offq[((size_t)Q4.z * q.ns + Q4.w) * 2 + t2];
+    int lq[4] = {la, lb, lc, ld};
+    // Fock offsets: an LS pair has its first function large, second small
+    int oa = t1 ? q.nskp : 0, ob = t1 ? 0 : q.nskp;
+    int oc = t2 ? q.nskp : 0, od = t2 ? 0 : q.nskp;
+    for (int c0 = 0; c0 < nlab; c0 += BCHUNK) {
+      int nch = min(BCHUNK, nlab - c0);
+      // first contraction: G[lab][set][i][q] = Z(q) sum_j sum_s E_j[s] W_ij(s+q)
+      for (int w = threadIdx.x; w < nch * 6 * ncd; w += blockDim.x) {
+        int lab = w / (6 * ncd), rem = w % (6 * ncd);
+        int set = rem / (3 * ncd), i = (rem / ncd) % 3, qq = rem % ncd;
+        const double2 *e = Eab + ((long long)(c0 + lab) * 2 + set) * 3 * nab;
+        int tq = c_t[qq], uq = c_u[qq], vq = c_v[qq];
+        double ax = 0.0, ay = 0.0;
+        for (int s = 0; s < nab; ++s) {
+          const double *wr = W + hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq) * 9 + 3 * i;
+          double2 e0 = e[s], e1 = e[nab + s], e2 = e[2 * nab + s];
+          double w0 = wr[0], w1 = wr[1], w2 = wr[2];
+          ax = fma(e0.x, w0, fma(e1.x, w1, fma(e2.x, w2, ax)));
+          ay = fma(e0.y, w0, fma(e1.y, w1, fma(e2.y, w2, ay)));
+        }
+        unsigned long long zm = ((tq + uq + vq) & 1) ? SGN : 0ULL;
+        G[((lab * 2 + set) * 3 + i) * NTB + qq] = make_double2(flip(ax, zm), flip(ay, zm));
+      }
+      __syncthreads();
+      // second contraction and exchange digestion
+      for (int w = threadIdx.x; w < nch * nlcd; w += blockDim.x) {
+        int lab = w / nlcd, lr = w % nlcd;
+        int ia = (c0 + lab) / nlb, ib = (c0 + lab) % nlb, ic = lr / nld, id = lr % nld;
+        int kq[4], mq[4], mm[4];
+        label_of(la, ia, kq[0], mm[0]);
+        label_of(lb, ib, kq[1], mm[1]);
+        label_of(lc, ic, kq[2], mm[2]);
+        label_of(ld, id, kq[3], mm[3]);
+        for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
+        if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
+        double pab = -pair_phase(kq[0], mm[0], kq[1], mm[1]);
+        double pcd = -pair_phase(kq[2], mm[2], kq[3], mm[3]);
+        double a0 = 0, b0 = 0, c0r = 0, d0 = 0, a1 = 0, b1 = 0, c1 = 0, d1 = 0;
+        double a2 = 0, b2 = 0, c2 = 0, d2 = 0, a3 = 0, b3 = 0, c3 = 0, d3 = 0;
+        for (int i = 0; i < 3; ++i) {
+          const double2 *g11 = G + ((lab * 2 + 0) * 3 + i) * NTB;
+          const double2 *g21 = G + ((lab * 2 + 1) * 3 + i) * NTB;
+          const double2 *e11 = Ecd + (((long long)lr * 2 + 0) * 3 + i) * ncd;
+          const double2 *e21 = Ecd + (((long long)lr * 2 + 1) * 3 + i) * ncd;
+          for (int k = 0; k < ncd; ++k) {
+            double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
+            a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
+            c0r = fma(u1.x, x1.y, c0r); d0 = fma(u1.y, x1.x, d0);
+            a1 = fma(u2.x, x1.x, a1); b1 = fma(u2.y, x1.y, b1);
+            c1 = fma(u2.x, x1.y, c1); d1 = fma(u2.y, x1.x, d1);
+            a2 = fma(u1.x, x2.x, a2); b2 = fma(u1.y, x2.y, b2);
+            c2 = fma(u1.x, x2.y, c2); d2 = fma(u1.y, x2.x, d2);
+            a3 = fma(u2.x, x2.x, a3); b3 = fma(u2.y, x2.y, b3);
+            c3 = fma(u2.x, x2.y, c3); d3 = fma(u2.y, x2.x, d3);
+          }
+        }
+        double2 s1 = {a0 - b0, c0r + d0}, s1c = {a0 + b0, d0 - c0r};
+        double2 s2 = {a1 - b1, c1 + d1}, s2c = {a1 + b1, d1 - c1};
+        double2 s3 = {a2 - b2, c2 + d2}, s3c = {a2 + b2, d2 - c2};
+        double2 s4 = {a3 - b3, c3 + d3}, s4c = {a3 + b3, d3 - c3};
+        unsigned long long ml = smask(pab), mlr = smask(pab * pcd);
+        double2 r[16];
+        r[0] = s1;
+        r[12] = make_double2(flip(s1c.x, ml), flip(s1c.y, ml));
+        r[15] = make_double2(flip(r[0].x, mlr), flip(r[0].y, mlr ^ SGN));
+        r[3] = make_double2(flip(r[12].x, mlr), flip(r[12].y, mlr ^ SGN));
+        r[2] = s2;
+        r[14] = make_double2(flip(s2c.x, ml), flip(s2c.y, ml));
+        r[13] = make_double2(flip(r[2].x, mlr ^ SGN), flip(r[2].y, mlr));
+        r[1] = make_double2(flip(r[14].x, mlr ^ SGN), flip(r[14].y, mlr));
+        r[8] = s3;
+        r[4] = make_double2(flip(s3c.x, ml ^ SGN), flip(s3c.y, ml ^ SGN));
+        r[7] = make_double2(flip(r[8].x, mlr ^ SGN), flip(r[8].y, mlr));
+        r[11] = make_double2(flip(r[4].x, mlr ^ SGN), flip(r[4].y, mlr));
+        r[10] = s4;
+        r[6] = make_double2(flip(s4c.x, ml ^ SGN), flip(s4c.y, ml ^ SGN));
+        r[5] = make_double2(flip(r[10].x, mlr), flip(r[10].y, mlr ^ SGN));
+        r[9] = make_double2(flip(r[6].x, mlr), flip(r[6].y, mlr ^ SGN));
+        int fa[2] = {A.fock[ia][0] + oa, A.fock[ia][1] + oa};
+        int fb[2] = {B.fock[ib][0] + ob, B.fock[ib][1] + ob};
+        int fc[2] = {C.fock[ic][0] + oc, C.fock[ic][1] + oc};
+        int fd[2] = {Dd.fock[id][0] + od, Dd.fock[id][1] + od};
+        if (q.isym == 0) {
+          for (int sa = 0; sa < 2; ++sa)
+            for (int sd = 0; sd < 2; ++sd) {
+              double kx = 0.0, ky = 0.0;
+              for (int sb = 0; sb < 2; ++sb)
+                for (int sc = 0; sc < 2; ++sc) {
+                  double2 v = r[8 * sa + 4 * sb + 2 * sc + sd], d = ldDB(q, fc[sc], fb[sb]);
+                  kx = fma(v.x, d.x, fma(-v.y, d.y, kx));
+                  ky = fma(v.x, d.y, fma(v.y, d.x, ky));
+                }
+              satomic(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], make_double2(kx, ky));
+            }
+          if (dual)
+            for (int sc = 0; sc < 2; ++sc)
+              for (int sb = 0; sb < 2; ++sb) {
+                double kx = 0.0, ky = 0.0;
+                for (int sa = 0; sa < 2; ++sa)
+                  for (int sd = 0; sd < 2; ++sd) {
+                    double2 v = r[8 * sa + 4 * sb + 2 * sc + sd], d = ldDB(q, fa[sa], fd[sd]);
+                    kx = fma(v.x, d.x, fma(-v.y, d.y, kx));
+                    ky = fma(v.x, d.y, fma(v.y, d.x, ky));
+                  }
+                satomic(&K2[(ic * 2 + sc) * MAXSP + ib * 2 + sb], make_double2(kx, ky));
+              }
+        } else {
+          // BRTMTZ: real parts, crossed exchange blocks
+          for (int s = 0; s < 2; ++s) {
+            double kv = 0.0;
+            for (int t = 0; t < 2; ++t)
+              kv = fma(r[8 * s + 4 * t + 2 * t + s].x, ldDB(q, fc[t], fb[t]).x, kv);
+            atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
+          }
+          if (dual)
+            for (int s = 0; s < 2; ++s) {
+              double kv = 0.0;
+              for (int t = 0; t < 2; ++t)
+                kv = fma(r[8 * t + 4 * s + 2 * s + t].x, ldDB(q, fa[t], fd[t]).x, kv);
+              atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
+            }
+        }
+      }
+      __syncthreads();
+    }
+    // flush shared accumulators
+    for (int w = threadIdx.x; w < 2 * nla * 2 * nld; w += blockDim.x) {
+      int a = w / (2 * nld), d = w % (2 * nld);
+      double2 v = Kl[a * MAXSP + d];
+      if (v.x == 0.0 && v.y == 0.0) continue;
+      int fa = A.fock[a >> 1][a & 1] + oa, fdd = Dd.fock[d >> 1][d & 1] + od;
+      double *dst = q.BX + 2 * ((size_t)fa + (size_t)q.ldf * fdd);
+      atomicAdd(dst, v.x);
+      atomicAdd(dst + 1, v.y);
+    }
+    if (dual)
+      for (int w = threadIdx.x; w < 2 * nlc * 2 * nlb; w += blockDim.x) {
+        int cc = w / (2 * nlb), b = w % (2 * nlb);
+        double2 v = K2[cc * MAXSP + b];
+        if (v.x == 0.0 && v.y == 0.0) continue;
+        int fcc = C.fock[cc >> 1][cc & 1] + oc, fbb = B.fock[b >> 1][b & 1] + ob;
+        double *dst = q.BX + 2 * ((size_t)fcc + (size_t)q.ldf * fbb);
+        atomicAdd(dst, v.x);
+        atomicAdd(dst + 1, v.y);
+      }
+    __syncthreads();
+  }
+}
+
+// BXCH(J,I) = conj(BXCH(I,J)) for I in the large and J in the small block
+// (BRTFAST :17630).  One thread per element of the n x n LS block.
+__global__ void k_conj_block(double2 *M, int n, int ld) {
+  long long tot = (long long)n * n;
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < tot;
+       w += (long long)gridDim.x * blockDim.x) {
+    int i = int(w % n), j = int(w / n);
+    double2 v = M[(size_t)i + (size_t)ld * (j + n)];
+    M[(size_t)(j + n) + (size_t)ld * i] = make_double2(v.x, -v.y);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Split-precision (double-float) path.
 // Every FP64 value v is carried as a pair of FP32 words (h, l), v = h + l,
 // |l| <= ulp(h)/2, about 48 significant bits.  Products are formed exactly
@@ -839,24 +1212,6 @@ __device__ inline void df_split(double v, float &h, float &l) {
 }
 
 __device__ inline double df_val(float h, float l) { return (double)h + (double)l; }
-
-// Exact float -> double on the integer pipe (the FP64 pipe is the scarce
-// resource).  FP32 zero and subnormals (|f| < 1.2e-38) map to 0.
-__device__ inline double f2d_int(float f) {
-  unsigned int u = __float_as_uint(f);
-  unsigned int e = (u >> 23) & 0xffu;
-  if (e == 0u) return 0.0;
-  unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
-                            ((unsigned long long)(e + 896u) << 52) |
-                            ((unsigned long long)(u & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
-}
-
-// shared-memory accumulate of a double-float value as its two exact parts
-__device__ inline void satomic_df(double *p, float h, float l) {
-  atomicAdd(p, f2d_int(h));
-  atomicAdd(p, f2d_int(l));
-}
 
 // Double-float copy of the E-coefficients, scaled per pair.
 __global__ void k_econv(const double2 *E, float4 *Edf, const PairE *pe, const Shell *sh,
@@ -1426,6 +1781,16 @@ struct bg_ctx {
   // split-precision copies
   float4 *d_Edf = nullptr, *d_Ddf = nullptr;
   int prec = BG_PREC_FP64;
+  // Breit: sigma-coupled LS/SL E-coefficients (generated on first use) and
+  // quartet lists of the classes (LS|LS) and (LS|SL)
+  int gaunt = 0;
+  double2 *d_EB = nullptr;
+  long long *d_offq = nullptr;
+  long long nEB = 0;
+  int *d_bquart[2] = {nullptr, nullptr};
+  long long nbquart[2] = {0, 0};
+  int bquart_ilev = -1;
+  double2 *d_BX = nullptr;
   long long launches = 0;
   std::string err;
   bool bad = false;
@@ -1628,6 +1993,93 @@ int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   return 0;
 }
 
+// sigma-coupled LS/SL E-coefficients of every ordered shell pair (the
+// EILS/EISL lists of EQSAVE, bertha-scf.f:33644), generated once per context.
+int breit_prepare(bg_ctx *c) {
+  if (c->d_EB) return 0;
+  int ns = c->ns;
+  std::vector<long long> offq((size_t)ns * ns * 2), wstart((size_t)ns * ns * 2 + 1);
+  long long off = 0, work = 0;
+  for (int a = 0; a < ns; ++a)
+    for (int b = 0; b < ns; ++b) {
+      int la = c->shells[a].l, lb = c->shells[b].l;
+      int nl = (2 * la + 1) * (2 * lb + 1);
+      for (int comp = 0; comp < 2; ++comp) {
+        size_t k = ((size_t)a * ns + b) * 2 + comp;
+        offq[k] = off;
+        off += (long long)nl * 6 * ntuv(la + lb + 1);
+        wstart[k] = work;
+        work += (long long)nl * 6;
+      }
+    }
+  wstart[(size_t)ns * ns * 2] = work;
+  long long *d_ws = nullptr;
+  CK(c, cudaMalloc(&c->d_EB, sizeof(double2) * std::max<long long>(off, 1)));
+  CK(c, cudaMalloc(&c->d_offq, sizeof(long long) * offq.size()));
+  CK(c, cudaMalloc(&d_ws, sizeof(long long) * wstart.size()));
+  CK(c, cudaMemcpy(c->d_offq, offq.data(), sizeof(long long) * offq.size(), cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(d_ws, wstart.data(), sizeof(long long) * wstart.size(), cudaMemcpyHostToDevice));
+  if (work > 0) k_eqgen_q<<<(unsigned)((work + 63) / 64), 64>>>(c->d_sh, ns, c->d_offq, c->d_EB, work, d_ws);
+  cudaError_t e = cudaDeviceSynchronize();
+  cudaFree(d_ws);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, "k_eqgen_q");
+  c->nEB = off;
+  return 0;
+}
+
+// Shell quartets of the Breit classes with BRTFAST's centre and stage rules
+// (bertha-scf.f:17262-17275) and the one-centre parity rule (:17330).
+// t2 = 0: (LS|LS), pairs ab >= cd only, each digested for both orders;
+// t2 = 1: (LS|SL), every ordered pair, digested for both orders, which
+// covers the (SL|LS) class.  The (SL|SL) class only feeds the SL block,
+// which BRTFAST overwrites by conjugation of the LS block.
+std::vector<int> build_breit_quartets(const bg_ctx *c, int t2, int ilev) {
+  std::vector<int> out;
+  std::vector<int> byl[MAXLB + 1];
+  for (int s = 0; s < c->ns; ++s) byl[c->shells[s].l].push_back(s);
+  for (int la = MAXLB; la >= 0; --la)
+  for (int lb = MAXLB; lb >= 0; --lb)
+  for (int lc = MAXLB; lc >= 0; --lc)
+  for (int ld = MAXLB; ld >= 0; --ld)
+    for (int a : byl[la])
+    for (int b : byl[lb])
+      for (int cc : byl[lc])
+      for (int d : byl[ld]) {
+        long long pab = (long long)a * c->ns + b, pcd = (long long)cc * c->ns + d;
+        if (t2 == 0 && pab < pcd) continue;
+        int s4[4] = {c->shells[a].cnt, c->shells[b].cnt, c->shells[cc].cnt, c->shells[d].cnt};
+        std::sort(s4, s4 + 4);
+        int mcnt = 1;
+        for (int k = 1; k < 4; ++k) mcnt += s4[k] != s4[k - 1];
+        if (mcnt == 1 && c->racah1) continue;
+        if (mcnt != 1 && ilev < 3) continue;
+        if (mcnt == 1 && ((la + lb) & 1) != ((lc + ld) & 1)) continue;
+        out.push_back(a); out.push_back(b); out.push_back(cc); out.push_back(d);
+      }
+  return out;
+}
+
+int launch_breit(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const double2 *d_D,
+                 int ldd, double *d_BX, int ldf, cudaStream_t st, int dual) {
+  if (nq <= 0) return 0;
+  static bool attr = false;
+  size_t smem = breit_smem();
+  if (!attr) {
+    CK(c, cudaFuncSetAttribute(k_breit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  BArgs a;
+  a.sh = c->d_sh; a.offq = c->d_offq; a.E = c->d_EB; a.D = d_D; a.BX = d_BX;
+  a.ns = c->ns; a.ldd = ldd; a.ldf = ldf; a.nskp = c->nskp; a.isym = c->isym;
+  a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual;
+  long long grid = std::min<long long>(nq, 152LL * 64);
+  k_breit<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  CK(c, cudaGetLastError());
+  c->launches++;
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1650,6 +2102,7 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
   c->hmlt = hmlt;
   c->isym = shape;
   c->racah1 = (flags & BG_FLAG_NO_RACAH1) ? 0 : 1;
+  c->gaunt = (flags & BG_FLAG_GAUNT) ? 1 : 0;
   c->ncomp = (hmlt == BG_HMLT_NORL) ? 1 : 2;
   c->lmax.resize(ncnt);
   int total = 0;
@@ -1920,6 +2373,75 @@ int bertha_gpu_clmfast(bg_ctx *c, const double *dent, int ldd, int ilev, double 
   return BG_OK;
 }
 
+int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev,
+                              double *d_bxch, int ldf, void *stream) {
+  if (!c) return BG_ERR_ARG;
+  if (c->bad) return BG_ERR_STATE;
+  if (ilev < 1 || ilev > 4 || ldd < c->ndim || ldf < c->ndim) return BG_ERR_ARG;
+  if (c->hmlt == BG_HMLT_NORL || c->hmlt == BG_HMLT_BARE) {
+    c->err = "bertha_gpu_brtfast: the Breit interaction needs a four-component Hamiltonian";
+    return BG_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  c->launches = 0;
+  int rc = breit_prepare(c);
+  if (rc) return rc;
+  k_zero2d<<<1024, 256, 0, st>>>(d_bxch, c->ndim, ldf);
+  CK(c, cudaGetLastError());
+  c->launches++;
+  if (c->bquart_ilev != ilev) {
+    for (int k = 0; k < 2; ++k) {
+      if (c->d_bquart[k]) cudaFree(c->d_bquart[k]);
+      c->d_bquart[k] = nullptr;
+      c->nbquart[k] = 0;
+      std::vector<int> q = build_breit_quartets(c, k, ilev);
+      c->nbquart[k] = (long long)q.size() / 4;
+      if (!q.empty()) {
+        CK(c, cudaMalloc(&c->d_bquart[k], sizeof(int) * q.size()));
+        CK(c, cudaMemcpy(c->d_bquart[k], q.data(), sizeof(int) * q.size(), cudaMemcpyHostToDevice));
+      }
+    }
+    c->bquart_ilev = ilev;
+  }
+  for (int k = 0; k < 2; ++k) {
+    rc = launch_breit(c, c->d_bquart[k], c->nbquart[k], 0, k, (const double2 *)d_dent, ldd,
+                      d_bxch, ldf, st, 1);
+    if (rc) return rc;
+  }
+  int n = c->nskp;
+  k_conj_block<<<1024, 256, 0, st>>>((double2 *)d_bxch, n, ldf);
+  CK(c, cudaGetLastError());
+  c->launches++;
+  return BG_OK;
+}
+
+int bertha_gpu_brtfast(bg_ctx *c, const double *dent, int ldd, int ilev, double *bxch,
+                       int ldf) {
+  if (!c || !dent || !bxch) return BG_ERR_ARG;
+  if (c->bad) return BG_ERR_STATE;
+  if (ilev < 1 || ilev > 4 || ldd < c->ndim || ldf < c->ndim) return BG_ERR_ARG;
+  if (c->hmlt == BG_HMLT_NORL || c->hmlt == BG_HMLT_BARE) {
+    c->err = "bertha_gpu_brtfast: the Breit interaction needs a four-component Hamiltonian";
+    return BG_ERR_ARG;
+  }
+  int n = c->ndim;
+  size_t bytes = sizeof(double2) * (size_t)n * n;
+  if (!c->d_D) {
+    CK(c, cudaMalloc(&c->d_D, bytes));
+    CK(c, cudaMalloc(&c->d_GD, bytes));
+    CK(c, cudaMalloc(&c->d_GX, bytes));
+  }
+  if (!c->d_BX) CK(c, cudaMalloc(&c->d_BX, bytes));
+  CK(c, cudaMemcpy2D(c->d_D, sizeof(double2) * n, dent, sizeof(double2) * ldd,
+                     sizeof(double2) * n, n, cudaMemcpyHostToDevice));
+  int rc = bertha_gpu_brtfast_device(c, (const double *)c->d_D, n, ilev, (double *)c->d_BX, n,
+                                     nullptr);
+  if (rc) return rc;
+  CK(c, cudaMemcpy2D(bxch, sizeof(double2) * ldf, c->d_BX, sizeof(double2) * n,
+                     sizeof(double2) * n, n, cudaMemcpyDeviceToHost));
+  return BG_OK;
+}
+
 void bertha_gpu_free(bg_ctx *c) {
   if (!c) return;
   cudaFree(c->d_sh);
@@ -1931,6 +2453,10 @@ void bertha_gpu_free(bg_ctx *c) {
   cudaFree(c->d_D);
   cudaFree(c->d_GD);
   cudaFree(c->d_GX);
+  cudaFree(c->d_EB);
+  cudaFree(c->d_offq);
+  for (int k = 0; k < 2; ++k) cudaFree(c->d_bquart[k]);
+  cudaFree(c->d_BX);
   delete c;
 }
 

@@ -1,16 +1,17 @@
 /*
  * bertha_gpu.h - C ABI of the GB300 (sm_103a) Dirac-Coulomb Fock build.
  *
- * Drop-in for the reference's multi-centre Coulomb Fock build:
+ * Drop-in for the reference's multi-centre Coulomb and Breit Fock builds:
  *   CALL EQSAVE   (bertha-scf.f:5287)  -> bertha_gpu_init
  *   CALL CLMFAST  (bertha-scf.f:5401)  -> bertha_gpu_clmfast
+ *   CALL BRTFAST  (bertha-scf.f:5441)  -> bertha_gpu_brtfast
  * The reference passes everything through COMMON blocks; here the same
  * arrays are passed explicitly, with their Fortran (column-major) layout and
  * leading dimensions, so a Fortran caller binds them with ISO_C_BINDING
  * (see INTEGRATION.md):
  *   /BSET/ BXYZ(3,MCT), NKAP(MCT), NFNC(0:MEL,MCT), BEXL(MBS,0:MEL,MCT)
  *   /DENS/ DENT(MDM,MDM)            COMPLEX*16
- *   /MTRX/ GDIR(MDM,MDM), GXCH(MDM,MDM)   COMPLEX*16
+ *   /MTRX/ GDIR(MDM,MDM), GXCH(MDM,MDM), BXCH(MDM,MDM)   COMPLEX*16
  * Complex arrays are interleaved (re, im) doubles.  Every entry point
  * returns 0 on success or a BG_ERR_* code; none calls exit().
  * A context is used by one host thread at a time.
@@ -43,6 +44,7 @@ extern "C" {
 
 /* init flags */
 #define BG_FLAG_NO_RACAH1 1 /* include one-centre quartets (RACAH1=.FALSE.) */
+#define BG_FLAG_GAUNT 2     /* Gaunt term only in the Breit build (GAUNT2) */
 
 /* precision of the two-electron contraction */
 #define BG_PREC_FP64 0 /* all FP64: the drop-in path */
@@ -99,6 +101,25 @@ int bertha_gpu_clmfast(bg_ctx *ctx, const double *dent, int ldd, int ilev,
 int bertha_gpu_clmfast_device(bg_ctx *ctx, const double *d_dent, int ldd,
                               int ilev, double *d_gdir, double *d_gxch,
                               int ldf, void *stream);
+
+/* Closed-shell multi-centre Breit exchange matrix, replacing CALL BRTFAST
+ * (bertha-scf.f:17060-17645; BIIFAST :18337, BRTMTG :19815, BRTMTZ :19172).
+ *   dent[ldd*ndim]  total density DENT
+ *   ilev            ILEV: multi-centre quartets from stage 3 on (:17272)
+ *   bxch[ldf*ndim]  output BXCH, overwritten
+ * Full Breit interaction -1/2 [a1.a2/r12 + (a1.r12)(a2.r12)/r12^3], or the
+ * Gaunt term -a1.a2/r12 alone when the context was made with BG_FLAG_GAUNT.
+ * BDIR is zero for closed shells and not produced.  The SL block is the
+ * conjugate transpose of the LS block, as BRTFAST completes it.  Needs a
+ * four-component Hamiltonian (BG_ERR_ARG for NORL and BARE); the reference
+ * calls it for DHFB and DHFQ.  The first call generates the sigma-coupled
+ * LS/SL E-coefficients (EILS/EISL of EQSAVE). */
+int bertha_gpu_brtfast(bg_ctx *ctx, const double *dent, int ldd, int ilev,
+                       double *bxch, int ldf);
+
+/* Same build on device-resident arrays, stream-ordered on `stream`. */
+int bertha_gpu_brtfast_device(bg_ctx *ctx, const double *d_dent, int ldd,
+                              int ilev, double *d_bxch, int ldf, void *stream);
 
 /* Fock-build digestion over an explicit list of ordered shell quartets
  * (device array, 4 ints each: shell a, b, c, d as numbered by
