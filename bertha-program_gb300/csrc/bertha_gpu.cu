@@ -551,8 +551,10 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
     int lq[4] = {la, lb, lc, ld};
     int oab = t1 ? q.nskp : 0, ocd = t2 ? q.nskp : 0;
     __syncthreads();
-    for (int c0 = 0; c0 < nlL; c0 += CHUNK) {
-      int nch = min(CHUNK, nlL - c0);
+    // left labels per pass: as many as the G buffer holds at this degree
+    int chunk = max(1, (CHUNK * 2 * NTE) / (2 * nR));
+    for (int c0 = 0; c0 < nlL; c0 += chunk) {
+      int nch = min(chunk, nlL - c0);
       // first contraction: G[lab][set][q] = Z(q) sum_s E_L[lab][set][s] R[s+q]
       for (int w = threadIdx.x; w < nch * 2 * nR; w += blockDim.x) {
         int lab = w / (2 * nR), rem = w % (2 * nR);
@@ -567,7 +569,7 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
           ay = fma(ev.y, rv, ay);
         }
         unsigned long long zm = ((tq + uq + vq) & 1) ? SGN : 0ULL;
-        G[(lab * 2 + set) * NTE + qq] = make_double2(flip(ax, zm), flip(ay, zm));
+        G[(lab * 2 + set) * nR + qq] = make_double2(flip(ax, zm), flip(ay, zm));
       }
       __syncthreads();
       // second contraction and digestion
@@ -586,7 +588,7 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
         double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
         double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
-        const double2 *g11 = G + (lab * 2 + 0) * NTE, *g21 = G + (lab * 2 + 1) * NTE;
+        const double2 *g11 = G + (lab * 2 + 0) * nR, *g21 = G + (lab * 2 + 1) * nR;
         const double2 *e11 = ER + ((long long)lr * 2 + 0) * nR;
         const double2 *e21 = ER + ((long long)lr * 2 + 1) * nR;
         // four complex products (E_R set) x (G set), kept as real partials
@@ -790,7 +792,7 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
 // ---------------------------------------------------------------------------
 constexpr int NTB = ntuv(2 * MAXLB + 1);  // E terms of an LS/SL pair (120)
 constexpr int NTW = ntuv(4 * MAXLB + 2);  // Breit kernel entries per quartet (680)
-constexpr int BCHUNK = 4;                 // ab labels per first-contraction pass
+constexpr int BCHUNK = 4;                 // ab labels per pass at the largest cd degree
 
 // sigma-coupled E-coefficients psi_a^+ sigma_q psi_b, q = x, y, z, for the
 // component pairs LS (comp 0: a large, b small, times i; EQLS :34937) and SL
@@ -1005,8 +1007,11 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
     // Fock offsets: an LS pair has its first function large, second small
     int oa = t1 ? q.nskp : 0, ob = t1 ? 0 : q.nskp;
     int oc = t2 ? q.nskp : 0, od = t2 ? 0 : q.nskp;
-    for (int c0 = 0; c0 < nlab; c0 += BCHUNK) {
-      int nch = min(BCHUNK, nlab - c0);
+    // as many ab labels per pass as the G buffer holds (fewer barriers and
+    // idle threads for low angular momenta)
+    int chunk = max(1, (BCHUNK * 2 * 3 * NTB) / (6 * ncd));
+    for (int c0 = 0; c0 < nlab; c0 += chunk) {
+      int nch = min(chunk, nlab - c0);
       // first contraction: G[lab][set][i][q] = Z(q) sum_j sum_s E_j[s] W_ij(s+q)
       for (int w = threadIdx.x; w < nch * 6 * ncd; w += blockDim.x) {
         int lab = w / (6 * ncd), rem = w % (6 * ncd);
@@ -1022,7 +1027,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
           ay = fma(e0.y, w0, fma(e1.y, w1, fma(e2.y, w2, ay)));
         }
         unsigned long long zm = ((tq + uq + vq) & 1) ? SGN : 0ULL;
-        G[((lab * 2 + set) * 3 + i) * NTB + qq] = make_double2(flip(ax, zm), flip(ay, zm));
+        G[((lab * 2 + set) * 3 + i) * ncd + qq] = make_double2(flip(ax, zm), flip(ay, zm));
       }
       __syncthreads();
       // second contraction and exchange digestion
@@ -1041,8 +1046,8 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
         double a0 = 0, b0 = 0, c0r = 0, d0 = 0, a1 = 0, b1 = 0, c1 = 0, d1 = 0;
         double a2 = 0, b2 = 0, c2 = 0, d2 = 0, a3 = 0, b3 = 0, c3 = 0, d3 = 0;
         for (int i = 0; i < 3; ++i) {
-          const double2 *g11 = G + ((lab * 2 + 0) * 3 + i) * NTB;
-          const double2 *g21 = G + ((lab * 2 + 1) * 3 + i) * NTB;
+          const double2 *g11 = G + ((lab * 2 + 0) * 3 + i) * ncd;
+          const double2 *g21 = G + ((lab * 2 + 1) * 3 + i) * ncd;
           const double2 *e11 = Ecd + (((long long)lr * 2 + 0) * 3 + i) * ncd;
           const double2 *e21 = Ecd + (((long long)lr * 2 + 1) * 3 + i) * ncd;
           for (int k = 0; k < ncd; ++k) {
@@ -1311,7 +1316,14 @@ __device__ void boys_block(double T, int lam, double *F) {
 
 constexpr int CHDF = 2;  // left labels per first-contraction pass (df path)
 constexpr int DFTHREADS = 128;  // 4 quartets in flight per SM
-constexpr int NCB = CHDF * MAXLAB * MAXLAB * 16;  // contribution buffer (float4)
+constexpr int NCB = CHDF * MAXLAB * MAXLAB * 16;  // contribution buffer (float4), with sym
+
+// doubles at the start of the df kernel's shared memory: R (FP64) or the
+// contribution buffer, whichever is larger (even, so what follows stays
+// 16-byte aligned)
+__host__ __device__ constexpr int df_region0(int sym) {
+  return (sym ? NCB : NCB / 2) * 2 > NTR ? (sym ? NCB : NCB / 2) * 2 : NTR + 1;
+}
 
 struct QArgsDF {
   const Shell *sh;
@@ -1361,17 +1373,22 @@ __device__ inline float4 rv_sign(const float4 (&sv)[8], int sa, int sb, int sc, 
 
 __global__ void __launch_bounds__(DFTHREADS, 4)
 k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
+  // Shared memory (sizes in df_smem_layout): the FP64 R-integrals are dead
+  // once their double-float copy Rf exists, so the contribution buffer Cb
+  // (J, K and, with sym, J2, K2: 4 targets each per label quartet) shares
+  // their space; R2, the recursion's second buffer, shares Rf's.
   extern __shared__ double smem[];
+  const int r0d = df_region0(q.sym);
   double *R = smem;                            // NTR (FP64)
-  float2 *Rf = (float2 *)(R + NTR);            // NTR (df)
+  float4 *Cb = (float4 *)smem;                 // CHDF*MAXLAB^2*(8 or 16)
+  float2 *Rf = (float2 *)(smem + r0d);         // NTR (df), padded to NTR+1 doubles
   double *R2 = (double *)Rf;                   // FP64 recursion buffer (aliases Rf)
-  double *F = R + 2 * NTR;                     // MAXLAM+2
+  double *F = smem + r0d + NTR + 1;            // MAXLAM+2
   float4 *EL = (float4 *)(F + MAXLAM + 2);     // CHDF*2*NTE
   float4 *G = EL + CHDF * 2 * NTE;             // CHDF*2*NTE
-  float4 *Cb = G + CHDF * 2 * NTE;             // NCB: J, K, J2, K2 (4 each) per label quartet
-  double2 *Jl = (double2 *)(Cb + NCB);         // MAXSP*MAXSP
+  double2 *Jl = (double2 *)(G + CHDF * 2 * NTE);  // MAXSP*MAXSP
   double2 *Kl = Jl + MAXSP * MAXSP;
-  double2 *J2 = Kl + MAXSP * MAXSP;
+  double2 *J2 = Kl + MAXSP * MAXSP;            // with sym only
   double2 *K2 = J2 + MAXSP * MAXSP;
   __shared__ double sgeo[8];
   __shared__ int sk;
@@ -1455,9 +1472,12 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
     for (int i = threadIdx.x; i < MAXSP * MAXSP; i += blockDim.x) {
       Jl[i] = make_double2(0.0, 0.0);
       Kl[i] = make_double2(0.0, 0.0);
-      J2[i] = make_double2(0.0, 0.0);
-      K2[i] = make_double2(0.0, 0.0);
+      if (q.sym) {
+        J2[i] = make_double2(0.0, 0.0);
+        K2[i] = make_double2(0.0, 0.0);
+      }
     }
+    __syncthreads();  // R is dead from here on: Cb may overwrite it
     bool dual = q.sym && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
     int ntg = dual ? 16 : 8;
     const float4 *Eab = q.E + pab_e.off[t1];
@@ -1554,7 +1574,7 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
             }
           }
           if (!valid) continue;
-          float4 *cb = Cb + (size_t)(lab * nlR + lr) * 16;
+          float4 *cb = Cb + (size_t)(lab * nlR + lr) * ntg;
           if (!active) {
             for (int tg = part; tg < ntg; tg += KS) cb[tg] = make_float4(0.f, 0.f, 0.f, 0.f);
             continue;
@@ -1636,45 +1656,52 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
       __syncthreads();
       // phase B: one thread per J or K target sums the chunk's contributions
       // in double-float and adds the FP64 value to the shared accumulator.
-      // Families: 0 J(ia,ib), 1 K(ia,id), 2 J(ic,id), 3 K(ic,ib).
+      // Families: 0 J(ia,ib), 1 K(ia,id), 2 J(ic,id), 3 K(ic,ib).  Only
+      // targets that this chunk's left labels can reach are enumerated: an
+      // index of the left pair ranges over the chunk's values, the others
+      // over all labels.
       {
         int nfam = dual ? 4 : 2;
-        int nx[4] = {nla, nla, nlc, nlc}, ny[4] = {nlb, nld, nld, nlb};
-        int tot = 0, start[5];
-        for (int f = 0; f < 4; ++f) { start[f] = tot; if (f < nfam) tot += nx[f] * ny[f] * 4; }
+        int l1lo = c0 / nl2L, l1hi = (c0 + nch - 1) / nl2L;
+        int l2lo = 0, l2hi = nl2L - 1;
+        if (l1lo == l1hi) { l2lo = c0 % nl2L; l2hi = (c0 + nch - 1) % nl2L; }
+        // label ranges of the roles a, b, c, d
+        int rlo[4] = {0, 0, 0, 0}, rhi[4] = {nla - 1, nlb - 1, nlc - 1, nld - 1};
+        int r1 = swp ? 2 : 0;
+        rlo[r1] = l1lo; rhi[r1] = l1hi;
+        rlo[r1 + 1] = l2lo; rhi[r1 + 1] = l2hi;
+        const int fx[4] = {0, 0, 2, 2}, fy[4] = {1, 3, 3, 1};
+        int tot = 0, start[5], ny[4];
+        for (int f = 0; f < 4; ++f) {
+          start[f] = tot;
+          ny[f] = rhi[fy[f]] - rlo[fy[f]] + 1;
+          if (f < nfam) tot += (rhi[fx[f]] - rlo[fx[f]] + 1) * ny[f] * 4;
+        }
         start[4] = tot;
         for (int w = threadIdx.x; w < tot; w += blockDim.x) {
           int f = 0;
           while (w >= start[f + 1]) ++f;
           int u = w - start[f], sig = u & 3, tgt = u >> 2;
-          int X = tgt / ny[f], Y = tgt % ny[f];
+          int X = rlo[fx[f]] + tgt / ny[f], Y = rlo[fy[f]] + tgt % ny[f];
           float sh_r = 0.f, sl_r = 0.f, sh_i = 0.f, sl_i = 0.f;
           int cnt = 0;
+          int fix[4] = {-1, -1, -1, -1};
+          fix[fx[f]] = X;
+          fix[fy[f]] = Y;
           // the left label is (l1,l2) = (ia,ib) or, swapped, (ic,id); the
-          // right label likewise; each family fixes one index on each side
-          // or two on one side
+          // right label likewise
+          int fl1 = fix[r1], fl2 = fix[r1 + 1];
+          int fr1 = fix[2 - r1], fr2 = fix[3 - r1];
+          int q1lo = 0, q1hi = nlR / nl2R, q2lo = 0, q2hi = nl2R;
+          if (fr1 >= 0) { q1lo = fr1; q1hi = fr1 + 1; }
+          if (fr2 >= 0) { q2lo = fr2; q2hi = fr2 + 1; }
           for (int lab = 0; lab < nch; ++lab) {
             int labL = c0 + lab;
             int l1 = labL / nl2L, l2 = labL % nl2L;
-            int Lia = swp ? -1 : l1, Lib = swp ? -1 : l2, Lic = swp ? l1 : -1, Lid = swp ? l2 : -1;
-            // constraint of this family on the left label
-            bool okL;
-            int fix_a = -1, fix_b = -1, fix_c = -1, fix_d = -1;
-            if (f == 0) { fix_a = X; fix_b = Y; }
-            else if (f == 1) { fix_a = X; fix_d = Y; }
-            else if (f == 2) { fix_c = X; fix_d = Y; }
-            else { fix_c = X; fix_b = Y; }
-            okL = (Lia < 0 || fix_a < 0 || Lia == fix_a) && (Lib < 0 || fix_b < 0 || Lib == fix_b) &&
-                  (Lic < 0 || fix_c < 0 || Lic == fix_c) && (Lid < 0 || fix_d < 0 || Lid == fix_d);
-            if (!okL) continue;
-            // right labels matching the remaining constraints
-            int r1lo = 0, r1hi = nlR / nl2R, r2lo = 0, r2hi = nl2R;
-            int fr1 = swp ? fix_a : fix_c, fr2 = swp ? fix_b : fix_d;
-            if (fr1 >= 0) { r1lo = fr1; r1hi = fr1 + 1; }
-            if (fr2 >= 0) { r2lo = fr2; r2hi = fr2 + 1; }
-            for (int r1 = r1lo; r1 < r1hi; ++r1)
-              for (int r2 = r2lo; r2 < r2hi; ++r2) {
-                float4 v = Cb[(size_t)(lab * nlR + r1 * nl2R + r2) * 16 + 4 * f + sig];
+            if ((fl1 >= 0 && l1 != fl1) || (fl2 >= 0 && l2 != fl2)) continue;
+            for (int q1 = q1lo; q1 < q1hi; ++q1)
+              for (int q2 = q2lo; q2 < q2hi; ++q2) {
+                float4 v = Cb[(size_t)(lab * nlR + q1 * nl2R + q2) * ntg + 4 * f + sig];
                 df_add(sh_r, sl_r, v.x, v.y, sh_r, sl_r);
                 df_add(sh_i, sl_i, v.z, v.w, sh_i, sl_i);
                 ++cnt;
@@ -1747,9 +1774,9 @@ __global__ void k_zero2d(double *a, int n, int ld) {
   }
 }
 
-size_t quartet_smem_df() {
-  return sizeof(double) * (2 * NTR + MAXLAM + 2) + sizeof(float4) * (2 * CHDF * 2 * NTE + NCB) +
-         sizeof(double2) * (4 * MAXSP * MAXSP);
+size_t quartet_smem_df(int sym) {
+  return sizeof(double) * (df_region0(sym) + NTR + 1 + MAXLAM + 2) +
+         sizeof(float4) * (2 * CHDF * 2 * NTE) + sizeof(double2) * ((sym ? 4 : 2) * MAXSP * MAXSP);
 }
 
 size_t quartet_smem() {
@@ -1924,9 +1951,10 @@ int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                        cudaStream_t st, float4 *ddf, int sym = 0) {
   if (nq <= 0) return 0;
   static bool attr_df = false;
-  size_t smem = quartet_smem_df();
+  size_t smem = quartet_smem_df(sym ? 1 : 0);
   if (!attr_df) {
-    CK(c, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(c, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)quartet_smem_df(1)));
     attr_df = true;
   }
   int n = c->ndim;
