@@ -75,8 +75,52 @@ def quartet_flops(basis, quart, t1, t2):
     lam = degab + degcd
     pab = (2 * la + 1) * (2 * lb + 1)
     pcd = (2 * lc + 1) * (2 * ld + 1)
-    fr = 6 * sum(nt(k) for k in range(0, 1))  # placeholder, replaced below
     fr = 6 * np.array([sum(nt(k) for k in range(int(L) + 1)) for L in lam])
     f1 = 2 * (4 * pab) * nt(degab) * nt(degcd)
     f2 = 2 * (4 * pab) * (4 * pcd) * nt(degcd)
+    return float(np.sum(fr + f1 + f2))
+
+
+def breit_quartets(basis, ilev=3, racah1=True):
+    """Shell quartets of the Breit build as the library lists them
+    (BRTFAST centre and stage rules): (LS|LS) with pair index ab >= cd and
+    (LS|SL) over every ordered pair; returns the two int32 [n, 4] arrays."""
+    sh = basis.shells()
+    cnt = np.array([s[0] for s in sh])
+    l = np.array([s[1] for s in sh])
+    ns = len(sh)
+    a, b, c, d = (x.ravel() for x in np.meshgrid(*(np.arange(ns),) * 4, indexing="ij"))
+    cen = np.sort(np.stack([cnt[a], cnt[b], cnt[c], cnt[d]], 1), 1)
+    mcnt = 1 + (np.diff(cen, axis=1) != 0).sum(1)
+    keep = np.ones(a.shape, bool)
+    if racah1:
+        keep &= mcnt != 1
+    if ilev < 3:
+        keep &= mcnt == 1
+    keep &= (mcnt != 1) | (((l[a] + l[b]) & 1) == ((l[c] + l[d]) & 1))
+    pab, pcd = a * ns + b, c * ns + d
+    q = np.stack([a, b, c, d], 1).astype(np.int32)
+    return q[keep & (pab >= pcd)], q[keep]
+
+
+def breit_flops(basis, quart, gaunt=False):
+    """Algorithmic FP64 flops of a Breit quartet list: R to order
+    Lambda_ab+Lambda_cd+2 (6 per entry), first contraction over three
+    Cartesian components of each electron 2*(4P_ab)*N_ab*N_cd*9 (3 for Gaunt)
+    and second contraction 2*(4P_ab)*(4P_cd)*N_cd*3, N of degree la+lb+1."""
+    sh = basis.shells()
+    l = np.array([s[1] for s in sh])
+    la, lb, lc, ld = (l[quart[:, j]] for j in range(4))
+
+    def nt(L):
+        return (L + 1) * (L + 2) * (L + 3) // 6
+
+    degab, degcd = la + lb + 1, lc + ld + 1
+    lam = degab + degcd + (0 if gaunt else 2)
+    pab = (2 * la + 1) * (2 * lb + 1)
+    pcd = (2 * lc + 1) * (2 * ld + 1)
+    cum = np.cumsum([nt(k) for k in range(40)])
+    fr = 6 * cum[lam]
+    f1 = 2 * (4 * pab) * nt(degab) * nt(degcd) * (3 if gaunt else 9)
+    f2 = 2 * (4 * pab) * (4 * pcd) * nt(degcd) * 3
     return float(np.sum(fr + f1 + f2))
