@@ -897,10 +897,10 @@ size_t breit_smem() {
 // R-integrals to order degab+degcd+2, the 3x3 Breit kernel table
 //   W_ij(N) = BFAC (delta_ij R_N - T_ij(N)),
 //   T_ij(N) = R_{N+e_i+e_j}/(2 alpha) - R_{N+e_i} PQ_j + N_j R_{N+e_i-e_j}
-// (BIIFAST :18650-18800; Gaunt: W_ij = -delta_ij R_N), the first contraction
+// (BIIFAST :18655-18880; Gaunt: W_ij = -delta_ij R_N), the first contraction
 // G_i = sum_j E_j(ab) W_ij for both E sets, the second contraction summed
 // over i, the 16 m-sign combinations with the Breit phases (Coulomb phases
-// negated, :17390) and the exchange digestion of BRTMTG/BRTMTZ batch type 5.
+// negated, :17528-17533 and :18899) and the exchange digestion of BRTMTG/BRTMTZ batch type 5.
 __global__ void __launch_bounds__(QTHREADS, 2)
 k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
   extern __shared__ double smem[];
@@ -1156,7 +1156,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
 }
 
 // BXCH(J,I) = conj(BXCH(I,J)) for I in the large and J in the small block
-// (BRTFAST :17630).  One thread per element of the n x n LS block.
+// (BRTFAST :17643-17654).  One thread per element of the n x n LS block.
 __global__ void k_conj_block(double2 *M, int n, int ld) {
   long long tot = (long long)n * n;
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < tot;
@@ -2057,7 +2057,7 @@ int breit_prepare(bg_ctx *c) {
 }
 
 // Shell quartets of the Breit classes with BRTFAST's centre and stage rules
-// (bertha-scf.f:17262-17275) and the one-centre parity rule (:17330).
+// (bertha-scf.f:17226-17231) and the one-centre parity rule (:17319-17329).
 // t2 = 0: (LS|LS), pairs ab >= cd only, each digested for both orders;
 // t2 = 1: (LS|SL), every ordered pair, digested for both orders, which
 // covers the (SL|LS) class.  The (SL|SL) class only feeds the SL block,

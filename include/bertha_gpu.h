@@ -103,9 +103,9 @@ int bertha_gpu_clmfast_device(bg_ctx *ctx, const double *d_dent, int ldd,
                               int ldf, void *stream);
 
 /* Closed-shell multi-centre Breit exchange matrix, replacing CALL BRTFAST
- * (bertha-scf.f:17060-17645; BIIFAST :18337, BRTMTG :19815, BRTMTZ :19172).
+ * (bertha-scf.f:17060-17670; BIIFAST :18337, BRTMTG :19815, BRTMTZ :19172).
  *   dent[ldd*ndim]  total density DENT
- *   ilev            ILEV: multi-centre quartets from stage 3 on (:17272)
+ *   ilev            ILEV: multi-centre quartets from stage 3 on (:17230-17231)
  *   bxch[ldf*ndim]  output BXCH, overwritten
  * Full Breit interaction -1/2 [a1.a2/r12 + (a1.r12)(a2.r12)/r12^3], or the
  * Gaunt term -a1.a2/r12 alone when the context was made with BG_FLAG_GAUNT.

@@ -832,7 +832,7 @@ EBlockQ make_eblock_q(const Basis &b, int ca, int lA, int cb, int lB, bool a_sma
 
 // Breit kernel between Cartesian components i (electron 2, cd) and j
 // (electron 1, ab) at Hermite index N = (t,u,v), from PRE*R-integrals of
-// order |N|+2 (BIIFAST first contraction :18650-18800):
+// order |N|+2 (BIIFAST first contraction :18655-18880):
 //   W_ij(N) = BFAC * (delta_ij R_N - T_ij(N)),
 //   T_ij(N) = R_{N+e_i+e_j}/(2 alpha) - R_{N+e_i} PQ_j + N_j R_{N+e_i-e_j},
 // PQ = Q - P, BFAC = -1/2.  Gaunt only: W_ij = -delta_ij R_N.
@@ -884,12 +884,12 @@ void bii_first(const EBlockQ &Eab, int ia, int ib, int ij, const std::vector<dou
     }
 }
 
-// Breit phase of a pair: the Coulomb one negated (BRTFAST :17390).
+// Breit phase of a pair: the Coulomb one negated (BRTFAST :17528-17533, BIIFAST :18899).
 inline double phase_breit(int kqa, int ma, int kqb, int mb) {
   return -phase_pair(kqa, ma, kqb, mb);
 }
 
-// Second contraction summed over the Cartesian component (BIIFAST :18870).
+// Second contraction summed over the Cartesian component (BIIFAST :18887-19145).
 void bii_second(const cplx *g11, const cplx *g21, const EBlockQ &Ecd, int ic, int id,
                 int kl, int ncd, double pab, double pcd, Eri16 &rr) {
   for (int s = 0; s < 16; ++s) rr.v[s] = 0.0;
@@ -944,7 +944,7 @@ void digest_x(const Eri16 &rr, const int na[2], const int nb[2], const int nc[2]
 // batches and reaches the other component classes through integral
 // permutation symmetry; this restatement evaluates the classes directly:
 // (LS|LS) -> LS block, (LS|SL) -> LL block, (SL|LS) -> SS block, and fills
-// the SL block by the final conjugation of BRTFAST (:17630):
+// the SL block by the final conjugation of BRTFAST (:17643-17654):
 // BXCH(J,I) = conj(BXCH(I,J)), I large, J small.
 void breit_full(const Basis &b, const Opts &o, bool gaunt, const Mat &D, Mat &BX) {
   for (int j = 0; j < b.ndim; ++j)

@@ -59,7 +59,7 @@ def test_breit_linear_real_digestion():
 
 def test_breit_one_centre_by_md():
     """RACAH1 off: one-centre quartets enter at every stage, multi-centre
-    ones from stage 3 (bertha-scf.f:17262-17275)."""
+    ones from stage 3 (bertha-scf.f:17226-17231)."""
     b = _basis()
     d = deck.density(b, seed=34)
     _cmp(b, d, 1, racah1=False)

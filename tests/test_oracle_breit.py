@@ -4,7 +4,7 @@ mathematics.
 - sigma-coupled LS/SL E-coefficients (EQLS/EQSL) reproduce i * psi_a^+ sigma_q
   psi_b (LS) and -i * psi_a^+ sigma_q psi_b (SL) evaluated on points;
 - the time-reversal relations with the Breit phase (the Coulomb phase
-  negated, bertha-scf.f:17390) that BIIFAST uses for 12 of its 16 m-sign
+  negated, bertha-scf.f:17528-17533) that BIIFAST uses for 12 of its 16 m-sign
   combinations;
 - the Breit kernel against direct quadrature of the Gaussian-smeared
   operator delta_ij/r + r_i r_j/r^3, and its Hermite derivatives against
