@@ -594,6 +594,16 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         // four complex products (E_R set) x (G set), kept as real partials
         double a0 = 0, b0 = 0, c0r = 0, d0 = 0, a1 = 0, b1 = 0, c1 = 0, d1 = 0;
         double a2 = 0, b2 = 0, c2 = 0, d2 = 0, a3 = 0, b3 = 0, c3 = 0, d3 = 0;
+        if (q.isym && !q.bound) {
+          // CLMMTZ reads only the real parts of combinations 0, 3, 12, 15
+          // (direct) and 0, 6, 9, 15 (exchange): sets 1 and 4 of ERIFAST's
+          // linear-molecule path (:12820-12912), 4 of the 16 products
+          for (int k = 0; k < nR; ++k) {
+            double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
+            a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
+            a3 = fma(u2.x, x2.x, a3); b3 = fma(u2.y, x2.y, b3);
+          }
+        } else
         for (int k = 0; k < nR; ++k) {
           double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
           a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
@@ -1050,6 +1060,15 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
           const double2 *g21 = G + ((lab * 2 + 1) * 3 + i) * ncd;
           const double2 *e11 = Ecd + (((long long)lr * 2 + 0) * 3 + i) * ncd;
           const double2 *e21 = Ecd + (((long long)lr * 2 + 1) * 3 + i) * ncd;
+          if (q.isym) {
+            // BRTMTZ reads only the real parts of combinations 0, 6, 9, 15
+            for (int k = 0; k < ncd; ++k) {
+              double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
+              a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
+              a3 = fma(u2.x, x2.x, a3); b3 = fma(u2.y, x2.y, b3);
+            }
+            continue;
+          }
           for (int k = 0; k < ncd; ++k) {
             double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
             a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
@@ -1552,6 +1571,20 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
             // right-side E from L2 with one iteration of register prefetch
             float4 u1n = make_float4(0.f, 0.f, 0.f, 0.f), u2n = u1n;
             if (part < nR) { u1n = e11[part]; u2n = e21[part]; }
+            if (q.isym) {
+              // CLMMTZ reads only the real parts of combinations 0, 3, 12,
+              // 15 and 0, 6, 9, 15: products (e11 x g11) and (e21 x g21),
+              // real-by-real and imaginary-by-imaginary (ERIFAST :12820-12912)
+              for (int k = part; k < nR; k += KS) {
+                float4 u1 = u1n, u2 = u2n;
+                if (k + KS < nR) { u1n = e11[k + KS]; u2n = e21[k + KS]; }
+                float4 x1 = g11[k], x2 = g21[k];
+                df_fma(u1.x, u1.y, x1.x, x1.y, acc[0][0], acc[0][1]);
+                df_fma(u1.z, u1.w, x1.z, x1.w, acc[1][0], acc[1][1]);
+                df_fma(u2.x, u2.y, x2.x, x2.y, acc[12][0], acc[12][1]);
+                df_fma(u2.z, u2.w, x2.z, x2.w, acc[13][0], acc[13][1]);
+              }
+            } else
             for (int k = part; k < nR; k += KS) {
               float4 u1 = u1n, u2 = u2n;
               if (k + KS < nR) { u1n = e11[k + KS]; u2n = e21[k + KS]; }
