@@ -893,6 +893,7 @@ struct BArgs {
   double *BX;
   int ns, ldd, ldf, nskp, isym, racah1, gaunt;
   int dual;  // also digest (cd|ab) = (ab|cd): K(c,b) += (ab|cd) D(a,d)
+  double *bound;  // non-null: write max |(ab|cd)| per quartet instead of digesting
 };
 
 __device__ inline double2 ldDB(const BArgs &q, int i, int j) {
@@ -949,6 +950,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
       sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
       sgeo[5] = 0.5 / aph;
       sgeo[6] = Qx - Px; sgeo[7] = Qy - Py; sgeo[8] = Qz - Pz;
+      sgeo[9] = 0.0;
     }
     __syncthreads();
     {
@@ -1060,7 +1062,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
           const double2 *g21 = G + ((lab * 2 + 1) * 3 + i) * ncd;
           const double2 *e11 = Ecd + (((long long)lr * 2 + 0) * 3 + i) * ncd;
           const double2 *e21 = Ecd + (((long long)lr * 2 + 1) * 3 + i) * ncd;
-          if (q.isym) {
+          if (q.isym && !q.bound) {
             // BRTMTZ reads only the real parts of combinations 0, 6, 9, 15
             for (int k = 0; k < ncd; ++k) {
               double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
@@ -1103,6 +1105,13 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
         r[6] = make_double2(flip(s4c.x, ml ^ SGN), flip(s4c.y, ml ^ SGN));
         r[5] = make_double2(flip(r[10].x, mlr), flip(r[10].y, mlr ^ SGN));
         r[9] = make_double2(flip(r[6].x, mlr), flip(r[6].y, mlr ^ SGN));
+        if (q.bound) {
+          // bound mode (Schwarz): largest |(ab|cd)| of the quartet
+          double m = 0.0;
+          for (int i = 0; i < 16; ++i) m = fmax(m, fmax(fabs(r[i].x), fabs(r[i].y)));
+          atomicMax((unsigned long long *)&sgeo[9], (unsigned long long)__double_as_longlong(m));
+          continue;
+        }
         int fa[2] = {A.fock[ia][0] + oa, A.fock[ia][1] + oa};
         int fb[2] = {B.fock[ib][0] + ob, B.fock[ib][1] + ob};
         int fc[2] = {C.fock[ic][0] + oc, C.fock[ic][1] + oc};
@@ -1149,6 +1158,11 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
         }
       }
       __syncthreads();
+    }
+    if (q.bound) {
+      if (threadIdx.x == 0) q.bound[qi] = sgeo[9];
+      __syncthreads();
+      continue;
     }
     // flush shared accumulators
     for (int w = threadIdx.x; w < 2 * nla * 2 * nld; w += blockDim.x) {
@@ -1850,6 +1864,7 @@ struct bg_ctx {
   int *d_bquart[2] = {nullptr, nullptr};
   long long nbquart[2] = {0, 0};
   int bquart_ilev = -1;
+  std::vector<double> bqbound;  // [pair] sqrt max |(ab|ab)| of the LS pair, Breit
   double2 *d_BX = nullptr;
   long long launches = 0;
   std::string err;
@@ -2091,12 +2106,19 @@ int breit_prepare(bg_ctx *c) {
 
 // Shell quartets of the Breit classes with BRTFAST's centre and stage rules
 // (bertha-scf.f:17226-17231) and the one-centre parity rule (:17319-17329).
+// With a Schwarz threshold, quartets with Q_ab Q_cd below it are left out:
+// the Breit kernel -1/2 (delta_ij/r + r_i r_j/r^3) is negative semidefinite
+// (its Fourier transform is -(4 pi/k^2)(delta_ij - k_i k_j/k^2)), so
+// |(ab|cd)| <= Q_ab Q_cd with Q^2 the largest |(ab|ab)| over labels and
+// m-signs (the Kramers partner of a density is its conjugate up to sign);
+// the SL pair cd has the bound of the LS pair dc ((ab|cd)* = (ba|dc)).
 // t2 = 0: (LS|LS), pairs ab >= cd only, each digested for both orders;
 // t2 = 1: (LS|SL), every ordered pair, digested for both orders, which
 // covers the (SL|LS) class.  The (SL|SL) class only feeds the SL block,
 // which BRTFAST overwrites by conjugation of the LS block.
 std::vector<int> build_breit_quartets(const bg_ctx *c, int t2, int ilev) {
   std::vector<int> out;
+  bool scr = c->screen > 0.0 && !c->bqbound.empty();
   std::vector<int> byl[MAXLB + 1];
   for (int s = 0; s < c->ns; ++s) byl[c->shells[s].l].push_back(s);
   for (int la = MAXLB; la >= 0; --la)
@@ -2116,13 +2138,18 @@ std::vector<int> build_breit_quartets(const bg_ctx *c, int t2, int ilev) {
         if (mcnt == 1 && c->racah1) continue;
         if (mcnt != 1 && ilev < 3) continue;
         if (mcnt == 1 && ((la + lb) & 1) != ((lc + ld) & 1)) continue;
+        // Schwarz: Q(LS pair ab) Q(cd as LS pair for t2 = 0, dc for SL)
+        if (scr && c->bqbound[pab] *
+                       c->bqbound[t2 == 0 ? pcd : (long long)d * c->ns + cc] < c->screen)
+          continue;
         out.push_back(a); out.push_back(b); out.push_back(cc); out.push_back(d);
       }
   return out;
 }
 
 int launch_breit(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const double2 *d_D,
-                 int ldd, double *d_BX, int ldf, cudaStream_t st, int dual) {
+                 int ldd, double *d_BX, int ldf, cudaStream_t st, int dual,
+                 double *bound = nullptr) {
   if (nq <= 0) return 0;
   static bool attr = false;
   size_t smem = breit_smem();
@@ -2133,11 +2160,36 @@ int launch_breit(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const 
   BArgs a;
   a.sh = c->d_sh; a.offq = c->d_offq; a.E = c->d_EB; a.D = d_D; a.BX = d_BX;
   a.ns = c->ns; a.ldd = ldd; a.ldf = ldf; a.nskp = c->nskp; a.isym = c->isym;
-  a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual;
+  a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual; a.bound = bound;
   long long grid = std::min<long long>(nq, 152LL * 64);
   k_breit<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
   c->launches++;
+  return 0;
+}
+
+// Schwarz bounds of the LS pairs for the Breit build: k_breit in bound mode
+// over the diagonal quartets (ab|ab) of the (LS|LS) class.
+int compute_breit_bounds(bg_ctx *c, cudaStream_t st) {
+  int ns = c->ns;
+  std::vector<int> diag;
+  for (int a = 0; a < ns; ++a)
+    for (int b = 0; b < ns; ++b) { diag.push_back(a); diag.push_back(b); diag.push_back(a); diag.push_back(b); }
+  long long np = (long long)ns * ns;
+  int *d_q = nullptr;
+  double *d_b = nullptr;
+  CK(c, cudaMalloc(&d_q, sizeof(int) * diag.size()));
+  CK(c, cudaMalloc(&d_b, sizeof(double) * np));
+  CK(c, cudaMemcpyAsync(d_q, diag.data(), sizeof(int) * diag.size(), cudaMemcpyHostToDevice, st));
+  int rc = launch_breit(c, d_q, np, 0, 0, nullptr, 0, nullptr, 0, st, 0, d_b);
+  if (rc) { cudaFree(d_q); cudaFree(d_b); return rc; }
+  std::vector<double> hb(np);
+  CK(c, cudaMemcpyAsync(hb.data(), d_b, sizeof(double) * np, cudaMemcpyDeviceToHost, st));
+  CK(c, cudaStreamSynchronize(st));
+  c->bqbound.resize(np);
+  for (long long p = 0; p < np; ++p) c->bqbound[p] = sqrt(hb[p]);
+  cudaFree(d_q);
+  cudaFree(d_b);
   return 0;
 }
 
@@ -2292,7 +2344,7 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
 
 int bertha_gpu_set_screening(bg_ctx *c, double threshold) {
   if (!c || !(threshold >= 0.0)) return BG_ERR_ARG;
-  if (threshold != c->screen) c->quart_ilev = -1;  // rebuild the lists
+  if (threshold != c->screen) c->quart_ilev = c->bquart_ilev = -1;  // rebuild the lists
   c->screen = threshold;
   return BG_OK;
 }
@@ -2450,6 +2502,10 @@ int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
   k_zero2d<<<1024, 256, 0, st>>>(d_bxch, c->ndim, ldf);
   CK(c, cudaGetLastError());
   c->launches++;
+  if (c->screen > 0.0 && c->bqbound.empty()) {
+    rc = compute_breit_bounds(c, st);
+    if (rc) return rc;
+  }
   if (c->bquart_ilev != ilev) {
     for (int k = 0; k < 2; ++k) {
       if (c->d_bquart[k]) cudaFree(c->d_bquart[k]);
