@@ -904,6 +904,15 @@ size_t breit_smem() {
   return sizeof(double) * NTW * 9 + sizeof(double2) * (BCHUNK * 2 * 3 * NTB + 2 * MAXSP * MAXSP);
 }
 
+// FP64 multiply-adds of the two contraction orders of a Breit quartet: the
+// left pair's E against the 3x3 kernel (3 components of each electron, 1
+// for the Gaunt term alone), then the second contraction over 3 components
+// with 16 products (4 when only the real digestion's are needed).
+__host__ __device__ inline long long breit_cost(int pl, int nl, int pr, int nr, int gaunt,
+                                                bool lin) {
+  return 2LL * pl * nl * nr * (gaunt ? 3 : 9) + 3LL * (lin ? 4 : 16) * pl * pr * nr;
+}
+
 // One CTA per shell quartet of component class (t1|t2), t = 0 LS, 1 SL.
 // R-integrals to order degab+degcd+2, the 3x3 Breit kernel table
 //   W_ij(N) = BFAC (delta_ij R_N - T_ij(N)),
@@ -934,6 +943,9 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
     int nab = ntuv(degab), ncd = ntuv(degcd);
     int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
     bool dual = q.dual && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
+    bool lin = q.isym && !q.bound;  // only the 4 products of the real digestion
+    bool swp = breit_cost(nlcd, ncd, nlab, nab, q.gaunt, lin) <
+               breit_cost(nlab, nab, nlcd, ncd, q.gaunt, lin);
     if (threadIdx.x == 0) {
       double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
       double Px = (A.alpha * A.x + B.alpha * B.x) / p;
@@ -945,11 +957,15 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
       double aph = p * qq / (p + qq);
       double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
       boys_ref(T, lam, F);
-      sgeo[0] = Px - Qx; sgeo[1] = Py - Qy; sgeo[2] = Pz - Qz;
+      // R and the kernel table are built for the left pair's centre minus
+      // the right pair's: the Breit kernel is even in P - Q, so swapping the
+      // pairs only flips the sign of odd Hermite orders
+      double sg = swp ? -1.0 : 1.0;
+      sgeo[0] = sg * (Px - Qx); sgeo[1] = sg * (Py - Qy); sgeo[2] = sg * (Pz - Qz);
       sgeo[3] = -2.0 * aph;
       sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
       sgeo[5] = 0.5 / aph;
-      sgeo[6] = Qx - Px; sgeo[7] = Qy - Py; sgeo[8] = Qz - Pz;
+      sgeo[6] = sg * (Qx - Px); sgeo[7] = sg * (Qy - Py); sgeo[8] = sg * (Qz - Pz);
       sgeo[9] = 0.0;
     }
     __syncthreads();
@@ -1015,37 +1031,44 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
     __syncthreads();
     const double2 *Eab = q.E + q.offq[((size_t)Q4.x * q.ns + Q4.y) * 2 + t1];
     const double2 *Ecd = q.E + q.offq[((size_t)Q4.z * q.ns + Q4.w) * 2 + t2];
+    // left/right roles
+    const double2 *EL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
+    int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
+    int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
+    int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;
     int lq[4] = {la, lb, lc, ld};
     // Fock offsets: an LS pair has its first function large, second small
     int oa = t1 ? q.nskp : 0, ob = t1 ? 0 : q.nskp;
     int oc = t2 ? q.nskp : 0, od = t2 ? 0 : q.nskp;
     // as many ab labels per pass as the G buffer holds (fewer barriers and
     // idle threads for low angular momenta)
-    int chunk = max(1, (BCHUNK * 2 * 3 * NTB) / (6 * ncd));
-    for (int c0 = 0; c0 < nlab; c0 += chunk) {
-      int nch = min(chunk, nlab - c0);
+    int chunk = max(1, (BCHUNK * 2 * 3 * NTB) / (6 * nR));
+    for (int c0 = 0; c0 < nlL; c0 += chunk) {
+      int nch = min(chunk, nlL - c0);
       // first contraction: G[lab][set][i][q] = Z(q) sum_j sum_s E_j[s] W_ij(s+q)
-      for (int w = threadIdx.x; w < nch * 6 * ncd; w += blockDim.x) {
-        int lab = w / (6 * ncd), rem = w % (6 * ncd);
-        int set = rem / (3 * ncd), i = (rem / ncd) % 3, qq = rem % ncd;
-        const double2 *e = Eab + ((long long)(c0 + lab) * 2 + set) * 3 * nab;
+      for (int w = threadIdx.x; w < nch * 6 * nR; w += blockDim.x) {
+        int lab = w / (6 * nR), rem = w % (6 * nR);
+        int set = rem / (3 * nR), i = (rem / nR) % 3, qq = rem % nR;
+        const double2 *e = EL + ((long long)(c0 + lab) * 2 + set) * 3 * nL;
         int tq = c_t[qq], uq = c_u[qq], vq = c_v[qq];
         double ax = 0.0, ay = 0.0;
-        for (int s = 0; s < nab; ++s) {
+        for (int s = 0; s < nL; ++s) {
           const double *wr = W + hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq) * 9 + 3 * i;
-          double2 e0 = e[s], e1 = e[nab + s], e2 = e[2 * nab + s];
+          double2 e0 = e[s], e1 = e[nL + s], e2 = e[2 * nL + s];
           double w0 = wr[0], w1 = wr[1], w2 = wr[2];
           ax = fma(e0.x, w0, fma(e1.x, w1, fma(e2.x, w2, ax)));
           ay = fma(e0.y, w0, fma(e1.y, w1, fma(e2.y, w2, ay)));
         }
         unsigned long long zm = ((tq + uq + vq) & 1) ? SGN : 0ULL;
-        G[((lab * 2 + set) * 3 + i) * ncd + qq] = make_double2(flip(ax, zm), flip(ay, zm));
+        G[((lab * 2 + set) * 3 + i) * nR + qq] = make_double2(flip(ax, zm), flip(ay, zm));
       }
       __syncthreads();
       // second contraction and exchange digestion
-      for (int w = threadIdx.x; w < nch * nlcd; w += blockDim.x) {
-        int lab = w / nlcd, lr = w % nlcd;
-        int ia = (c0 + lab) / nlb, ib = (c0 + lab) % nlb, ic = lr / nld, id = lr % nld;
+      for (int w = threadIdx.x; w < nch * nlR; w += blockDim.x) {
+        int lab = w / nlR, lr = w % nlR;
+        int labL = c0 + lab;
+        int l1 = labL / nl2L, l2 = labL % nl2L, r1 = lr / nl2R, r2 = lr % nl2R;
+        int ia = swp ? r1 : l1, ib = swp ? r2 : l2, ic = swp ? l1 : r1, id = swp ? l2 : r2;
         int kq[4], mq[4], mm[4];
         label_of(la, ia, kq[0], mm[0]);
         label_of(lb, ib, kq[1], mm[1]);
@@ -1055,23 +1078,24 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
         if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
         double pab = -pair_phase(kq[0], mm[0], kq[1], mm[1]);
         double pcd = -pair_phase(kq[2], mm[2], kq[3], mm[3]);
+        double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
         double a0 = 0, b0 = 0, c0r = 0, d0 = 0, a1 = 0, b1 = 0, c1 = 0, d1 = 0;
         double a2 = 0, b2 = 0, c2 = 0, d2 = 0, a3 = 0, b3 = 0, c3 = 0, d3 = 0;
         for (int i = 0; i < 3; ++i) {
-          const double2 *g11 = G + ((lab * 2 + 0) * 3 + i) * ncd;
-          const double2 *g21 = G + ((lab * 2 + 1) * 3 + i) * ncd;
-          const double2 *e11 = Ecd + (((long long)lr * 2 + 0) * 3 + i) * ncd;
-          const double2 *e21 = Ecd + (((long long)lr * 2 + 1) * 3 + i) * ncd;
-          if (q.isym && !q.bound) {
+          const double2 *g11 = G + ((lab * 2 + 0) * 3 + i) * nR;
+          const double2 *g21 = G + ((lab * 2 + 1) * 3 + i) * nR;
+          const double2 *e11 = ER + (((long long)lr * 2 + 0) * 3 + i) * nR;
+          const double2 *e21 = ER + (((long long)lr * 2 + 1) * 3 + i) * nR;
+          if (lin) {
             // BRTMTZ reads only the real parts of combinations 0, 6, 9, 15
-            for (int k = 0; k < ncd; ++k) {
+            for (int k = 0; k < nR; ++k) {
               double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
               a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
               a3 = fma(u2.x, x2.x, a3); b3 = fma(u2.y, x2.y, b3);
             }
             continue;
           }
-          for (int k = 0; k < ncd; ++k) {
+          for (int k = 0; k < nR; ++k) {
             double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
             a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
             c0r = fma(u1.x, x1.y, c0r); d0 = fma(u1.y, x1.x, d0);
@@ -1087,7 +1111,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
         double2 s2 = {a1 - b1, c1 + d1}, s2c = {a1 + b1, d1 - c1};
         double2 s3 = {a2 - b2, c2 + d2}, s3c = {a2 + b2, d2 - c2};
         double2 s4 = {a3 - b3, c3 + d3}, s4c = {a3 + b3, d3 - c3};
-        unsigned long long ml = smask(pab), mlr = smask(pab * pcd);
+        unsigned long long ml = smask(pl), mlr = smask(pl * pr);
         double2 r[16];
         r[0] = s1;
         r[12] = make_double2(flip(s1c.x, ml), flip(s1c.y, ml));
@@ -1112,6 +1136,9 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
           atomicMax((unsigned long long *)&sgeo[9], (unsigned long long)__double_as_longlong(m));
           continue;
         }
+        // (ab|cd) m-sign index from the (left|right) one
+#define RB(sa, sb, sc, sd) (swp ? r[8 * (sc) + 4 * (sd) + 2 * (sa) + (sb)] \
+                                : r[8 * (sa) + 4 * (sb) + 2 * (sc) + (sd)])
         int fa[2] = {A.fock[ia][0] + oa, A.fock[ia][1] + oa};
         int fb[2] = {B.fock[ib][0] + ob, B.fock[ib][1] + ob};
         int fc[2] = {C.fock[ic][0] + oc, C.fock[ic][1] + oc};
@@ -1122,7 +1149,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
               double kx = 0.0, ky = 0.0;
               for (int sb = 0; sb < 2; ++sb)
                 for (int sc = 0; sc < 2; ++sc) {
-                  double2 v = r[8 * sa + 4 * sb + 2 * sc + sd], d = ldDB(q, fc[sc], fb[sb]);
+                  double2 v = RB(sa, sb, sc, sd), d = ldDB(q, fc[sc], fb[sb]);
                   kx = fma(v.x, d.x, fma(-v.y, d.y, kx));
                   ky = fma(v.x, d.y, fma(v.y, d.x, ky));
                 }
@@ -1134,7 +1161,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
                 double kx = 0.0, ky = 0.0;
                 for (int sa = 0; sa < 2; ++sa)
                   for (int sd = 0; sd < 2; ++sd) {
-                    double2 v = r[8 * sa + 4 * sb + 2 * sc + sd], d = ldDB(q, fa[sa], fd[sd]);
+                    double2 v = RB(sa, sb, sc, sd), d = ldDB(q, fa[sa], fd[sd]);
                     kx = fma(v.x, d.x, fma(-v.y, d.y, kx));
                     ky = fma(v.x, d.y, fma(v.y, d.x, ky));
                   }
@@ -1145,17 +1172,18 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
           for (int s = 0; s < 2; ++s) {
             double kv = 0.0;
             for (int t = 0; t < 2; ++t)
-              kv = fma(r[8 * s + 4 * t + 2 * t + s].x, ldDB(q, fc[t], fb[t]).x, kv);
+              kv = fma(RB(s, t, t, s).x, ldDB(q, fc[t], fb[t]).x, kv);
             atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
           }
           if (dual)
             for (int s = 0; s < 2; ++s) {
               double kv = 0.0;
               for (int t = 0; t < 2; ++t)
-                kv = fma(r[8 * t + 4 * s + 2 * s + t].x, ldDB(q, fa[t], fd[t]).x, kv);
+                kv = fma(RB(t, s, s, t).x, ldDB(q, fa[t], fd[t]).x, kv);
               atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
             }
         }
+#undef RB
       }
       __syncthreads();
     }
