@@ -22,6 +22,7 @@
 //   CLMFAST 11489-12266  loop structure, selection rules, stage gating
 //   EQLS 34937, EQSL 35433  sigma-coupled LS/SL E-coefficients
 //   BRTFAST 17060, BIIFAST 18337, BRTMTG 19815 / BRTMTZ 19172  Breit exchange
+//   ONEEL 6996, OVRLP 6683  overlap, nuclear attraction, kinetic coupling
 //   FOCKIND 2582, CARTIND 2651  index layouts
 
 #include <algorithm>
@@ -1031,6 +1032,119 @@ void breit_full(const Basis &b, const Opts &o, bool gaunt, const Mat &D, Mat &BX
     for (int j = b.nskp; j < b.ndim; ++j) BX(j, i) = std::conj(BX(i, j));
 }
 
+// ---------------------------------------------------------------------------
+// One-electron matrices (ONEEL bertha-scf.f:6996-7990, OVRLP :6683)
+// ---------------------------------------------------------------------------
+const double CLIGHT = 137.035999084;  // speed of light (bertha-scf.f:974)
+
+// The four m-sign combinations of a one-electron element from sets
+// (-|ma|,-|mb|) and (+|ma|,-|mb|): (-,+) = -PHS conj(+,-), (+,+) = PHS conj(-,-)
+// (ONEEL :7106-7109, PHS as the Coulomb pair phase).
+void put4(Mat &M, const int ra[2], const int cb[2], cplx x11, cplx x21, double phs) {
+  M(ra[0], cb[0]) = x11;
+  M(ra[1], cb[0]) = x21;
+  M(ra[0], cb[1]) = -phs * std::conj(x21);
+  M(ra[1], cb[1]) = phs * std::conj(x11);
+}
+
+// Nuclear attraction of one primitive pair density with E-coefficients e
+// (degree deg) to every nucleus: point (xi = 0; APH = p, PNC = 2 pi Z/p) or
+// Gaussian (APH = p xi/(p+xi), PNC = 2 pi Z sqrt(xi/(p+xi))/p), ONEEL
+// :7250-7330.  Returns -sum_C PNC sum_tuv E_tuv R_tuv(APH, C - P).
+cplx nuc_attr(const cplx *e, int deg, double p, const double *P, const Basis &b,
+              const double *znuc, const double *xi) {
+  cplx v(0.0);
+  std::vector<double> R(ntuv(deg));
+  for (int c = 0; c < b.ncnt; ++c) {
+    double cp[3];
+    for (int x = 0; x < 3; ++x) cp[x] = b.xyz[3 * c + x] - P[x];
+    double aph, pnc;
+    if (xi[c] > 0.0) {
+      aph = p * xi[c] / (p + xi[c]);
+      pnc = 2.0 * PI * znuc[c] * std::sqrt(xi[c] / (p + xi[c])) / p;
+    } else {
+      aph = p;
+      pnc = 2.0 * PI * znuc[c] / p;
+    }
+    rints(cp, aph, deg, R.data());
+    cplx acc(0.0);
+    for (int k = 0; k < ntuv(deg); ++k) acc += e[k] * R[k];
+    v -= pnc * acc;
+  }
+  return v;
+}
+
+// OVLP, HNUC = V (LL), V - 2c^2 S (SS), HKIN = c sqrt((2l+3) alpha) S_SS
+// couplings (ONEEL parts 1-4) or, for NORL, the non-relativistic kinetic
+// matrix (:7420-7470).  Every ordered shell pair is computed directly.
+void oneel_full(const Basis &b, int hmlt, const double *znuc, const double *xi, Mat &S, Mat &V,
+                Mat &T) {
+  for (int j = 0; j < b.ndim; ++j)
+    for (int i = 0; i < b.ndim; ++i) S(i, j) = V(i, j) = T(i, j) = 0.0;
+  const Cart &C = cart();
+  bool norl = hmlt == 0;
+  for (int ca = 0; ca < b.ncnt; ++ca)
+  for (int cb = 0; cb < b.ncnt; ++cb)
+  for (int lA = 0; lA <= b.lmax[ca]; ++lA)
+  for (int lB = 0; lB <= b.lmax[cb]; ++lB) {
+    std::vector<Label> la = labels_for(lA), lb = labels_for(lB);
+    const double *A = &b.xyz[3 * ca], *B = &b.xyz[3 * cb];
+    for (size_t ia = 0; ia < la.size(); ++ia)
+    for (size_t ib = 0; ib < lb.size(); ++ib) {
+      double phs = phase_pair(la[ia].kq, la[ia].ma, lb[ib].kq, lb[ib].ma);
+      int mqa = 2 * la[ia].ma - 1, mqb = 2 * lb[ib].ma - 1;
+      for (size_t i = 0; i < b.ex[ca][lA].size(); ++i)
+      for (size_t j = 0; j < b.ex[cb][lB].size(); ++j) {
+        double ea = b.ex[ca][lA][i], eb = b.ex[cb][lB][j], p = ea + eb;
+        double P[3];
+        for (int x = 0; x < 3; ++x) P[x] = (A[x] * ea + B[x] * eb) / p;
+        double eroot = std::pow(PI / p, 1.5);
+        int ra[2] = {b.lrge[ca][la[ia].ka][2 * la[ia].ma - 2] + (int)i,
+                     b.lrge[ca][la[ia].ka][2 * la[ia].ma - 1] + (int)i};
+        int cl[2] = {b.lrge[cb][lb[ib].ka][2 * lb[ib].ma - 2] + (int)j,
+                     b.lrge[cb][lb[ib].ka][2 * lb[ib].ma - 1] + (int)j};
+        HVec l11 = eq_pair(la[ia].kq, -mqa, ea, A, lb[ib].kq, -mqb, eb, B, false);
+        HVec l21 = eq_pair(la[ia].kq, mqa, ea, A, lb[ib].kq, -mqb, eb, B, false);
+        put4(S, ra, cl, eroot * l11[0], eroot * l21[0], phs);
+        put4(V, ra, cl, nuc_attr(l11.data(), lA + lB, p, P, b, znuc, xi),
+             nuc_attr(l21.data(), lA + lB, p, P, b, znuc, xi), phs);
+        if (norl) {
+          double PB[3] = {P[0] - B[0], P[1] - B[1], P[2] - B[2]};
+          double pb2 = PB[0] * PB[0] + PB[1] * PB[1] + PB[2] * PB[2];
+          double e0 = eb * (2 * lB + 3) - 2.0 * eb * eb * pb2 - 3.0 * eb * eb / p;
+          double e1 = 4.0 * eb * eb;
+          cplx t[2];
+          const HVec *ee[2] = {&l11, &l21};
+          for (int s2 = 0; s2 < 2; ++s2) {
+            const HVec &e = *ee[s2];
+            cplx tr = e0 * e[0];
+            if (lA + lB >= 1)
+              tr -= e1 * (PB[0] * e[C.idx[1][0][0]] + PB[1] * e[C.idx[0][1][0]] +
+                          PB[2] * e[C.idx[0][0][1]]);
+            if (lA + lB >= 2)
+              tr -= e1 * (e[C.idx[2][0][0]] + e[C.idx[0][2][0]] + e[C.idx[0][0][2]]);
+            t[s2] = eroot * tr;
+          }
+          put4(T, ra, cl, t[0], t[1], phs);
+          continue;
+        }
+        HVec s11 = eq_pair(la[ia].kq, -mqa, ea, A, lb[ib].kq, -mqb, eb, B, true);
+        HVec s21 = eq_pair(la[ia].kq, mqa, ea, A, lb[ib].kq, -mqb, eb, B, true);
+        int rs[2] = {ra[0] + b.nskp, ra[1] + b.nskp}, cs[2] = {cl[0] + b.nskp, cl[1] + b.nskp};
+        cplx ss11 = eroot * s11[0], ss21 = eroot * s21[0];
+        put4(S, rs, cs, ss11, ss21, phs);
+        double cv2 = 2.0 * CLIGHT * CLIGHT;
+        put4(V, rs, cs, nuc_attr(s11.data(), lA + lB + 2, p, P, b, znuc, xi) - cv2 * ss11,
+             nuc_attr(s21.data(), lA + lB + 2, p, P, b, znuc, xi) - cv2 * ss21, phs);
+        double fsl = CLIGHT * std::sqrt((2 * lB + 3) * eb);  // T(a_S, b_L)
+        double fls = CLIGHT * std::sqrt((2 * lA + 3) * ea);  // T(a_L, b_S)
+        put4(T, rs, cl, fsl * ss11, fsl * ss21, phs);
+        put4(T, ra, cs, fls * ss11, fls * ss21, phs);
+      }
+    }
+  }
+}
+
 Basis make_basis(int ncnt, const double *xyz, const int *lmax, const int *nfn,
                  const double *ex, int maxl1, int maxbs, bool norl) {
   Basis b;
@@ -1410,6 +1524,16 @@ int orc_brtfast(int ncnt, const double *xyz, const int *lmax, const int *nfn,
   Opts o{ilev, isym, 2, racah1, 0, 0};
   Mat D{(cplx *)dent, ldd}, BX{(cplx *)bxch, ldf};
   breit_full(b, o, gaunt != 0, D, BX);
+  return b.ndim;
+}
+
+// One-electron matrices OVLP, HNUC, HKIN of ONEEL (xi = 0: point nucleus).
+int orc_oneel(int ncnt, const double *xyz, const int *lmax, const int *nfn, const double *ex,
+              int maxl1, int maxbs, int hmlt, const double *znuc, const double *xi,
+              double *ovlp, double *hnuc, double *hkin, int ldf) {
+  Basis b = make_basis(ncnt, xyz, lmax, nfn, ex, maxl1, maxbs, hmlt == 0);
+  Mat S{(cplx *)ovlp, ldf}, V{(cplx *)hnuc, ldf}, T{(cplx *)hkin, ldf};
+  oneel_full(b, hmlt, znuc, xi, S, V, T);
   return b.ndim;
 }
 

@@ -38,6 +38,7 @@ def lib():
         L.orc_breit_kernel.argtypes = [P, d, i, i, i, i, P]
         L.orc_bii_quartet.argtypes = [P, P, P, i, i, i, P]
         L.orc_brtfast.argtypes = [i, P, P, P, P, i, i, i, i, i, i, P, i, P, i]
+        L.orc_oneel.argtypes = [i, P, P, P, P, i, i, i, P, P, P, P, P, i]
         _LIB = L
     return _LIB
 
@@ -175,6 +176,20 @@ def brtfast(basis, dent, ilev, racah1=True, gaunt=False):
                       int(basis.isym), int(ilev), int(racah1), int(gaunt), _p(D), nd,
                       _p(bx), nd)
     return bx
+
+
+def oneel(basis, znuc, xi):
+    """One-electron matrices (OVLP, HNUC, HKIN) of ONEEL; xi[c] is the
+    Gaussian nuclear exponent of centre c (0 for a point nucleus)."""
+    xyz, lmax, nfn, ex = _basis_arrays(basis)
+    maxl1, maxbs = ex.shape[1], ex.shape[2]
+    nd = basis.ndim
+    z = np.ascontiguousarray(znuc, dtype=np.float64)
+    x = np.ascontiguousarray(xi, dtype=np.float64)
+    out = [np.zeros((nd, nd), dtype=np.complex128, order="F") for _ in range(3)]
+    lib().orc_oneel(basis.ncnt, _p(xyz), _p(lmax), _p(nfn), _p(ex), maxl1, maxbs,
+                    int(basis.hmlt), _p(z), _p(x), _p(out[0]), _p(out[1]), _p(out[2]), nd)
+    return tuple(out)
 
 
 class QuartetOracle:
