@@ -1,4 +1,4 @@
-"""GB300-native Dirac-Coulomb Fock build for BERTHA (host side).
+"""GB300-native Dirac-Coulomb-Breit Fock build for BERTHA (host side).
 
 The compute path is libberthagpu.so (CUDA, sm_103a) behind the C ABI of
 include/bertha_gpu.h; this package only describes the basis, reads decks and
@@ -7,5 +7,5 @@ calls the library.
 from ._lib import BerthaGPUError, HMLT, SHAPE, lib  # noqa: F401
 from .build import build  # noqa: F401
 from .deck import (Basis, c6h6_basis, density, geometric, h2o_basis,  # noqa: F401
-                   make_basis, read_deck, shape_isym, tlf_basis)
+                   make_basis, read_deck, shape_isym, tlf_basis, tlf_small_basis)
 from .fock import FockBuilder  # noqa: F401

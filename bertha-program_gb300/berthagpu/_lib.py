@@ -43,6 +43,8 @@ def lib():
         L.bertha_gpu_clmfast_device.argtypes = [P, P, i, i, P, P, i, P]
         L.bertha_gpu_brtfast.argtypes = [P, P, i, i, P, i]
         L.bertha_gpu_brtfast_device.argtypes = [P, P, i, i, P, i, P]
+        L.bertha_gpu_oneel.argtypes = [P, P, P, P, P, P, i]
+        L.bertha_gpu_oneel_device.argtypes = [P, P, P, P, P, P, i, P]
         L.bertha_gpu_quartets.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
         L.bertha_gpu_quartets_noalloc.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
         L.bertha_gpu_shells.argtypes = [P, P, P, P, P]
@@ -61,6 +63,7 @@ EXPORTED = [
     "bertha_gpu_init", "bertha_gpu_set_screening", "bertha_gpu_set_precision",
     "bertha_gpu_dims", "bertha_gpu_clmfast",
     "bertha_gpu_clmfast_device", "bertha_gpu_brtfast", "bertha_gpu_brtfast_device",
+    "bertha_gpu_oneel", "bertha_gpu_oneel_device",
     "bertha_gpu_quartets", "bertha_gpu_quartets_noalloc",
     "bertha_gpu_shells",
     "bertha_gpu_layout", "bertha_gpu_launches", "bertha_gpu_last_error",

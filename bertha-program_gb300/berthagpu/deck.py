@@ -22,6 +22,7 @@ class Basis:
     hmlt: int = HMLT["DHFR"]
     isym: int = 0              # CLMFAST ISYM: 0 general, 1 linear, 2 atomic
     znuc: tuple = ()
+    anuc: tuple = ()
     name: str = ""
 
     @property
@@ -89,6 +90,27 @@ def shape_isym(xyz):
     return SHAPE["LINEAR"] if np.all(np.sum(perp ** 2, axis=1) < 1e-6) else SHAPE["NOSYMM"]
 
 
+CFM = 5.29177211e4  # fm per bohr (bertha-scf.f:1013)
+PRAD = 0.842        # proton rms charge radius, fm (bertha-scf.f:989)
+
+
+def nuclear_exponents(znuc, anuc):
+    """Gaussian nuclear exponents xi = 1.5/r_rms^2 (bohr^-2) of NUCCOUL
+    (bertha-scf.f:1183-1210): r_rms = 0.842 fm for Z = 1, 0.836 A^(1/3) +
+    0.57 fm for 1 < Z < 90, 0.770 A^(1/3) + 0.98 fm otherwise."""
+    out = []
+    for z, a in zip(znuc, anuc):
+        if int(z) == 1:
+            rfm = PRAD
+        elif 1.0 < z < 90.0:
+            rfm = 0.836 * a ** (1.0 / 3.0) + 0.57
+        else:
+            rfm = 0.770 * a ** (1.0 / 3.0) + 0.98
+        r = rfm / CFM
+        out.append(1.5 / (r * r))
+    return np.array(out)
+
+
 def geometric(alpha, beta, n):
     """Even-tempered exponents alpha*beta^k, k = 0..n-1 (CARDIN :361-387)."""
     return [alpha * beta ** k for k in range(n)]
@@ -125,12 +147,13 @@ def read_deck(path):
         raise ValueError(f"unknown HMLT {hmlt}")
     rec(); readin = rec()[0].upper().startswith(".T")
     rec(); ncnt = int(rec()[0])
-    centres, znuc = [], []
+    centres, znuc, anuc = [], [], []
     for _ in range(ncnt):
         rec(); rec()
         pos = [_num(t) for t in rec()[:3]]
         rec(); nuc = rec()
         znuc.append(_num(nuc[1]))
+        anuc.append(_num(nuc[2]) if len(nuc) > 2 else 2.0 * _num(nuc[1]))
         rec(); bt = rec()
         btyp, lmax = bt[0], int(bt[1])
         rec(); cnf = rec()
@@ -159,7 +182,7 @@ def read_deck(path):
     rec(); rec()
     rec(); ilev = int(rec()[0])
     basis = make_basis(centres, hmlt=hmlt, name=molcl)
-    basis.znuc = tuple(znuc)
+    basis.znuc, basis.anuc = tuple(znuc), tuple(anuc)
     if hmlt == "NORL":
         ilev = 1
     if ncnt == 1 or readin:
@@ -175,8 +198,10 @@ def h2o_basis():
     H at (+-1.430, 0, 1.107) bohr; Dirac-Coulomb."""
     o = {0: geometric(0.10, 2.8, 10), 1: geometric(0.10, 2.8, 6), 2: geometric(0.10, 2.8, 2)}
     h = {0: geometric(0.08, 3.0, 6), 1: geometric(0.08, 3.0, 2)}
-    return make_basis([((0, 0, 0), o), ((1.430, 0, 1.107), h), ((-1.430, 0, 1.107), h)],
-                      hmlt="DHFR", name="H2O")
+    b = make_basis([((0, 0, 0), o), ((1.430, 0, 1.107), h), ((-1.430, 0, 1.107), h)],
+                   hmlt="DHFR", name="H2O")
+    b.znuc, b.anuc = (8.0, 1.0, 1.0), (16.0, 1.0, 1.0)
+    return b
 
 
 def tlf_basis():
@@ -185,7 +210,21 @@ def tlf_basis():
     tl = {0: geometric(0.02, 2.2, 28), 1: geometric(0.02, 2.2, 24),
           2: geometric(0.02, 2.2, 16), 3: geometric(0.02, 2.2, 12)}
     f = {0: geometric(0.06, 2.6, 14), 1: geometric(0.06, 2.6, 9), 2: geometric(0.06, 2.6, 3)}
-    return make_basis([((0, 0, 0), tl), ((0, 0, 3.94), f)], hmlt="DHFB", name="TlF")
+    b = make_basis([((0, 0, 0), tl), ((0, 0, 3.94), f)], hmlt="DHFB", name="TlF")
+    b.znuc, b.anuc = (81.0, 9.0), (205.0, 19.0)
+    return b
+
+
+def tlf_small_basis():
+    """TlF with the same geometry, angular momenta and exponent ranges as
+    tlf_basis but few functions (Tl 7s6p4d3f, F 4s3p1d): a case that keeps
+    TlF's quartet classes at about 1 % of its size (profiling, tests)."""
+    tl = {0: geometric(0.02, 2.2 ** 4.5, 7), 1: geometric(0.02, 2.2 ** 4.6, 6),
+          2: geometric(0.02, 2.2 ** 5.0, 4), 3: geometric(0.02, 2.2 ** 5.5, 3)}
+    f = {0: geometric(0.06, 2.6 ** 4.3, 4), 1: geometric(0.06, 2.6 ** 4.0, 3), 2: [0.5]}
+    b = make_basis([((0, 0, 0), tl), ((0, 0, 3.94), f)], hmlt="DHFB", name="TlF-small")
+    b.znuc, b.anuc = (81.0, 9.0), (205.0, 19.0)
+    return b
 
 
 def c6h6_basis():
@@ -203,7 +242,9 @@ def c6h6_basis():
         ang = math.pi / 3 * k
         u = np.array([math.cos(ang), math.sin(ang), 0.0])
         cent.append(((2.637 + 2.048) * u, h))
-    return make_basis(cent, hmlt="DHFR", name="C6H6")
+    b = make_basis(cent, hmlt="DHFR", name="C6H6")
+    b.znuc, b.anuc = (6.0,) * 6 + (1.0,) * 6, (12.0,) * 6 + (1.0,) * 6
+    return b
 
 
 def density(basis, seed=0, nocc=None, real=False):

@@ -102,6 +102,25 @@ class FockBuilder:
                                               ctypes.c_void_p(d_bxch), ld,
                                               ctypes.c_void_p(stream)), self._ctx)
 
+    def oneel(self, znuc, xi):
+        """CALL OVRLP + ONEEL: returns (OVLP, HNUC, HKIN)."""
+        n = self.ndim
+        z = np.ascontiguousarray(znuc, dtype=np.float64)
+        x = np.ascontiguousarray(xi, dtype=np.float64)
+        if z.shape != (self.basis.ncnt,) or x.shape != (self.basis.ncnt,):
+            raise BerthaGPUError(_lib.BG_ERR_ARG, "znuc and xi need one value per centre")
+        out = [np.zeros((n, n), dtype=np.complex128, order="F") for _ in range(3)]
+        check(lib().bertha_gpu_oneel(self._ctx, _p(z), _p(x), _p(out[0]), _p(out[1]),
+                                     _p(out[2]), n), self._ctx)
+        return tuple(out)
+
+    def oneel_device(self, znuc, xi, d_ovlp, d_hnuc, d_hkin, ld, stream=0):
+        z = np.ascontiguousarray(znuc, dtype=np.float64)
+        x = np.ascontiguousarray(xi, dtype=np.float64)
+        check(lib().bertha_gpu_oneel_device(self._ctx, _p(z), _p(x), ctypes.c_void_p(d_ovlp),
+                                            ctypes.c_void_p(d_hnuc), ctypes.c_void_p(d_hkin),
+                                            ld, ctypes.c_void_p(stream)), self._ctx)
+
     def clmfast_device(self, d_dent, d_gdir, d_gxch, ilev, ld, stream=0):
         """Device-resident build: pointers are integers (e.g. tensor.data_ptr())."""
         check(lib().bertha_gpu_clmfast_device(self._ctx, ctypes.c_void_p(d_dent), ld, int(ilev),

@@ -797,6 +797,157 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
 
 
 // ---------------------------------------------------------------------------
+// One-electron matrices (ONEEL bertha-scf.f:6996-7990, OVRLP :6683), FP64.
+// ---------------------------------------------------------------------------
+constexpr double CLIGHT = 137.035999084;  // speed of light (bertha-scf.f:974)
+
+// Hermite R-integrals R_tuv(alpha, X) for t+u+v <= lam by the same
+// recursion as RMAKE, serially in one thread; R and tmp hold NTE values.
+__device__ void rints_serial(double X, double Y, double Z, double alpha, int lam,
+                             const double *F, double *R, double *tmp) {
+  double *cur = R, *nxt = tmp;
+  for (int n = lam; n >= 0; --n) {
+    int cnt = ntuv(lam - n);
+    for (int k = 0; k < cnt; ++k) {
+      double val;
+      if (k == 0) {
+        double pw = 1.0;
+        for (int i = 0; i < n; ++i) pw *= -2.0 * alpha;
+        val = pw * F[n];
+      } else {
+        int t = c_t[k], u = c_u[k], v = c_v[k];
+        if (t > 0) {
+          val = X * cur[hidx(t - 1, u, v)];
+          if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
+        } else if (u > 0) {
+          val = Y * cur[hidx(t, u - 1, v)];
+          if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
+        } else {
+          val = Z * cur[hidx(t, u, v - 1)];
+          if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
+        }
+      }
+      nxt[k] = val;
+    }
+    double *t = cur; cur = nxt; nxt = t;
+  }
+  if (cur != R)
+    for (int k = 0; k < ntuv(lam); ++k) R[k] = cur[k];
+}
+
+// -sum_C PNC sum_tuv E_tuv R_tuv(APH, P - C) for the two E sets of one
+// label pair: point nuclei (xi = 0) APH = p, PNC = 2 pi Z/p; Gaussian nuclei
+// APH = p xi/(p+xi), PNC = 2 pi Z sqrt(xi/(p+xi))/p (ONEEL :7250-7330).
+__device__ void nuc_attr2(const double2 *e11, const double2 *e21, int deg, double p,
+                          const double *P, const double *nuc, int ncnt, double2 &v11,
+                          double2 &v21, double *R, double *tmp) {
+  v11 = v21 = make_double2(0.0, 0.0);
+  double F[MAXLAM + 2];
+  for (int c = 0; c < ncnt; ++c) {
+    const double *N = nuc + 5 * c;
+    double xi = N[4], aph, pnc;
+    if (xi > 0.0) {
+      aph = p * xi / (p + xi);
+      pnc = 2.0 * 3.1415926535897932 * N[3] * sqrt(xi / (p + xi)) / p;
+    } else {
+      aph = p;
+      pnc = 2.0 * 3.1415926535897932 * N[3] / p;
+    }
+    double X = P[0] - N[0], Y = P[1] - N[1], Z = P[2] - N[2];
+    boys_ref(aph * (X * X + Y * Y + Z * Z), deg, F);
+    rints_serial(X, Y, Z, aph, deg, F, R, tmp);
+    double a1 = 0.0, b1 = 0.0, a2 = 0.0, b2 = 0.0;
+    for (int k = 0; k < ntuv(deg); ++k) {
+      a1 = fma(e11[k].x, R[k], a1); b1 = fma(e11[k].y, R[k], b1);
+      a2 = fma(e21[k].x, R[k], a2); b2 = fma(e21[k].y, R[k], b2);
+    }
+    v11.x -= pnc * a1; v11.y -= pnc * b1;
+    v21.x -= pnc * a2; v21.y -= pnc * b2;
+  }
+}
+
+// the four m-sign elements of a one-electron matrix from sets (-|ma|,-|mb|)
+// and (+|ma|,-|mb|): (-,+) = -PHS conj(+,-), (+,+) = PHS conj(-,-) (ONEEL
+// :7106-7109)
+__device__ inline void put4(double2 *M, int ld, const int *r, const int *c, double2 x11,
+                           double2 x21, double phs) {
+  M[(size_t)r[0] + (size_t)ld * c[0]] = x11;
+  M[(size_t)r[1] + (size_t)ld * c[0]] = x21;
+  M[(size_t)r[0] + (size_t)ld * c[1]] = make_double2(-phs * x21.x, phs * x21.y);
+  M[(size_t)r[1] + (size_t)ld * c[1]] = make_double2(phs * x11.x, -phs * x11.y);
+}
+
+// One CTA per ordered shell pair, one thread per label pair: OVLP, HNUC
+// (V for LL; V - 2c^2 S for SS) and HKIN (c sqrt((2l+3) alpha) S_SS for the
+// LS and SL couplings, or the non-relativistic kinetic matrix for NORL).
+// nuc: [ncnt][x, y, z, Z, xi].
+__global__ void k_oneel(const Shell *sh, int ns, const PairE *pe, const double2 *E,
+                        const double *nuc, int ncnt, int nskp, int norl, double2 *S,
+                        double2 *V, double2 *T, int ld) {
+  int pair = blockIdx.x;
+  const Shell &A = sh[pair / ns], &B = sh[pair % ns];
+  int nla = 2 * A.l + 1, nlb = 2 * B.l + 1;
+  int lab = threadIdx.x;
+  if (lab >= nla * nlb) return;
+  int ia = lab / nlb, ib = lab % nlb;
+  int ka, ma, kb, mb;
+  label_of(A.l, ia, ka, ma);
+  label_of(B.l, ib, kb, mb);
+  double phs = pair_phase(ka, ma, kb, mb);
+  double p = A.alpha + B.alpha;
+  double P[3] = {(A.alpha * A.x + B.alpha * B.x) / p, (A.alpha * A.y + B.alpha * B.y) / p,
+                 (A.alpha * A.z + B.alpha * B.z) / p};
+  double eroot = pow(3.1415926535897932 / p, 1.5);
+  int r[2] = {A.fock[ia][0], A.fock[ia][1]}, c[2] = {B.fock[ib][0], B.fock[ib][1]};
+  double R[NTE], tmp[NTE];
+  // LL
+  int degl = A.l + B.l, ntl = ntuv(degl);
+  const double2 *l11 = E + pe[pair].off[0] + (long long)(lab * 2 + 0) * ntl;
+  const double2 *l21 = l11 + ntl;
+  put4(S, ld, r, c, cscale(l11[0], eroot), cscale(l21[0], eroot), phs);
+  double2 v11, v21;
+  nuc_attr2(l11, l21, degl, p, P, nuc, ncnt, v11, v21, R, tmp);
+  put4(V, ld, r, c, v11, v21, phs);
+  if (norl) {
+    double PB[3] = {P[0] - B.x, P[1] - B.y, P[2] - B.z};
+    double pb2 = PB[0] * PB[0] + PB[1] * PB[1] + PB[2] * PB[2], eb = B.alpha;
+    double e0 = eb * (2 * B.l + 3) - 2.0 * eb * eb * pb2 - 3.0 * eb * eb / p, e1 = 4.0 * eb * eb;
+    double2 t[2];
+    const double2 *ee[2] = {l11, l21};
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const double2 *e = ee[s2];
+      double2 tr = cscale(e[0], e0);
+      if (degl >= 1) {
+        double2 d = cadd(cadd(cscale(e[hidx(1, 0, 0)], PB[0]), cscale(e[hidx(0, 1, 0)], PB[1])),
+                         cscale(e[hidx(0, 0, 1)], PB[2]));
+        tr = cadd(tr, cscale(d, -e1));
+      }
+      if (degl >= 2) {
+        double2 d = cadd(cadd(e[hidx(2, 0, 0)], e[hidx(0, 2, 0)]), e[hidx(0, 0, 2)]);
+        tr = cadd(tr, cscale(d, -e1));
+      }
+      t[s2] = cscale(tr, eroot);
+    }
+    put4(T, ld, r, c, t[0], t[1], phs);
+    return;
+  }
+  // SS
+  int degs = degl + 2, nts = ntuv(degs);
+  const double2 *s11 = E + pe[pair].off[1] + (long long)(lab * 2 + 0) * nts;
+  const double2 *s21 = s11 + nts;
+  int rs[2] = {r[0] + nskp, r[1] + nskp}, cs[2] = {c[0] + nskp, c[1] + nskp};
+  double2 ss11 = cscale(s11[0], eroot), ss21 = cscale(s21[0], eroot);
+  put4(S, ld, rs, cs, ss11, ss21, phs);
+  nuc_attr2(s11, s21, degs, p, P, nuc, ncnt, v11, v21, R, tmp);
+  double cv2 = 2.0 * CLIGHT * CLIGHT;
+  put4(V, ld, rs, cs, cadd(v11, cscale(ss11, -cv2)), cadd(v21, cscale(ss21, -cv2)), phs);
+  double fsl = CLIGHT * sqrt((2 * B.l + 3) * B.alpha);  // T(a_S, b_L)
+  double fls = CLIGHT * sqrt((2 * A.l + 3) * A.alpha);  // T(a_L, b_S)
+  put4(T, ld, rs, c, cscale(ss11, fsl), cscale(ss21, fsl), phs);
+  put4(T, ld, r, cs, cscale(ss11, fls), cscale(ss21, fls), phs);
+}
+
+// ---------------------------------------------------------------------------
 // Breit / Gaunt interaction (BRTFAST :17060, BIIFAST :18337, BRTMTG :19815,
 // BRTMTZ :19172), FP64.
 // ---------------------------------------------------------------------------
@@ -1865,6 +2016,7 @@ size_t quartet_smem() {
 // ---------------------------------------------------------------------------
 struct bg_ctx {
   int ncnt = 0, ndim = 0, nskp = 0, hmlt = 0, isym = 0, racah1 = 1;
+  std::vector<double> cxyz;  // BXYZ of the centres
   int ns = 0, ncomp = 1;
   std::vector<Shell> shells;
   std::vector<int> lmax;
@@ -2240,6 +2392,7 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
   }
   bg_ctx *c = new bg_ctx();
   c->ncnt = ncnt;
+  c->cxyz.assign(bxyz, bxyz + 3 * ncnt);
   c->hmlt = hmlt;
   c->isym = shape;
   c->racah1 = (flags & BG_FLAG_NO_RACAH1) ? 0 : 1;
@@ -2585,6 +2738,63 @@ int bertha_gpu_brtfast(bg_ctx *c, const double *dent, int ldd, int ilev, double 
   CK(c, cudaMemcpy2D(bxch, sizeof(double2) * ldf, c->d_BX, sizeof(double2) * n,
                      sizeof(double2) * n, n, cudaMemcpyDeviceToHost));
   return BG_OK;
+}
+
+int bertha_gpu_oneel_device(bg_ctx *c, const double *znuc, const double *xi, double *d_ovlp,
+                             double *d_hnuc, double *d_hkin, int ldf, void *stream) {
+  if (!c || !znuc || !xi || !d_ovlp || !d_hnuc || !d_hkin) return BG_ERR_ARG;
+  if (c->bad) return BG_ERR_STATE;
+  if (ldf < c->ndim) return BG_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<double> nuc((size_t)c->ncnt * 5);
+  for (int i = 0; i < c->ncnt; ++i) {
+    if (!(xi[i] >= 0.0)) return BG_ERR_ARG;
+    for (int x = 0; x < 3; ++x) nuc[5 * i + x] = c->cxyz[3 * i + x];
+    nuc[5 * i + 3] = znuc[i];
+    nuc[5 * i + 4] = xi[i];
+  }
+  double *d_nuc = nullptr;
+  CK(c, cudaMalloc(&d_nuc, sizeof(double) * nuc.size()));
+  CK(c, cudaMemcpyAsync(d_nuc, nuc.data(), sizeof(double) * nuc.size(), cudaMemcpyHostToDevice, st));
+  c->launches = 0;
+  k_zero2d<<<1024, 256, 0, st>>>(d_ovlp, c->ndim, ldf);
+  k_zero2d<<<1024, 256, 0, st>>>(d_hnuc, c->ndim, ldf);
+  k_zero2d<<<1024, 256, 0, st>>>(d_hkin, c->ndim, ldf);
+  k_oneel<<<(unsigned)((long long)c->ns * c->ns), 64, 0, st>>>(
+      c->d_sh, c->ns, c->d_pe, c->d_E, d_nuc, c->ncnt, c->nskp, c->hmlt == BG_HMLT_NORL,
+      (double2 *)d_ovlp, (double2 *)d_hnuc, (double2 *)d_hkin, ldf);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_nuc);
+  if (e != cudaSuccess) return cuda_fail(c, e, "k_oneel");
+  c->launches += 4;
+  return BG_OK;
+}
+
+int bertha_gpu_oneel(bg_ctx *c, const double *znuc, const double *xi, double *ovlp,
+                     double *hnuc, double *hkin, int ldf) {
+  if (!c || !ovlp || !hnuc || !hkin) return BG_ERR_ARG;
+  if (c->bad) return BG_ERR_STATE;
+  if (ldf < c->ndim) return BG_ERR_ARG;
+  int n = c->ndim;
+  size_t bytes = sizeof(double2) * (size_t)n * n;
+  double *d[3] = {nullptr, nullptr, nullptr};
+  for (int k = 0; k < 3; ++k) {
+    cudaError_t e = cudaMalloc(&d[k], bytes);
+    if (e != cudaSuccess) {
+      for (int j = 0; j < k; ++j) cudaFree(d[j]);
+      return cuda_fail(c, e, "cudaMalloc");
+    }
+  }
+  int rc = bertha_gpu_oneel_device(c, znuc, xi, d[0], d[1], d[2], n, nullptr);
+  double *h[3] = {ovlp, hnuc, hkin};
+  for (int k = 0; k < 3 && rc == BG_OK; ++k) {
+    cudaError_t e = cudaMemcpy2D(h[k], sizeof(double2) * ldf, d[k], sizeof(double2) * n,
+                                 sizeof(double2) * n, n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaMemcpy2D");
+  }
+  for (int k = 0; k < 3; ++k) cudaFree(d[k]);
+  return rc;
 }
 
 void bertha_gpu_free(bg_ctx *c) {

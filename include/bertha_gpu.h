@@ -5,6 +5,8 @@
  *   CALL EQSAVE   (bertha-scf.f:5287)  -> bertha_gpu_init
  *   CALL CLMFAST  (bertha-scf.f:5401)  -> bertha_gpu_clmfast
  *   CALL BRTFAST  (bertha-scf.f:5441)  -> bertha_gpu_brtfast
+ * and, for a host SCF driver, the one-electron matrices:
+ *   CALL OVRLP; CALL ONEEL (bertha-scf.f:5345-5346) -> bertha_gpu_oneel
  * The reference passes everything through COMMON blocks; here the same
  * arrays are passed explicitly, with their Fortran (column-major) layout and
  * leading dimensions, so a Fortran caller binds them with ISO_C_BINDING
@@ -120,6 +122,23 @@ int bertha_gpu_brtfast(bg_ctx *ctx, const double *dent, int ldd, int ilev,
 /* Same build on device-resident arrays, stream-ordered on `stream`. */
 int bertha_gpu_brtfast_device(bg_ctx *ctx, const double *d_dent, int ldd,
                               int ilev, double *d_bxch, int ldf, void *stream);
+
+/* One-electron matrices, replacing CALL OVRLP and CALL ONEEL
+ * (bertha-scf.f:6683, 6996-7990):
+ *   znuc[ncnt]   nuclear charges ZNUC
+ *   xi[ncnt]     Gaussian nuclear exponents XNUC(IZ,0) = 1.5/RNUC^2 of
+ *                NUCCOUL (:1183-1210), 0 for a point nucleus
+ *   ovlp, hnuc, hkin [ldf*ndim] outputs, overwritten: OVLP (LL and SS
+ *                blocks), HNUC (nuclear attraction; SS block minus
+ *                2 c^2 S_SS), HKIN (c sigma.p couplings between L and S, or
+ *                the non-relativistic kinetic matrix for NORL). */
+int bertha_gpu_oneel(bg_ctx *ctx, const double *znuc, const double *xi,
+                     double *ovlp, double *hnuc, double *hkin, int ldf);
+
+/* Same on device-resident outputs (znuc, xi stay host arrays). */
+int bertha_gpu_oneel_device(bg_ctx *ctx, const double *znuc, const double *xi,
+                            double *d_ovlp, double *d_hnuc, double *d_hkin,
+                            int ldf, void *stream);
 
 /* Fock-build digestion over an explicit list of ordered shell quartets
  * (device array, 4 ints each: shell a, b, c, d as numbered by
