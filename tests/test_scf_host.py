@@ -1,0 +1,23 @@
+"""The SCF loop (berthagpu.scf.DHFSCF) on the oracle backend, on the CPU:
+the helium atom's Dirac-Hartree-Fock energy against its published value
+(-2.8618133 Eh, finite basis: within 2e-6), which pins the one-electron
+matrices, the MD one-centre two-electron integrals with CLMMTZ's real
+digestion, and the driver's energy, occupation and DIIS logic at once."""
+import pytest
+import torch
+
+from berthagpu import deck
+from berthagpu.scf import DHFSCF
+from scf_oracle import OracleBackend
+
+
+def test_helium_dhf_energy():
+    he = deck.make_basis([((0.0, 0.0, 0.0), {0: deck.geometric(0.06, 2.1, 18)})], hmlt="DHFR")
+    he.znuc, he.anuc = (2.0,), (4.0,)
+    scf = DHFSCF(he, nocc=2, torch=torch, backend=OracleBackend(he, racah1=False))
+    r = scf.run(max_iter=30, etol=1e-10)
+    assert r["converged"]
+    assert abs(r["energy"] - (-2.8618133)) < 2e-6
+    # Kramers-degenerate 1s1/2 pair
+    e = r["orbital_energies"]
+    assert abs(e[0] - e[1]) < 1e-10 and abs(e[0] - (-0.91799)) < 1e-4
