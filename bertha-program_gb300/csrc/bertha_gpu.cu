@@ -336,6 +336,30 @@ __global__ void k_eqgen(const Shell *sh, int ns, const PairE *pe, int ncomp,
   for (int k = 0; k < nt; ++k) dst[k] = cscale(acc[k], nrm);
 }
 
+// Sparse copy of an E-coefficient block: the nonzero coefficients of each
+// (pair, component, label pair, set[, Cartesian component]) block packed to
+// the front at the same offset, with their Hermite indices in Eci and the
+// sentinel 255 after the last one.  For pairs on a common axis or centre
+// most coefficients vanish by symmetry (exact zeros of the recursion); the
+// reference skips them through its E masks (E0LLCD0, BIIFAST IABR11).
+constexpr unsigned char ENDIDX = 255;
+__global__ void k_ecompact(const double2 *E, double2 *Ecv, unsigned char *Eci, long long nblk,
+                           const long long *boff, const int *bnt) {
+  long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (b >= nblk) return;
+  long long o = boff[b];
+  int nt = bnt[b], c = 0;
+  for (int k = 0; k < nt; ++k) {
+    double2 v = E[o + k];
+    if (v.x != 0.0 || v.y != 0.0) {
+      Ecv[o + c] = v;
+      Eci[o + c] = (unsigned char)k;
+      ++c;
+    }
+  }
+  if (c < nt) Eci[o + c] = ENDIDX;
+}
+
 // ---------------------------------------------------------------------------
 // Boys function in the reference's four regimes (FUNFM, bertha-scf.f:32465).
 // The power series multiplies by tabulated reciprocals 1/(2n+1) instead of
@@ -375,6 +399,8 @@ struct QArgs {
   const Shell *sh;
   const PairE *pe;
   const double2 *E;
+  const double2 *Ecv;        // sparse E values (k_ecompact), same offsets as E
+  const unsigned char *Eci;  // their Hermite indices
   const double2 *D;
   double *GD, *GX;
   int ns, ldd, ldf, nskp, isym, racah1;
@@ -544,7 +570,11 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
     const double2 *Eab = q.E + q.pe[Q4.x * q.ns + Q4.y].off[t1];
     const double2 *Ecd = q.E + q.pe[Q4.z * q.ns + Q4.w].off[t2];
     // left/right roles
-    const double2 *EL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
+    const double2 *ER = swp ? Eab : Ecd;
+    long long oL = swp ? q.pe[Q4.z * q.ns + Q4.w].off[t2] : q.pe[Q4.x * q.ns + Q4.y].off[t1];
+    long long oR = swp ? q.pe[Q4.x * q.ns + Q4.y].off[t1] : q.pe[Q4.z * q.ns + Q4.w].off[t2];
+    const double2 *ELv = q.Ecv + oL, *ERv = q.Ecv + oR;
+    const unsigned char *ELi = q.Eci + oL, *ERi = q.Eci + oR;
     int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
     int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
     int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;  // second label count
@@ -559,12 +589,17 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
       for (int w = threadIdx.x; w < nch * 2 * nR; w += blockDim.x) {
         int lab = w / (2 * nR), rem = w % (2 * nR);
         int set = rem / nR, qq = rem % nR;
-        const double2 *e = EL + ((long long)(c0 + lab) * 2 + set) * nL;
+        long long eo = ((long long)(c0 + lab) * 2 + set) * nL;
+        const double2 *ev_ = ELv + eo;
+        const unsigned char *ei = ELi + eo;
         int tq = c_t[qq], uq = c_u[qq], vq = c_v[qq];
         double ax = 0.0, ay = 0.0;
-        for (int s = 0; s < nL; ++s) {
+        // nonzero E terms only (sparse copy; see k_ecompact)
+        for (int k = 0; k < nL; ++k) {
+          int s = ei[k];
+          if (s == ENDIDX) break;
           double rv = R[hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq)];
-          double2 ev = e[s];
+          double2 ev = ev_[k];
           ax = fma(ev.x, rv, ax);
           ay = fma(ev.y, rv, ay);
         }
@@ -597,10 +632,21 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         if (q.isym && !q.bound) {
           // CLMMTZ reads only the real parts of combinations 0, 3, 12, 15
           // (direct) and 0, 6, 9, 15 (exchange): sets 1 and 4 of ERIFAST's
-          // linear-molecule path (:12820-12912), 4 of the 16 products
+          // linear-molecule path (:12820-12912), 4 of the 16 products, over
+          // the nonzero E terms of each set
+          long long eo = (long long)lr * 2 * nR;
+          const double2 *v1 = ERv + eo, *v2 = v1 + nR;
+          const unsigned char *i1 = ERi + eo, *i2 = i1 + nR;
           for (int k = 0; k < nR; ++k) {
-            double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
+            int kk = i1[k];
+            if (kk == ENDIDX) break;
+            double2 u1 = v1[k], x1 = g11[kk];
             a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
+          }
+          for (int k = 0; k < nR; ++k) {
+            int kk = i2[k];
+            if (kk == ENDIDX) break;
+            double2 u2 = v2[k], x2 = g21[kk];
             a3 = fma(u2.x, x2.x, a3); b3 = fma(u2.y, x2.y, b3);
           }
         } else
@@ -1040,6 +1086,8 @@ struct BArgs {
   const Shell *sh;
   const long long *offq;
   const double2 *E;
+  const double2 *Ecv;        // sparse E values (k_ecompact), same offsets as E
+  const unsigned char *Eci;  // their Hermite indices
   const double2 *D;
   double *BX;
   int ns, ldd, ldf, nskp, isym, racah1, gaunt;
@@ -1183,7 +1231,11 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
     const double2 *Eab = q.E + q.offq[((size_t)Q4.x * q.ns + Q4.y) * 2 + t1];
     const double2 *Ecd = q.E + q.offq[((size_t)Q4.z * q.ns + Q4.w) * 2 + t2];
     // left/right roles
-    const double2 *EL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
+    const double2 *ER = swp ? Eab : Ecd;
+    long long oL = q.offq[swp ? ((size_t)Q4.z * q.ns + Q4.w) * 2 + t2 : ((size_t)Q4.x * q.ns + Q4.y) * 2 + t1];
+    long long oR = q.offq[swp ? ((size_t)Q4.x * q.ns + Q4.y) * 2 + t1 : ((size_t)Q4.z * q.ns + Q4.w) * 2 + t2];
+    const double2 *ELv = q.Ecv + oL, *ERv = q.Ecv + oR;
+    const unsigned char *ELi = q.Eci + oL, *ERi = q.Eci + oR;
     int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
     int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
     int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;
@@ -1200,15 +1252,21 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
       for (int w = threadIdx.x; w < nch * 6 * nR; w += blockDim.x) {
         int lab = w / (6 * nR), rem = w % (6 * nR);
         int set = rem / (3 * nR), i = (rem / nR) % 3, qq = rem % nR;
-        const double2 *e = EL + ((long long)(c0 + lab) * 2 + set) * 3 * nL;
+        long long eo = ((long long)(c0 + lab) * 2 + set) * 3 * nL;
         int tq = c_t[qq], uq = c_u[qq], vq = c_v[qq];
         double ax = 0.0, ay = 0.0;
-        for (int s = 0; s < nL; ++s) {
-          const double *wr = W + hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq) * 9 + 3 * i;
-          double2 e0 = e[s], e1 = e[nL + s], e2 = e[2 * nL + s];
-          double w0 = wr[0], w1 = wr[1], w2 = wr[2];
-          ax = fma(e0.x, w0, fma(e1.x, w1, fma(e2.x, w2, ax)));
-          ay = fma(e0.y, w0, fma(e1.y, w1, fma(e2.y, w2, ay)));
+        // nonzero E terms of each Cartesian component j (sparse copy)
+        for (int j = 0; j < 3; ++j) {
+          const double2 *ev_ = ELv + eo + j * nL;
+          const unsigned char *ei = ELi + eo + j * nL;
+          for (int k = 0; k < nL; ++k) {
+            int s = ei[k];
+            if (s == ENDIDX) break;
+            double w = W[hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq) * 9 + 3 * i + j];
+            double2 ev = ev_[k];
+            ax = fma(ev.x, w, ax);
+            ay = fma(ev.y, w, ay);
+          }
         }
         unsigned long long zm = ((tq + uq + vq) & 1) ? SGN : 0ULL;
         G[((lab * 2 + set) * 3 + i) * nR + qq] = make_double2(flip(ax, zm), flip(ay, zm));
@@ -1238,10 +1296,20 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
           const double2 *e11 = ER + (((long long)lr * 2 + 0) * 3 + i) * nR;
           const double2 *e21 = ER + (((long long)lr * 2 + 1) * 3 + i) * nR;
           if (lin) {
-            // BRTMTZ reads only the real parts of combinations 0, 6, 9, 15
+            // BRTMTZ reads only the real parts of combinations 0, 6, 9, 15;
+            // nonzero E terms of each set only
+            long long e1o = (((long long)lr * 2 + 0) * 3 + i) * nR;
+            long long e2o = (((long long)lr * 2 + 1) * 3 + i) * nR;
             for (int k = 0; k < nR; ++k) {
-              double2 u1 = e11[k], u2 = e21[k], x1 = g11[k], x2 = g21[k];
+              int kk = ERi[e1o + k];
+              if (kk == ENDIDX) break;
+              double2 u1 = ERv[e1o + k], x1 = g11[kk];
               a0 = fma(u1.x, x1.x, a0); b0 = fma(u1.y, x1.y, b0);
+            }
+            for (int k = 0; k < nR; ++k) {
+              int kk = ERi[e2o + k];
+              if (kk == ENDIDX) break;
+              double2 u2 = ERv[e2o + k], x2 = g21[kk];
               a3 = fma(u2.x, x2.x, a3); b3 = fma(u2.y, x2.y, b3);
             }
             continue;
@@ -2025,6 +2093,8 @@ struct bg_ctx {
   PairE *d_pe = nullptr;
   double2 *d_E = nullptr;
   long long nE = 0;
+  double2 *d_Ecv = nullptr;        // sparse copies of d_E (k_ecompact)
+  unsigned char *d_Eci = nullptr;
   // quartet lists for the Fock build, one per (t1,t2) component class
   int *d_quart[4] = {nullptr, nullptr, nullptr, nullptr};
   long long nquart[4] = {0, 0, 0, 0};
@@ -2040,6 +2110,8 @@ struct bg_ctx {
   int gaunt = 0;
   double2 *d_EB = nullptr;
   long long *d_offq = nullptr;
+  double2 *d_EBcv = nullptr;       // sparse copies of d_EB
+  unsigned char *d_EBci = nullptr;
   long long nEB = 0;
   int *d_bquart[2] = {nullptr, nullptr};
   long long nbquart[2] = {0, 0};
@@ -2239,6 +2311,7 @@ int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   }
   QArgs a;
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_E; a.D = d_D;
+  a.Ecv = c->d_Ecv; a.Eci = c->d_Eci;
   a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = ldd; a.ldf = ldf;
   a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym;
   a.bound = bound;
@@ -2246,6 +2319,29 @@ int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   k_quartet<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
   c->launches++;
+  return 0;
+}
+
+// Sparse copies (k_ecompact) of an E array made of blocks of nt coefficients
+// at the offsets given.
+int compact_e(bg_ctx *c, const double2 *E, long long n, const std::vector<long long> &boff,
+              const std::vector<int> &bnt, double2 **cv, unsigned char **ci) {
+  CK(c, cudaMalloc(cv, sizeof(double2) * std::max<long long>(n, 1)));
+  CK(c, cudaMalloc(ci, std::max<long long>(n, 1)));
+  long long nb = (long long)boff.size();
+  if (nb == 0) return 0;
+  long long *d_off = nullptr;
+  int *d_nt = nullptr;
+  CK(c, cudaMalloc(&d_off, sizeof(long long) * nb));
+  CK(c, cudaMalloc(&d_nt, sizeof(int) * nb));
+  CK(c, cudaMemcpy(d_off, boff.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(d_nt, bnt.data(), sizeof(int) * nb, cudaMemcpyHostToDevice));
+  k_ecompact<<<(unsigned)((nb + 127) / 128), 128>>>(E, *cv, *ci, nb, d_off, d_nt);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaGetLastError();
+  cudaFree(d_off);
+  cudaFree(d_nt);
+  if (e != cudaSuccess) return cuda_fail(c, e, "k_ecompact");
   return 0;
 }
 
@@ -2281,7 +2377,19 @@ int breit_prepare(bg_ctx *c) {
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(c, e, "k_eqgen_q");
   c->nEB = off;
-  return 0;
+  std::vector<long long> boff;
+  std::vector<int> bnt;
+  for (int a = 0; a < ns; ++a)
+    for (int b = 0; b < ns; ++b) {
+      int la = c->shells[a].l, lb = c->shells[b].l, nt = ntuv(la + lb + 1);
+      int nblk = (2 * la + 1) * (2 * lb + 1) * 6;
+      for (int comp = 0; comp < 2; ++comp)
+        for (int k = 0; k < nblk; ++k) {
+          boff.push_back(offq[((size_t)a * ns + b) * 2 + comp] + (long long)k * nt);
+          bnt.push_back(nt);
+        }
+    }
+  return compact_e(c, c->d_EB, off, boff, bnt, &c->d_EBcv, &c->d_EBci);
 }
 
 // Shell quartets of the Breit classes with BRTFAST's centre and stage rules
@@ -2339,6 +2447,7 @@ int launch_breit(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const 
   }
   BArgs a;
   a.sh = c->d_sh; a.offq = c->d_offq; a.E = c->d_EB; a.D = d_D; a.BX = d_BX;
+  a.Ecv = c->d_EBcv; a.Eci = c->d_EBci;
   a.ns = c->ns; a.ldd = ldd; a.ldf = ldf; a.nskp = c->nskp; a.isym = c->isym;
   a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual; a.bound = bound;
   long long grid = std::min<long long>(nq, 152LL * 64);
@@ -2518,6 +2627,27 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
     cuda_fail(nullptr, e, "k_econv");
     bertha_gpu_free(c);
     return BG_ERR_CUDA;
+  }
+  {
+    std::vector<long long> boff;
+    std::vector<int> bnt;
+    for (int a = 0; a < ns; ++a)
+      for (int b = 0; b < ns; ++b) {
+        int la = c->shells[a].l, lb = c->shells[b].l;
+        int nblk = (2 * la + 1) * (2 * lb + 1) * 2;
+        for (int comp = 0; comp < ncomp; ++comp) {
+          int nt = ntuv(la + lb + 2 * comp);
+          for (int k = 0; k < nblk; ++k) {
+            boff.push_back(pe[(size_t)a * ns + b].off[comp] + (long long)k * nt);
+            bnt.push_back(nt);
+          }
+        }
+      }
+    if (compact_e(c, c->d_E, off, boff, bnt, &c->d_Ecv, &c->d_Eci)) {
+      g_init_err = c->err;
+      bertha_gpu_free(c);
+      return BG_ERR_CUDA;
+    }
   }
   *out = c;
   return BG_OK;
@@ -2810,6 +2940,10 @@ void bertha_gpu_free(bg_ctx *c) {
   cudaFree(c->d_GX);
   cudaFree(c->d_EB);
   cudaFree(c->d_offq);
+  cudaFree(c->d_Ecv);
+  cudaFree(c->d_Eci);
+  cudaFree(c->d_EBcv);
+  cudaFree(c->d_EBci);
   for (int k = 0; k < 2; ++k) cudaFree(c->d_bquart[k]);
   cudaFree(c->d_BX);
   delete c;
