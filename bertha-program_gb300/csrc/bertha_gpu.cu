@@ -339,7 +339,7 @@ __global__ void k_eqgen(const Shell *sh, int ns, const PairE *pe, int ncomp,
 // Sparse copy of an E-coefficient block: the nonzero coefficients of each
 // (pair, component, label pair, set[, Cartesian component]) block packed to
 // the front at the same offset, with their Hermite indices in Eci and the
-// sentinel 255 after the last one.  For pairs on a common axis or centre
+// sentinel 255 in every slot after the last one.  For pairs on a common axis or centre
 // most coefficients vanish by symmetry (exact zeros of the recursion); the
 // reference skips them through its E masks (E0LLCD0, BIIFAST IABR11).
 constexpr unsigned char ENDIDX = 255;
@@ -357,7 +357,7 @@ __global__ void k_ecompact(const double2 *E, double2 *Ecv, unsigned char *Eci, l
       ++c;
     }
   }
-  if (c < nt) Eci[o + c] = ENDIDX;
+  for (int k = c; k < nt; ++k) Eci[o + k] = ENDIDX;  // every slot after the last is a sentinel
 }
 
 // ---------------------------------------------------------------------------
@@ -1609,6 +1609,7 @@ struct QArgsDF {
   const Shell *sh;
   const PairE *pe;
   const float4 *E;
+  const unsigned char *Eci;  // Hermite indices of the nonzero E terms (k_ecompact)
   const float4 *D;  // n x n, leading dimension n
   double *GD, *GX;
   int ns, ldd, ldf, nskp, isym, racah1;
@@ -1670,6 +1671,7 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
   double2 *Kl = Jl + MAXSP * MAXSP;
   double2 *J2 = Kl + MAXSP * MAXSP;            // with sym only
   double2 *K2 = J2 + MAXSP * MAXSP;
+  __shared__ unsigned char ELi[CHDF * 2 * NTE];  // Hermite indices of the staged E
   __shared__ double sgeo[8];
   __shared__ int sk;
 
@@ -1763,6 +1765,8 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
     const float4 *Eab = q.E + pab_e.off[t1];
     const float4 *Ecd = q.E + pcd_e.off[t2];
     const float4 *EGL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
+    const unsigned char *EGi = q.Eci + (swp ? pcd_e.off[t2] : pab_e.off[t1]);
+    const unsigned char *ERi = q.Eci + (swp ? pab_e.off[t1] : pcd_e.off[t2]);
     int kL = swp ? pcd_e.kexp : pab_e.kexp, kR = swp ? pab_e.kexp : pcd_e.kexp;
     int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
     int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
@@ -1773,11 +1777,15 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
     __syncthreads();
     for (int c0 = 0; c0 < nlL; c0 += CHDF) {
       int nch = min(CHDF, nlL - c0);
-      // stage the left E-coefficients rescaled to this quartet's exponent
+      // stage the nonzero left E-coefficients (packed, with their Hermite
+      // indices) rescaled to this quartet's exponent
       for (int w = threadIdx.x; w < nch * 2 * nL; w += blockDim.x) {
-        int s = w % nL;
+        long long g = (long long)c0 * 2 * nL + w;
+        int s = EGi[g];
+        ELi[w] = (unsigned char)s;
+        if (s == ENDIDX) continue;
         int L = c_t[s] + c_u[s] + c_v[s];
-        float4 v = EGL[(long long)c0 * 2 * nL + w];
+        float4 v = EGL[g - (w % nL) + s];
         float f = ldexpf(1.0f, (kq0 - kL) * L);
         EL[w] = make_float4(v.x * f, v.y * f, v.z * f, v.w * f);
       }
@@ -1786,11 +1794,14 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
       for (int w = threadIdx.x; w < nch * 2 * nR; w += blockDim.x) {
         int ls = w / nR, qq = w % nR;
         const float4 *e = EL + ls * nL;
+        const unsigned char *ei = ELi + ls * nL;
         int tq = c_t[qq], uq = c_u[qq], vq = c_v[qq];
         float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-        for (int s = 0; s < nL; ++s) {
+        for (int k = 0; k < nL; ++k) {
+          int s = ei[k];
+          if (s == ENDIDX) break;
           float2 rv = Rf[hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq)];
-          float4 ev = e[s];
+          float4 ev = e[k];
           df_fma(ev.x, ev.y, rv.x, rv.y, rh, rl);
           df_fma(ev.z, ev.w, rv.x, rv.y, ih, il);
         }
@@ -1835,13 +1846,20 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
             if (q.isym) {
               // CLMMTZ reads only the real parts of combinations 0, 3, 12,
               // 15 and 0, 6, 9, 15: products (e11 x g11) and (e21 x g21),
-              // real-by-real and imaginary-by-imaginary (ERIFAST :12820-12912)
+              // real-by-real and imaginary-by-imaginary (ERIFAST :12820-12912),
+              // over the nonzero E terms of each set
+              const unsigned char *i1 = ERi + (long long)lr * 2 * nR, *i2 = i1 + nR;
               for (int k = part; k < nR; k += KS) {
-                float4 u1 = u1n, u2 = u2n;
-                if (k + KS < nR) { u1n = e11[k + KS]; u2n = e21[k + KS]; }
-                float4 x1 = g11[k], x2 = g21[k];
+                int kk = i1[k];
+                if (kk == ENDIDX) break;
+                float4 u1 = e11[kk], x1 = g11[kk];
                 df_fma(u1.x, u1.y, x1.x, x1.y, acc[0][0], acc[0][1]);
                 df_fma(u1.z, u1.w, x1.z, x1.w, acc[1][0], acc[1][1]);
+              }
+              for (int k = part; k < nR; k += KS) {
+                int kk = i2[k];
+                if (kk == ENDIDX) break;
+                float4 u2 = e21[kk], x2 = g21[kk];
                 df_fma(u2.x, u2.y, x2.x, x2.y, acc[12][0], acc[12][1]);
                 df_fma(u2.z, u2.w, x2.z, x2.w, acc[13][0], acc[13][1]);
               }
@@ -2260,7 +2278,7 @@ int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   int n = c->ndim;
   k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, ddf);
   QArgsDF a;
-  a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = ddf;
+  a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = ddf; a.Eci = c->d_Eci;
   a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = n; a.ldf = ldf;
   a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym;
   long long grid = std::min<long long>(nq, 152LL * 128);
