@@ -205,7 +205,7 @@ def h2o_fock_build(torch, with_cpu):
         out[f"{prec}_s"] = float(np.median(ts))
     e = {}
     for prec, (gd, gx) in res.items():
-        e[prec] = (0.5 * np.sum(dent * gd.T).real, 0.5 * np.sum(dent * gx.T).real)
+        e[prec] = (0.5 * np.sum(dent * gd).real, 0.5 * np.sum(dent * gx).real)
     out["energy_j_eh"], out["energy_k_eh"] = e["fp64"]
     out["split_energy_err_eh"] = float(max(abs(e["df32"][0] - e["fp64"][0]),
                                            abs(e["df32"][1] - e["fp64"][1])))
@@ -264,7 +264,30 @@ def h2o_breit_build(torch):
             "flops": flops, "tflops": flops / t / 1e12,
             "host_api_s": float(np.median(ts)),
             "host_vs_device_max_abs": float(np.abs(bx_h - bx).max()),
-            "energy_bx_eh": float(0.5 * np.sum(dent * bx.T).real)}
+            "energy_bx_eh": float(0.5 * np.sum(dent * bx).real)}
+
+
+def h2o_scf(torch):
+    """The H2O Dirac-Coulomb SCF configuration: closed shell, Gaussian
+    nuclei, Schwarz 1e-12, converged to |dE| < 1e-9 Eh from the bare-nucleus
+    guess; every iteration's Fock build, eigensolve and DIIS on the GPU.
+    Run with the FP64 and the split-precision Fock build; the difference of
+    the converged total energies is the precision's energy error."""
+    from berthagpu import deck
+    from berthagpu.scf import DHFSCF
+    a = torch.randn(64, 64, dtype=torch.complex128, device="cuda")
+    torch.linalg.eigh(a + a.conj().T)  # cuSOLVER initialisation outside the timing
+    torch.cuda.synchronize()
+    b = deck.h2o_basis()
+    out = {"molecule": "H2O", "ndim": b.ndim, "nocc": 10, "screen": 1e-12, "etol_eh": 1e-9}
+    for prec in ("fp64", "df32"):
+        scf = DHFSCF(b, nocc=10, precision=prec, screen=1e-12, torch=torch)
+        r = scf.run(max_iter=60, etol=1e-9)
+        scf.close()
+        out[prec] = {k: r[k] for k in ("energy", "iterations", "converged", "wall_s", "fock_s",
+                                       "linalg_s", "oneel_s")}
+    out["energy_diff_split_vs_fp64_eh"] = abs(out["df32"]["energy"] - out["fp64"]["energy"])
+    return out
 
 
 def fp64_peak(torch):
@@ -380,7 +403,8 @@ def run_gpu(args):
     scale = max(np.abs(gd64).max(), np.abs(gx64).max())
 
     def e2(gd, gx):
-        return (0.5 * np.sum(dent * gd.T).real, 0.5 * np.sum(dent * gx.T).real)
+        # 1/2 sum_ij D_ij G_ij, the reference's energy sum (ENRGIES)
+        return (0.5 * np.sum(dent * gd).real, 0.5 * np.sum(dent * gx).real)
 
     ej64, ek64 = e2(gd64, gx64)
     ejm, ekm = e2(gdm, gxm)
@@ -436,10 +460,11 @@ def run_gpu(args):
     traffic = read_traffic()
 
     line = None
-    h2o = breit = None
+    h2o = breit = scf = None
     if rank == 0 and not args.no_h2o:
         h2o = h2o_fock_build(torch, with_cpu=(world == 1))
         breit = h2o_breit_build(torch)
+        scf = h2o_scf(torch)
     if rank == 0:
         cpu = None
         if world == 1:
@@ -478,6 +503,7 @@ def run_gpu(args):
             "clocks": clocks,
             "fock_build_h2o": h2o,
             "breit_build_h2o": breit,
+            "scf_h2o": scf,
         }
         print(json.dumps(line), flush=True)
     fb.close()

@@ -6,7 +6,7 @@
 Cases: h2o, tlf, tlf-small, c6h6.  The density is a seeded random Hermitian
 one (DENSTY form); the output is one JSON line with the wall time of each
 call through the host-array entry points and the energy terms
-1/2 Re tr(D G) of the matrices built.
+1/2 sum_ij D_ij G_ij of the matrices built (ENRGIES' convention).
 """
 import argparse
 import json
@@ -54,8 +54,8 @@ def main(argv=None):
             gd, gx = fb.clmfast(dent, a.ilev)
             ts.append(time.perf_counter() - t0)
         out["coulomb_s"] = ts
-        out["energy_j_eh"] = float(0.5 * np.sum(dent * gd.T).real)
-        out["energy_k_eh"] = float(0.5 * np.sum(dent * gx.T).real)
+        out["energy_j_eh"] = float(0.5 * np.sum(dent * gd).real)
+        out["energy_k_eh"] = float(0.5 * np.sum(dent * gx).real)
     if a.build in ("breit", "both"):
         ts = []
         for _ in range(a.repeat):
@@ -63,7 +63,7 @@ def main(argv=None):
             bx = fb.brtfast(dent, a.ilev)
             ts.append(time.perf_counter() - t0)
         out["breit_s"] = ts
-        out["energy_bx_eh"] = float(0.5 * np.sum(dent * bx.T).real)
+        out["energy_bx_eh"] = float(0.5 * np.sum(dent * bx).real)
     fb.close()
     print(json.dumps(out), flush=True)
 

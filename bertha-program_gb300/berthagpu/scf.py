@@ -99,7 +99,10 @@ class DHFSCF:
         self.backend = backend or GPUBackend(basis, precision, screen, breit, racah1, torch)
         self.n = self.backend.n
 
-    def run(self, max_iter=60, etol=1e-9, ndiis=8, verbose=False):
+    def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, verbose=False):
+        """Iterate to |dE| < etol.  shift: LEVSHFT's virtual-space level shift
+        SHLV in Eh (the H2O deck's stage-3 value 0.5), applied from the second
+        iteration on; it moves the path, not the converged solution."""
         t = self.torch
         be = self.backend
         dev = be.device
@@ -120,9 +123,9 @@ class DHFSCF:
             nneg = int((e < -CLIGHT * CLIGHT).sum().item())
             occ = C[:, nneg:nneg + self.nocc]
             # DENSTY: D_ij = sum_occ conj(C_i) C_j
-            return e, nneg, occ.conj() @ occ.T
+            return e, nneg, occ.conj() @ occ.T, C
 
-        eps, nneg, D = solve(H1)
+        eps, nneg, D, C = solve(H1)
         hist_F, hist_E = [], []
         energy, last = None, None
         iters, t_fock, t_lin = [], 0.0, 0.0
@@ -135,6 +138,11 @@ class DHFSCF:
             F = H1 + G
             # ENRGIES on the density that built F
             energy = enuc + float(t.sum(D * (H1 + 0.5 * G)).real.item())
+            if shift and it > 1:
+                # LEVSHFT (:3641): F += SHLV sum_vir (S c_v)(S c_v)^+ over the
+                # positive-energy virtuals of the last diagonalisation
+                A = S @ C[:, nneg + self.nocc:]
+                F = F + shift * (A @ A.conj().T)
             # DIIS on the commutator F P S - S P F, P = D^T
             P = D.T
             err = F @ P @ S - S @ P @ F
@@ -157,7 +165,7 @@ class DHFSCF:
                 rhs[m] = -1.0
                 w = t.linalg.solve(B, rhs)
                 F = sum(w[i] * hist_F[i] for i in range(m))
-            eps, nneg, D = solve(F)
+            eps, nneg, D, C = solve(F)
             be.sync()
             t_lin += time.perf_counter() - tf
             de = None if last is None else energy - last
