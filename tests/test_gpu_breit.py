@@ -116,3 +116,30 @@ def test_breit_schwarz_screening():
     bx = fb.brtfast(dent, 3)
     assert np.abs(bx - ref).max() <= TOL * np.abs(ref).max()
     fb.close()
+
+
+def _tlf_like():
+    """TlF geometry with f functions on Tl and d on F, a few exponents each:
+    linear real digestion, high l, sparse E and both contraction orders."""
+    tl = {0: deck.geometric(0.5, 12.0, 3), 1: deck.geometric(0.4, 10.0, 2), 2: [0.8, 6.0],
+          3: [1.5]}
+    f = {0: deck.geometric(0.3, 9.0, 2), 1: [0.6], 2: [1.1]}
+    return deck.make_basis([((0, 0, 0), tl), ((0, 0, 3.94), f)], hmlt="DHFB")
+
+
+def test_tlf_like_coulomb_and_breit():
+    b = _tlf_like()
+    assert b.isym == 1
+    d = deck.density(b, seed=3, real=True)
+    fb = berthagpu.FockBuilder(b)
+    gd, gx = fb.clmfast(d, 3)
+    bx = fb.brtfast(d, 3)
+    fb.set_precision("df32")
+    gdm, gxm = fb.clmfast(d, 3)
+    fb.close()
+    rd, rx = orc.clmfast(b, d, 3)
+    rb = orc.brtfast(b, d, 3)
+    s = max(np.abs(rd).max(), np.abs(rx).max())
+    assert np.abs(gd - rd).max() <= TOL * s and np.abs(gx - rx).max() <= TOL * s
+    assert np.abs(gdm - rd).max() <= 1e-10 * s and np.abs(gxm - rx).max() <= 1e-10 * s
+    assert np.abs(bx - rb).max() <= TOL * np.abs(rb).max()
