@@ -39,6 +39,7 @@ def lib():
         L.bertha_gpu_dims.argtypes = [P, P, P]
         L.bertha_gpu_set_precision.argtypes = [P, i]
         L.bertha_gpu_set_screening.argtypes = [P, ctypes.c_double]
+        L.bertha_gpu_set_list_limits.argtypes = [P, ll, ll]
         L.bertha_gpu_clmfast.argtypes = [P, P, i, i, P, P, i]
         L.bertha_gpu_clmfast_device.argtypes = [P, P, i, i, P, P, i, P]
         L.bertha_gpu_brtfast.argtypes = [P, P, i, i, P, i]
@@ -61,6 +62,7 @@ def lib():
 
 EXPORTED = [
     "bertha_gpu_init", "bertha_gpu_set_screening", "bertha_gpu_set_precision",
+    "bertha_gpu_set_list_limits",
     "bertha_gpu_dims", "bertha_gpu_clmfast",
     "bertha_gpu_clmfast_device", "bertha_gpu_brtfast", "bertha_gpu_brtfast_device",
     "bertha_gpu_oneel", "bertha_gpu_oneel_device",

@@ -48,6 +48,12 @@ class FockBuilder:
         """Schwarz threshold on Q_ab*Q_cd (0 = off, the reference default)."""
         check(lib().bertha_gpu_set_screening(self._ctx, float(threshold)), self._ctx)
 
+    def set_list_limits(self, cache_quartets=0, chunk_quartets=0):
+        """Quartet-list memory: cached up to cache_quartets, streamed in chunks
+        of chunk_quartets above (0: library defaults)."""
+        check(lib().bertha_gpu_set_list_limits(self._ctx, int(cache_quartets),
+                                               int(chunk_quartets)), self._ctx)
+
     def close(self):
         if self._ctx:
             lib().bertha_gpu_free(self._ctx)

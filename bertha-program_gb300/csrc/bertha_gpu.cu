@@ -2117,6 +2117,12 @@ struct bg_ctx {
   int *d_quart[4] = {nullptr, nullptr, nullptr, nullptr};
   long long nquart[4] = {0, 0, 0, 0};
   int quart_ilev = -1;
+  // lists too large to keep: regenerated every build and streamed in chunks
+  // through two pinned host and two device buffers
+  bool stream_lists = false;
+  long long cache_q = 0, chunk_q = 0;  // limits in quartets (0: defaults)
+  int *h_chunk[2] = {nullptr, nullptr}, *d_chunk[2] = {nullptr, nullptr};
+  cudaEvent_t chunk_ev[2] = {nullptr, nullptr};
   double screen = 0.0;          // Schwarz threshold on Q_ab*Q_cd, 0 = off
   std::vector<double> qbound;   // [pair*2+comp] sqrt max |(ab|ab)|
   double2 *d_D = nullptr, *d_GD = nullptr, *d_GX = nullptr;
@@ -2189,49 +2195,71 @@ int upload_tables() {
 
 // Ordered shell quartets of the multi-centre build for one component class,
 // with CLMFAST's centre and stage rules (bertha-scf.f:11672-11677,
-// 12045-12084) and the one-centre parity rule (:11753-11764).
+// 12045-12084) and the one-centre parity rule (:11753-11764), handed to
+// sink(a, b, c, d) one by one.
 // With `sym`, (ab|cd) = (cd|ab) is used: only pairs ab >= cd (pair index
 // a*ns+b) are listed for LL|LL and SS|SS, LL|SS lists every ordered pair and
 // SS|LL none; the kernels digest each listed quartet for both orders.
 // Quartets come out grouped by angular class (l_a,l_b,l_c,l_d), highest
 // first, so neighbouring CTAs carry similar work.  With a Schwarz threshold
 // quartets with Q_ab Q_cd below it are left out (SCHWARZ :37889, at the
-// level of shell pairs).
-std::vector<int> build_quartets(const bg_ctx *c, int t1, int t2, int ilev, bool sym) {
-  std::vector<int> out;
+// level of shell pairs); within a class the pairs are visited in order of
+// decreasing bound, so the scan of cd pairs stops at the first one below
+// threshold/Q_ab.
+struct PairRec {
+  int a, b;
+  double q;
+  long long idx;
+};
+
+void pair_lists(const bg_ctx *c, int t, bool scr, std::vector<PairRec> (&pl)[MAXLB + 1][MAXLB + 1]) {
+  for (int a = 0; a < c->ns; ++a)
+    for (int b = 0; b < c->ns; ++b) {
+      long long idx = (long long)a * c->ns + b;
+      pl[c->shells[a].l][c->shells[b].l].push_back({a, b, scr ? c->qbound[idx * 2 + t] : 1.0, idx});
+    }
+  if (scr)
+    for (auto &row : pl)
+      for (auto &v : row)
+        std::stable_sort(v.begin(), v.end(),
+                         [](const PairRec &x, const PairRec &y) { return x.q > y.q; });
+}
+
+template <class Sink>
+void gen_quartets(const bg_ctx *c, int t1, int t2, int ilev, bool sym, Sink &&sink) {
   int itt = 1 + 2 * t1 + t2;
-  if (sym && t1 == 1 && t2 == 0) return out;
-  std::vector<int> byl[MAXLB + 1];
-  for (int s = 0; s < c->ns; ++s) byl[c->shells[s].l].push_back(s);
+  if (sym && t1 == 1 && t2 == 0) return;
   bool scr = c->screen > 0.0 && !c->qbound.empty();
+  std::vector<PairRec> pl1[MAXLB + 1][MAXLB + 1], pl2[MAXLB + 1][MAXLB + 1];
+  pair_lists(c, t1, scr, pl1);
+  if (t2 != t1) pair_lists(c, t2, scr, pl2);
+  auto &P2 = (t2 != t1) ? pl2 : pl1;
   for (int la = MAXLB; la >= 0; --la)
   for (int lb = MAXLB; lb >= 0; --lb)
   for (int lc = MAXLB; lc >= 0; --lc)
   for (int ld = MAXLB; ld >= 0; --ld) {
-    for (int a : byl[la])
-    for (int b : byl[lb]) {
-      long long pab = (long long)a * c->ns + b;
-      double qab = scr ? c->qbound[pab * 2 + t1] : 0.0;
-      for (int cc : byl[lc])
-      for (int d : byl[ld]) {
-        long long pcd = (long long)cc * c->ns + d;
-        if (sym && t1 == t2 && pab < pcd) continue;
-        const Shell &A = c->shells[a], &B = c->shells[b], &C = c->shells[cc], &D = c->shells[d];
-        int s4[4] = {A.cnt, B.cnt, C.cnt, D.cnt};
-        std::sort(s4, s4 + 4);
-        int mcnt = 1;
-        for (int k = 1; k < 4; ++k) mcnt += s4[k] != s4[k - 1];
+    const std::vector<PairRec> &X = pl1[la][lb], &Y = P2[lc][ld];
+    if (X.empty() || Y.empty()) continue;
+    bool par = ((la + lb) & 1) != ((lc + ld) & 1);
+    for (const PairRec &x : X) {
+      if (scr && x.q * Y[0].q < c->screen) break;
+      const Shell &A = c->shells[x.a], &B = c->shells[x.b];
+      for (const PairRec &y : Y) {
+        if (scr && x.q * y.q < c->screen) break;
+        if (sym && t1 == t2 && x.idx < y.idx) continue;
+        const Shell &C = c->shells[y.a], &D = c->shells[y.b];
+        int mcnt = 1 + (B.cnt != A.cnt) + (C.cnt != A.cnt && C.cnt != B.cnt) +
+                   (D.cnt != A.cnt && D.cnt != B.cnt && D.cnt != C.cnt);
         if (mcnt == 1 && c->racah1) continue;
         if (ilev == 1 && itt > 1 && mcnt != 1) continue;
         if (ilev == 2 && itt > 3 && mcnt != 1) continue;
-        if (mcnt == 1 && !c->racah1 && ((la + lb) & 1) != ((lc + ld) & 1)) continue;
-        if (scr && qab * c->qbound[pcd * 2 + t2] < c->screen) continue;
-        out.push_back(a); out.push_back(b); out.push_back(cc); out.push_back(d);
+        if (mcnt == 1 && par) continue;
+        sink(x.a, x.b, y.a, y.b);
       }
     }
   }
-  return out;
 }
+
 
 int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                     const double2 *d_D, int ldd, double *d_GD, double *d_GX,
@@ -2500,6 +2528,53 @@ int compute_breit_bounds(bg_ctx *c, cudaStream_t st) {
   return 0;
 }
 
+// Quartets kept as cached device lists per context at most; above this the
+// lists are streamed (regenerated on the host every build, CHUNK_Q at a
+// time, overlapping the kernels of the previous chunk).
+constexpr long long CACHE_Q = 1LL << 25;  // 32M quartets, 512 MB (default)
+constexpr long long CHUNK_Q = 1LL << 23;  // 8M quartets, 128 MB per buffer (default)
+
+int stream_class(bg_ctx *c, int t1, int t2, int ilev, const double2 *d_D, int ldd, double *d_GD,
+                 double *d_GX, int ldf, cudaStream_t st) {
+  long long chunk = c->chunk_q > 0 ? c->chunk_q : CHUNK_Q;
+  if (!c->h_chunk[0]) {
+    for (int k = 0; k < 2; ++k) {
+      CK(c, cudaMallocHost(&c->h_chunk[k], sizeof(int4) * chunk));
+      CK(c, cudaMalloc(&c->d_chunk[k], sizeof(int4) * chunk));
+      CK(c, cudaEventCreateWithFlags(&c->chunk_ev[k], cudaEventDisableTiming));
+    }
+  }
+  // both buffers may still be read by the previous class's last copies
+  for (int k = 0; k < 2; ++k) {
+    cudaError_t e = cudaEventSynchronize(c->chunk_ev[k]);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaEventSynchronize");
+  }
+  int cur = 0, rc = 0;
+  long long fill = 0;
+  auto flush = [&]() {
+    if (!fill || rc) return;
+    cudaError_t e = cudaMemcpyAsync(c->d_chunk[cur], c->h_chunk[cur], sizeof(int4) * fill,
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { rc = cuda_fail(c, e, "cudaMemcpyAsync"); return; }
+    rc = launch_quartets(c, c->d_chunk[cur], fill, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, 1);
+    if (rc) return;
+    cudaEventRecord(c->chunk_ev[cur], st);
+    cur ^= 1;
+    // the other buffer was last read by the chunk before: wait for it
+    e = cudaEventSynchronize(c->chunk_ev[cur]);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaEventSynchronize");
+    fill = 0;
+  };
+  gen_quartets(c, t1, t2, ilev, true, [&](int a, int b, int cc, int d) {
+    if (rc) return;
+    int *h = c->h_chunk[cur] + 4 * fill;
+    h[0] = a; h[1] = b; h[2] = cc; h[3] = d;
+    if (++fill == chunk) flush();
+  });
+  flush();
+  return rc;
+}
+
 }  // namespace
 
 extern "C" {
@@ -2685,6 +2760,15 @@ int bertha_gpu_set_precision(bg_ctx *c, int prec) {
   return BG_OK;
 }
 
+int bertha_gpu_set_list_limits(bg_ctx *c, long long cache_quartets, long long chunk_quartets) {
+  if (!c || cache_quartets < 0 || chunk_quartets < 0) return BG_ERR_ARG;
+  if (c->h_chunk[0] && chunk_quartets != c->chunk_q) return BG_ERR_STATE;  // buffers exist
+  c->cache_q = cache_quartets;
+  c->chunk_q = chunk_quartets;
+  c->quart_ilev = -1;
+  return BG_OK;
+}
+
 int bertha_gpu_dims(const bg_ctx *c, int *ndim, int *nskp) {
   if (!c) return BG_ERR_ARG;
   if (ndim) *ndim = c->ndim;
@@ -2768,23 +2852,37 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
       c->d_quart[k] = nullptr;
       c->nquart[k] = 0;
     }
-    for (int t1 = 0; t1 < c->ncomp; ++t1)
-      for (int t2 = 0; t2 < c->ncomp; ++t2) {
-        std::vector<int> q = build_quartets(c, t1, t2, ilev, true);
+    c->stream_lists = false;
+    long long total = 0;
+    std::vector<int> q[4];
+    for (int t1 = 0; t1 < c->ncomp && !c->stream_lists; ++t1)
+      for (int t2 = 0; t2 < c->ncomp && !c->stream_lists; ++t2) {
         int k = 2 * t1 + t2;
-        c->nquart[k] = (long long)q.size() / 4;
-        if (!q.empty()) {
-          CK(c, cudaMalloc(&c->d_quart[k], sizeof(int) * q.size()));
-          CK(c, cudaMemcpy(c->d_quart[k], q.data(), sizeof(int) * q.size(), cudaMemcpyHostToDevice));
+        gen_quartets(c, t1, t2, ilev, true, [&](int a, int b, int cc, int d) {
+          if (c->stream_lists) return;
+          q[k].push_back(a); q[k].push_back(b); q[k].push_back(cc); q[k].push_back(d);
+          if (++total > (c->cache_q > 0 ? c->cache_q : CACHE_Q)) c->stream_lists = true;
+        });
+      }
+    if (!c->stream_lists)
+      for (int k = 0; k < 4; ++k) {
+        c->nquart[k] = (long long)q[k].size() / 4;
+        if (!q[k].empty()) {
+          CK(c, cudaMalloc(&c->d_quart[k], sizeof(int) * q[k].size()));
+          CK(c, cudaMemcpy(c->d_quart[k], q[k].data(), sizeof(int) * q[k].size(),
+                           cudaMemcpyHostToDevice));
         }
       }
     c->quart_ilev = ilev;
   }
   for (int t1 = c->ncomp - 1; t1 >= 0; --t1)
     for (int t2 = c->ncomp - 1; t2 >= 0; --t2) {
-      int k = 2 * t1 + t2;
-      int rc = launch_quartets(c, c->d_quart[k], c->nquart[k], t1, t2, (const double2 *)d_dent,
-                               ldd, d_gdir, d_gxch, ldf, st, 1);
+      int k = 2 * t1 + t2, rc;
+      if (c->stream_lists)
+        rc = stream_class(c, t1, t2, ilev, (const double2 *)d_dent, ldd, d_gdir, d_gxch, ldf, st);
+      else
+        rc = launch_quartets(c, c->d_quart[k], c->nquart[k], t1, t2, (const double2 *)d_dent,
+                             ldd, d_gdir, d_gxch, ldf, st, 1);
       if (rc) return rc;
     }
   return BG_OK;
@@ -2958,6 +3056,11 @@ void bertha_gpu_free(bg_ctx *c) {
   cudaFree(c->d_GX);
   cudaFree(c->d_EB);
   cudaFree(c->d_offq);
+  for (int k = 0; k < 2; ++k) {
+    if (c->h_chunk[k]) cudaFreeHost(c->h_chunk[k]);
+    cudaFree(c->d_chunk[k]);
+    if (c->chunk_ev[k]) cudaEventDestroy(c->chunk_ev[k]);
+  }
   cudaFree(c->d_Ecv);
   cudaFree(c->d_Eci);
   cudaFree(c->d_EBcv);

@@ -84,6 +84,16 @@ int bertha_gpu_set_precision(bg_ctx *ctx, int prec);
  * m-signs and component, falls below it are skipped; 0 turns it off. */
 int bertha_gpu_set_screening(bg_ctx *ctx, double threshold);
 
+/* Quartet-list memory of the Coulomb build: a context keeps its lists on
+ * the device while they hold at most cache_quartets quartets (0: 2^25);
+ * larger lists are regenerated on the host every build and streamed
+ * through pinned buffers of chunk_quartets quartets (0: 2^23), generation
+ * overlapping the kernels of the previous chunk.  Cached lists make a build
+ * capturable in a CUDA graph; streamed ones do not (they synchronise on
+ * events).  No counterpart in the reference. */
+int bertha_gpu_set_list_limits(bg_ctx *ctx, long long cache_quartets,
+                               long long chunk_quartets);
+
 /* Fock dimension NDIM and small-component offset NSKP (CARDIN :423-430). */
 int bertha_gpu_dims(const bg_ctx *ctx, int *ndim, int *nskp);
 

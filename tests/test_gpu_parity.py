@@ -159,3 +159,23 @@ def test_schwarz_screening():
     scale = max(np.abs(rd).max(), np.abs(rx).max())
     assert np.abs(gd - rd).max() <= TOL * scale
     fb.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "df32"])
+def test_streamed_quartet_lists(prec):
+    """Lists above the cache limit are regenerated and streamed in chunks:
+    tiny limits force several chunks per class on a small basis."""
+    b = _small(lmax=2)
+    d = deck.density(b, seed=41)
+    fb = berthagpu.FockBuilder(b)
+    fb.set_precision(prec)
+    fb.set_screening(1e-12)
+    fb.set_list_limits(1000, 777)
+    gd, gx = fb.clmfast(d, 3)
+    gd2, gx2 = fb.clmfast(d, 3)
+    fb.close()
+    rd, rx = orc.clmfast(b, d, 3)
+    scale = max(np.abs(rd).max(), np.abs(rx).max())
+    tol = (TOL if prec == "fp64" else DF_TOL) * scale + 1e-9
+    for g, r in ((gd, rd), (gx, rx), (gd2, rd), (gx2, rx)):
+        assert np.abs(g - r).max() <= tol
