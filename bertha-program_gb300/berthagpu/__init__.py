@@ -6,6 +6,7 @@ calls the library.
 """
 from ._lib import BerthaGPUError, HMLT, SHAPE, lib  # noqa: F401
 from .build import build  # noqa: F401
-from .deck import (Basis, c6h6_basis, density, geometric, h2o_basis,  # noqa: F401
-                   make_basis, read_deck, shape_isym, tlf_basis, tlf_small_basis)
-from .fock import FockBuilder  # noqa: F401
+from .deck import (Basis, atom_basis, batched_atoms, c6h6_basis, density,  # noqa: F401
+                   geometric, h2o_basis, make_basis, read_deck, shape_isym, tlf_basis,
+                   tlf_small_basis)
+from .fock import FockBatch, FockBuilder  # noqa: F401

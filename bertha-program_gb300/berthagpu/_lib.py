@@ -56,6 +56,17 @@ def lib():
         L.bertha_gpu_last_error.restype = ctypes.c_char_p
         L.bertha_gpu_free.argtypes = [P]
         L.bertha_gpu_free.restype = None
+        L.bertha_gpu_batch_create.argtypes = [ctypes.POINTER(P), i, P, P, P]
+        L.bertha_gpu_batch_set_precision.argtypes = [P, i]
+        L.bertha_gpu_batch_clmfast_device.argtypes = [P, P, i, P, P, P]
+        L.bertha_gpu_batch_quartets.argtypes = [P]
+        L.bertha_gpu_batch_quartets.restype = ll
+        L.bertha_gpu_batch_launches.argtypes = [P]
+        L.bertha_gpu_batch_launches.restype = ll
+        L.bertha_gpu_batch_last_error.argtypes = [P]
+        L.bertha_gpu_batch_last_error.restype = ctypes.c_char_p
+        L.bertha_gpu_batch_free.argtypes = [P]
+        L.bertha_gpu_batch_free.restype = None
         _L = L
     return _L
 
@@ -70,10 +81,19 @@ EXPORTED = [
     "bertha_gpu_shells",
     "bertha_gpu_layout", "bertha_gpu_launches", "bertha_gpu_last_error",
     "bertha_gpu_free",
+    "bertha_gpu_batch_create", "bertha_gpu_batch_set_precision",
+    "bertha_gpu_batch_clmfast_device", "bertha_gpu_batch_quartets",
+    "bertha_gpu_batch_launches", "bertha_gpu_batch_last_error", "bertha_gpu_batch_free",
 ]
 
 
 def check(rc, ctx=None):
     if rc != BG_OK:
         msg = lib().bertha_gpu_last_error(ctx)
+        raise BerthaGPUError(rc, msg.decode() if msg else "")
+
+
+def check_batch(rc, batch=None):
+    if rc != BG_OK:
+        msg = lib().bertha_gpu_batch_last_error(batch)
         raise BerthaGPUError(rc, msg.decode() if msg else "")

@@ -247,6 +247,37 @@ def c6h6_basis():
     return b
 
 
+# Atoms whose ground configuration fills every occupied subshell (closed
+# shells from He to Rn), with the mass number of their most abundant isotope.
+CLOSED_SHELL_ATOMS = {
+    2: ("He", 4), 4: ("Be", 9), 10: ("Ne", 20), 12: ("Mg", 24), 18: ("Ar", 40),
+    20: ("Ca", 40), 30: ("Zn", 64), 36: ("Kr", 84), 38: ("Sr", 88), 46: ("Pd", 106),
+    48: ("Cd", 114), 54: ("Xe", 132), 56: ("Ba", 138), 70: ("Yb", 174), 80: ("Hg", 202),
+    86: ("Rn", 222),
+}
+
+
+def atom_basis(z, hmlt="DHFR"):
+    """Even-tempered closed-shell atom: n_s = 8 + Z/4, n_p = 6 + Z/5,
+    n_d = Z/12, n_f = Z/24 functions (integer division), exponents
+    0.03*2.4^k, one centre (ATOMIC); Gaussian nucleus of the most abundant
+    isotope."""
+    name, a = CLOSED_SHELL_ATOMS[int(z)]
+    counts = (8 + z // 4, 6 + z // 5, z // 12, z // 24)
+    exps = {l: geometric(0.03, 2.4, n) for l, n in enumerate(counts) if n > 0}
+    b = make_basis([((0.0, 0.0, 0.0), exps)], hmlt=hmlt, name=name)
+    b.znuc, b.anuc = (float(z),), (float(a),)
+    return b
+
+
+def batched_atoms(n=96, seed=2024, zset=None):
+    """n closed-shell atoms with Z drawn uniformly (seeded) from zset
+    (default: every closed-shell atom from He to Rn)."""
+    zs = sorted(zset if zset is not None else CLOSED_SHELL_ATOMS)
+    rng = np.random.default_rng(seed)
+    return [atom_basis(int(z)) for z in rng.choice(zs, size=n)]
+
+
 def density(basis, seed=0, nocc=None, real=False):
     """Seeded Hermitian positive semi-definite density D = C C^H (DENSTY
     form, bertha-scf.f:3600-3610) of nocc random orbitals."""

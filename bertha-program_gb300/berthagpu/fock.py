@@ -11,7 +11,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import BerthaGPUError, check, lib
+from ._lib import BerthaGPUError, check, check_batch, lib
 
 
 def _p(a):
@@ -141,3 +141,53 @@ class FockBuilder:
 
     def launches(self):
         return int(lib().bertha_gpu_launches(self._ctx))
+
+
+class FockBatch:
+    """Batched CLMFAST over independent instances (one FockBuilder each, all
+    with the same Hamiltonian, shape and RACAH1 flag): one kernel launch per
+    component class for every instance.  ``moff``/``ld`` place instance k's
+    matrices at complex element moff[k] + i + ld[k]*j of the device arrays;
+    the default packs them one after another with ld = NDIM.  The builders
+    may be closed once the batch exists."""
+
+    def __init__(self, builders, moff=None, ld=None):
+        n = len(builders)
+        arr = (ctypes.c_void_p * n)(*[b.ctx.value for b in builders])
+        self.ndim = [b.ndim for b in builders]
+        if moff is None:
+            moff = np.concatenate([[0], np.cumsum([d * d for d in self.ndim])[:-1]])
+        if ld is None:
+            ld = self.ndim
+        self.moff = np.ascontiguousarray(moff, dtype=np.int64)
+        self.ld = np.ascontiguousarray(ld, dtype=np.int32)
+        self._b = ctypes.c_void_p()
+        rc = lib().bertha_gpu_batch_create(ctypes.byref(self._b), n, arr, _p(self.moff),
+                                           _p(self.ld))
+        check_batch(rc, None)
+        self.n = n
+
+    def set_precision(self, prec):
+        check_batch(lib().bertha_gpu_batch_set_precision(self._b, _lib.PREC[prec]), self._b)
+
+    def clmfast_device(self, d_dent, d_gdir, d_gxch, ilev=3, stream=0):
+        check_batch(lib().bertha_gpu_batch_clmfast_device(
+            self._b, ctypes.c_void_p(d_dent), int(ilev), ctypes.c_void_p(d_gdir),
+            ctypes.c_void_p(d_gxch), ctypes.c_void_p(stream)), self._b)
+
+    def quartets(self):
+        return int(lib().bertha_gpu_batch_quartets(self._b))
+
+    def launches(self):
+        return int(lib().bertha_gpu_batch_launches(self._b))
+
+    def close(self):
+        if self._b:
+            lib().bertha_gpu_batch_free(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

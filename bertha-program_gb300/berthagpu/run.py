@@ -7,6 +7,12 @@ Cases: h2o, tlf, tlf-small, c6h6.  The density is a seeded random Hermitian
 one (DENSTY form); the output is one JSON line with the wall time of each
 call through the host-array entry points and the energy terms
 1/2 sum_ij D_ij G_ij of the matrices built (ENRGIES' convention).
+
+Batched closed-shell atoms (one FockBatch launch per component class for
+all of them), the Fock build timed on the device in both precisions and,
+with --scf, the batched DHF SCF in both precisions:
+
+  python -m berthagpu.run --atoms 96 [--zmax 86] [--scf]
 """
 import argparse
 import json
@@ -26,6 +32,9 @@ def main(argv=None):
     g = p.add_mutually_exclusive_group(required=True)
     g.add_argument("--case", choices=sorted(CASES))
     g.add_argument("--deck")
+    g.add_argument("--atoms", type=int, help="batch of N seeded closed-shell atoms")
+    p.add_argument("--zmax", type=int, default=86, help="largest Z drawn for --atoms")
+    p.add_argument("--scf", action="store_true", help="--atoms: run the batched SCF too")
     p.add_argument("--build", choices=["coulomb", "breit", "both"], default="coulomb")
     p.add_argument("--precision", choices=["fp64", "df32"], default="fp64")
     p.add_argument("--ilev", type=int, default=3)
@@ -35,6 +44,9 @@ def main(argv=None):
     p.add_argument("--no-racah1", action="store_true")
     p.add_argument("--gaunt", action="store_true")
     a = p.parse_args(argv)
+    if a.atoms:
+        print(json.dumps(atoms_main(a)), flush=True)
+        return
     b = CASES[a.case]() if a.case else deck.read_deck(a.deck)
     if a.build != "coulomb" and b.hmlt < deck.HMLT["DHFR"]:
         b = dataclasses_replace(b, deck.HMLT["DHFB"])
@@ -66,6 +78,84 @@ def main(argv=None):
         out["energy_bx_eh"] = float(0.5 * np.sum(dent * bx).real)
     fb.close()
     print(json.dumps(out), flush=True)
+
+
+def atoms_main(a):
+    """Batched Fock builds (and SCF) of a seeded draw of closed-shell atoms."""
+    import torch
+
+    from .fock import FockBatch
+    from .scf import BatchedDHFSCF
+
+    zset = [z for z in deck.CLOSED_SHELL_ATOMS if z <= a.zmax]
+    bases = deck.batched_atoms(a.atoms, seed=a.seed, zset=zset)
+    zs = [int(b.znuc[0]) for b in bases]
+    out = {"atoms": a.atoms, "z_drawn_from": zset, "z": zs,
+           "ndim": [b.ndim for b in bases], "screen": a.screen or 1e-12}
+    screen = a.screen or 1e-12
+    dens = [np.asarray(deck.density(b, seed=a.seed + k, nocc=z, real=True))
+            for k, (b, z) in enumerate(zip(bases, zs))]
+    D = torch.from_numpy(np.concatenate([d.ravel(order="F") for d in dens])).cuda()
+    for prec in ("fp64", "df32"):
+        t0 = time.perf_counter()
+        fbs = []
+        for b in bases:
+            fb = FockBuilder(b, racah1=False)
+            fb.set_precision(prec)
+            fb.set_screening(screen)
+            fbs.append(fb)
+        batch = FockBatch(fbs)
+        for fb in fbs:
+            fb.close()
+        t_init = time.perf_counter() - t0
+        J, K = torch.zeros_like(D), torch.zeros_like(D)
+        t0 = time.perf_counter()
+        batch.clmfast_device(D.data_ptr(), J.data_ptr(), K.data_ptr(), 3)
+        torch.cuda.synchronize()
+        t_first = time.perf_counter() - t0
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        batch.clmfast_device(D.data_ptr(), J.data_ptr(), K.data_ptr(), 3, st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        nq = batch.quartets()
+        Jh, Kh = J.cpu().numpy(), K.cpu().numpy()
+        ej, ek, off = [], [], 0
+        for d in dens:
+            n = d.shape[0]
+            ej.append(float(0.5 * np.sum(d * Jh[off:off + n * n].reshape(n, n, order="F")).real))
+            ek.append(float(0.5 * np.sum(d * Kh[off:off + n * n].reshape(n, n, order="F")).real))
+            off += n * n
+        out[prec] = {"init_s": t_init, "first_call_s": t_first, "device_s": ms / 1e3,
+                     "quartets": nq, "quartets_per_s": nq / (ms / 1e3),
+                     "launches": batch.launches(), "energy_j_eh": ej, "energy_k_eh": ek}
+        batch.close()
+    out["df32_energy_max_abs_err_eh"] = max(
+        max(abs(x - y) for x, y in zip(out["fp64"]["energy_j_eh"], out["df32"]["energy_j_eh"])),
+        max(abs(x - y) for x, y in zip(out["fp64"]["energy_k_eh"], out["df32"]["energy_k_eh"])))
+    for prec in ("fp64", "df32"):
+        for key in ("energy_j_eh", "energy_k_eh"):
+            out[prec][key] = out[prec][key][:8]  # keep the line short
+    if a.scf:
+        res = {}
+        for prec in ("fp64", "df32"):
+            s = BatchedDHFSCF(bases, zs, precision=prec, screen=screen)
+            r = s.run(etol=1e-9, max_iter=80)
+            s.close()
+            r.pop("history")
+            res[prec] = r
+        de = [abs(x - y) for x, y in zip(res["fp64"]["energy"], res["df32"]["energy"])]
+        out["scf"] = {
+            "fp64": {k: v for k, v in res["fp64"].items() if k != "energy"},
+            "df32": {k: v for k, v in res["df32"].items() if k != "energy"},
+            "energy_fp64_by_z": {str(z): e for z, e in zip(zs, res["fp64"]["energy"])},
+            "df32_vs_fp64_max_abs_eh": max(de),
+            "all_converged": all(res["fp64"]["converged"]) and all(res["df32"]["converged"])}
+        for prec in ("fp64", "df32"):
+            out["scf"][prec]["converged"] = int(sum(out["scf"][prec]["converged"]))
+    return out
 
 
 def dataclasses_replace(b, hmlt):

@@ -20,7 +20,7 @@ import time
 import numpy as np
 
 from . import deck
-from .fock import FockBuilder
+from .fock import FockBatch, FockBuilder
 
 CLIGHT = 137.035999084
 
@@ -186,3 +186,175 @@ class DHFSCF:
 
     def close(self):
         self.backend.close()
+
+
+class BatchedDHFSCF:
+    """Closed-shell DHF SCF of many independent instances at once (atoms
+    and ions of different basis sizes), every step batched on the GPU.
+
+    The instances' matrices are padded to the largest NDIM N and held as
+    [n, N, N] tensors; the two-electron build is one FockBatch call (one
+    kernel launch per component class for all instances), captured once as
+    a CUDA graph and replayed every iteration.  Per instance the loop is the
+    one of DHFSCF (HFSCF's order: Fock build, ENRGIES, LEVSHFT, DIIS, ZHEGV,
+    DENSTY).  Padding rows and columns carry S = 1 and a large positive
+    diagonal in F, so they form eigenvectors of their own that are never
+    occupied; near-singular overlap directions are shifted out the same way.
+    """
+
+    PAD = 1.0e4
+
+    def __init__(self, bases, nocc, precision="fp64", screen=1e-12, racah1=False, torch=None,
+                 graph=True):
+        if torch is None:
+            import torch as _t
+            torch = _t
+        t = self.torch = torch
+        self.bases = list(bases)
+        self.nocc = [int(x) for x in nocc]
+        n = self.n = len(self.bases)
+        builders = [FockBuilder(b, racah1=racah1) for b in self.bases]
+        for fb in builders:
+            fb.set_precision(precision)
+            fb.set_screening(screen)
+        self.ndim = [fb.ndim for fb in builders]
+        N = self.N = max(self.ndim)
+        z = dict(dtype=t.complex128, device="cuda")
+        S, V, T = (t.zeros((n, N, N), **z) for _ in range(3))
+        st = t.cuda.current_stream().cuda_stream
+        for k, (b, fb) in enumerate(zip(self.bases, builders)):
+            xi = deck.nuclear_exponents(b.znuc, b.anuc)
+            fb.oneel_device(b.znuc, xi, S[k].data_ptr(), V[k].data_ptr(), T[k].data_ptr(), N, st)
+        self.batch = FockBatch(builders, moff=[k * N * N for k in range(n)], ld=[N] * n)
+        for fb in builders:
+            fb.close()
+        # column-major buffers -> matrices
+        self.S = S.transpose(1, 2).contiguous()
+        self.H1 = (V + T).transpose(1, 2).contiguous()
+        idx = t.arange(N, device="cuda")
+        nd = t.tensor(self.ndim, device="cuda")
+        inside = idx[None, :] < nd[:, None]                      # [n, N]
+        self.block = (inside[:, :, None] & inside[:, None, :]).to(t.float64)
+        pad = (~inside).to(t.complex128)
+        self.S = self.S + t.diag_embed(pad)
+        self.H1 = self.H1 + self.PAD * t.diag_embed(pad)
+        self.enuc = t.tensor([nuclear_repulsion(b) for b in self.bases], dtype=t.float64,
+                             device="cuda")
+        self.bufs = [t.zeros((n, N, N), **z) for _ in range(3)]
+        self.graph = None
+        self.precision = precision
+        if graph:
+            bd, bj, bk = self.bufs
+            s = t.cuda.Stream()
+            s.wait_stream(t.cuda.current_stream())
+            with t.cuda.stream(s):
+                # first call: quartet lists and scratch (host work, allocation)
+                self.batch.clmfast_device(bd.data_ptr(), bj.data_ptr(), bk.data_ptr(), 3,
+                                          s.cuda_stream)
+            s.synchronize()
+            g = t.cuda.CUDAGraph()
+            with t.cuda.graph(g, stream=s):
+                self.batch.clmfast_device(bd.data_ptr(), bj.data_ptr(), bk.data_ptr(), 3,
+                                          t.cuda.current_stream().cuda_stream)
+            self.graph = g
+
+    def fock(self, D):
+        """G = GDIR - GXCH of every instance for the densities D [n, N, N]."""
+        bd, bj, bk = self.bufs
+        bd.copy_(D.transpose(1, 2))
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.batch.clmfast_device(bd.data_ptr(), bj.data_ptr(), bk.data_ptr(), 3,
+                                      self.torch.cuda.current_stream().cuda_stream)
+        return (bj - bk).transpose(1, 2)
+
+    def quartets(self):
+        return self.batch.quartets()
+
+    def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, verbose=False):
+        t = self.torch
+        n, N = self.n, self.N
+        t0 = time.perf_counter()
+        S, H1 = self.S, self.H1
+        s, U = t.linalg.eigh(S)
+        keep = s > 1e-10 * s.max(dim=1, keepdim=True).values
+        X = U * t.where(keep, s.clamp_min(1e-300).rsqrt(), t.zeros_like(s))[:, None, :]
+        drop = t.diag_embed((~keep).to(t.complex128)) * self.PAD
+        Xh = X.conj().transpose(1, 2)
+        nocc = t.tensor(self.nocc, device="cuda")
+        col = t.arange(N, device="cuda")[None, :]
+        c2 = CLIGHT * CLIGHT
+
+        def solve(F):
+            e, Cp = t.linalg.eigh(Xh @ F @ X + drop)
+            C = X @ Cp
+            nneg = (e < -c2).sum(dim=1, keepdim=True)
+            occ = ((col >= nneg) & (col < nneg + nocc[:, None])).to(t.complex128)
+            vir = ((col >= nneg + nocc[:, None]) & (e < 0.5 * self.PAD)).to(t.complex128)
+            Co = C * occ[:, None, :]
+            # DENSTY: D_ij = sum_occ conj(C_i) C_j
+            return e, Co.conj() @ Co.transpose(1, 2), C * vir[:, None, :], nneg
+
+        eps, D, Cv, nneg = solve(H1)
+        t.cuda.synchronize()
+        t_one = time.perf_counter() - t0
+        hist_F, hist_E = [], []
+        last = None
+        done = t.zeros(n, dtype=t.bool, device="cuda")
+        iters, t_fock, t_lin = [], 0.0, 0.0
+        energy = None
+        for it in range(1, max_iter + 1):
+            ti = time.perf_counter()
+            G = self.fock(D)
+            t.cuda.synchronize()
+            tf = time.perf_counter()
+            t_fock += tf - ti
+            F = H1 + G
+            energy = self.enuc + (D * (H1 + 0.5 * G) * self.block).sum(dim=(1, 2)).real
+            if shift and it > 1:
+                A = S @ Cv
+                F = F + shift * (A @ A.conj().transpose(1, 2))
+            P = D.transpose(1, 2)
+            err = F @ P @ S - S @ P @ F
+            hist_F.append(F)
+            hist_E.append(err)
+            if len(hist_F) > ndiis:
+                hist_F.pop(0)
+                hist_E.pop(0)
+            m = len(hist_F)
+            if m > 1:
+                Es = t.stack(hist_E, 1).reshape(n, m, -1)
+                B = t.zeros((n, m + 1, m + 1), dtype=t.float64, device="cuda")
+                B[:, :m, :m] = (Es.conj() @ Es.transpose(1, 2)).real
+                # scale-invariant regularisation for instances already converged
+                tr = B[:, :m, :m].diagonal(dim1=1, dim2=2).mean(1).clamp_min(1e-300)
+                B[:, :m, :m] += 1e-14 * tr[:, None, None] * t.eye(m, device="cuda")
+                B[:, m, :m] = -1.0
+                B[:, :m, m] = -1.0
+                rhs = t.zeros((n, m + 1), dtype=t.float64, device="cuda")
+                rhs[:, m] = -1.0
+                w = t.linalg.solve(B, rhs)[:, :m].to(t.complex128)
+                F = (t.stack(hist_F, 1) * w[:, :, None, None]).sum(1)
+            eps, D, Cv, nneg = solve(F)
+            t.cuda.synchronize()
+            t_lin += time.perf_counter() - tf
+            de = None if last is None else energy - last
+            if de is not None:
+                done = de.abs() < etol
+            iters.append({"iter": it, "max_abs_de": None if de is None else float(de.abs().max()),
+                          "converged": int(done.sum()), "s": time.perf_counter() - ti})
+            if verbose:
+                print(iters[-1], flush=True)
+            if bool(done.all()):
+                break
+            last = energy
+        return {"energy": energy.cpu().numpy().tolist(),
+                "converged": done.cpu().numpy().tolist(),
+                "iterations": len(iters), "oneel_s": t_one, "fock_s": t_fock,
+                "linalg_s": t_lin, "wall_s": t_one + t_fock + t_lin,
+                "quartets_per_build": self.quartets(), "history": iters}
+
+    def close(self):
+        self.graph = None
+        self.batch.close()

@@ -56,8 +56,18 @@ __host__ __device__ inline int hidx(int t, int u, int v) {
 
 struct Shell {
   double x, y, z, alpha;
-  int l, cnt, ibas, pad;
+  int l, cnt, ibas;
+  int inst;             // instance of a batched build (0 for a single context)
+  int prow;             // pair-table row: pair (this, b) is pe[prow + b]
+  int pad;
   int fock[MAXLAB][2];  // large-component Fock index of m<0 / m>0
+};
+
+// Placement of one instance's matrices in a batched build: element (i, j)
+// of its D, J and K sits at off + i + ld*j (complex units).
+struct Inst {
+  long long off;
+  int ld, nskp;
 };
 
 struct PairE {
@@ -404,8 +414,10 @@ struct QArgs {
   const double2 *D;
   double *GD, *GX;
   int ns, ldd, ldf, nskp, isym, racah1;
-  int sym;  // also digest the swapped quartet (cd|ab) = (ab|cd) when ab != cd
+  int sym;  // 1: also digest the swapped quartet (cd|ab) = (ab|cd) when ab != cd;
+            // 2: as 1, lists halved by (ba|dc) = (ab|cd)* (weights, completion)
   double *bound;  // non-null: write max |(ab|cd)| per quartet instead of digesting
+  const Inst *inst;  // batched build: per-instance placement (shell .inst), else null
 };
 
 constexpr unsigned long long SGN = 0x8000000000000000ULL;
@@ -461,8 +473,8 @@ __device__ bool label_ok(int isym, int racah1, int mcnt, const int *kq, const in
   return true;
 }
 
-__device__ inline double2 ldD(const QArgs &q, int i, int j) {
-  return q.D[(size_t)i + (size_t)q.ldd * j];
+__device__ inline double2 ldD(const double2 *D, size_t ld, int i, int j) {
+  return D[(size_t)i + ld * j];
 }
 
 __device__ inline void satomic(double2 *p, double2 v) {
@@ -504,6 +516,18 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
     int nab = ntuv(degab), ncd = ntuv(degcd);
     bool swp = contraction_cost(nlcd, ncd, nlab, nab) < contraction_cost(nlab, nab, nlcd, ncd);
     int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
+    // matrix placement: the call's arrays, or this quartet's instance in a batch
+    const double2 *Dm = q.D;
+    double *GDm = q.GD, *GXm = q.GX;
+    size_t lddm = q.ldd, ldfm = q.ldf;
+    int nskpm = q.nskp;
+    if (q.inst) {
+      const Inst I = q.inst[A.inst];
+      if (Dm) Dm += I.off;
+      if (GDm) { GDm += 2 * I.off; GXm += 2 * I.off; }
+      lddm = ldfm = (size_t)I.ld;
+      nskpm = I.nskp;
+    }
     if (threadIdx.x == 0) {
       double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
       double Px = (A.alpha * A.x + B.alpha * B.x) / p;
@@ -567,19 +591,19 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
       K2[k] = make_double2(0.0, 0.0);
     }
     bool dual = q.sym && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
-    const double2 *Eab = q.E + q.pe[Q4.x * q.ns + Q4.y].off[t1];
-    const double2 *Ecd = q.E + q.pe[Q4.z * q.ns + Q4.w].off[t2];
+    const double2 *Eab = q.E + q.pe[A.prow + Q4.y].off[t1];
+    const double2 *Ecd = q.E + q.pe[C.prow + Q4.w].off[t2];
     // left/right roles
     const double2 *ER = swp ? Eab : Ecd;
-    long long oL = swp ? q.pe[Q4.z * q.ns + Q4.w].off[t2] : q.pe[Q4.x * q.ns + Q4.y].off[t1];
-    long long oR = swp ? q.pe[Q4.x * q.ns + Q4.y].off[t1] : q.pe[Q4.z * q.ns + Q4.w].off[t2];
+    long long oL = swp ? q.pe[C.prow + Q4.w].off[t2] : q.pe[A.prow + Q4.y].off[t1];
+    long long oR = swp ? q.pe[A.prow + Q4.y].off[t1] : q.pe[C.prow + Q4.w].off[t2];
     const double2 *ELv = q.Ecv + oL, *ERv = q.Ecv + oR;
     const unsigned char *ELi = q.Eci + oL, *ERi = q.Eci + oR;
     int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
     int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
     int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;  // second label count
     int lq[4] = {la, lb, lc, ld};
-    int oab = t1 ? q.nskp : 0, ocd = t2 ? q.nskp : 0;
+    int oab = t1 ? nskpm : 0, ocd = t2 ? nskpm : 0;
     __syncthreads();
     // left labels per pass: as many as the G buffer holds at this degree
     int chunk = max(1, (CHUNK * 2 * NTE) / (2 * nR));
@@ -704,8 +728,8 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
           double2 Dcd[4], Dcb[4];
           for (int x = 0; x < 2; ++x)
             for (int y = 0; y < 2; ++y) {
-              Dcd[2 * x + y] = ldD(q, fc[x], fd[y]);
-              Dcb[2 * x + y] = ldD(q, fc[x], fb[y]);
+              Dcd[2 * x + y] = ldD(Dm, lddm, fc[x], fd[y]);
+              Dcb[2 * x + y] = ldD(Dm, lddm, fc[x], fb[y]);
             }
           for (int sa = 0; sa < 2; ++sa)
             for (int sb = 0; sb < 2; ++sb) {
@@ -735,8 +759,8 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
             double2 Dab[4], Dad[4];
             for (int x = 0; x < 2; ++x)
               for (int y = 0; y < 2; ++y) {
-                Dab[2 * x + y] = ldD(q, fa[x], fb[y]);
-                Dad[2 * x + y] = ldD(q, fa[x], fd[y]);
+                Dab[2 * x + y] = ldD(Dm, lddm, fa[x], fb[y]);
+                Dad[2 * x + y] = ldD(Dm, lddm, fa[x], fd[y]);
               }
             for (int sc = 0; sc < 2; ++sc)
               for (int sd = 0; sd < 2; ++sd) {
@@ -766,8 +790,8 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
           for (int s = 0; s < 2; ++s) {
             double jv = 0.0, kv = 0.0;
             for (int t = 0; t < 2; ++t) {
-              jv = fma(RV(s, s, t, t).x, ldD(q, fc[t], fd[t]).x, jv);
-              kv = fma(RV(s, t, t, s).x, ldD(q, fc[t], fb[t]).x, kv);
+              jv = fma(RV(s, s, t, t).x, ldD(Dm, lddm, fc[t], fd[t]).x, jv);
+              kv = fma(RV(s, t, t, s).x, ldD(Dm, lddm, fc[t], fb[t]).x, kv);
             }
             atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, jv);
             atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
@@ -777,8 +801,8 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
             for (int s = 0; s < 2; ++s) {
               double jv = 0.0, kv = 0.0;
               for (int t = 0; t < 2; ++t) {
-                jv = fma(RV(t, t, s, s).x, ldD(q, fa[t], fb[t]).x, jv);
-                kv = fma(RV(t, s, s, t).x, ldD(q, fa[t], fd[t]).x, kv);
+                jv = fma(RV(t, t, s, s).x, ldD(Dm, lddm, fa[t], fb[t]).x, jv);
+                kv = fma(RV(t, s, s, t).x, ldD(Dm, lddm, fa[t], fd[t]).x, kv);
               }
               atomicAdd(&J2[(ic * 2 + s) * MAXSP + id * 2 + s].x, jv);
               atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
@@ -794,6 +818,10 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
       __syncthreads();
       continue;
     }
+    // weight 1/2 for a quartet equal to its (ba|dc) image, or to its
+    // (dc|ba) image within one class: the completion adds it again
+    const double wq = (q.sym == 2 && ((Q4.x == Q4.y && Q4.z == Q4.w) ||
+                                      (t1 == t2 && Q4.x == Q4.w && Q4.y == Q4.z))) ? 0.5 : 1.0;
     // flush shared accumulators
     {
       int nsa = 2 * nla;
@@ -801,8 +829,9 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         int a = w / (2 * nlb), b = w % (2 * nlb);
         double2 v = Jl[a * MAXSP + b];
         if (v.x == 0.0 && v.y == 0.0) continue;
+        v.x *= wq; v.y *= wq;
         int fa = A.fock[a >> 1][a & 1] + oab, fbb = B.fock[b >> 1][b & 1] + oab;
-        double *dst = q.GD + 2 * ((size_t)fa + (size_t)q.ldf * fbb);
+        double *dst = GDm + 2 * ((size_t)fa + ldfm * fbb);
         atomicAdd(dst, v.x);
         atomicAdd(dst + 1, v.y);
       }
@@ -810,8 +839,9 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
         int a = w / (2 * nld), d = w % (2 * nld);
         double2 v = Kl[a * MAXSP + d];
         if (v.x == 0.0 && v.y == 0.0) continue;
+        v.x *= wq; v.y *= wq;
         int fa = A.fock[a >> 1][a & 1] + oab, fdd = Dd.fock[d >> 1][d & 1] + ocd;
-        double *dst = q.GX + 2 * ((size_t)fa + (size_t)q.ldf * fdd);
+        double *dst = GXm + 2 * ((size_t)fa + ldfm * fdd);
         atomicAdd(dst, v.x);
         atomicAdd(dst + 1, v.y);
       }
@@ -821,8 +851,9 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
           int c = w / (2 * nld), d = w % (2 * nld);
           double2 v = J2[c * MAXSP + d];
           if (v.x == 0.0 && v.y == 0.0) continue;
+          v.x *= wq; v.y *= wq;
           int fcc = C.fock[c >> 1][c & 1] + ocd, fdd = Dd.fock[d >> 1][d & 1] + ocd;
-          double *dst = q.GD + 2 * ((size_t)fcc + (size_t)q.ldf * fdd);
+          double *dst = GDm + 2 * ((size_t)fcc + ldfm * fdd);
           atomicAdd(dst, v.x);
           atomicAdd(dst + 1, v.y);
         }
@@ -830,8 +861,9 @@ k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
           int c = w / (2 * nlb), b = w % (2 * nlb);
           double2 v = K2[c * MAXSP + b];
           if (v.x == 0.0 && v.y == 0.0) continue;
+          v.x *= wq; v.y *= wq;
           int fcc = C.fock[c >> 1][c & 1] + ocd, fbb = B.fock[b >> 1][b & 1] + oab;
-          double *dst = q.GX + 2 * ((size_t)fcc + (size_t)q.ldf * fbb);
+          double *dst = GXm + 2 * ((size_t)fcc + ldfm * fbb);
           atomicAdd(dst, v.x);
           atomicAdd(dst + 1, v.y);
         }
@@ -1610,10 +1642,12 @@ struct QArgsDF {
   const PairE *pe;
   const float4 *E;
   const unsigned char *Eci;  // Hermite indices of the nonzero E terms (k_ecompact)
-  const float4 *D;  // n x n, leading dimension n
+  const float4 *D;  // n x n, leading dimension n (batched: the Inst placement)
   double *GD, *GX;
   int ns, ldd, ldf, nskp, isym, racah1;
-  int sym;  // also digest the swapped quartet (cd|ab) = (ab|cd) when ab != cd
+  int sym;  // 1: also digest the swapped quartet (cd|ab) = (ab|cd) when ab != cd;
+            // 2: as 1, lists halved by (ba|dc) = (ab|cd)* (weights, completion)
+  const Inst *inst;  // batched build: per-instance placement (shell .inst), else null
 };
 
 // complex double-float product accumulate: (acc) += u * v
@@ -1686,7 +1720,19 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
     int nab = ntuv(degab), ncd = ntuv(degcd);
     bool swp = contraction_cost(nlcd, ncd, nlab, nab) < contraction_cost(nlab, nab, nlcd, ncd);
     int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
-    const PairE &pab_e = q.pe[Q4.x * q.ns + Q4.y], &pcd_e = q.pe[Q4.z * q.ns + Q4.w];
+    // matrix placement: the call's arrays, or this quartet's instance in a batch
+    const float4 *Dm = q.D;
+    double *GDm = q.GD, *GXm = q.GX;
+    size_t lddm = q.ldd, ldfm = q.ldf;
+    int nskpm = q.nskp;
+    if (q.inst) {
+      const Inst I = q.inst[A.inst];
+      if (Dm) Dm += I.off;
+      if (GDm) { GDm += 2 * I.off; GXm += 2 * I.off; }
+      lddm = ldfm = (size_t)I.ld;
+      nskpm = I.nskp;
+    }
+    const PairE &pab_e = q.pe[A.prow + Q4.y], &pcd_e = q.pe[C.prow + Q4.w];
     if (threadIdx.x == 0) {
       double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
       double Px = (A.alpha * A.x + B.alpha * B.x) / p;
@@ -1772,7 +1818,7 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
     int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
     int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;
     int lq[4] = {la, lb, lc, ld};
-    int oab = t1 ? q.nskp : 0, ocd = t2 ? q.nskp : 0;
+    int oab = t1 ? nskpm : 0, ocd = t2 ? nskpm : 0;
     int kq0 = sk;
     __syncthreads();
     for (int c0 = 0; c0 < nlL; c0 += CHDF) {
@@ -1912,7 +1958,7 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
           int fb[2] = {B.fock[ib][0] + oab, B.fock[ib][1] + oab};
           int fc[2] = {C.fock[ic][0] + ocd, C.fock[ic][1] + ocd};
           int fd[2] = {Dd.fock[id][0] + ocd, Dd.fock[id][1] + ocd};
-          const size_t ld = (size_t)q.ldd;
+          const size_t ld = lddm;
           // phase A: targets tg = 4*family + sig.  family 0 J(a,b) sig=(sa,sb),
           // 1 K(a,d) sig=(sa,sd), 2 J(c,d) of (cd|ab) sig=(sc,sd),
           // 3 K(c,b) of (cd|ab) sig=(sc,sb)
@@ -1928,13 +1974,13 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
                   int sa, sb, sc2, sd;
                   float4 dv;
                   if (fam == 0) {
-                    sa = s1; sb = s2; sc2 = x; sd = y; dv = q.D[fc[sc2] + ld * fd[sd]];
+                    sa = s1; sb = s2; sc2 = x; sd = y; dv = Dm[fc[sc2] + ld * fd[sd]];
                   } else if (fam == 1) {
-                    sa = s1; sd = s2; sb = x; sc2 = y; dv = q.D[fc[sc2] + ld * fb[sb]];
+                    sa = s1; sd = s2; sb = x; sc2 = y; dv = Dm[fc[sc2] + ld * fb[sb]];
                   } else if (fam == 2) {
-                    sc2 = s1; sd = s2; sa = x; sb = y; dv = q.D[fa[sa] + ld * fb[sb]];
+                    sc2 = s1; sd = s2; sa = x; sb = y; dv = Dm[fa[sa] + ld * fb[sb]];
                   } else {
-                    sc2 = s1; sb = s2; sa = x; sd = y; dv = q.D[fa[sa] + ld * fd[sd]];
+                    sc2 = s1; sb = s2; sa = x; sd = y; dv = Dm[fa[sa] + ld * fd[sd]];
                   }
                   float4 v = swp ? rv_sign<true>(sv, sa, sb, sc2, sd, sl_, slr)
                                  : rv_sign<false>(sv, sa, sb, sc2, sd, sl_, slr);
@@ -1948,13 +1994,13 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
                 int sa, sb, sc2, sd;
                 float4 dv;
                 if (fam == 0) {
-                  sa = sg; sb = sg; sc2 = tt; sd = tt; dv = q.D[fc[tt] + ld * fd[tt]];
+                  sa = sg; sb = sg; sc2 = tt; sd = tt; dv = Dm[fc[tt] + ld * fd[tt]];
                 } else if (fam == 1) {
-                  sa = sg; sb = tt; sc2 = tt; sd = sg; dv = q.D[fc[tt] + ld * fb[tt]];
+                  sa = sg; sb = tt; sc2 = tt; sd = sg; dv = Dm[fc[tt] + ld * fb[tt]];
                 } else if (fam == 2) {
-                  sa = tt; sb = tt; sc2 = sg; sd = sg; dv = q.D[fa[tt] + ld * fb[tt]];
+                  sa = tt; sb = tt; sc2 = sg; sd = sg; dv = Dm[fa[tt] + ld * fb[tt]];
                 } else {
-                  sa = tt; sb = sg; sc2 = sg; sd = tt; dv = q.D[fa[tt] + ld * fd[tt]];
+                  sa = tt; sb = sg; sc2 = sg; sd = tt; dv = Dm[fa[tt] + ld * fd[tt]];
                 }
                 float4 v = swp ? rv_sign<true>(sv, sa, sb, sc2, sd, sl_, slr)
                                : rv_sign<false>(sv, sa, sb, sc2, sd, sl_, slr);
@@ -2029,6 +2075,10 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
       }
       __syncthreads();
     }
+    // weight 1/2 for a quartet equal to its (ba|dc) image, or to its
+    // (dc|ba) image within one class: the completion adds it again
+    const double wq = (q.sym == 2 && ((Q4.x == Q4.y && Q4.z == Q4.w) ||
+                                      (t1 == t2 && Q4.x == Q4.w && Q4.y == Q4.z))) ? 0.5 : 1.0;
     // flush shared accumulators (FP64)
     {
       int nsa = 2 * nla;
@@ -2036,8 +2086,9 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
         int a = w / (2 * nlb), b = w % (2 * nlb);
         double2 v = Jl[a * MAXSP + b];
         if (v.x == 0.0 && v.y == 0.0) continue;
+        v.x *= wq; v.y *= wq;
         int fa = A.fock[a >> 1][a & 1] + oab, fbb = B.fock[b >> 1][b & 1] + oab;
-        double *dst = q.GD + 2 * ((size_t)fa + (size_t)q.ldf * fbb);
+        double *dst = GDm + 2 * ((size_t)fa + ldfm * fbb);
         atomicAdd(dst, v.x);
         atomicAdd(dst + 1, v.y);
       }
@@ -2045,8 +2096,9 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
         int a = w / (2 * nld), d = w % (2 * nld);
         double2 v = Kl[a * MAXSP + d];
         if (v.x == 0.0 && v.y == 0.0) continue;
+        v.x *= wq; v.y *= wq;
         int fa = A.fock[a >> 1][a & 1] + oab, fdd = Dd.fock[d >> 1][d & 1] + ocd;
-        double *dst = q.GX + 2 * ((size_t)fa + (size_t)q.ldf * fdd);
+        double *dst = GXm + 2 * ((size_t)fa + ldfm * fdd);
         atomicAdd(dst, v.x);
         atomicAdd(dst + 1, v.y);
       }
@@ -2056,8 +2108,9 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
           int c = w / (2 * nld), d = w % (2 * nld);
           double2 v = J2[c * MAXSP + d];
           if (v.x == 0.0 && v.y == 0.0) continue;
+          v.x *= wq; v.y *= wq;
           int fcc = C.fock[c >> 1][c & 1] + ocd, fdd = Dd.fock[d >> 1][d & 1] + ocd;
-          double *dst = q.GD + 2 * ((size_t)fcc + (size_t)q.ldf * fdd);
+          double *dst = GDm + 2 * ((size_t)fcc + ldfm * fdd);
           atomicAdd(dst, v.x);
           atomicAdd(dst + 1, v.y);
         }
@@ -2065,14 +2118,75 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
           int c = w / (2 * nlb), b = w % (2 * nlb);
           double2 v = K2[c * MAXSP + b];
           if (v.x == 0.0 && v.y == 0.0) continue;
+          v.x *= wq; v.y *= wq;
           int fcc = C.fock[c >> 1][c & 1] + ocd, fbb = B.fock[b >> 1][b & 1] + oab;
-          double *dst = q.GX + 2 * ((size_t)fcc + (size_t)q.ldf * fbb);
+          double *dst = GXm + 2 * ((size_t)fcc + ldfm * fbb);
           atomicAdd(dst, v.x);
           atomicAdd(dst + 1, v.y);
         }
       }
     }
     __syncthreads();
+  }
+}
+
+// Hermitian completion G <- G + G^H of the n x n block(s) (CLMFAST's
+// completion of a symmetry-reduced build, bertha-scf.f:12164-12205): one
+// thread per element pair (i, j), i <= j.  With `inst`, block k of a batch
+// (placement inst[k], size ndim[k]); else the one block at G, leading
+// dimension ld.
+__global__ void k_herm_complete(double2 *G, int n, long long ld, const Inst *inst,
+                                const int *ndim, int ninst) {
+  for (int k = blockIdx.x; k < ninst; k += gridDim.x) {
+    double2 *M = G;
+    long long m = n, l = ld;
+    if (inst) {
+      M = G + inst[k].off;
+      m = ndim[k];
+      l = inst[k].ld;
+    }
+    for (long long w = threadIdx.x + (long long)blockDim.x * blockIdx.y; w < m * m;
+         w += (long long)blockDim.x * gridDim.y) {
+      long long i = w % m, j = w / m;
+      if (i > j) continue;
+      double2 a = M[i + l * j];
+      if (i == j) {
+        M[i + l * j] = make_double2(2.0 * a.x, 0.0);
+      } else {
+        double2 b = M[j + l * i];
+        double2 x = make_double2(a.x + b.x, a.y - b.y);
+        M[i + l * j] = x;
+        M[j + l * i] = make_double2(x.x, -x.y);
+      }
+    }
+  }
+}
+
+// Zeroes the ndim x ndim block of every instance of a batched build.
+__global__ void k_zero_inst(double *a, const Inst *inst, const int *ndim, int ninst) {
+  for (int k = blockIdx.x; k < ninst; k += gridDim.x) {
+    Inst I = inst[k];
+    long long tot = (long long)ndim[k] * ndim[k];
+    for (long long i = threadIdx.x + (long long)blockDim.x * blockIdx.y; i < tot;
+         i += (long long)blockDim.x * gridDim.y) {
+      long long r = i % ndim[k], c = i / ndim[k];
+      double *p = a + 2 * (I.off + r + (long long)I.ld * c);
+      p[0] = 0.0;
+      p[1] = 0.0;
+    }
+  }
+}
+
+// Double-float copy of n consecutive complex elements (a batched density in
+// the caller's placement).
+__global__ void k_dconv1(const double2 *D, long long n, float4 *Ddf) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double2 v = D[i];
+    float4 o;
+    df_split(v.x, o.x, o.y);
+    df_split(v.y, o.z, o.w);
+    Ddf[i] = o;
   }
 }
 
@@ -2147,6 +2261,32 @@ struct bg_ctx {
   bool bad = false;
 };
 
+// Batched build over independent instances (one context each): shells,
+// pair tables and E-coefficients of all instances concatenated on the
+// device, quartet lists of every instance merged per component class and
+// grouped by angular class, one kernel launch per class for all instances.
+struct bg_batch {
+  int n = 0, ncomp = 1, hmlt = 0, isym = 0, racah1 = 1, prec = BG_PREC_FP64;
+  std::vector<bg_ctx *> shadow;  // host copies of the instances' shells, bounds and rules
+  std::vector<int> sbase;        // first batch shell of each instance
+  std::vector<int> ndim;
+  std::vector<Inst> inst;
+  long long span = 0;            // complex elements the placement covers
+  Shell *d_sh = nullptr;
+  PairE *d_pe = nullptr;
+  double2 *d_E = nullptr, *d_Ecv = nullptr;
+  unsigned char *d_Eci = nullptr;
+  float4 *d_Edf = nullptr, *d_Ddf = nullptr;
+  Inst *d_inst = nullptr;
+  int *d_ndim = nullptr;
+  int *d_quart[4] = {nullptr, nullptr, nullptr, nullptr};
+  long long nquart[4] = {0, 0, 0, 0};
+  int quart_ilev = -1;
+  long long launches = 0;
+  std::string err;
+  bool bad = false;
+};
+
 namespace {
 std::string g_init_err;
 
@@ -2199,7 +2339,12 @@ int upload_tables() {
 // sink(a, b, c, d) one by one.
 // With `sym`, (ab|cd) = (cd|ab) is used: only pairs ab >= cd (pair index
 // a*ns+b) are listed for LL|LL and SS|SS, LL|SS lists every ordered pair and
-// SS|LL none; the kernels digest each listed quartet for both orders.
+// SS|LL none; the kernels digest each listed quartet for both orders.  The
+// spinor relation (ba|dc) = (ab|cd)* halves the lists once more: of a
+// quartet and its image only one is listed, and for a Hermitian density the
+// image's J and K contributions are the conjugate transposes of the listed
+// quartet's, which k_herm_complete adds at the end (quartets equal to their
+// own image are digested with weight 1/2).
 // Quartets come out grouped by angular class (l_a,l_b,l_c,l_d), highest
 // first, so neighbouring CTAs carry similar work.  With a Schwarz threshold
 // quartets with Q_ab Q_cd below it are left out (SCHWARZ :37889, at the
@@ -2247,6 +2392,14 @@ void gen_quartets(const bg_ctx *c, int t1, int t2, int ilev, bool sym, Sink &&si
       for (const PairRec &y : Y) {
         if (scr && x.q * y.q < c->screen) break;
         if (sym && t1 == t2 && x.idx < y.idx) continue;
+        if (sym) {
+          // (ba|dc) = (ab|cd)*: keep the lexicographic maximum of the
+          // quartet's orbit, the pair indices of (ab|cd) against those of
+          // (ba|dc) and, within one class, of (dc|ba)
+          long long pb = (long long)x.b * c->ns + x.a, qb = (long long)y.b * c->ns + y.a;
+          if (x.idx < pb || (x.idx == pb && y.idx < qb)) continue;
+          if (t1 == t2 && (x.idx < qb || (x.idx == qb && y.idx < pb))) continue;
+        }
         const Shell &C = c->shells[y.a], &D = c->shells[y.b];
         int mcnt = 1 + (B.cnt != A.cnt) + (C.cnt != A.cnt && C.cnt != B.cnt) +
                    (D.cnt != A.cnt && D.cnt != B.cnt && D.cnt != C.cnt);
@@ -2306,6 +2459,7 @@ int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   int n = c->ndim;
   k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, ddf);
   QArgsDF a;
+  a.inst = nullptr;
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = ddf; a.Eci = c->d_Eci;
   a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = n; a.ldf = ldf;
   a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym;
@@ -2356,6 +2510,7 @@ int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
     attr = true;
   }
   QArgs a;
+  a.inst = nullptr;
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_E; a.D = d_D;
   a.Ecv = c->d_Ecv; a.Eci = c->d_Eci;
   a.GD = d_GD; a.GX = d_GX; a.ns = c->ns; a.ldd = ldd; a.ldf = ldf;
@@ -2556,7 +2711,7 @@ int stream_class(bg_ctx *c, int t1, int t2, int ilev, const double2 *d_D, int ld
     cudaError_t e = cudaMemcpyAsync(c->d_chunk[cur], c->h_chunk[cur], sizeof(int4) * fill,
                                     cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) { rc = cuda_fail(c, e, "cudaMemcpyAsync"); return; }
-    rc = launch_quartets(c, c->d_chunk[cur], fill, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, 1);
+    rc = launch_quartets(c, c->d_chunk[cur], fill, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, 2);
     if (rc) return;
     cudaEventRecord(c->chunk_ev[cur], st);
     cur ^= 1;
@@ -2573,6 +2728,102 @@ int stream_class(bg_ctx *c, int t1, int t2, int ilev, const double2 *d_D, int ld
   });
   flush();
   return rc;
+}
+
+
+int batch_fail(bg_batch *b, cudaError_t e, const char *what) {
+  b->err = std::string(what) + ": " + cudaGetErrorString(e);
+  b->bad = true;
+  return BG_ERR_CUDA;
+}
+
+#define BK(b, call)                                      \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return batch_fail(b, e_, #call); \
+  } while (0)
+
+// Quartet lists of a batch for one stage: every instance's lists (CLMFAST
+// rules of that instance, its Schwarz screening) in batch shell numbering,
+// merged per component class and grouped by angular class, highest first.
+int batch_lists(bg_batch *b, int ilev) {
+  for (int k = 0; k < 4; ++k) {
+    if (b->d_quart[k]) cudaFree(b->d_quart[k]);
+    b->d_quart[k] = nullptr;
+    b->nquart[k] = 0;
+  }
+  constexpr int NKEY = (MAXLB + 1) * (MAXLB + 1) * (MAXLB + 1) * (MAXLB + 1);
+  for (int t1 = 0; t1 < b->ncomp; ++t1)
+    for (int t2 = 0; t2 < b->ncomp; ++t2) {
+      std::vector<std::vector<int>> bucket(NKEY);
+      for (int i = 0; i < b->n; ++i) {
+        const bg_ctx *c = b->shadow[i];
+        int s0 = b->sbase[i];
+        gen_quartets(c, t1, t2, ilev, true, [&](int a, int bb, int cc, int d) {
+          int key = ((c->shells[a].l * (MAXLB + 1) + c->shells[bb].l) * (MAXLB + 1) +
+                     c->shells[cc].l) * (MAXLB + 1) + c->shells[d].l;
+          std::vector<int> &v = bucket[NKEY - 1 - key];
+          v.push_back(a + s0); v.push_back(bb + s0); v.push_back(cc + s0); v.push_back(d + s0);
+        });
+      }
+      size_t tot = 0;
+      for (auto &v : bucket) tot += v.size();
+      int k = 2 * t1 + t2;
+      b->nquart[k] = (long long)tot / 4;
+      if (!tot) continue;
+      BK(b, cudaMalloc(&b->d_quart[k], sizeof(int) * tot));
+      size_t pos = 0;
+      for (auto &v : bucket) {
+        if (v.empty()) continue;
+        BK(b, cudaMemcpy(b->d_quart[k] + pos, v.data(), sizeof(int) * v.size(),
+                         cudaMemcpyHostToDevice));
+        pos += v.size();
+        std::vector<int>().swap(v);
+      }
+    }
+  b->quart_ilev = ilev;
+  return 0;
+}
+
+// One launch of the FP64 or split-precision quartet kernel over a batch's
+// list of one component class, both orders of each listed quartet digested.
+int batch_launch(bg_batch *b, int t1, int t2, const double2 *d_D, double *d_GD, double *d_GX,
+                 cudaStream_t st) {
+  int k = 2 * t1 + t2;
+  long long nq = b->nquart[k];
+  if (nq <= 0) return 0;
+  if (b->prec == BG_PREC_DF32) {
+    static bool attr_df = false;  // set once: no attribute call inside a graph capture
+    if (!attr_df) {
+      BK(b, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)quartet_smem_df(1)));
+      attr_df = true;
+    }
+    QArgsDF a;
+    a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_Edf; a.D = b->d_Ddf; a.Eci = b->d_Eci;
+    a.GD = d_GD; a.GX = d_GX; a.ns = 0; a.ldd = 0; a.ldf = 0; a.nskp = 0;
+    a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.inst = b->d_inst;
+    long long grid = std::min<long long>(nq, 152LL * 128);
+    k_quartet_df<<<(unsigned)grid, DFTHREADS, quartet_smem_df(1), st>>>(
+        a, (const int4 *)b->d_quart[k], nq, t1, t2);
+  } else {
+    static bool attr = false;
+    if (!attr) {
+      BK(b, cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)quartet_smem()));
+      attr = true;
+    }
+    QArgs a;
+    a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_E; a.D = d_D; a.Ecv = b->d_Ecv; a.Eci = b->d_Eci;
+    a.GD = d_GD; a.GX = d_GX; a.ns = 0; a.ldd = 0; a.ldf = 0; a.nskp = 0;
+    a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.bound = nullptr; a.inst = b->d_inst;
+    long long grid = std::min<long long>(nq, 152LL * 64);
+    k_quartet<<<(unsigned)grid, QTHREADS, quartet_smem(), st>>>(
+        a, (const int4 *)b->d_quart[k], nq, t1, t2);
+  }
+  BK(b, cudaGetLastError());
+  b->launches++;
+  return 0;
 }
 
 }  // namespace
@@ -2654,6 +2905,10 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
       }
     }
   c->ns = (int)c->shells.size();
+  for (int a = 0; a < c->ns; ++a) {
+    c->shells[a].inst = 0;
+    c->shells[a].prow = a * c->ns;
+  }
   if (upload_tables()) { g_init_err = "constant table upload failed"; delete c; return BG_ERR_CUDA; }
   k_boys_table<<<(NBGRID + 127) / 128, 128>>>();
   // E-coefficient storage for every ordered shell pair and component
@@ -2882,9 +3137,15 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
         rc = stream_class(c, t1, t2, ilev, (const double2 *)d_dent, ldd, d_gdir, d_gxch, ldf, st);
       else
         rc = launch_quartets(c, c->d_quart[k], c->nquart[k], t1, t2, (const double2 *)d_dent,
-                             ldd, d_gdir, d_gxch, ldf, st, 1);
+                             ldd, d_gdir, d_gxch, ldf, st, 2);
       if (rc) return rc;
     }
+  k_herm_complete<<<dim3(1, 256), 256, 0, st>>>((double2 *)d_gdir, c->ndim, ldf, nullptr,
+                                                nullptr, 1);
+  k_herm_complete<<<dim3(1, 256), 256, 0, st>>>((double2 *)d_gxch, c->ndim, ldf, nullptr,
+                                                nullptr, 1);
+  CK(c, cudaGetLastError());
+  c->launches += 2;
   return BG_OK;
 }
 
@@ -3068,6 +3329,185 @@ void bertha_gpu_free(bg_ctx *c) {
   for (int k = 0; k < 2; ++k) cudaFree(c->d_bquart[k]);
   cudaFree(c->d_BX);
   delete c;
+}
+
+int bertha_gpu_batch_create(bg_batch **out, int n, bg_ctx *const *ctxs,
+                            const long long *moff, const int *ld) {
+  if (!out) return BG_ERR_ARG;
+  *out = nullptr;
+  if (n < 1 || !ctxs) { g_init_err = "invalid argument"; return BG_ERR_ARG; }
+  for (int i = 0; i < n; ++i) {
+    if (!ctxs[i]) { g_init_err = "null context"; return BG_ERR_ARG; }
+    if (ctxs[i]->bad) { g_init_err = "context failed earlier"; return BG_ERR_STATE; }
+    const bg_ctx *c = ctxs[i], *c0 = ctxs[0];
+    if (c->hmlt != c0->hmlt || c->isym != c0->isym || c->racah1 != c0->racah1) {
+      g_init_err = "batched instances must share hmlt, shape and the RACAH1 flag";
+      return BG_ERR_ARG;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    bg_ctx *c = ctxs[i];
+    if (c->screen > 0.0 && c->qbound.empty()) {
+      int rc = compute_bounds(c, nullptr);
+      if (rc) { g_init_err = c->err; return rc; }
+    }
+  }
+  bg_batch *b = new bg_batch();
+  b->n = n;
+  b->ncomp = ctxs[0]->ncomp; b->hmlt = ctxs[0]->hmlt; b->isym = ctxs[0]->isym;
+  b->racah1 = ctxs[0]->racah1; b->prec = ctxs[0]->prec;
+  std::vector<long long> pbase(n), ebase(n);
+  long long nst = 0, npt = 0, net = 0, packed = 0;
+  std::vector<Shell> sh;
+  for (int i = 0; i < n; ++i) {
+    const bg_ctx *c = ctxs[i];
+    b->sbase.push_back((int)nst);
+    pbase[i] = npt;
+    ebase[i] = net;
+    Inst I;
+    I.off = moff ? moff[i] : packed;
+    I.ld = ld ? ld[i] : c->ndim;
+    I.nskp = c->nskp;
+    if (I.off < 0 || I.ld < c->ndim) {
+      g_init_err = "invalid placement of instance " + std::to_string(i);
+      bertha_gpu_batch_free(b);
+      return BG_ERR_ARG;
+    }
+    b->inst.push_back(I);
+    b->ndim.push_back(c->ndim);
+    if (c->ndim > 0)
+      b->span = std::max(b->span, I.off + (long long)I.ld * (c->ndim - 1) + c->ndim);
+    packed += (long long)c->ndim * c->ndim;
+    for (int a = 0; a < c->ns; ++a) {
+      Shell s2 = c->shells[a];
+      s2.inst = i;
+      s2.prow = (int)(npt + (long long)a * c->ns - nst);
+      sh.push_back(s2);
+    }
+    nst += c->ns;
+    npt += (long long)c->ns * c->ns;
+    net += c->nE;
+    if (npt > 0x7fffffffLL) {
+      g_init_err = "batch pair table beyond 2^31 entries";
+      bertha_gpu_batch_free(b);
+      return BG_ERR_CAPACITY;
+    }
+    bg_ctx *h = new bg_ctx();
+    h->ns = c->ns; h->ncomp = c->ncomp; h->racah1 = c->racah1;
+    h->shells = c->shells; h->qbound = c->qbound; h->screen = c->screen;
+    b->shadow.push_back(h);
+  }
+  cudaError_t e = cudaSuccess;
+  auto fail = [&](const char *what) {
+    g_init_err = std::string(what) + ": " + cudaGetErrorString(e);
+    bertha_gpu_batch_free(b);
+    return BG_ERR_CUDA;
+  };
+  if ((e = cudaMalloc(&b->d_sh, sizeof(Shell) * std::max<long long>(nst, 1))) ||
+      (e = cudaMalloc(&b->d_pe, sizeof(PairE) * std::max<long long>(npt, 1))) ||
+      (e = cudaMalloc(&b->d_E, sizeof(double2) * std::max<long long>(net, 1))) ||
+      (e = cudaMalloc(&b->d_Ecv, sizeof(double2) * std::max<long long>(net, 1))) ||
+      (e = cudaMalloc(&b->d_Eci, std::max<long long>(net, 1))) ||
+      (e = cudaMalloc(&b->d_Edf, sizeof(float4) * std::max<long long>(net, 1))) ||
+      (e = cudaMalloc(&b->d_inst, sizeof(Inst) * n)) ||
+      (e = cudaMalloc(&b->d_ndim, sizeof(int) * n)))
+    return fail("cudaMalloc");
+  if ((e = cudaMemcpy(b->d_sh, sh.data(), sizeof(Shell) * nst, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(Inst) * n, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(b->d_ndim, b->ndim.data(), sizeof(int) * n, cudaMemcpyHostToDevice)))
+    return fail("cudaMemcpy");
+  for (int i = 0; i < n; ++i) {
+    const bg_ctx *c = ctxs[i];
+    long long np = (long long)c->ns * c->ns, ne = c->nE;
+    std::vector<PairE> pe(np);
+    if ((e = cudaMemcpy(pe.data(), c->d_pe, sizeof(PairE) * np, cudaMemcpyDeviceToHost)))
+      return fail("cudaMemcpy");
+    for (PairE &p : pe)
+      for (int t = 0; t < 2; ++t)
+        if (p.off[t] >= 0) p.off[t] += ebase[i];
+    if ((e = cudaMemcpy(b->d_pe + pbase[i], pe.data(), sizeof(PairE) * np,
+                        cudaMemcpyHostToDevice)))
+      return fail("cudaMemcpy");
+    if (ne > 0 &&
+        ((e = cudaMemcpy(b->d_E + ebase[i], c->d_E, sizeof(double2) * ne, cudaMemcpyDeviceToDevice)) ||
+         (e = cudaMemcpy(b->d_Ecv + ebase[i], c->d_Ecv, sizeof(double2) * ne, cudaMemcpyDeviceToDevice)) ||
+         (e = cudaMemcpy(b->d_Eci + ebase[i], c->d_Eci, ne, cudaMemcpyDeviceToDevice)) ||
+         (e = cudaMemcpy(b->d_Edf + ebase[i], c->d_Edf, sizeof(float4) * ne, cudaMemcpyDeviceToDevice))))
+      return fail("cudaMemcpy");
+  }
+  *out = b;
+  return BG_OK;
+}
+
+int bertha_gpu_batch_set_precision(bg_batch *b, int prec) {
+  if (!b) return BG_ERR_ARG;
+  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32) return BG_ERR_ARG;
+  b->prec = prec;
+  return BG_OK;
+}
+
+int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev, double *d_gdir,
+                                    double *d_gxch, void *stream) {
+  if (!b) return BG_ERR_ARG;
+  if (b->bad) return BG_ERR_STATE;
+  if (ilev < 1 || ilev > 4 || !d_dent || !d_gdir || !d_gxch) return BG_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  b->launches = 0;
+  if (b->hmlt == BG_HMLT_BARE) return BG_OK;
+  unsigned gx = (unsigned)std::min(b->n, 1024);
+  k_zero_inst<<<dim3(gx, 16), 256, 0, st>>>(d_gdir, b->d_inst, b->d_ndim, b->n);
+  k_zero_inst<<<dim3(gx, 16), 256, 0, st>>>(d_gxch, b->d_inst, b->d_ndim, b->n);
+  BK(b, cudaGetLastError());
+  b->launches += 2;
+  if (b->quart_ilev != ilev) {
+    int rc = batch_lists(b, ilev);
+    if (rc) return rc;
+  }
+  if (b->prec == BG_PREC_DF32) {
+    if (!b->d_Ddf) BK(b, cudaMalloc(&b->d_Ddf, sizeof(float4) * std::max<long long>(b->span, 1)));
+    k_dconv1<<<1024, 256, 0, st>>>((const double2 *)d_dent, b->span, b->d_Ddf);
+    BK(b, cudaGetLastError());
+    b->launches++;
+  }
+  for (int t1 = b->ncomp - 1; t1 >= 0; --t1)
+    for (int t2 = b->ncomp - 1; t2 >= 0; --t2) {
+      int rc = batch_launch(b, t1, t2, (const double2 *)d_dent, d_gdir, d_gxch, st);
+      if (rc) return rc;
+    }
+  k_herm_complete<<<dim3(gx, 16), 256, 0, st>>>((double2 *)d_gdir, 0, 0, b->d_inst, b->d_ndim,
+                                                b->n);
+  k_herm_complete<<<dim3(gx, 16), 256, 0, st>>>((double2 *)d_gxch, 0, 0, b->d_inst, b->d_ndim,
+                                                b->n);
+  BK(b, cudaGetLastError());
+  b->launches += 2;
+  return BG_OK;
+}
+
+long long bertha_gpu_batch_quartets(const bg_batch *b) {
+  if (!b) return 0;
+  return b->nquart[0] + b->nquart[1] + b->nquart[2] + b->nquart[3];
+}
+
+long long bertha_gpu_batch_launches(const bg_batch *b) { return b ? b->launches : 0; }
+
+const char *bertha_gpu_batch_last_error(const bg_batch *b) {
+  return b ? b->err.c_str() : g_init_err.c_str();
+}
+
+void bertha_gpu_batch_free(bg_batch *b) {
+  if (!b) return;
+  for (bg_ctx *h : b->shadow) delete h;
+  cudaFree(b->d_sh);
+  cudaFree(b->d_pe);
+  cudaFree(b->d_E);
+  cudaFree(b->d_Ecv);
+  cudaFree(b->d_Eci);
+  cudaFree(b->d_Edf);
+  cudaFree(b->d_Ddf);
+  cudaFree(b->d_inst);
+  cudaFree(b->d_ndim);
+  for (int k = 0; k < 4; ++k) cudaFree(b->d_quart[k]);
+  delete b;
 }
 
 }  // extern "C"

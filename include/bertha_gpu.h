@@ -104,7 +104,10 @@ int bertha_gpu_dims(const bg_ctx *ctx, int *ndim, int *nskp);
  *   gdir, gxch      [ldf*ndim] outputs, overwritten (CLMFAST zeroes them)
  * Semantics follow CLMFAST with CLMMTG (shape GENERAL) or CLMMTZ (LINEAR,
  * ATOMIC) digestion; one-centre quartets are skipped unless
- * BG_FLAG_NO_RACAH1 was given. */
+ * BG_FLAG_NO_RACAH1 was given.  Like CLMFAST with INTSYM (its default), the
+ * build evaluates a symmetry-reduced quartet set and completes GDIR and GXCH
+ * as Hermitian matrices (:12164-12205), which assumes a Hermitian DENT (as
+ * DENSTY makes it). */
 int bertha_gpu_clmfast(bg_ctx *ctx, const double *dent, int ldd, int ilev,
                        double *gdir, double *gxch, int ldf);
 
@@ -179,6 +182,48 @@ int bertha_gpu_quartets_noalloc(bg_ctx *ctx, const int *d_quartets,
                                 long long nq, int t1, int t2,
                                 const double *d_dent, int ldd, double *d_gdir,
                                 double *d_gxch, int ldf, void *stream);
+
+/* Batched Fock builds of independent instances (atoms, ions, molecules of
+ * different basis sizes), one kernel launch per component class for all
+ * of them.  The reference runs such instances as separate bertha-scf
+ * processes; this replaces CALL CLMFAST (bertha-scf.f:5401) of each of them
+ * by one stream-ordered call.  No counterpart in the reference. */
+typedef struct bg_batch bg_batch;
+
+/* Make a batch from n contexts (bertha_gpu_init).  The instances must share
+ * hmlt, shape and the RACAH1 flag; each keeps its own Schwarz threshold
+ * (bertha_gpu_set_screening before this call) and quartet rules.  The batch
+ * copies what it needs: the contexts may be freed afterwards.  Placement of
+ * the matrices in the batch's device arrays: element (i, j) of instance k's
+ * density and outputs is complex element moff[k] + i + ld[k]*j; moff = NULL
+ * packs the instances one after another with ld = NDIM (ld = NULL: NDIM).
+ * The precision is taken from ctxs[0] (bertha_gpu_set_precision). */
+int bertha_gpu_batch_create(bg_batch **b, int n, bg_ctx *const *ctxs,
+                            const long long *moff, const int *ld);
+
+/* Contraction precision of the batch's later builds (BG_PREC_*). */
+int bertha_gpu_batch_set_precision(bg_batch *b, int prec);
+
+/* CLMFAST of every instance at stage ilev on device arrays in the batch's
+ * placement: d_dent holds all densities; d_gdir, d_gxch get all GDIR and
+ * GXCH, each instance's NDIM x NDIM block overwritten (other elements are
+ * left alone).  The first call at a stage builds the quartet lists (host
+ * work and allocation); later calls at that stage only launch kernels on
+ * `stream` and can be captured in a CUDA graph. */
+int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
+                                    double *d_gdir, double *d_gxch, void *stream);
+
+/* Shell quartets in the batch's lists at the last stage built. */
+long long bertha_gpu_batch_quartets(const bg_batch *b);
+
+/* Kernel launches issued by the last batched build call. */
+long long bertha_gpu_batch_launches(const bg_batch *b);
+
+/* Message of the last error on this batch (or of bertha_gpu_batch_create
+ * when b is NULL). */
+const char *bertha_gpu_batch_last_error(const bg_batch *b);
+
+void bertha_gpu_batch_free(bg_batch *b);
 
 /* Number of primitive shells and, per shell (centre, l, index in the
  * exponent list), in the order centre, l, exponent. */
