@@ -45,7 +45,8 @@ def parse():
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-h2o", action="store_true",
-                   help="skip the H2O Coulomb and Breit build timings reported beside the headline")
+                   help="skip the other configurations (H2O builds and SCF, TlF builds, "
+                        "batched atoms) reported beside the headline")
     p.add_argument("--precision", default="df32", choices=["fp64", "df32"],
                    help="precision of the headline value; the other is timed beside it")
     return p.parse_args()
@@ -259,7 +260,8 @@ def h2o_breit_build(torch):
     return {"ndim": n, "hmlt": "DHFB", "ilev": 3,
             "quartets": int(len(q1) + len(q2)),
             "classes": {"LS|LS (ab>=cd, both orders digested)": int(len(q1)),
-                        "LS|SL (also digested as SL|LS)": int(len(q2))},
+                        "LS|SL (one of each (ab|cd), (dc|ba) pair; also digested as SL|LS)":
+                            int(len(q2))},
             "device_s": t, "quartets_per_s": (len(q1) + len(q2)) / t,
             "flops": flops, "tflops": flops / t / 1e12,
             "host_api_s": float(np.median(ts)),
@@ -291,6 +293,138 @@ def h2o_scf(torch):
         out[prec] = {k: r[k] for k in ("energy", "iterations", "converged", "wall_s", "fock_s",
                                        "linalg_s", "oneel_s")}
     out["energy_diff_split_vs_fp64_eh"] = abs(out["df32"]["energy"] - out["fp64"]["energy"])
+    return out
+
+
+def _device_time(torch, fn, reps=1):
+    """Median device time (s) of fn() on the current stream, CUDA events."""
+    st = torch.cuda.current_stream()
+    ms = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fn(st.cuda_stream)
+        e1.record(st)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return float(np.median(ms)) * 1e-3
+
+
+def tlf_builds(torch):
+    """The TlF Dirac-Coulomb-Breit configuration (R = 3.94 bohr on z, Tl
+    28s24p16d12f and F 14s9p3d even-tempered, Schwarz 1e-12, DIATOM: real
+    digestion): one stage-3 Coulomb build in FP64 and in the autotuned mixed
+    mode, and the Breit build in FP64, on device arrays (seeded Hermitian
+    density), each timed with CUDA events after a first call that builds
+    the lists (and, for the mixed mode, tunes the kernel per class)."""
+    import berthagpu
+    from berthagpu import deck
+    b = deck.tlf_basis()
+    dent = deck.density(b, seed=1, real=True)
+    n = b.ndim
+    d_D = torch.from_numpy(np.ascontiguousarray(dent.T)).cuda()
+    J, K, B = (torch.zeros((n, n), dtype=torch.complex128, device="cuda") for _ in range(3))
+    out = {"ndim": n, "shells": len(b.shells()), "hmlt": "DHFB", "screen": 1e-12, "ilev": 3}
+    for prec in ("fp64", "auto"):
+        fb = berthagpu.FockBuilder(b)
+        fb.set_precision(prec)
+        fb.set_screening(1e-12)
+        t0 = time.perf_counter()
+        fb.clmfast_device(d_D.data_ptr(), J.data_ptr(), K.data_ptr(), 3, n)
+        torch.cuda.synchronize()
+        first = time.perf_counter() - t0
+        t = _device_time(torch, lambda s: fb.clmfast_device(d_D.data_ptr(), J.data_ptr(),
+                                                           K.data_ptr(), 3, n, s))
+        r = {"first_call_s": first, "device_s": t,
+             "energy_j_eh": float(0.5 * torch.sum(d_D * J).real),
+             "energy_k_eh": float(0.5 * torch.sum(d_D * K).real)}
+        if prec == "auto":
+            r["auto"] = fb.auto_stats()
+        else:
+            fb.brtfast_device(d_D.data_ptr(), B.data_ptr(), 3, n)
+            torch.cuda.synchronize()
+            out["breit_fp64"] = {
+                "device_s": _device_time(torch, lambda s: fb.brtfast_device(
+                    d_D.data_ptr(), B.data_ptr(), 3, n, s)),
+                "energy_bx_eh": float(0.5 * torch.sum(d_D * B).real)}
+        fb.close()
+        out["coulomb_" + prec] = r
+    out["auto_vs_fp64_energy_abs_eh"] = max(
+        abs(out["coulomb_auto"]["energy_j_eh"] - out["coulomb_fp64"]["energy_j_eh"]),
+        abs(out["coulomb_auto"]["energy_k_eh"] - out["coulomb_fp64"]["energy_k_eh"]))
+    out["dcb_fock_build_fp64_s"] = out["coulomb_fp64"]["device_s"] + out["breit_fp64"]["device_s"]
+    return out
+
+
+def batched_atoms(torch):
+    """The batched-atoms configuration: 96 closed-shell atoms (Z drawn,
+    seeded, from the closed-shell atoms He..Rn; n_s = 8+Z/4, n_p = 6+Z/5,
+    n_d = Z/12, n_f = Z/24 even-tempered functions, Dirac-Coulomb, Schwarz
+    1e-12) in one batched Fock build (one launch per component class for all
+    96, or per tuned run of classes), FP64 and autotuned mixed precision,
+    timed with CUDA events; and the batched SCF of 96 atoms drawn from He..Ca
+    (the lighter half of the table, so that the whole SCF stays within the
+    benchmark's time) to |dE| < 1e-9 Eh per atom in both precisions."""
+    from berthagpu import deck
+    from berthagpu.fock import FockBatch, FockBuilder
+    from berthagpu.scf import BatchedDHFSCF
+    bases = deck.batched_atoms(96, seed=2024)
+    zs = [int(b.znuc[0]) for b in bases]
+    dens = [deck.density(b, seed=2024 + k, nocc=z, real=True) for k, (b, z) in enumerate(zip(bases, zs))]
+    D = torch.from_numpy(np.concatenate([d.ravel(order="F") for d in dens])).cuda()
+    J, K = torch.zeros_like(D), torch.zeros_like(D)
+    out = {"atoms": 96, "ndim_min": min(b.ndim for b in bases),
+           "ndim_max": max(b.ndim for b in bases), "ndim_total": sum(b.ndim for b in bases)}
+    energies = {}
+    for prec in ("fp64", "auto"):
+        fbs = []
+        for b in bases:
+            fb = FockBuilder(b, racah1=False)
+            fb.set_precision(prec)
+            fb.set_screening(1e-12)
+            fbs.append(fb)
+        batch = FockBatch(fbs)
+        for fb in fbs:
+            fb.close()
+        t0 = time.perf_counter()
+        batch.clmfast_device(D.data_ptr(), J.data_ptr(), K.data_ptr(), 3)
+        torch.cuda.synchronize()
+        first = time.perf_counter() - t0
+        t = _device_time(torch, lambda s: batch.clmfast_device(D.data_ptr(), J.data_ptr(),
+                                                              K.data_ptr(), 3, s))
+        nq = batch.quartets()
+        r = {"first_call_s": first, "device_s": t, "quartets": nq, "quartets_per_s": nq / t,
+             "launches": batch.launches()}
+        if prec == "auto":
+            r["auto"] = batch.auto_stats()
+        Jh, Kh = J.cpu().numpy(), K.cpu().numpy()
+        e, off = [], 0
+        for d in dens:
+            m = d.shape[0] * d.shape[0]
+            e.append(0.5 * np.sum(d.ravel(order="F") * (Jh[off:off + m] - Kh[off:off + m])).real)
+            off += m
+        energies[prec] = np.array(e)
+        batch.close()
+        out["build_" + prec] = r
+    out["build_auto_vs_fp64_energy_max_abs_eh"] = float(
+        np.abs(energies["auto"] - energies["fp64"]).max())
+    light = deck.batched_atoms(96, seed=2024, zset=[z for z in deck.CLOSED_SHELL_ATOMS if z <= 20])
+    lz = [int(b.znuc[0]) for b in light]
+    res = {}
+    for prec in ("fp64", "auto"):
+        s = BatchedDHFSCF(light, lz, precision=prec, screen=1e-12, torch=torch)
+        r = s.run(etol=1e-9, max_iter=80)
+        s.close()
+        res[prec] = r
+    de = np.abs(np.array(res["auto"]["energy"]) - np.array(res["fp64"]["energy"]))
+    out["scf_light"] = {
+        "atoms": 96, "z": sorted(set(lz)), "etol_eh": 1e-9,
+        "fp64": {k: res["fp64"][k] for k in ("iterations", "wall_s", "fock_s", "linalg_s",
+                                              "quartets_per_build")},
+        "auto": {k: res["auto"][k] for k in ("iterations", "wall_s", "fock_s", "linalg_s")},
+        "all_converged": bool(all(res["fp64"]["converged"]) and all(res["auto"]["converged"])),
+        "energy_auto_vs_fp64_max_abs_eh": float(de.max()),
+        "energy_fp64_by_z": {str(z): e for z, e in zip(lz, res["fp64"]["energy"])}}
     return out
 
 
@@ -464,11 +598,13 @@ def run_gpu(args):
     traffic = read_traffic()
 
     line = None
-    h2o = breit = scf = None
+    h2o = breit = scf = tlf = atoms = None
     if rank == 0 and not args.no_h2o:
         h2o = h2o_fock_build(torch, with_cpu=(world == 1))
         breit = h2o_breit_build(torch)
         scf = h2o_scf(torch)
+        tlf = tlf_builds(torch)
+        atoms = batched_atoms(torch)
     if rank == 0:
         cpu = None
         if world == 1:
@@ -508,6 +644,8 @@ def run_gpu(args):
             "fock_build_h2o": h2o,
             "breit_build_h2o": breit,
             "scf_h2o": scf,
+            "fock_build_tlf": tlf,
+            "batched_atoms": atoms,
         }
         print(json.dumps(line), flush=True)
     fb.close()

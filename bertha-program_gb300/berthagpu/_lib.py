@@ -13,7 +13,7 @@ HMLT = {"NORL": 0, "BARE": 1, "DHFR": 2, "DHFP": 3, "DHFB": 4, "DHFQ": 5}
 SHAPE = {"NOSYMM": 0, "PLANAR": 0, "GENERAL": 0, "DIATOM": 1, "LINEAR": 1, "ATOMIC": 2}
 FLAG_NO_RACAH1 = 1
 FLAG_GAUNT = 2
-PREC = {"fp64": 0, "df32": 1}
+PREC = {"fp64": 0, "df32": 1, "auto": 2}
 MAX_L = 3
 
 _CODES = {1: "invalid argument", 2: "capacity exceeded", 3: "CUDA error", 4: "context unusable"}
@@ -56,6 +56,8 @@ def lib():
         L.bertha_gpu_last_error.restype = ctypes.c_char_p
         L.bertha_gpu_free.argtypes = [P]
         L.bertha_gpu_free.restype = None
+        L.bertha_gpu_auto_stats.argtypes = [P, P, P, P]
+        L.bertha_gpu_batch_auto_stats.argtypes = [P, P, P, P]
         L.bertha_gpu_batch_create.argtypes = [ctypes.POINTER(P), i, P, P, P]
         L.bertha_gpu_batch_set_precision.argtypes = [P, i]
         L.bertha_gpu_batch_clmfast_device.argtypes = [P, P, i, P, P, P]
@@ -84,6 +86,7 @@ EXPORTED = [
     "bertha_gpu_batch_create", "bertha_gpu_batch_set_precision",
     "bertha_gpu_batch_clmfast_device", "bertha_gpu_batch_quartets",
     "bertha_gpu_batch_launches", "bertha_gpu_batch_last_error", "bertha_gpu_batch_free",
+    "bertha_gpu_auto_stats", "bertha_gpu_batch_auto_stats",
 ]
 
 

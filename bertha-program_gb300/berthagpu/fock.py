@@ -40,7 +40,9 @@ class FockBuilder:
         self.precision = "fp64"
 
     def set_precision(self, prec):
-        """'fp64' (drop-in) or 'df32' (split precision on the FP32 pipes)."""
+        """'fp64' (drop-in), 'df32' (split precision on the FP32 pipes) or
+        'auto' (per angular class the faster of the two, timed on the first
+        build)."""
         check(lib().bertha_gpu_set_precision(self._ctx, _lib.PREC[prec]), self._ctx)
         self.precision = prec
 
@@ -142,6 +144,13 @@ class FockBuilder:
     def launches(self):
         return int(lib().bertha_gpu_launches(self._ctx))
 
+    def auto_stats(self):
+        """Under precision 'auto': quartets on the FP64 and split kernels, runs."""
+        f, d, r = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+        check(lib().bertha_gpu_auto_stats(self._ctx, ctypes.byref(f), ctypes.byref(d),
+                                          ctypes.byref(r)), self._ctx)
+        return {"fp64_quartets": f.value, "df32_quartets": d.value, "runs": r.value}
+
 
 class FockBatch:
     """Batched CLMFAST over independent instances (one FockBuilder each, all
@@ -177,6 +186,12 @@ class FockBatch:
 
     def quartets(self):
         return int(lib().bertha_gpu_batch_quartets(self._b))
+
+    def auto_stats(self):
+        f, d, r = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+        check_batch(lib().bertha_gpu_batch_auto_stats(self._b, ctypes.byref(f), ctypes.byref(d),
+                                                      ctypes.byref(r)), self._b)
+        return {"fp64_quartets": f.value, "df32_quartets": d.value, "runs": r.value}
 
     def launches(self):
         return int(lib().bertha_gpu_batch_launches(self._b))

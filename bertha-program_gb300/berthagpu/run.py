@@ -36,7 +36,7 @@ def main(argv=None):
     p.add_argument("--zmax", type=int, default=86, help="largest Z drawn for --atoms")
     p.add_argument("--scf", action="store_true", help="--atoms: run the batched SCF too")
     p.add_argument("--build", choices=["coulomb", "breit", "both"], default="coulomb")
-    p.add_argument("--precision", choices=["fp64", "df32"], default="fp64")
+    p.add_argument("--precision", choices=["fp64", "df32", "auto"], default="fp64")
     p.add_argument("--ilev", type=int, default=3)
     p.add_argument("--screen", type=float, default=0.0)
     p.add_argument("--repeat", type=int, default=1)
@@ -66,6 +66,8 @@ def main(argv=None):
             gd, gx = fb.clmfast(dent, a.ilev)
             ts.append(time.perf_counter() - t0)
         out["coulomb_s"] = ts
+        if a.precision == "auto":
+            out["auto"] = fb.auto_stats()
         out["energy_j_eh"] = float(0.5 * np.sum(dent * gd).real)
         out["energy_k_eh"] = float(0.5 * np.sum(dent * gx).real)
     if a.build in ("breit", "both"):
@@ -96,7 +98,7 @@ def atoms_main(a):
     dens = [np.asarray(deck.density(b, seed=a.seed + k, nocc=z, real=True))
             for k, (b, z) in enumerate(zip(bases, zs))]
     D = torch.from_numpy(np.concatenate([d.ravel(order="F") for d in dens])).cuda()
-    for prec in ("fp64", "df32"):
+    for prec in ("fp64", "df32", "auto"):
         t0 = time.perf_counter()
         fbs = []
         for b in bases:
@@ -131,11 +133,14 @@ def atoms_main(a):
         out[prec] = {"init_s": t_init, "first_call_s": t_first, "device_s": ms / 1e3,
                      "quartets": nq, "quartets_per_s": nq / (ms / 1e3),
                      "launches": batch.launches(), "energy_j_eh": ej, "energy_k_eh": ek}
+        if prec == "auto":
+            out[prec]["auto"] = batch.auto_stats()
         batch.close()
-    out["df32_energy_max_abs_err_eh"] = max(
-        max(abs(x - y) for x, y in zip(out["fp64"]["energy_j_eh"], out["df32"]["energy_j_eh"])),
-        max(abs(x - y) for x, y in zip(out["fp64"]["energy_k_eh"], out["df32"]["energy_k_eh"])))
-    for prec in ("fp64", "df32"):
+    for prec in ("df32", "auto"):
+        out[prec + "_energy_max_abs_err_eh"] = max(
+            max(abs(x - y) for x, y in zip(out["fp64"]["energy_j_eh"], out[prec]["energy_j_eh"])),
+            max(abs(x - y) for x, y in zip(out["fp64"]["energy_k_eh"], out[prec]["energy_k_eh"])))
+    for prec in ("fp64", "df32", "auto"):
         for key in ("energy_j_eh", "energy_k_eh"):
             out[prec][key] = out[prec][key][:8]  # keep the line short
     if a.scf:

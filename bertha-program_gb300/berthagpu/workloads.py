@@ -84,7 +84,9 @@ def quartet_flops(basis, quart, t1, t2):
 def breit_quartets(basis, ilev=3, racah1=True):
     """Shell quartets of the Breit build as the library lists them
     (BRTFAST centre and stage rules): (LS|LS) with pair index ab >= cd and
-    (LS|SL) over every ordered pair; returns the two int32 [n, 4] arrays."""
+    (LS|SL) with (ab, cd) >= (dc, ba) in pair-index order (one of each
+    quartet and its conjugate image (dc|ba)); returns the two int32 [n, 4]
+    arrays."""
     sh = basis.shells()
     cnt = np.array([s[0] for s in sh])
     l = np.array([s[1] for s in sh])
@@ -99,8 +101,10 @@ def breit_quartets(basis, ilev=3, racah1=True):
         keep &= mcnt == 1
     keep &= (mcnt != 1) | (((l[a] + l[b]) & 1) == ((l[c] + l[d]) & 1))
     pab, pcd = a * ns + b, c * ns + d
+    pdc, pba = d * ns + c, b * ns + a
     q = np.stack([a, b, c, d], 1).astype(np.int32)
-    return q[keep & (pab >= pcd)], q[keep]
+    half = (pab > pdc) | ((pab == pdc) & (pcd >= pba))
+    return q[keep & (pab >= pcd)], q[keep & half]
 
 
 def breit_flops(basis, quart, gaunt=False):

@@ -1123,7 +1123,8 @@ struct BArgs {
   const double2 *D;
   double *BX;
   int ns, ldd, ldf, nskp, isym, racah1, gaunt;
-  int dual;  // also digest (cd|ab) = (ab|cd): K(c,b) += (ab|cd) D(a,d)
+  int dual;  // also digest (cd|ab) = (ab|cd): K(c,b) += (ab|cd) D(a,d); 2: the
+             // (LS|SL) list is also halved by (dc|ba) = (ab|cd)* (weights)
   double *bound;  // non-null: write max |(ab|cd)| per quartet instead of digesting
 };
 
@@ -1443,11 +1444,14 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
       __syncthreads();
       continue;
     }
-    // flush shared accumulators
+    // flush shared accumulators; in a halved (LS|SL) list a quartet equal
+    // to its (dc|ba) image counts 1/2 (the completion adds it again)
+    const double wq = (q.dual == 2 && t2 == 1 && Q4.x == Q4.w && Q4.y == Q4.z) ? 0.5 : 1.0;
     for (int w = threadIdx.x; w < 2 * nla * 2 * nld; w += blockDim.x) {
       int a = w / (2 * nld), d = w % (2 * nld);
       double2 v = Kl[a * MAXSP + d];
       if (v.x == 0.0 && v.y == 0.0) continue;
+      v.x *= wq; v.y *= wq;
       int fa = A.fock[a >> 1][a & 1] + oa, fdd = Dd.fock[d >> 1][d & 1] + od;
       double *dst = q.BX + 2 * ((size_t)fa + (size_t)q.ldf * fdd);
       atomicAdd(dst, v.x);
@@ -1458,6 +1462,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
         int cc = w / (2 * nlb), b = w % (2 * nlb);
         double2 v = K2[cc * MAXSP + b];
         if (v.x == 0.0 && v.y == 0.0) continue;
+        v.x *= wq; v.y *= wq;
         int fcc = C.fock[cc >> 1][cc & 1] + oc, fbb = B.fock[b >> 1][b & 1] + ob;
         double *dst = q.BX + 2 * ((size_t)fcc + (size_t)q.ldf * fbb);
         atomicAdd(dst, v.x);
@@ -2214,6 +2219,13 @@ size_t quartet_smem() {
 // ---------------------------------------------------------------------------
 // Context and C ABI
 // ---------------------------------------------------------------------------
+// A run of consecutive entries of a quartet list and the kernel that
+// digests it under BG_PREC_AUTO (df: the split-precision kernel).
+struct Run {
+  long long start, count;
+  int df;
+};
+
 struct bg_ctx {
   int ncnt = 0, ndim = 0, nskp = 0, hmlt = 0, isym = 0, racah1 = 1;
   std::vector<double> cxyz;  // BXYZ of the centres
@@ -2240,6 +2252,11 @@ struct bg_ctx {
   double screen = 0.0;          // Schwarz threshold on Q_ab*Q_cd, 0 = off
   std::vector<double> qbound;   // [pair*2+comp] sqrt max |(ab|ab)|
   double2 *d_D = nullptr, *d_GD = nullptr, *d_GX = nullptr;
+  // BG_PREC_AUTO: angular-class segments of the cached lists and the tuned
+  // kernel of each run of them (see tune_runs)
+  std::vector<long long> seg[4];
+  std::vector<Run> runs[4];
+  bool tuned = false;
   // split-precision copies
   float4 *d_Edf = nullptr, *d_Ddf = nullptr;
   int prec = BG_PREC_FP64;
@@ -2282,6 +2299,9 @@ struct bg_batch {
   int *d_quart[4] = {nullptr, nullptr, nullptr, nullptr};
   long long nquart[4] = {0, 0, 0, 0};
   int quart_ilev = -1;
+  std::vector<long long> seg[4];  // BG_PREC_AUTO, as in bg_ctx
+  std::vector<Run> runs[4];
+  bool tuned = false;
   long long launches = 0;
   std::string err;
   bool bad = false;
@@ -2493,15 +2513,29 @@ float4 *noalloc_scratch(bg_ctx *c, int *rc) {
   return addr[dev];
 }
 
+int launch_quartets_fp64(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
+                         const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
+                         cudaStream_t st, int sym, double *bound);
+
+// FP64 or split-precision launch as the context's precision says
+// (BG_PREC_AUTO takes the split kernel here: explicit and streamed lists
+// are not tuned per class); bound mode is always FP64.
 int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                     const double2 *d_D, int ldd, double *d_GD, double *d_GX,
                     int ldf, cudaStream_t st, int sym = 0, double *bound = nullptr) {
   if (nq <= 0) return 0;
-  if (c->prec == BG_PREC_DF32 && !bound) {
+  if (c->prec != BG_PREC_FP64 && !bound) {
     int n = c->ndim;
     if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
     return launch_quartets_df(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, c->d_Ddf, sym);
   }
+  return launch_quartets_fp64(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, sym, bound);
+}
+
+int launch_quartets_fp64(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
+                         const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
+                         cudaStream_t st, int sym, double *bound) {
+  if (nq <= 0) return 0;
   static bool attr = false;
   size_t smem = quartet_smem();
 
@@ -2602,9 +2636,11 @@ int breit_prepare(bg_ctx *c) {
 // m-signs (the Kramers partner of a density is its conjugate up to sign);
 // the SL pair cd has the bound of the LS pair dc ((ab|cd)* = (ba|dc)).
 // t2 = 0: (LS|LS), pairs ab >= cd only, each digested for both orders;
-// t2 = 1: (LS|SL), every ordered pair, digested for both orders, which
-// covers the (SL|LS) class.  The (SL|SL) class only feeds the SL block,
-// which BRTFAST overwrites by conjugation of the LS block.
+// t2 = 1: (LS|SL), digested for both orders, which covers the (SL|LS)
+// class; of a quartet and its image (dc|ba) = (ab|cd)* only one is listed,
+// the LL and SS blocks it feeds being completed as Hermitian matrices
+// afterwards (Hermitian density).  The (SL|SL) class only feeds the SL
+// block, which BRTFAST overwrites by conjugation of the LS block.
 std::vector<int> build_breit_quartets(const bg_ctx *c, int t2, int ilev) {
   std::vector<int> out;
   bool scr = c->screen > 0.0 && !c->bqbound.empty();
@@ -2620,6 +2656,11 @@ std::vector<int> build_breit_quartets(const bg_ctx *c, int t2, int ilev) {
       for (int d : byl[ld]) {
         long long pab = (long long)a * c->ns + b, pcd = (long long)cc * c->ns + d;
         if (t2 == 0 && pab < pcd) continue;
+        if (t2 == 1) {
+          // (dc|ba) = (ab|cd)* within (LS|SL): keep the larger of the two
+          long long pdc = (long long)d * c->ns + cc, pba = (long long)b * c->ns + a;
+          if (pab < pdc || (pab == pdc && pcd < pba)) continue;
+        }
         int s4[4] = {c->shells[a].cnt, c->shells[b].cnt, c->shells[cc].cnt, c->shells[d].cnt};
         std::sort(s4, s4 + 4);
         int mcnt = 1;
@@ -2688,6 +2729,97 @@ int compute_breit_bounds(bg_ctx *c, cudaStream_t st) {
 // time, overlapping the kernels of the previous chunk).
 constexpr long long CACHE_Q = 1LL << 25;  // 32M quartets, 512 MB (default)
 constexpr long long CHUNK_Q = 1LL << 23;  // 8M quartets, 128 MB per buffer (default)
+
+// Autotuner of BG_PREC_AUTO.  A list sorted by angular class has segments
+// seg[i]..seg[i+1] of one class (l_a,l_b,l_c,l_d) each.  For every segment
+// of at least TUNE_MIN quartets the FP64 and the split-precision kernels
+// are timed on its first min(size, TUNE_SAMPLE) quartets (CUDA events on
+// `st`, the second of two runs, into scratch outputs) and the faster is
+// kept; smaller segments take the FP64 kernel (their cost is launch- and
+// latency-bound either way).  Neighbouring segments with the same choice
+// merge into one run, so a build issues one launch per run.
+// launch(df, start, count) issues one kernel over list entries
+// [start, start + count).
+constexpr long long TUNE_MIN = 2048, TUNE_SAMPLE = 16384;
+
+template <class Launch>
+int tune_runs(const std::vector<long long> &seg, cudaStream_t st, Launch &&launch,
+              std::vector<Run> &runs) {
+  runs.clear();
+  if (seg.size() < 2) return 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -1;
+  int rc = 0;
+  for (size_t i = 0; i + 1 < seg.size() && !rc; ++i) {
+    long long n = seg[i + 1] - seg[i];
+    if (n <= 0) continue;
+    int df = 0;
+    if (n >= TUNE_MIN) {
+      long long m = std::min(n, TUNE_SAMPLE);
+      float t[2] = {0.f, 0.f};
+      for (int k = 0; k < 2 && !rc; ++k)
+        for (int rep = 0; rep < 2 && !rc; ++rep) {
+          cudaEventRecord(e0, st);
+          rc = launch(k, seg[i], m);
+          cudaEventRecord(e1, st);
+          if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = -1;
+          if (!rc) cudaEventElapsedTime(&t[k], e0, e1);
+        }
+      df = t[1] < t[0];
+    }
+    if (!runs.empty() && runs.back().df == df && runs.back().start + runs.back().count == seg[i])
+      runs.back().count += n;
+    else
+      runs.push_back({seg[i], n, df});
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+// Angular-class segment boundaries of a quartet list (entries grouped by
+// class): start of every class, then the list size.
+std::vector<long long> class_segments(const std::vector<Shell> &sh, const std::vector<int> &q,
+                                      int sbase = 0) {
+  std::vector<long long> seg;
+  long long n = (long long)q.size() / 4;
+  int last = -1;
+  for (long long i = 0; i < n; ++i) {
+    const int *e = &q[4 * i];
+    int key = ((sh[e[0] - sbase].l * 4 + sh[e[1] - sbase].l) * 4 + sh[e[2] - sbase].l) * 4 +
+              sh[e[3] - sbase].l;
+    if (key != last) { seg.push_back(i); last = key; }
+  }
+  seg.push_back(n);
+  return seg;
+}
+
+// Tunes the cached lists of a context (first BG_PREC_AUTO build after the
+// lists were made), with scratch outputs of NDIM^2.
+int tune_ctx(bg_ctx *c, const double2 *d_D, int ldd, cudaStream_t st) {
+  int n = c->ndim;
+  double *gd = nullptr, *gx = nullptr;
+  CK(c, cudaMalloc(&gd, sizeof(double2) * (size_t)n * n));
+  CK(c, cudaMalloc(&gx, sizeof(double2) * (size_t)n * n));
+  if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
+  int rc = 0;
+  for (int t1 = 0; t1 < c->ncomp && !rc; ++t1)
+    for (int t2 = 0; t2 < c->ncomp && !rc; ++t2) {
+      int k = 2 * t1 + t2;
+      const int *q = c->d_quart[k];
+      rc = tune_runs(c->seg[k], st, [&](int df, long long start, long long m) {
+        return df ? launch_quartets_df(c, q + 4 * start, m, t1, t2, d_D, ldd, gd, gx, n, st,
+                                       c->d_Ddf, 2)
+                  : launch_quartets_fp64(c, q + 4 * start, m, t1, t2, d_D, ldd, gd, gx, n, st,
+                                         2, nullptr);
+      }, c->runs[k]);
+    }
+  cudaFree(gd);
+  cudaFree(gx);
+  if (rc) return rc > 0 ? rc : cuda_fail(c, cudaGetLastError(), "autotuning");
+  c->tuned = true;
+  return 0;
+}
 
 int stream_class(bg_ctx *c, int t1, int t2, int ilev, const double2 *d_D, int ldd, double *d_GD,
                  double *d_GX, int ldf, cudaStream_t st) {
@@ -2770,29 +2902,35 @@ int batch_lists(bg_batch *b, int ilev) {
       for (auto &v : bucket) tot += v.size();
       int k = 2 * t1 + t2;
       b->nquart[k] = (long long)tot / 4;
+      b->seg[k].clear();
+      b->runs[k].clear();
       if (!tot) continue;
       BK(b, cudaMalloc(&b->d_quart[k], sizeof(int) * tot));
       size_t pos = 0;
       for (auto &v : bucket) {
         if (v.empty()) continue;
+        b->seg[k].push_back((long long)pos / 4);  // one angular class per bucket
         BK(b, cudaMemcpy(b->d_quart[k] + pos, v.data(), sizeof(int) * v.size(),
                          cudaMemcpyHostToDevice));
         pos += v.size();
         std::vector<int>().swap(v);
       }
+      b->seg[k].push_back(b->nquart[k]);
     }
   b->quart_ilev = ilev;
+  b->tuned = false;
   return 0;
 }
 
-// One launch of the FP64 or split-precision quartet kernel over a batch's
-// list of one component class, both orders of each listed quartet digested.
-int batch_launch(bg_batch *b, int t1, int t2, const double2 *d_D, double *d_GD, double *d_GX,
-                 cudaStream_t st) {
+// One launch of the FP64 (df = 0) or split-precision (df = 1) quartet
+// kernel over entries [start, start + nq) of a batch's list of one
+// component class, both orders of each listed quartet digested.
+int batch_launch(bg_batch *b, int t1, int t2, int df, long long start, long long nq,
+                 const double2 *d_D, double *d_GD, double *d_GX, cudaStream_t st) {
   int k = 2 * t1 + t2;
-  long long nq = b->nquart[k];
   if (nq <= 0) return 0;
-  if (b->prec == BG_PREC_DF32) {
+  const int4 *quart = (const int4 *)b->d_quart[k] + start;
+  if (df) {
     static bool attr_df = false;  // set once: no attribute call inside a graph capture
     if (!attr_df) {
       BK(b, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2804,8 +2942,7 @@ int batch_launch(bg_batch *b, int t1, int t2, const double2 *d_D, double *d_GD, 
     a.GD = d_GD; a.GX = d_GX; a.ns = 0; a.ldd = 0; a.ldf = 0; a.nskp = 0;
     a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.inst = b->d_inst;
     long long grid = std::min<long long>(nq, 152LL * 128);
-    k_quartet_df<<<(unsigned)grid, DFTHREADS, quartet_smem_df(1), st>>>(
-        a, (const int4 *)b->d_quart[k], nq, t1, t2);
+    k_quartet_df<<<(unsigned)grid, DFTHREADS, quartet_smem_df(1), st>>>(a, quart, nq, t1, t2);
   } else {
     static bool attr = false;
     if (!attr) {
@@ -2818,8 +2955,7 @@ int batch_launch(bg_batch *b, int t1, int t2, const double2 *d_D, double *d_GD, 
     a.GD = d_GD; a.GX = d_GX; a.ns = 0; a.ldd = 0; a.ldf = 0; a.nskp = 0;
     a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.bound = nullptr; a.inst = b->d_inst;
     long long grid = std::min<long long>(nq, 152LL * 64);
-    k_quartet<<<(unsigned)grid, QTHREADS, quartet_smem(), st>>>(
-        a, (const int4 *)b->d_quart[k], nq, t1, t2);
+    k_quartet<<<(unsigned)grid, QTHREADS, quartet_smem(), st>>>(a, quart, nq, t1, t2);
   }
   BK(b, cudaGetLastError());
   b->launches++;
@@ -3010,7 +3146,8 @@ int bertha_gpu_set_screening(bg_ctx *c, double threshold) {
 
 int bertha_gpu_set_precision(bg_ctx *c, int prec) {
   if (!c) return BG_ERR_ARG;
-  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32) return BG_ERR_ARG;
+  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32 && prec != BG_PREC_AUTO) return BG_ERR_ARG;
+  if (prec != c->prec) c->tuned = false;
   c->prec = prec;
   return BG_OK;
 }
@@ -3049,6 +3186,34 @@ int bertha_gpu_layout(const bg_ctx *c, int *lrge) {
 }
 
 long long bertha_gpu_launches(const bg_ctx *c) { return c ? c->launches : 0; }
+
+namespace {
+void auto_stats(const std::vector<Run> (&runs)[4], long long *nf, long long *nd, int *nr) {
+  long long f = 0, d = 0;
+  int r = 0;
+  for (int k = 0; k < 4; ++k)
+    for (const Run &x : runs[k]) {
+      (x.df ? d : f) += x.count;
+      ++r;
+    }
+  if (nf) *nf = f;
+  if (nd) *nd = d;
+  if (nr) *nr = r;
+}
+}  // namespace
+
+int bertha_gpu_auto_stats(const bg_ctx *c, long long *nq_fp64, long long *nq_df32, int *nruns) {
+  if (!c) return BG_ERR_ARG;
+  auto_stats(c->runs, nq_fp64, nq_df32, nruns);
+  return BG_OK;
+}
+
+int bertha_gpu_batch_auto_stats(const bg_batch *b, long long *nq_fp64, long long *nq_df32,
+                                int *nruns) {
+  if (!b) return BG_ERR_ARG;
+  auto_stats(b->runs, nq_fp64, nq_df32, nruns);
+  return BG_OK;
+}
 
 const char *bertha_gpu_last_error(const bg_ctx *c) {
   return c ? c->err.c_str() : g_init_err.c_str();
@@ -3119,8 +3284,11 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
           if (++total > (c->cache_q > 0 ? c->cache_q : CACHE_Q)) c->stream_lists = true;
         });
       }
+    c->tuned = false;
     if (!c->stream_lists)
       for (int k = 0; k < 4; ++k) {
+        c->seg[k] = class_segments(c->shells, q[k]);
+        c->runs[k].clear();
         c->nquart[k] = (long long)q[k].size() / 4;
         if (!q[k].empty()) {
           CK(c, cudaMalloc(&c->d_quart[k], sizeof(int) * q[k].size()));
@@ -3130,11 +3298,25 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
       }
     c->quart_ilev = ilev;
   }
+  bool autoprec = c->prec == BG_PREC_AUTO && !c->stream_lists;
+  if (autoprec && !c->tuned) {
+    int rc = tune_ctx(c, (const double2 *)d_dent, ldd, st);
+    if (rc) return rc;
+  }
   for (int t1 = c->ncomp - 1; t1 >= 0; --t1)
     for (int t2 = c->ncomp - 1; t2 >= 0; --t2) {
-      int k = 2 * t1 + t2, rc;
+      int k = 2 * t1 + t2, rc = 0;
       if (c->stream_lists)
         rc = stream_class(c, t1, t2, ilev, (const double2 *)d_dent, ldd, d_gdir, d_gxch, ldf, st);
+      else if (autoprec)
+        for (const Run &r : c->runs[k]) {
+          const int *q = c->d_quart[k] + 4 * r.start;
+          rc = r.df ? launch_quartets_df(c, q, r.count, t1, t2, (const double2 *)d_dent, ldd,
+                                         d_gdir, d_gxch, ldf, st, c->d_Ddf, 2)
+                    : launch_quartets_fp64(c, q, r.count, t1, t2, (const double2 *)d_dent, ldd,
+                                           d_gdir, d_gxch, ldf, st, 2, nullptr);
+          if (rc) break;
+        }
       else
         rc = launch_quartets(c, c->d_quart[k], c->nquart[k], t1, t2, (const double2 *)d_dent,
                              ldd, d_gdir, d_gxch, ldf, st, 2);
@@ -3210,10 +3392,16 @@ int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
   }
   for (int k = 0; k < 2; ++k) {
     rc = launch_breit(c, c->d_bquart[k], c->nbquart[k], 0, k, (const double2 *)d_dent, ldd,
-                      d_bxch, ldf, st, 1);
+                      d_bxch, ldf, st, 2);
     if (rc) return rc;
   }
   int n = c->nskp;
+  // LL and SS blocks: add the (dc|ba) images of the halved (LS|SL) list
+  k_herm_complete<<<dim3(1, 256), 256, 0, st>>>((double2 *)d_bxch, n, ldf, nullptr, nullptr, 1);
+  k_herm_complete<<<dim3(1, 256), 256, 0, st>>>((double2 *)d_bxch + n + (size_t)ldf * n, n, ldf,
+                                                nullptr, nullptr, 1);
+  CK(c, cudaGetLastError());
+  c->launches += 2;
   k_conj_block<<<1024, 256, 0, st>>>((double2 *)d_bxch, n, ldf);
   CK(c, cudaGetLastError());
   c->launches++;
@@ -3441,7 +3629,8 @@ int bertha_gpu_batch_create(bg_batch **out, int n, bg_ctx *const *ctxs,
 
 int bertha_gpu_batch_set_precision(bg_batch *b, int prec) {
   if (!b) return BG_ERR_ARG;
-  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32) return BG_ERR_ARG;
+  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32 && prec != BG_PREC_AUTO) return BG_ERR_ARG;
+  if (prec != b->prec) b->tuned = false;
   b->prec = prec;
   return BG_OK;
 }
@@ -3463,15 +3652,43 @@ int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
     int rc = batch_lists(b, ilev);
     if (rc) return rc;
   }
-  if (b->prec == BG_PREC_DF32) {
+  if (b->prec != BG_PREC_FP64) {
     if (!b->d_Ddf) BK(b, cudaMalloc(&b->d_Ddf, sizeof(float4) * std::max<long long>(b->span, 1)));
     k_dconv1<<<1024, 256, 0, st>>>((const double2 *)d_dent, b->span, b->d_Ddf);
     BK(b, cudaGetLastError());
     b->launches++;
   }
+  const double2 *D = (const double2 *)d_dent;
+  if (b->prec == BG_PREC_AUTO && !b->tuned) {
+    // kernel choice per angular class, timed into scratch outputs
+    double *gd = nullptr, *gx = nullptr;
+    size_t bytes = sizeof(double2) * std::max<long long>(b->span, 1);
+    BK(b, cudaMalloc(&gd, bytes));
+    BK(b, cudaMalloc(&gx, bytes));
+    int rc = 0;
+    for (int t1 = 0; t1 < b->ncomp && !rc; ++t1)
+      for (int t2 = 0; t2 < b->ncomp && !rc; ++t2) {
+        int k = 2 * t1 + t2;
+        rc = tune_runs(b->seg[k], st, [&](int df, long long start, long long m) {
+          return batch_launch(b, t1, t2, df, start, m, D, gd, gx, st);
+        }, b->runs[k]);
+      }
+    cudaFree(gd);
+    cudaFree(gx);
+    if (rc) return rc > 0 ? rc : batch_fail(b, cudaGetLastError(), "autotuning");
+    b->tuned = true;
+  }
   for (int t1 = b->ncomp - 1; t1 >= 0; --t1)
     for (int t2 = b->ncomp - 1; t2 >= 0; --t2) {
-      int rc = batch_launch(b, t1, t2, (const double2 *)d_dent, d_gdir, d_gxch, st);
+      int k = 2 * t1 + t2, rc = 0;
+      if (b->prec == BG_PREC_AUTO)
+        for (const Run &r : b->runs[k]) {
+          rc = batch_launch(b, t1, t2, r.df, r.start, r.count, D, d_gdir, d_gxch, st);
+          if (rc) break;
+        }
+      else
+        rc = batch_launch(b, t1, t2, b->prec == BG_PREC_DF32, 0, b->nquart[k], D, d_gdir,
+                          d_gxch, st);
       if (rc) return rc;
     }
   k_herm_complete<<<dim3(gx, 16), 256, 0, st>>>((double2 *)d_gdir, 0, 0, b->d_inst, b->d_ndim,

@@ -52,6 +52,8 @@ extern "C" {
 #define BG_PREC_FP64 0 /* all FP64: the drop-in path */
 #define BG_PREC_DF32 1 /* split precision: FP32 double-float contractions and
                           digestion products, FP64 Boys/R and J/K sums */
+#define BG_PREC_AUTO 2 /* per angular class the faster of the two kernels,
+                          chosen by timing both on the first build */
 
 /* compiled limits */
 #define BG_MAX_L 3 /* highest orbital angular momentum of a basis shell */
@@ -77,6 +79,17 @@ int bertha_gpu_init(bg_ctx **ctx, int ncnt, const double *bxyz,
  * (about 48 significant bits) on the FP32 pipes.  No counterpart in the
  * reference, which is FP64 throughout. */
 int bertha_gpu_set_precision(bg_ctx *ctx, int prec);
+
+/* BG_PREC_AUTO is the autotuned mixed mode: the first build after the
+ * quartet lists are made times the FP64 and the split-precision kernels on
+ * a sample of every angular class (l_a,l_b,l_c,l_d) of every component
+ * class (classes under 2048 quartets take FP64) and later builds launch the
+ * faster kernel per run of classes.  Its results carry at most the split
+ * path's error.  Streamed lists and bertha_gpu_quartets take the split
+ * kernel.  After a build, the quartets each kernel digests and the number
+ * of runs (launches per build): */
+int bertha_gpu_auto_stats(const bg_ctx *ctx, long long *nq_fp64, long long *nq_df32,
+                          int *nruns);
 
 /* Schwarz screening of the Fock build (SCHWARZ/CLMDIAG, bertha-scf.f:37889,
  * :38126; off by default there, SCHWRZ=.FALSE. :5257).  With threshold > 0,
@@ -128,7 +141,9 @@ int bertha_gpu_clmfast_device(bg_ctx *ctx, const double *d_dent, int ldd,
  * conjugate transpose of the LS block, as BRTFAST completes it.  Needs a
  * four-component Hamiltonian (BG_ERR_ARG for NORL and BARE); the reference
  * calls it for DHFB and DHFQ.  The first call generates the sigma-coupled
- * LS/SL E-coefficients (EILS/EISL of EQSAVE). */
+ * LS/SL E-coefficients (EILS/EISL of EQSAVE).  The (LS|SL) quartets that
+ * feed the LL and SS blocks are halved by (dc|ba) = (ab|cd)* and those
+ * blocks completed as Hermitian matrices, which assumes a Hermitian DENT. */
 int bertha_gpu_brtfast(bg_ctx *ctx, const double *dent, int ldd, int ilev,
                        double *bxch, int ldf);
 
@@ -201,8 +216,14 @@ typedef struct bg_batch bg_batch;
 int bertha_gpu_batch_create(bg_batch **b, int n, bg_ctx *const *ctxs,
                             const long long *moff, const int *ld);
 
-/* Contraction precision of the batch's later builds (BG_PREC_*). */
+/* Contraction precision of the batch's later builds (BG_PREC_*; with
+ * BG_PREC_AUTO the batch's merged lists are tuned per angular class on the
+ * first build, as for a context). */
 int bertha_gpu_batch_set_precision(bg_batch *b, int prec);
+
+/* bertha_gpu_auto_stats of a batch. */
+int bertha_gpu_batch_auto_stats(const bg_batch *b, long long *nq_fp64, long long *nq_df32,
+                                int *nruns);
 
 /* CLMFAST of every instance at stage ilev on device arrays in the batch's
  * placement: d_dent holds all densities; d_gdir, d_gxch get all GDIR and
