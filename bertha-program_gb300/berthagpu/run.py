@@ -34,7 +34,11 @@ def main(argv=None):
     g.add_argument("--deck")
     g.add_argument("--atoms", type=int, help="batch of N seeded closed-shell atoms")
     p.add_argument("--zmax", type=int, default=86, help="largest Z drawn for --atoms")
-    p.add_argument("--scf", action="store_true", help="--atoms: run the batched SCF too")
+    p.add_argument("--scf", action="store_true",
+                   help="run the closed-shell DHF SCF (with --atoms: the batched SCF too)")
+    p.add_argument("--nocc", type=int, default=0, help="--scf: occupied spinors (0: sum of Z)")
+    p.add_argument("--no-breit", action="store_true", help="--scf: Dirac-Coulomb only")
+    p.add_argument("--etol", type=float, default=1e-9, help="--scf: |dE| convergence, Eh")
     p.add_argument("--build", choices=["coulomb", "breit", "both"], default="coulomb")
     p.add_argument("--precision", choices=["fp64", "df32", "auto"], default="fp64")
     p.add_argument("--ilev", type=int, default=3)
@@ -50,6 +54,9 @@ def main(argv=None):
     b = CASES[a.case]() if a.case else deck.read_deck(a.deck)
     if a.build != "coulomb" and b.hmlt < deck.HMLT["DHFR"]:
         b = dataclasses_replace(b, deck.HMLT["DHFB"])
+    if a.scf:
+        print(json.dumps(scf_main(a, b)), flush=True)
+        return
     dent = deck.density(b, seed=a.seed, real=b.isym != 0)
     out = {"case": a.case or a.deck, "ndim": b.ndim, "shells": len(b.shells()),
            "isym": int(b.isym), "build": a.build, "precision": a.precision,
@@ -80,6 +87,24 @@ def main(argv=None):
         out["energy_bx_eh"] = float(0.5 * np.sum(dent * bx).real)
     fb.close()
     print(json.dumps(out), flush=True)
+
+
+def scf_main(a, b):
+    """Closed-shell DHF SCF of one molecule on the GPU (every step on the
+    device), FP64 or mixed precision as --precision says."""
+    from .scf import DHFSCF
+    nocc = a.nocc or int(round(sum(b.znuc)))
+    s = DHFSCF(b, nocc, precision=a.precision, screen=a.screen or 1e-12,
+               breit=False if a.no_breit else None, racah1=False)
+    r = s.run(etol=a.etol, max_iter=80)
+    s.close()
+    hist = r.pop("history")
+    r["orbital_energies"] = r["orbital_energies"][-4:]
+    r.update({"case": a.case or a.deck, "ndim": b.ndim, "nocc": nocc,
+              "precision": a.precision, "breit": not a.no_breit and b.hmlt >= deck.HMLT["DHFB"],
+              "screen": a.screen or 1e-12, "iter_s": [h["s"] for h in hist],
+              "energies": [h["energy"] for h in hist]})
+    return r
 
 
 def atoms_main(a):

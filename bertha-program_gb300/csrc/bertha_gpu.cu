@@ -2727,7 +2727,7 @@ int compute_breit_bounds(bg_ctx *c, cudaStream_t st) {
 // Quartets kept as cached device lists per context at most; above this the
 // lists are streamed (regenerated on the host every build, CHUNK_Q at a
 // time, overlapping the kernels of the previous chunk).
-constexpr long long CACHE_Q = 1LL << 25;  // 32M quartets, 512 MB (default)
+constexpr long long CACHE_Q = 1LL << 28;  // 268M quartets, 4.3 GB (default)
 constexpr long long CHUNK_Q = 1LL << 23;  // 8M quartets, 128 MB per buffer (default)
 
 // Autotuner of BG_PREC_AUTO.  A list sorted by angular class has segments

@@ -98,7 +98,7 @@ int bertha_gpu_auto_stats(const bg_ctx *ctx, long long *nq_fp64, long long *nq_d
 int bertha_gpu_set_screening(bg_ctx *ctx, double threshold);
 
 /* Quartet-list memory of the Coulomb build: a context keeps its lists on
- * the device while they hold at most cache_quartets quartets (0: 2^25);
+ * the device while they hold at most cache_quartets quartets (0: 2^28);
  * larger lists are regenerated on the host every build and streamed
  * through pinned buffers of chunk_quartets quartets (0: 2^23), generation
  * overlapping the kernels of the previous chunk.  Cached lists make a build
