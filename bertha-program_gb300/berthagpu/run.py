@@ -39,6 +39,11 @@ def main(argv=None):
     p.add_argument("--nocc", type=int, default=0, help="--scf: occupied spinors (0: sum of Z)")
     p.add_argument("--no-breit", action="store_true", help="--scf: Dirac-Coulomb only")
     p.add_argument("--etol", type=float, default=1e-9, help="--scf: |dE| convergence, Eh")
+    p.add_argument("--shift", type=float, default=0.5, help="--scf: level shift, Eh")
+    p.add_argument("--mom", type=int, default=0,
+                   help="--scf: maximum-overlap occupation from this iteration (0: aufbau)")
+    p.add_argument("--ndiis", type=int, default=8, help="--scf: DIIS subspace size")
+    p.add_argument("--max-iter", type=int, default=80, help="--scf: iteration limit")
     p.add_argument("--build", choices=["coulomb", "breit", "both"], default="coulomb")
     p.add_argument("--precision", choices=["fp64", "df32", "auto"], default="fp64")
     p.add_argument("--ilev", type=int, default=3)
@@ -96,13 +101,14 @@ def scf_main(a, b):
     nocc = a.nocc or int(round(sum(b.znuc)))
     s = DHFSCF(b, nocc, precision=a.precision, screen=a.screen or 1e-12,
                breit=False if a.no_breit else None, racah1=False)
-    r = s.run(etol=a.etol, max_iter=80)
+    r = s.run(etol=a.etol, max_iter=a.max_iter, ndiis=a.ndiis, shift=a.shift, mom=a.mom)
     s.close()
     hist = r.pop("history")
     r["orbital_energies"] = r["orbital_energies"][-4:]
     r.update({"case": a.case or a.deck, "ndim": b.ndim, "nocc": nocc,
               "precision": a.precision, "breit": not a.no_breit and b.hmlt >= deck.HMLT["DHFB"],
-              "screen": a.screen or 1e-12, "iter_s": [h["s"] for h in hist],
+              "screen": a.screen or 1e-12, "shift": a.shift, "mom": a.mom, "ndiis": a.ndiis,
+              "iter_s": [h["s"] for h in hist],
               "energies": [h["energy"] for h in hist]})
     return r
 

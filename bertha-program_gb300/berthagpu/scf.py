@@ -99,10 +99,14 @@ class DHFSCF:
         self.backend = backend or GPUBackend(basis, precision, screen, breit, racah1, torch)
         self.n = self.backend.n
 
-    def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, verbose=False):
+    def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, mom=0, verbose=False):
         """Iterate to |dE| < etol.  shift: LEVSHFT's virtual-space level shift
         SHLV in Eh (the H2O deck's stage-3 value 0.5), applied from the second
-        iteration on; it moves the path, not the converged solution."""
+        iteration on; it moves the path, not the converged solution.
+        mom: from this iteration on (0: never) the occupied spinors are the
+        positive-energy eigenvectors that overlap most with the previous
+        occupied space (maximum overlap) instead of the lowest ones, which
+        stops occupations from flipping between near-degenerate levels."""
         t = self.torch
         be = self.backend
         dev = be.device
@@ -117,11 +121,27 @@ class DHFSCF:
         be.sync()
         t_one = time.perf_counter() - t0
 
-        def solve(F):
+        state = {"occ": None}
+
+        def solve(F, use_mom=False):
             e, Cp = t.linalg.eigh(X.conj().T @ F @ X)
             C = X @ Cp
             nneg = int((e < -CLIGHT * CLIGHT).sum().item())
-            occ = C[:, nneg:nneg + self.nocc]
+            if use_mom and state["occ"] is not None:
+                # projections of the positive-energy eigenvectors on the
+                # previous occupied space, S-metric
+                P = state["occ"].conj().T @ (S @ C[:, nneg:])
+                w = (P.abs() ** 2).sum(0)
+                idx = t.sort(t.topk(w, self.nocc).indices).values + nneg
+                occ = C[:, idx]
+            else:
+                idx = t.arange(nneg, nneg + self.nocc, device=C.device)
+                occ = C[:, nneg:nneg + self.nocc]
+            state["occ"] = occ
+            vmask = t.ones(C.shape[1], dtype=t.bool, device=C.device)
+            vmask[:nneg] = False
+            vmask[idx] = False
+            state["vir"] = C[:, vmask]
             # DENSTY: D_ij = sum_occ conj(C_i) C_j
             return e, nneg, occ.conj() @ occ.T, C
 
@@ -141,7 +161,7 @@ class DHFSCF:
             if shift and it > 1:
                 # LEVSHFT (:3641): F += SHLV sum_vir (S c_v)(S c_v)^+ over the
                 # positive-energy virtuals of the last diagonalisation
-                A = S @ C[:, nneg + self.nocc:]
+                A = S @ state["vir"]
                 F = F + shift * (A @ A.conj().T)
             # DIIS on the commutator F P S - S P F, P = D^T
             P = D.T
@@ -165,7 +185,7 @@ class DHFSCF:
                 rhs[m] = -1.0
                 w = t.linalg.solve(B, rhs)
                 F = sum(w[i] * hist_F[i] for i in range(m))
-            eps, nneg, D, C = solve(F)
+            eps, nneg, D, C = solve(F, use_mom=bool(mom) and it >= mom)
             be.sync()
             t_lin += time.perf_counter() - tf
             de = None if last is None else energy - last

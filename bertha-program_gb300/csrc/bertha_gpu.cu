@@ -43,8 +43,9 @@ constexpr int MAXDEGE = 2 * MAXLB + 2;    // E degree (SS)
 constexpr int MAXLAM = 2 * MAXDEGE;       // R order (SS|SS)
 constexpr int NTE = ntuv(MAXDEGE);        // 165
 constexpr int NTR = ntuv(MAXLAM);         // 969
-constexpr int CHUNK = 8;                  // ab labels per first-contraction pass
-constexpr int QTHREADS = 256;
+constexpr int CHUNK = 5;                  // ab labels per first-contraction pass (at N = 165)
+constexpr int QTHREADS = 256;             // k_breit
+constexpr int QT64 = 128;                 // k_quartet: four 128-thread CTAs per SM
 
 __constant__ signed char c_t[NTR], c_u[NTR], c_v[NTR];
 
@@ -492,7 +493,7 @@ __host__ __device__ inline long long contraction_cost(int pab, int nab, int pcd,
 // the first contraction is the "left" pair; it is ab (the reference's order,
 // ERIFAST :12676) unless the other order needs fewer multiply-adds, in which
 // case (cd|ab) = (ab|cd) is evaluated and the m-sign index is remapped.
-__global__ void __launch_bounds__(QTHREADS, 2)
+__global__ void __launch_bounds__(QT64, 4)
 k_quartet(QArgs q, const int4 *quart, long long nq, int t1, int t2) {
   extern __shared__ double smem[];
   double *R = smem;                          // NTR
@@ -2551,7 +2552,7 @@ int launch_quartets_fp64(bg_ctx *c, const int *d_q, long long nq, int t1, int t2
   a.nskp = c->nskp; a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym;
   a.bound = bound;
   long long grid = std::min<long long>(nq, 152LL * 64);
-  k_quartet<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  k_quartet<<<(unsigned)grid, QT64, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
   c->launches++;
   return 0;
@@ -2955,7 +2956,7 @@ int batch_launch(bg_batch *b, int t1, int t2, int df, long long start, long long
     a.GD = d_GD; a.GX = d_GX; a.ns = 0; a.ldd = 0; a.ldf = 0; a.nskp = 0;
     a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.bound = nullptr; a.inst = b->d_inst;
     long long grid = std::min<long long>(nq, 152LL * 64);
-    k_quartet<<<(unsigned)grid, QTHREADS, quartet_smem(), st>>>(a, quart, nq, t1, t2);
+    k_quartet<<<(unsigned)grid, QT64, quartet_smem(), st>>>(a, quart, nq, t1, t2);
   }
   BK(b, cudaGetLastError());
   b->launches++;

@@ -161,10 +161,11 @@ def test_schwarz_screening():
     fb.close()
 
 
-@pytest.mark.parametrize("prec", ["fp64", "df32"])
+@pytest.mark.parametrize("prec", ["fp64", "df32", "auto"])
 def test_streamed_quartet_lists(prec):
     """Lists above the cache limit are regenerated and streamed in chunks:
-    tiny limits force several chunks per class on a small basis."""
+    tiny limits force several chunks per class on a small basis (the
+    autotuned mode takes the split kernel for streamed lists)."""
     b = _small(lmax=2)
     d = deck.density(b, seed=41)
     fb = berthagpu.FockBuilder(b)
