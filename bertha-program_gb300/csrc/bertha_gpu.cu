@@ -1632,15 +1632,24 @@ __device__ void boys_block(double T, int lam, double *F) {
   }
 }
 
-constexpr int CHDF = 2;  // left labels per first-contraction pass (df path)
+constexpr int CHDF = 2;  // most left labels per first-contraction pass (df path)
 constexpr int DFTHREADS = 128;  // 4 quartets in flight per SM
-constexpr int NCB = CHDF * MAXLAB * MAXLAB * 16;  // contribution buffer (float4), with sym
+
+// Left labels per pass: 2 for explicit lists; 1 when both quartet orders
+// are digested (sym), whose contribution buffer holds twice the targets, so
+// that both modes stay under 48 KB of shared memory and four CTAs per SM.
+__host__ __device__ constexpr int df_chunk(int sym) { return sym ? 1 : CHDF; }
+
+// contribution buffer (float4): chunk labels x MAXLAB^2 label pairs x targets
+__host__ __device__ constexpr int df_ncb(int sym) {
+  return df_chunk(sym) * MAXLAB * MAXLAB * (sym ? 16 : 8);
+}
 
 // doubles at the start of the df kernel's shared memory: R (FP64) or the
 // contribution buffer, whichever is larger (even, so what follows stays
 // 16-byte aligned)
 __host__ __device__ constexpr int df_region0(int sym) {
-  return (sym ? NCB : NCB / 2) * 2 > NTR ? (sym ? NCB : NCB / 2) * 2 : NTR + 1;
+  return df_ncb(sym) * 2 > NTR ? df_ncb(sym) * 2 : NTR + 1;
 }
 
 struct QArgsDF {
@@ -1700,14 +1709,15 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
   // their space; R2, the recursion's second buffer, shares Rf's.
   extern __shared__ double smem[];
   const int r0d = df_region0(q.sym);
+  const int ch = df_chunk(q.sym);              // left labels per pass
   double *R = smem;                            // NTR (FP64)
-  float4 *Cb = (float4 *)smem;                 // CHDF*MAXLAB^2*(8 or 16)
+  float4 *Cb = (float4 *)smem;                 // df_ncb(sym)
   float2 *Rf = (float2 *)(smem + r0d);         // NTR (df), padded to NTR+1 doubles
   double *R2 = (double *)Rf;                   // FP64 recursion buffer (aliases Rf)
   double *F = smem + r0d + NTR + 1;            // MAXLAM+2
-  float4 *EL = (float4 *)(F + MAXLAM + 2);     // CHDF*2*NTE
-  float4 *G = EL + CHDF * 2 * NTE;             // CHDF*2*NTE
-  double2 *Jl = (double2 *)(G + CHDF * 2 * NTE);  // MAXSP*MAXSP
+  float4 *EL = (float4 *)(F + MAXLAM + 2);     // ch*2*NTE
+  float4 *G = EL + ch * 2 * NTE;               // ch*2*NTE
+  double2 *Jl = (double2 *)(G + ch * 2 * NTE);  // MAXSP*MAXSP
   double2 *Kl = Jl + MAXSP * MAXSP;
   double2 *J2 = Kl + MAXSP * MAXSP;            // with sym only
   double2 *K2 = J2 + MAXSP * MAXSP;
@@ -1827,8 +1837,8 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
     int oab = t1 ? nskpm : 0, ocd = t2 ? nskpm : 0;
     int kq0 = sk;
     __syncthreads();
-    for (int c0 = 0; c0 < nlL; c0 += CHDF) {
-      int nch = min(CHDF, nlL - c0);
+    for (int c0 = 0; c0 < nlL; c0 += ch) {
+      int nch = min(ch, nlL - c0);
       // stage the nonzero left E-coefficients (packed, with their Hermite
       // indices) rescaled to this quartet's exponent
       for (int w = threadIdx.x; w < nch * 2 * nL; w += blockDim.x) {
@@ -2208,8 +2218,12 @@ __global__ void k_zero2d(double *a, int n, int ld) {
 
 size_t quartet_smem_df(int sym) {
   return sizeof(double) * (df_region0(sym) + NTR + 1 + MAXLAM + 2) +
-         sizeof(float4) * (2 * CHDF * 2 * NTE) + sizeof(double2) * ((sym ? 4 : 2) * MAXSP * MAXSP);
+         sizeof(float4) * (2 * df_chunk(sym) * 2 * NTE) +
+         sizeof(double2) * ((sym ? 4 : 2) * MAXSP * MAXSP);
 }
+
+// dynamic shared memory attribute of k_quartet_df: the larger mode
+size_t quartet_smem_df_max() { return std::max(quartet_smem_df(0), quartet_smem_df(1)); }
 
 size_t quartet_smem() {
   return sizeof(double) * (2 * NTR + MAXLAM + 2) + sizeof(double2) * (CHUNK * 2 * NTE + 4 * MAXSP * MAXSP);
@@ -2474,7 +2488,7 @@ int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   size_t smem = quartet_smem_df(sym ? 1 : 0);
   if (!attr_df) {
     CK(c, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)quartet_smem_df(1)));
+                               (int)quartet_smem_df_max()));
     attr_df = true;
   }
   int n = c->ndim;
@@ -2935,7 +2949,7 @@ int batch_launch(bg_batch *b, int t1, int t2, int df, long long start, long long
     static bool attr_df = false;  // set once: no attribute call inside a graph capture
     if (!attr_df) {
       BK(b, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)quartet_smem_df(1)));
+                                 (int)quartet_smem_df_max()));
       attr_df = true;
     }
     QArgsDF a;
