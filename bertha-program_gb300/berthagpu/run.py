@@ -44,6 +44,10 @@ def main(argv=None):
                    help="--scf: maximum-overlap occupation from this iteration (0: aufbau)")
     p.add_argument("--ndiis", type=int, default=8, help="--scf: DIIS subspace size")
     p.add_argument("--max-iter", type=int, default=80, help="--scf: iteration limit")
+    p.add_argument("--guess", choices=["bare", "atomic"], default="bare",
+                   help="--scf: bare-nucleus start or superposed atomic densities")
+    p.add_argument("--wfn-in", help="--scf: start from this .wfn file")
+    p.add_argument("--wfn-out", help="--scf: write the final eigenvectors as a .wfn file")
     p.add_argument("--build", choices=["coulomb", "breit", "both"], default="coulomb")
     p.add_argument("--precision", choices=["fp64", "df32", "auto"], default="fp64")
     p.add_argument("--ilev", type=int, default=3)
@@ -101,7 +105,19 @@ def scf_main(a, b):
     nocc = a.nocc or int(round(sum(b.znuc)))
     s = DHFSCF(b, nocc, precision=a.precision, screen=a.screen or 1e-12,
                breit=False if a.no_breit else None, racah1=False)
-    r = s.run(etol=a.etol, max_iter=a.max_iter, ndiis=a.ndiis, shift=a.shift, mom=a.mom)
+    guess = None
+    t0 = time.perf_counter()
+    if a.wfn_in:
+        from . import wfn
+        guess = wfn.read_wfn(a.wfn_in, b.ndim)
+    elif a.guess == "atomic":
+        from .scf import atomic_guess
+        guess = atomic_guess(b)
+    t_guess = time.perf_counter() - t0
+    r = s.run(etol=a.etol, max_iter=a.max_iter, ndiis=a.ndiis, shift=a.shift, mom=a.mom,
+              guess=guess, wfn_out=a.wfn_out)
+    r["guess"] = "wfn" if a.wfn_in else a.guess
+    r["guess_s"] = t_guess
     s.close()
     hist = r.pop("history")
     r["orbital_energies"] = r["orbital_energies"][-4:]

@@ -19,7 +19,7 @@ import time
 
 import numpy as np
 
-from . import deck
+from . import deck, wfn
 from .fock import FockBatch, FockBuilder
 
 CLIGHT = 137.035999084
@@ -99,14 +99,21 @@ class DHFSCF:
         self.backend = backend or GPUBackend(basis, precision, screen, breit, racah1, torch)
         self.n = self.backend.n
 
-    def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, mom=0, verbose=False):
+    def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, mom=0, verbose=False,
+            guess=None, wfn_out=None, return_density=False):
         """Iterate to |dE| < etol.  shift: LEVSHFT's virtual-space level shift
         SHLV in Eh (the H2O deck's stage-3 value 0.5), applied from the second
         iteration on; it moves the path, not the converged solution.
         mom: from this iteration on (0: never) the occupied spinors are the
         positive-energy eigenvectors that overlap most with the previous
         occupied space (maximum overlap) instead of the lowest ones, which
-        stops occupations from flipping between near-degenerate levels."""
+        stops occupations from flipping between near-degenerate levels.
+        guess: None for the bare-nucleus start (diagonalised H1), a density
+        matrix (NDIM x NDIM), (EIGN, COEF) of a wavefunction file (DENSTY of
+        its occupied states) or "atomic" (superposed atomic densities, see
+        atomic_guess).  wfn_out: write the last eigenvalues and eigenvectors
+        as a `.wfn` file (virtual eigenvalues without the level shift, as
+        HFSCF writes them)."""
         t = self.torch
         be = self.backend
         dev = be.device
@@ -145,7 +152,18 @@ class DHFSCF:
             # DENSTY: D_ij = sum_occ conj(C_i) C_j
             return e, nneg, occ.conj() @ occ.T, C
 
-        eps, nneg, D, C = solve(H1)
+        if guess is None:
+            eps, nneg, D, C = solve(H1)
+        else:
+            if isinstance(guess, str) and guess == "atomic":
+                guess = atomic_guess(self.basis, torch=t,
+                                     backend_factory=getattr(be, "atom_factory", None))
+            if isinstance(guess, tuple):
+                eign, coef = guess
+                nskp = int((np.asarray(eign) < -CLIGHT * CLIGHT).sum())
+                guess = wfn.density(coef, nskp, self.nocc)
+            D = t.as_tensor(np.asarray(guess), dtype=t.complex128, device=dev)
+            eps, nneg, C = None, 0, None
         hist_F, hist_E = [], []
         energy, last = None, None
         iters, t_fock, t_lin = [], 0.0, 0.0
@@ -197,15 +215,67 @@ class DHFSCF:
             if last is not None and abs(de) < etol:
                 break
             last = energy
-        return {"energy": energy, "enuc": enuc, "iterations": len(iters),
-                "converged": bool(iters and iters[-1]["de"] is not None
-                                  and abs(iters[-1]["de"]) < etol),
-                "oneel_s": t_one, "fock_s": t_fock, "linalg_s": t_lin,
-                "wall_s": t_one + t_fock + t_lin, "history": iters,
-                "orbital_energies": eps[nneg:nneg + self.nocc].cpu().numpy().tolist()}
+        if wfn_out:
+            n = self.n
+            e = eps.cpu().numpy().copy()
+            Cn = C.cpu().numpy()
+            if shift and len(iters) > 1:
+                vir = np.ones(len(e), bool)
+                vir[:nneg] = False
+                occ_e = sorted(e[nneg:])[:self.nocc]
+                vir &= ~np.isin(e, occ_e)
+                e[vir] -= shift
+            # the orthogonaliser may drop near-singular directions: pad to
+            # NDIM records with zero vectors
+            eign = np.zeros(n)
+            coef = np.zeros((n, n), dtype=np.complex128)
+            eign[:len(e)] = e
+            coef[:, :Cn.shape[1]] = Cn
+            wfn.write_wfn(wfn_out, eign, coef)
+        out = {"energy": energy, "enuc": enuc, "iterations": len(iters),
+               "converged": bool(iters and iters[-1]["de"] is not None
+                                 and abs(iters[-1]["de"]) < etol),
+               "oneel_s": t_one, "fock_s": t_fock, "linalg_s": t_lin,
+               "wall_s": t_one + t_fock + t_lin, "history": iters,
+               "orbital_energies": eps[nneg:nneg + self.nocc].cpu().numpy().tolist()}
+        if return_density:
+            out["density"] = D
+        return out
 
     def close(self):
         self.backend.close()
+
+
+def atomic_guess(basis, torch=None, backend_factory=None, max_iter=25, etol=1e-6):
+    """Starting density of a molecule from SCFs of its atoms (the role of the
+    atomic wavefunctions the reference reads from bertha-atomic): for every
+    centre, a Dirac-Coulomb SCF of the centre's own basis functions with
+    NOCC = Z spinors occupied (maximum-overlap occupation, so that an odd
+    electron count keeps one spinor of its Kramers pair), its density placed
+    on the centre's rows and columns of the molecular layout (FOCKIND).
+    Centres with the same charge and exponents share one atomic SCF.
+    backend_factory(atom) makes the Fock-build backend of an atom (default:
+    the GPU library)."""
+    if torch is None:
+        import torch as _t
+        torch = _t
+    hm = "NORL" if basis.hmlt == deck.HMLT["NORL"] else "DHFR"
+    cache, dens = {}, []
+    for c in range(basis.ncnt):
+        z = int(round(float(basis.znuc[c])))
+        if z <= 0:
+            dens.append(None)
+            continue
+        atom = wfn.atom_of_centre(basis, c, hmlt=hm)
+        key = (z, atom.ex.tobytes(), atom.nfn.tobytes())
+        if key not in cache:
+            be = backend_factory(atom) if backend_factory else None
+            s = DHFSCF(atom, nocc=z, screen=1e-12, racah1=False, torch=torch, backend=be)
+            r = s.run(max_iter=max_iter, etol=etol, mom=2, return_density=True)
+            s.close()
+            cache[key] = r["density"].cpu().numpy()
+        dens.append(cache[key])
+    return wfn.embed_atomic_densities(basis, dens)
 
 
 class BatchedDHFSCF:

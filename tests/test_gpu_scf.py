@@ -32,3 +32,26 @@ def test_scf_gpu_matches_oracle(hmlt):
         scf.close()
         assert r["converged"]
         assert abs(r["energy"] - ref["energy"]) < tol, (prec, r["energy"], ref["energy"])
+
+
+def test_scf_atomic_guess_and_wfn_restart(tmp_path):
+    """The superposed atomic start and a restart from the `.wfn` file the
+    converged run wrote reach the bare-nucleus SCF's energy; the restart
+    needs two iterations (the first already at the converged energy)."""
+    from berthagpu import wfn
+    b = _water_small()
+    path = str(tmp_path / "water.wfn")
+    s = DHFSCF(b, nocc=10, screen=0.0)
+    r0 = s.run(max_iter=40, etol=1e-10, wfn_out=path)
+    s.close()
+    s = DHFSCF(b, nocc=10, screen=0.0)
+    r1 = s.run(max_iter=40, etol=1e-10, guess="atomic")
+    s.close()
+    eign, coef = wfn.read_wfn(path, b.ndim)
+    s = DHFSCF(b, nocc=10, screen=0.0)
+    r2 = s.run(max_iter=40, etol=1e-10, guess=(eign, coef))
+    s.close()
+    assert r0["converged"] and r1["converged"] and r2["converged"]
+    assert abs(r1["energy"] - r0["energy"]) < 1e-9
+    assert abs(r2["energy"] - r0["energy"]) < 1e-9
+    assert r2["iterations"] <= 3
