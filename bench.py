@@ -353,6 +353,21 @@ def tlf_builds(torch):
         abs(out["coulomb_auto"]["energy_j_eh"] - out["coulomb_fp64"]["energy_j_eh"]),
         abs(out["coulomb_auto"]["energy_k_eh"] - out["coulomb_fp64"]["energy_k_eh"]))
     out["dcb_fock_build_fp64_s"] = out["coulomb_fp64"]["device_s"] + out["breit_fp64"]["device_s"]
+    # the precision's effect on a converged DCB total energy: the small TlF
+    # case (same geometry, angular momenta and exponent range) from the
+    # bare-nucleus start with maximum-overlap occupation from iteration 3,
+    # FP64 and autotuned mixed precision
+    from berthagpu.scf import DHFSCF
+    bs = deck.tlf_small_basis()
+    scf = {"case": "TlF, Tl 7s6p4d3f / F 4s3p1d, DHFB", "ndim": bs.ndim, "nocc": 90,
+           "guess": "bare nucleus, maximum overlap from iteration 3", "etol_eh": 1e-9}
+    for prec in ("fp64", "auto"):
+        s = DHFSCF(bs, nocc=90, precision=prec, screen=1e-12, torch=torch)
+        r = s.run(max_iter=100, etol=1e-9, mom=3)
+        s.close()
+        scf[prec] = {k: r[k] for k in ("energy", "iterations", "converged", "wall_s", "fock_s")}
+    scf["energy_auto_vs_fp64_eh"] = abs(scf["auto"]["energy"] - scf["fp64"]["energy"])
+    out["scf_tlf_small"] = scf
     return out
 
 
