@@ -44,8 +44,7 @@ constexpr int MAXLAM = 2 * MAXDEGE;       // R order (SS|SS)
 constexpr int NTE = ntuv(MAXDEGE);        // 165
 constexpr int NTR = ntuv(MAXLAM);         // 969
 constexpr int CHUNK = 5;                  // ab labels per first-contraction pass (at N = 165)
-constexpr int QTHREADS = 256;             // k_breit
-constexpr int QT64 = 128;                 // k_quartet: four 128-thread CTAs per SM
+constexpr int QT64 = 128;                 // k_quartet, k_breit: four 128-thread CTAs per SM
 
 __constant__ signed char c_t[NTR], c_u[NTR], c_v[NTR];
 
@@ -1032,7 +1031,7 @@ __global__ void k_oneel(const Shell *sh, int ns, const PairE *pe, const double2 
 // ---------------------------------------------------------------------------
 constexpr int NTB = ntuv(2 * MAXLB + 1);  // E terms of an LS/SL pair (120)
 constexpr int NTW = ntuv(4 * MAXLB + 2);  // Breit kernel entries per quartet (680)
-constexpr int BCHUNK = 4;                 // ab labels per pass at the largest cd degree
+constexpr int BCHUNK = 1;                 // ab labels per pass at the largest cd degree
 
 // sigma-coupled E-coefficients psi_a^+ sigma_q psi_b, q = x, y, z, for the
 // component pairs LS (comp 0: a large, b small, times i; EQLS :34937) and SL
@@ -1133,8 +1132,17 @@ __device__ inline double2 ldDB(const BArgs &q, int i, int j) {
   return q.D[(size_t)i + (size_t)q.ldd * j];
 }
 
+// The Breit kernel table is symmetric, W_ij(N) = W_ji(N) (the operator's
+// Cartesian part delta_ij/r + r_i r_j/r^3 is), so 6 entries per N are kept:
+// xx, yy, zz, xy, xz, yz.
+__host__ __device__ inline int sym6(int i, int j) { return i == j ? i : i + j + 2; }
+
+// doubles of the region after the table: the first contraction's G buffer,
+// which the two R recursion buffers alias
+constexpr int BREG = (BCHUNK * 2 * 3 * NTB * 2 > 2 * NTR) ? BCHUNK * 2 * 3 * NTB * 2 : 2 * NTR;
+
 size_t breit_smem() {
-  return sizeof(double) * NTW * 9 + sizeof(double2) * (BCHUNK * 2 * 3 * NTB + 2 * MAXSP * MAXSP);
+  return sizeof(double) * (NTW * 6 + BREG) + sizeof(double2) * (2 * MAXSP * MAXSP);
 }
 
 // FP64 multiply-adds of the two contraction orders of a Breit quartet: the
@@ -1154,14 +1162,14 @@ __host__ __device__ inline long long breit_cost(int pl, int nl, int pr, int nr, 
 // G_i = sum_j E_j(ab) W_ij for both E sets, the second contraction summed
 // over i, the 16 m-sign combinations with the Breit phases (Coulomb phases
 // negated, :17528-17533 and :18899) and the exchange digestion of BRTMTG/BRTMTZ batch type 5.
-__global__ void __launch_bounds__(QTHREADS, 2)
+__global__ void __launch_bounds__(QT64, 4)
 k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
   extern __shared__ double smem[];
-  double *W = smem;                          // NTW*9
-  double2 *G = (double2 *)(W + NTW * 9);     // BCHUNK*2*3*NTB
+  double *W = smem;                          // NTW*6 (symmetric table)
+  double2 *G = (double2 *)(W + NTW * 6);     // BCHUNK*2*3*NTB
   double *R = (double *)G;                   // R recursion scratch (aliases G)
   double *R2 = R + NTR;
-  double2 *Kl = G + BCHUNK * 2 * 3 * NTB;    // MAXSP*MAXSP  K(a,d)
+  double2 *Kl = (double2 *)((double *)G + BREG);  // MAXSP*MAXSP  K(a,d)
   double2 *K2 = Kl + MAXSP * MAXSP;          // MAXSP*MAXSP  K(c,b) of (cd|ab)
   __shared__ double sgeo[10];
   __shared__ double F[MAXLAM + 2];
@@ -1236,8 +1244,9 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
       double pq[3] = {sgeo[6], sgeo[7], sgeo[8]};
       double bfac = q.gaunt ? -1.0 : -0.5;
       int nw = ntuv(lamn);
-      for (int w = threadIdx.x; w < nw * 9; w += blockDim.x) {
-        int n = w / 9, ij = w % 9, i = ij / 3, j = ij % 3;
+      for (int w = threadIdx.x; w < nw * 6; w += blockDim.x) {
+        int n = w / 6, e = w % 6;
+        int i = e < 3 ? e : (e == 5 ? 1 : 0), j = e < 3 ? e : (e == 3 ? 1 : 2);
         int N[3] = {c_t[n], c_u[n], c_v[n]};
         double rn = cur[n] * pre;
         double val;
@@ -1296,7 +1305,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
           for (int k = 0; k < nL; ++k) {
             int s = ei[k];
             if (s == ENDIDX) break;
-            double w = W[hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq) * 9 + 3 * i + j];
+            double w = W[hidx(c_t[s] + tq, c_u[s] + uq, c_v[s] + vq) * 6 + sym6(i, j)];
             double2 ev = ev_[k];
             ax = fma(ev.x, w, ax);
             ay = fma(ev.y, w, ay);
@@ -2708,7 +2717,7 @@ int launch_breit(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const 
   a.ns = c->ns; a.ldd = ldd; a.ldf = ldf; a.nskp = c->nskp; a.isym = c->isym;
   a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual; a.bound = bound;
   long long grid = std::min<long long>(nq, 152LL * 64);
-  k_breit<<<(unsigned)grid, QTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  k_breit<<<(unsigned)grid, QT64, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
   c->launches++;
   return 0;
