@@ -21,3 +21,23 @@ def test_helium_dhf_energy():
     # Kramers-degenerate 1s1/2 pair
     e = r["orbital_energies"]
     assert abs(e[0] - e[1]) < 1e-10 and abs(e[0] - (-0.91799)) < 1e-4
+
+
+def test_helium_maximum_overlap_and_wfn(tmp_path):
+    """Maximum-overlap occupation from the second iteration reaches the same
+    helium energy as aufbau, and the `.wfn` file it writes restarts the SCF
+    at convergence."""
+    from berthagpu import wfn
+    he = deck.make_basis([((0.0, 0.0, 0.0), {0: deck.geometric(0.06, 2.1, 18)})], hmlt="DHFR")
+    he.znuc, he.anuc = (2.0,), (4.0,)
+    path = str(tmp_path / "he.wfn")
+    scf = DHFSCF(he, nocc=2, torch=torch, backend=OracleBackend(he, racah1=False))
+    r = scf.run(max_iter=30, etol=1e-10, mom=2, wfn_out=path)
+    assert r["converged"]
+    assert abs(r["energy"] - (-2.8618133)) < 2e-6
+    eign, coef = wfn.read_wfn(path, he.ndim)
+    assert abs(eign[he.nskp] - r["orbital_energies"][0]) < 1e-12
+    scf = DHFSCF(he, nocc=2, torch=torch, backend=OracleBackend(he, racah1=False))
+    r2 = scf.run(max_iter=30, etol=1e-10, guess=(eign, coef))
+    assert r2["converged"] and r2["iterations"] <= 3
+    assert abs(r2["energy"] - r["energy"]) < 1e-9
