@@ -1846,8 +1846,13 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
     int oab = t1 ? nskpm : 0, ocd = t2 ? nskpm : 0;
     int kq0 = sk;
     __syncthreads();
-    for (int c0 = 0; c0 < nlL; c0 += ch) {
-      int nch = min(ch, nlL - c0);
+    // left labels per pass: as many as the staging buffers (EL and G,
+    // ch*2*NTE float4 each) and the contribution buffer (df_ncb) take at
+    // this class's degrees; ch at the largest degree, more for low l
+    int chunk = min((ch * 2 * NTE) / (2 * max(nL, nR)), df_ncb(q.sym) / (nlR * ntg));
+    chunk = max(1, chunk);
+    for (int c0 = 0; c0 < nlL; c0 += chunk) {
+      int nch = min(chunk, nlL - c0);
       // stage the nonzero left E-coefficients (packed, with their Hermite
       // indices) rescaled to this quartet's exponent
       for (int w = threadIdx.x; w < nch * 2 * nL; w += blockDim.x) {
@@ -1878,7 +1883,7 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
         }
         int lq_ = tq + uq + vq;
         float f = ldexpf((lq_ & 1) ? -1.0f : 1.0f, (kq0 - kR) * lq_);
-        G[ls * NTE + qq] = make_float4(rh * f, rl * f, ih * f, il * f);
+        G[ls * nR + qq] = make_float4(rh * f, rl * f, ih * f, il * f);
       }
       __syncthreads();
       {
@@ -1908,7 +1913,7 @@ k_quartet_df(QArgsDF q, const int4 *quart, long long nq, int t1, int t2) {
 #pragma unroll
           for (int i = 0; i < 16; ++i) { acc[i][0] = 0.f; acc[i][1] = 0.f; }
           if (active) {
-            const float4 *g11 = G + (lab * 2 + 0) * NTE, *g21 = G + (lab * 2 + 1) * NTE;
+            const float4 *g11 = G + (lab * 2 + 0) * nR, *g21 = G + (lab * 2 + 1) * nR;
             const float4 *e11 = ER + ((long long)lr * 2 + 0) * nR;
             const float4 *e21 = ER + ((long long)lr * 2 + 1) * nR;
             // right-side E from L2 with one iteration of register prefetch
