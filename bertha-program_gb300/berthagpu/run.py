@@ -34,6 +34,8 @@ def main(argv=None):
     g.add_argument("--deck")
     g.add_argument("--atoms", type=int, help="batch of N seeded closed-shell atoms")
     p.add_argument("--zmax", type=int, default=86, help="largest Z drawn for --atoms")
+    p.add_argument("--scf-only", action="store_true",
+                   help="--atoms: only the batched SCF, in --precision")
     p.add_argument("--scf", action="store_true",
                    help="run the closed-shell DHF SCF (with --atoms: the batched SCF too)")
     p.add_argument("--nocc", type=int, default=0, help="--scf: occupied spinors (0: sum of Z)")
@@ -139,6 +141,19 @@ def atoms_main(a):
     zset = [z for z in deck.CLOSED_SHELL_ATOMS if z <= a.zmax]
     bases = deck.batched_atoms(a.atoms, seed=a.seed, zset=zset)
     zs = [int(b.znuc[0]) for b in bases]
+    if a.scf_only:
+        s = BatchedDHFSCF(bases, zs, precision=a.precision, screen=a.screen or 1e-12)
+        r = s.run(etol=a.etol, max_iter=a.max_iter, mom=a.mom, shift=a.shift)
+        s.close()
+        hist = r.pop("history")
+        e = r.pop("energy")
+        conv = r.pop("converged")
+        r.update({"atoms": a.atoms, "precision": a.precision, "converged": int(sum(conv)),
+                  "iter_s": [h["s"] for h in hist],
+                  "max_abs_de": [h["max_abs_de"] for h in hist],
+                  "energy_by_z": {str(z): v for z, v in zip(zs, e)},
+                  "unconverged_z": sorted({z for z, c in zip(zs, conv) if not c})})
+        return r
     out = {"atoms": a.atoms, "z_drawn_from": zset, "z": zs,
            "ndim": [b.ndim for b in bases], "screen": a.screen or 1e-12}
     screen = a.screen or 1e-12

@@ -362,7 +362,9 @@ class BatchedDHFSCF:
     def quartets(self):
         return self.batch.quartets()
 
-    def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, verbose=False):
+    def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, mom=0, verbose=False):
+        """As DHFSCF.run for every instance at once (mom: maximum-overlap
+        occupation from that iteration on, per instance)."""
         t = self.torch
         n, N = self.n, self.N
         t0 = time.perf_counter()
@@ -376,13 +378,28 @@ class BatchedDHFSCF:
         col = t.arange(N, device="cuda")[None, :]
         c2 = CLIGHT * CLIGHT
 
-        def solve(F):
+        state = {"occ": None}
+
+        def solve(F, use_mom=False):
             e, Cp = t.linalg.eigh(Xh @ F @ X + drop)
             C = X @ Cp
             nneg = (e < -c2).sum(dim=1, keepdim=True)
-            occ = ((col >= nneg) & (col < nneg + nocc[:, None])).to(t.complex128)
-            vir = ((col >= nneg + nocc[:, None]) & (e < 0.5 * self.PAD)).to(t.complex128)
+            # positive-energy eigenvectors (padding and dropped directions
+            # sit at PAD)
+            pos = (col >= nneg) & (e < 0.5 * self.PAD)
+            if use_mom and state["occ"] is not None:
+                # the NOCC positive-energy eigenvectors with the largest
+                # projection on the previous occupied space, per instance
+                w = ((state["occ"].conj().transpose(1, 2) @ (S @ C)).abs() ** 2).sum(1)
+                w = t.where(pos, w, t.full_like(w, -1.0))
+                rank = t.argsort(t.argsort(-w, dim=1), dim=1)
+                occb = rank < nocc[:, None]
+            else:
+                occb = (col >= nneg) & (col < nneg + nocc[:, None])
+            occ = occb.to(t.complex128)
+            vir = (pos & ~occb).to(t.complex128)
             Co = C * occ[:, None, :]
+            state["occ"] = Co
             # DENSTY: D_ij = sum_occ conj(C_i) C_j
             return e, Co.conj() @ Co.transpose(1, 2), C * vir[:, None, :], nneg
 
@@ -426,7 +443,7 @@ class BatchedDHFSCF:
                 rhs[:, m] = -1.0
                 w = t.linalg.solve(B, rhs)[:, :m].to(t.complex128)
                 F = (t.stack(hist_F, 1) * w[:, :, None, None]).sum(1)
-            eps, D, Cv, nneg = solve(F)
+            eps, D, Cv, nneg = solve(F, use_mom=bool(mom) and it >= mom)
             t.cuda.synchronize()
             t_lin += time.perf_counter() - tf
             de = None if last is None else energy - last
