@@ -227,9 +227,11 @@ int bertha_gpu_batch_auto_stats(const bg_batch *b, long long *nq_fp64, long long
 /* CLMFAST of every instance at stage ilev on device arrays in the batch's
  * placement: d_dent holds all densities; d_gdir, d_gxch get all GDIR and
  * GXCH, each instance's NDIM x NDIM block overwritten (other elements are
- * left alone).  The first call at a stage builds the quartet lists (host
- * work and allocation); later calls at that stage only launch kernels on
- * `stream` and can be captured in a CUDA graph. */
+ * left alone).  Like bertha_gpu_clmfast, each instance's density must be
+ * Hermitian (the build is symmetry-reduced and completed).  The first call
+ * at a stage builds the quartet lists (host work and allocation; under
+ * BG_PREC_AUTO it also tunes the kernel choice); later calls at that stage
+ * only launch kernels on `stream` and can be captured in a CUDA graph. */
 int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
                                     double *d_gdir, double *d_gxch, void *stream);
 
