@@ -183,3 +183,19 @@ def test_breit_exchange_blocks_hermitian():
     assert np.abs(bx - bx.conj().T).max() <= 1e-12 * s
     for blk in (bx[:n, :n], bx[n:, n:], bx[:n, n:]):
         assert np.abs(blk).max() > 1e-6 * s
+
+
+def test_breit_kernel_table_is_symmetric():
+    """W_ij(N) = W_ji(N): the Cartesian part of the Breit operator,
+    delta_ij/r + r_i r_j/r^3, is symmetric, so its Hermite table is too (the
+    GPU kernel keeps 6 of the 9 entries per N)."""
+    rng = np.random.default_rng(11)
+    for _ in range(100):
+        qp = rng.normal(size=3) * rng.uniform(0.0, 2.0)
+        alpha = float(np.exp(rng.uniform(-3.0, 8.0)))
+        t, u, v = (int(x) for x in rng.integers(0, 4, 3))
+        for gaunt in (False, True):
+            W = orc.breit_kernel(qp, alpha, t, u, v, gaunt=gaunt)
+            scale = np.abs(W).max()
+            if scale > 0:
+                assert np.abs(W - W.T).max() <= 1e-13 * scale
