@@ -44,22 +44,23 @@ def parse():
     p.add_argument("--quartets", type=int, default=1 << 20)
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--ref-quartets", type=int, default=131072,
+                   help="quartets per step of the reference arm (a bounded sample)")
     p.add_argument("--no-h2o", action="store_true",
                    help="skip the other configurations (H2O builds and SCF, TlF builds, "
                         "batched atoms) reported beside the headline")
-    p.add_argument("--precision", default="df32", choices=["fp64", "df32"],
-                   help="precision of the headline value; the other is timed beside it")
+    p.add_argument("--precision", default="tc32", choices=["fp64", "df32", "tc32"],
+                   help="precision of the headline value; the others are timed beside it")
     return p.parse_args()
 
 
-def config(args, extra=None):
-    c = {"workload": WORKLOAD, "quartets_per_step": args.quartets, "seed": args.seed,
-         "pool": "32 centres x 4 l x 2 exponents (256 shells, NDIM 4096)",
-         "l2": "flushed between timed steps (256 MiB write)",
-         "parallelism": f"replicas x{args.gpus}"}
-    if extra:
-        c.update(extra)
-    return c
+def config(args):
+    """The workload, identical in both arms' lines (per-run figures such as
+    the quartets of a step live outside it)."""
+    return {"workload": WORKLOAD, "seed": args.seed,
+            "pool": "32 centres x 4 l x 2 exponents (256 shells, NDIM 4096)",
+            "l2": "flushed between timed steps (256 MiB write)",
+            "parallelism": f"replicas x{args.gpus}"}
 
 
 # ---------------------------------------------------------------------------
@@ -89,28 +90,48 @@ def cpu_rate(basis, quarts, dent, seconds, nthreads):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of ERIFAST/CLMMTG (the Fortran
+    reference cannot be built on either machine) on all host cores.  A step
+    is a bounded sample of the workload, the same number of quartets every
+    step (equal per component class, drawn from the workload's lists in
+    order), sized so that the whole run stays within a few minutes;
+    ms_per_step is the measured time of that sample."""
+    from oracle import oracle as orc
     from berthagpu import deck, workloads
     basis = workloads.microbench_pool(seed=args.seed)
     quarts = workloads.microbench_quartets(basis, args.quartets, seed=args.seed)
     dent = deck.density(basis, seed=args.seed)
     cores = os.cpu_count() or 1
-    rates = []
-    per_step = max(2.0, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
+    n = basis.ndim
+    O = orc.QuartetOracle(basis)
+    gd = np.zeros((n, n), complex, order="F")
+    gx = np.zeros((n, n), complex, order="F")
+    per_class = max(512, int(args.ref_quartets) // len(quarts))
+    sample = {cls: q[:per_class] for cls, q in quarts.items()}
+    for cls, q in sample.items():
+        O.prepare(q, *cls)
+    times = []
     for i in range(args.warmup + args.steps):
-        r, nq, t = cpu_rate(basis, quarts, dent, per_step, cores)
+        t0 = time.perf_counter()
+        for cls, q in sample.items():
+            O.digest(q, *cls, dent, gd, gx, nthreads=cores)
+        dt = time.perf_counter() - t0
         if i >= args.warmup:
-            rates.append((r, nq, t))
-    value = float(np.mean([r for r, _, _ in rates]))
-    sample = (f"{rates[-1][1]} quartets per step (equal per component class) of the "
-              f"{args.quartets}-quartet workload, {rates[-1][2]:.1f} s")
+            times.append(dt)
+    O.close()
+    nq = sum(len(q) for q in sample.values())
+    ms = 1e3 * float(np.mean(times))
+    value = nq / (ms * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * args.quartets / value, "higher_is_better": True,
+        "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config(args), "impl": "reference",
+        "config": config(args), "impl": "reference", "quartets_per_step": nq,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": f"{nq} quartets per step ({per_class} per component class, "
+                                   f"the first of each class's list) of the "
+                                   f"{args.quartets}-quartet workload"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -175,6 +196,11 @@ class ClockSampler:
 # scaled by 16 to the full step's 262144-quartet launch (DRAM traffic grows
 # with the quartet count: the E-coefficients of the pool's random pairs).
 TRAFFIC_BYTES_PER_LAUNCH = 10.749e9
+
+
+# DRAM bytes per k_quartet_tc launch of this workload (dram__bytes_read.sum
+# + dram__bytes_write.sum of an ncu capture); None until captured.
+TC_TRAFFIC_BYTES_PER_STEP = None
 
 
 def read_traffic():
@@ -462,12 +488,40 @@ def fp64_peak(torch):
     return best
 
 
+def tf32_peak(torch):
+    """Dense TF32 tensor-core peak of this GPU measured now: cuBLAS FP32 GEMM
+    with TF32 allowed, 8192^3, best of 5."""
+    n = 8192
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    a = torch.randn(n, n, dtype=torch.float32, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float32, device="cuda")
+    a @ b
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        e.synchronize()
+        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = old
+    del a, b
+    return best
+
+
+PATHS = ("fp64", "df32", "tc32")
+DTYPE = {"fp64": "f64",
+         "df32": "f32x2 double-float contractions; f64 Boys, R, J/K sums",
+         "tc32": "tf32x3 tcgen05 contractions (fp32 accumulate); f64 Boys, R, J/K sums"}
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
 
     import berthagpu
-    from berthagpu import deck, replicas, workloads
+    from berthagpu import _lib, deck, replicas, workloads
     from berthagpu.build import build as build_lib
 
     rank = int(os.environ.get("RANK", 0))
@@ -483,9 +537,16 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
 
     basis = workloads.microbench_pool(seed=args.seed)
-    quarts = workloads.microbench_quartets(basis, args.quartets, seed=args.seed)
+    raw = workloads.microbench_quartets(basis, args.quartets, seed=args.seed)
+    # each component class's list grouped by angular class (CLMFAST's L-block
+    # order); the segment table lets the tensor-core path size its launches
+    quarts, segs = {}, {}
+    for cls, q in raw.items():
+        qq, seg, lcl = workloads.group_by_class(basis, q)
+        quarts[cls], segs[cls] = qq, (seg, lcl)
     dent = deck.density(basis, seed=args.seed)
     flops = {cls: workloads.quartet_flops(basis, q, *cls) for cls, q in quarts.items()}
+    cflops = {cls: workloads.contraction_flops(basis, q, *cls) for cls, q in quarts.items()}
     fb = berthagpu.FockBuilder(basis)
     n = fb.ndim
     # complex matrices as interleaved doubles; the column-major (n x n) array
@@ -504,23 +565,26 @@ def run_gpu(args):
         for k, (cls, q) in enumerate(dq.items()):
             if events is not None:
                 events[k][0].record(stream)
-            fb.quartets(q.data_ptr(), q.shape[0], cls[0], cls[1], D.data_ptr(),
-                        GD.data_ptr(), GX.data_ptr(), n, sp)
+            seg, lcl = segs[cls]
+            fb.quartets_segments(q.data_ptr(), seg, lcl, cls[0], cls[1], D.data_ptr(),
+                                 GD.data_ptr(), GX.data_ptr(), n, sp)
             launches += fb.launches()
             if events is not None:
                 events[k][1].record(stream)
         return launches
 
+    def matrices():
+        gd = GD.cpu().numpy().view(np.complex128).reshape(n, n).T
+        gx = GX.cpu().numpy().view(np.complex128).reshape(n, n).T
+        return gd, gx
+
     def energy_terms():
-        # one clean step; J/K contracted with the density (the two-electron
-        # energy terms 1/2 Re tr(D J), 1/2 Re tr(D K), ENRGIES form)
+        # one clean step; J/K as matrices
         GD.zero_()
         GX.zero_()
         step()
         torch.cuda.synchronize()
-        gd = GD.cpu().numpy().view(np.complex128).reshape(n, n).T
-        gx = GX.cpu().numpy().view(np.complex128).reshape(n, n).T
-        return gd, gx
+        return matrices()
 
     def timed(prec):
         fb.set_precision(prec)
@@ -535,25 +599,31 @@ def run_gpu(args):
             if world > 1:
                 dist.barrier()
             torch.cuda.synchronize()
-            for s in range(args.steps):
+            for s_ in range(args.steps):
                 flush.zero_()
-                launches += step(ev[s])
+                launches += step(ev[s_])
             torch.cuda.synchronize()
             if world > 1:
                 dist.barrier()
-        kern_ms = np.array([[ev[s][k][0].elapsed_time(ev[s][k][1]) for k in range(len(dq))]
-                            for s in range(args.steps)])
+        kern_ms = np.array([[ev[s_][k][0].elapsed_time(ev[s_][k][1]) for k in range(len(dq))]
+                            for s_ in range(args.steps)])
         return kern_ms, launches, clk.summary()
 
     peak64 = fp64_peak(torch)
-    other = "fp64" if args.precision == "df32" else "df32"
-    kern_other, _, _ = timed(other)
-    kern_ms, launches, clocks = timed(args.precision)
-    fb.set_precision("fp64")
-    gd64, gx64 = energy_terms()
-    fb.set_precision("df32")
-    gdm, gxm = energy_terms()
+    peak_tf32 = tf32_peak(torch)
+    res = {}
+    for prec in PATHS:
+        if prec != args.precision:
+            res[prec] = timed(prec)
+    res[args.precision] = timed(args.precision)
+    kern_ms, launches, clocks = res[args.precision]
+    mats = {}
+    for prec in PATHS:
+        fb.set_precision(prec)
+        mats[prec] = energy_terms()
+    status = _lib.device_status()
     fb.set_precision(args.precision)
+    gd64, gx64 = mats["fp64"]
     scale = max(np.abs(gd64).max(), np.abs(gx64).max())
 
     def e2(gd, gx):
@@ -561,19 +631,83 @@ def run_gpu(args):
         return (0.5 * np.sum(dent * gd).real, 0.5 * np.sum(dent * gx).real)
 
     ej64, ek64 = e2(gd64, gx64)
-    ejm, ekm = e2(gdm, gxm)
-    accuracy = {"j_max_abs": float(np.abs(gdm - gd64).max()),
-                "k_max_abs": float(np.abs(gxm - gx64).max()),
-                "rel_to_max_element": float(max(np.abs(gdm - gd64).max(),
-                                                np.abs(gxm - gx64).max()) / scale),
-                "energy_j_abs_eh": float(abs(ejm - ej64)),
-                "energy_k_abs_eh": float(abs(ekm - ek64)),
-                "energy_j_eh": float(ej64), "energy_k_eh": float(ek64)}
+    accuracy = {"reference": "FP64 GPU path (itself within 1e-11 of the oracle in the tests)",
+                "energy_j_eh": float(ej64), "energy_k_eh": float(ek64),
+                "device_status": status}
+    for prec in PATHS[1:]:
+        gdm, gxm = mats[prec]
+        ejm, ekm = e2(gdm, gxm)
+        accuracy[prec] = {
+            "j_max_abs": float(np.abs(gdm - gd64).max()),
+            "k_max_abs": float(np.abs(gxm - gx64).max()),
+            "rel_to_max_element": float(max(np.abs(gdm - gd64).max(),
+                                            np.abs(gxm - gx64).max()) / scale),
+            "energy_j_abs_eh": float(abs(ejm - ej64)),
+            "energy_k_abs_eh": float(abs(ekm - ek64))}
+    # a sample of the workload digested by the oracle: the FP64 path and
+    # the headline path against the reference's arithmetic
+    from oracle import oracle as orc
+    O = orc.QuartetOracle(basis)
+    osamp = {}
+    for prec in ("fp64", args.precision):
+        fb.set_precision(prec)
+        err = 0.0
+        sc = 0.0
+        for cls, q in raw.items():
+            sub = q[:1024]
+            rd = np.zeros((n, n), complex, order="F")
+            rx = np.zeros((n, n), complex, order="F")
+            O.prepare(sub, *cls)
+            O.digest(sub, *cls, dent, rd, rx, nthreads=os.cpu_count() or 1)
+            dsub = torch.from_numpy(np.ascontiguousarray(sub)).to(dev)
+            GD.zero_()
+            GX.zero_()
+            fb.quartets(dsub.data_ptr(), sub.shape[0], cls[0], cls[1], D.data_ptr(),
+                        GD.data_ptr(), GX.data_ptr(), n, sp)
+            torch.cuda.synchronize()
+            gd, gx = matrices()
+            err = max(err, float(np.abs(gd - rd).max()), float(np.abs(gx - rx).max()))
+            sc = max(sc, float(np.abs(rd).max()), float(np.abs(rx).max()))
+        osamp[prec] = {"max_abs": err, "rel_to_max_element": err / sc}
+    O.close()
+    accuracy["vs_oracle_4096_quartets"] = osamp
+    fb.set_precision(args.precision)
+
     step_ms = float(kern_ms.sum(1).max() if args.steps else 0.0)
     step_ms_mean = float(kern_ms.sum(1).mean())
     ms_per_step = replicas.job_step_ms(step_ms_mean, dist if world > 1 else None, dev)
     value = replicas.job_throughput(args.quartets, world, ms_per_step)
-    other_value = args.quartets * world / (float(kern_other.sum(1).mean()) * 1e-3)
+    path_values = {p: {"value": args.quartets * world / (float(r[0].sum(1).mean()) * 1e-3),
+                       "unit": UNIT, "ms_per_step": float(r[0].sum(1).mean())}
+                   for p, r in res.items()}
+
+    # quartets/s per angular class (l_a,l_b,l_c,l_d), all component classes
+    # together, FP64 and the headline path: one launch per class segment
+    per_ang = {}
+    for prec in ("fp64", args.precision):
+        fb.set_precision(prec)
+        evs = []
+        for cls, q in dq.items():
+            seg, lcl = segs[cls]
+            for i in range(len(seg) - 1):
+                key = "".join(str(int(x)) for x in lcl[i])
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fb.quartets_segments(q[int(seg[i]):].data_ptr(), seg[i:i + 2] - seg[i],
+                                     lcl[i:i + 1], cls[0], cls[1], D.data_ptr(), GD.data_ptr(),
+                                     GX.data_ptr(), n, sp)
+                b.record(stream)
+                evs.append((key, int(seg[i + 1] - seg[i]), a, b))
+        torch.cuda.synchronize()
+        for key, m, a, b in evs:
+            e = per_ang.setdefault(key, {"quartets": 0})
+            e["quartets"] += m
+            e[prec + "_ms"] = e.get(prec + "_ms", 0.0) + a.elapsed_time(b)
+    per_angular_class = {k: {"quartets": v["quartets"],
+                             **{p + "_qps": v["quartets"] / (v[p + "_ms"] * 1e-3)
+                                for p in ("fp64", args.precision)}}
+                         for k, v in sorted(per_ang.items(), reverse=True)}
+    fb.set_precision(args.precision)
 
     # end to end through the C ABI: host density and quartet lists in pinned
     # memory copied in, J/K copied back, every step
@@ -584,7 +718,7 @@ def run_gpu(args):
     h2d = hD.numel() * 8 + sum(v.numel() * 4 for v in hq.values())
     d2h = 2 * hGD.numel() * 8
     e_ms = []
-    for s in range(max(1, min(args.steps, 3))):
+    for s_ in range(max(1, min(args.steps, 3))):
         flush.zero_()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -602,16 +736,31 @@ def run_gpu(args):
         e_ms.append(a.elapsed_time(b))
     e2e_value = args.quartets / (float(np.mean(e_ms)) * 1e-3)
 
+    # rooflines: the headline kernel (tensor pipe for tc32: 3 TF32 MMAs per
+    # product of the dense contraction count; FP64 pipe otherwise) and the
+    # FP64 kernel beside it
     tot_flops = sum(flops.values())
+    tot_cflops = sum(cflops.values())
     kern_mean = kern_ms.mean(0)
-    achieved = tot_flops / (kern_mean.sum() * 1e-3) / 1e12
-    kern64 = kern_ms if args.precision == "fp64" else kern_other
-    achieved64 = tot_flops / (kern64.mean(0).sum() * 1e-3) / 1e12
-    per_class = {f"{'LS'[c[0]]}{'LS'[c[0]]}|{'LS'[c[1]]}{'LS'[c[1]]}":
-                 {"ms": float(kern_mean[k]), "quartets_per_s": float(quarts[c].shape[0] / (kern_mean[k] * 1e-3)),
-                  "tflops": float(flops[c] / (kern_mean[k] * 1e-3) / 1e12)}
-                 for k, c in enumerate(dq)}
-    traffic = read_traffic()
+    t_head = kern_mean.sum() * 1e-3
+    t64 = res["fp64"][0].mean(0).sum() * 1e-3
+    fp64_roof = {"bound": "fp64", "kernel": "k_quartet", "achieved": tot_flops / t64 / 1e12,
+                 "peak": peak64, "unit": "TFLOP/s", "frac": tot_flops / t64 / 1e12 / peak64,
+                 "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}
+    if args.precision == "tc32":
+        ach = 3.0 * tot_cflops / t_head / 1e12
+        roofline = {"bound": "tensor", "kernel": "k_quartet_tc", "achieved": ach,
+                    "peak": peak_tf32, "unit": "TFLOP/s", "frac": ach / peak_tf32,
+                    "peak_source": "cuBLAS TF32 GEMM 8192^3 measured in this run "
+                                   "(MEASURED_PEAKS.json has no TF32 entry)",
+                    "flops_per_step": 3.0 * tot_cflops,
+                    "traffic": (TC_TRAFFIC_BYTES_PER_STEP / len(dq)
+                                if TC_TRAFFIC_BYTES_PER_STEP else None),
+                    "fp64_kernel": fp64_roof}
+    else:
+        roofline = dict(fp64_roof)
+        roofline["traffic"] = read_traffic()
+        roofline["flops_per_step"] = tot_flops
 
     line = None
     h2o = breit = scf = tlf = atoms = None
@@ -624,7 +773,7 @@ def run_gpu(args):
     if rank == 0:
         cpu = None
         if world == 1:
-            r, nq, t = cpu_rate(basis, quarts, dent, args.cpu_seconds, os.cpu_count() or 1)
+            r, nq, t = cpu_rate(basis, raw, dent, args.cpu_seconds, os.cpu_count() or 1)
             cpu = {"value": r, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                    "sample": f"{nq} quartets (equal per class) of the same workload, {t:.1f} s, "
                              "C++ restatement of bertha-scf.f ERIFAST/CLMMTG"}
@@ -632,26 +781,20 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": ("f64" if args.precision == "fp64" else
-                      "f32x2 double-float contractions; f64 Boys, R, J/K sums"),
+            "dtype": DTYPE[args.precision],
             "data": "synthetic",
-            "config": config(args, {"precision": args.precision, "per_class": per_class,
-                                    "step_ms_max": step_ms}),
-            "fp64_path": {"value": value if args.precision == "fp64" else other_value,
-                          "unit": UNIT},
-            "split_precision_path": {"value": value if args.precision == "df32" else other_value,
-                                     "unit": UNIT},
-            "speedup_split_vs_fp64": (value / other_value if args.precision == "df32"
-                                      else other_value / value),
-            "accuracy_split_vs_fp64": accuracy,
-            "roofline": {"bound": "fp64", "kernel": "k_quartet (FP64 path)",
-                         "achieved": achieved64,
-                         "peak": peak64, "unit": "TFLOP/s", "frac": achieved64 / peak64,
-                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
-                                        "(MEASURED_PEAKS.json has no FP64 entry)",
-                         "traffic": traffic,
-                         "flops_per_step": tot_flops,
-                         "split_path_effective_tflops": achieved},
+            "config": config(args),
+            "quartets_per_step": args.quartets,
+            "precision": args.precision,
+            "step_ms_max": step_ms,
+            "paths": path_values,
+            "speedup_vs_fp64": {p: path_values[p]["value"] / path_values["fp64"]["value"]
+                                for p in PATHS},
+            "accuracy_vs_fp64": accuracy,
+            "per_component_class_ms": {f"{'LS'[c[0]]}{'LS'[c[0]]}|{'LS'[c[1]]}{'LS'[c[1]]}":
+                                       float(kern_mean[k]) for k, c in enumerate(dq)},
+            "per_angular_class": per_angular_class,
+            "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},

@@ -13,7 +13,7 @@ HMLT = {"NORL": 0, "BARE": 1, "DHFR": 2, "DHFP": 3, "DHFB": 4, "DHFQ": 5}
 SHAPE = {"NOSYMM": 0, "PLANAR": 0, "GENERAL": 0, "DIATOM": 1, "LINEAR": 1, "ATOMIC": 2}
 FLAG_NO_RACAH1 = 1
 FLAG_GAUNT = 2
-PREC = {"fp64": 0, "df32": 1, "auto": 2}
+PREC = {"fp64": 0, "df32": 1, "auto": 2, "tc32": 3}
 MAX_L = 3
 
 _CODES = {1: "invalid argument", 2: "capacity exceeded", 3: "CUDA error", 4: "context unusable"}
@@ -48,6 +48,7 @@ def lib():
         L.bertha_gpu_oneel_device.argtypes = [P, P, P, P, P, P, i, P]
         L.bertha_gpu_quartets.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
         L.bertha_gpu_quartets_noalloc.argtypes = [P, P, ll, i, i, P, i, P, P, i, P]
+        L.bertha_gpu_quartets_segments.argtypes = [P, P, i, P, P, i, i, P, i, P, P, i, P]
         L.bertha_gpu_shells.argtypes = [P, P, P, P, P]
         L.bertha_gpu_layout.argtypes = [P, P]
         L.bertha_gpu_launches.argtypes = [P]
@@ -58,6 +59,11 @@ def lib():
         L.bertha_gpu_free.restype = None
         L.bertha_gpu_auto_stats.argtypes = [P, P, P, P]
         L.bertha_gpu_batch_auto_stats.argtypes = [P, P, P, P]
+        L.bertha_gpu_kernel_stats.argtypes = [P, P, P]
+        L.bertha_gpu_batch_kernel_stats.argtypes = [P, P, P]
+        L.bertha_gpu_set_error_budget.argtypes = [P, ctypes.c_double]
+        L.bertha_gpu_batch_set_error_budget.argtypes = [P, ctypes.c_double]
+        L.bertha_gpu_device_status.argtypes = [P]
         L.bertha_gpu_batch_create.argtypes = [ctypes.POINTER(P), i, P, P, P]
         L.bertha_gpu_batch_set_precision.argtypes = [P, i]
         L.bertha_gpu_batch_clmfast_device.argtypes = [P, P, i, P, P, P]
@@ -79,7 +85,7 @@ EXPORTED = [
     "bertha_gpu_dims", "bertha_gpu_clmfast",
     "bertha_gpu_clmfast_device", "bertha_gpu_brtfast", "bertha_gpu_brtfast_device",
     "bertha_gpu_oneel", "bertha_gpu_oneel_device",
-    "bertha_gpu_quartets", "bertha_gpu_quartets_noalloc",
+    "bertha_gpu_quartets", "bertha_gpu_quartets_noalloc", "bertha_gpu_quartets_segments",
     "bertha_gpu_shells",
     "bertha_gpu_layout", "bertha_gpu_launches", "bertha_gpu_last_error",
     "bertha_gpu_free",
@@ -87,7 +93,18 @@ EXPORTED = [
     "bertha_gpu_batch_clmfast_device", "bertha_gpu_batch_quartets",
     "bertha_gpu_batch_launches", "bertha_gpu_batch_last_error", "bertha_gpu_batch_free",
     "bertha_gpu_auto_stats", "bertha_gpu_batch_auto_stats",
+    "bertha_gpu_kernel_stats", "bertha_gpu_batch_kernel_stats",
+    "bertha_gpu_set_error_budget", "bertha_gpu_batch_set_error_budget",
+    "bertha_gpu_device_status",
 ]
+
+
+def device_status():
+    """Tensor-core kernel status since the last call (synchronises): 0 when
+    every quartet was digested (see bertha_gpu_device_status)."""
+    v = ctypes.c_int()
+    check(lib().bertha_gpu_device_status(ctypes.byref(v)))
+    return v.value
 
 
 def check(rc, ctx=None):

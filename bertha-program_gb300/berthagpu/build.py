@@ -28,7 +28,9 @@ def needs_build():
         return True
     t = os.path.getmtime(LIB)
     hdr = os.path.join(INC, "bertha_gpu.h")
-    return any(os.path.getmtime(p) > t for p in (SRC, hdr, __file__))
+    csrc = os.path.dirname(SRC)
+    deps = [os.path.join(csrc, f) for f in os.listdir(csrc) if f.endswith((".cu", ".cuh"))]
+    return any(os.path.getmtime(p) > t for p in deps + [hdr, __file__])
 
 
 def build(force=False, verbose=False):

@@ -40,11 +40,17 @@ class FockBuilder:
         self.precision = "fp64"
 
     def set_precision(self, prec):
-        """'fp64' (drop-in), 'df32' (split precision on the FP32 pipes) or
-        'auto' (per angular class the faster of the two, timed on the first
-        build)."""
+        """'fp64' (drop-in), 'df32' (split precision on the FP32 pipes),
+        'tc32' (3xTF32 contractions on the tensor cores) or 'auto' (per
+        angular class the fastest kernel within the error budget, chosen on
+        the first build)."""
         check(lib().bertha_gpu_set_precision(self._ctx, _lib.PREC[prec]), self._ctx)
         self.precision = prec
+
+    def set_error_budget(self, eh):
+        """Energy error (Eh) the 'auto' tuner may spend on tensor-core
+        classes per Coulomb build."""
+        check(lib().bertha_gpu_set_error_budget(self._ctx, float(eh)), self._ctx)
 
     def set_screening(self, threshold):
         """Schwarz threshold on Q_ab*Q_cd (0 = off, the reference default)."""
@@ -141,15 +147,28 @@ class FockBuilder:
                                         ctypes.c_void_p(d_gdir), ctypes.c_void_p(d_gxch), ld,
                                         ctypes.c_void_p(stream)), self._ctx)
 
+    def quartets_segments(self, d_quart, seg, lclass, t1, t2, d_dent, d_gdir, d_gxch, ld,
+                          stream=0):
+        """Explicit list grouped by angular class: seg (nseg+1 offsets) and
+        lclass (nseg x 4 angular momenta) are host arrays."""
+        sg = np.ascontiguousarray(seg, dtype=np.int64)
+        lc = np.ascontiguousarray(lclass, dtype=np.int32)
+        check(lib().bertha_gpu_quartets_segments(
+            self._ctx, ctypes.c_void_p(d_quart), len(sg) - 1, _p(sg), _p(lc), int(t1), int(t2),
+            ctypes.c_void_p(d_dent), ld, ctypes.c_void_p(d_gdir), ctypes.c_void_p(d_gxch), ld,
+            ctypes.c_void_p(stream)), self._ctx)
+
     def launches(self):
         return int(lib().bertha_gpu_launches(self._ctx))
 
     def auto_stats(self):
-        """Under precision 'auto': quartets on the FP64 and split kernels, runs."""
-        f, d, r = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
-        check(lib().bertha_gpu_auto_stats(self._ctx, ctypes.byref(f), ctypes.byref(d),
-                                          ctypes.byref(r)), self._ctx)
-        return {"fp64_quartets": f.value, "df32_quartets": d.value, "runs": r.value}
+        """Under precision 'auto' (or 'tc32'): quartets on the FP64, split and
+        tensor-core kernels, runs (launches per build)."""
+        nq = (ctypes.c_longlong * 3)()
+        r = ctypes.c_int()
+        check(lib().bertha_gpu_kernel_stats(self._ctx, nq, ctypes.byref(r)), self._ctx)
+        return {"fp64_quartets": nq[0], "df32_quartets": nq[1], "tc32_quartets": nq[2],
+                "runs": r.value}
 
 
 class FockBatch:
@@ -179,6 +198,9 @@ class FockBatch:
     def set_precision(self, prec):
         check_batch(lib().bertha_gpu_batch_set_precision(self._b, _lib.PREC[prec]), self._b)
 
+    def set_error_budget(self, eh):
+        check_batch(lib().bertha_gpu_batch_set_error_budget(self._b, float(eh)), self._b)
+
     def clmfast_device(self, d_dent, d_gdir, d_gxch, ilev=3, stream=0):
         check_batch(lib().bertha_gpu_batch_clmfast_device(
             self._b, ctypes.c_void_p(d_dent), int(ilev), ctypes.c_void_p(d_gdir),
@@ -188,10 +210,11 @@ class FockBatch:
         return int(lib().bertha_gpu_batch_quartets(self._b))
 
     def auto_stats(self):
-        f, d, r = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
-        check_batch(lib().bertha_gpu_batch_auto_stats(self._b, ctypes.byref(f), ctypes.byref(d),
-                                                      ctypes.byref(r)), self._b)
-        return {"fp64_quartets": f.value, "df32_quartets": d.value, "runs": r.value}
+        nq = (ctypes.c_longlong * 3)()
+        r = ctypes.c_int()
+        check_batch(lib().bertha_gpu_batch_kernel_stats(self._b, nq, ctypes.byref(r)), self._b)
+        return {"fp64_quartets": nq[0], "df32_quartets": nq[1], "tc32_quartets": nq[2],
+                "runs": r.value}
 
     def launches(self):
         return int(lib().bertha_gpu_batch_launches(self._b))

@@ -100,8 +100,12 @@ class DHFSCF:
         self.n = self.backend.n
 
     def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, mom=0, verbose=False,
-            guess=None, wfn_out=None, return_density=False):
-        """Iterate to |dE| < etol.  shift: LEVSHFT's virtual-space level shift
+            guess=None, wfn_out=None, return_density=False, dtol=None):
+        """Iterate to |dE| < etol and, with dtol, until the largest element of
+        the DIIS error F P S - S P F (the orbital gradient; zero at a
+        stationary point) is below dtol too, so that a converged energy does
+        not depend on where a slowly drifting iteration happened to stop.
+        shift: LEVSHFT's virtual-space level shift
         SHLV in Eh (the H2O deck's stage-3 value 0.5), applied from the second
         iteration on; it moves the path, not the converged solution.
         mom: from this iteration on (0: never) the occupied spinors are the
@@ -212,7 +216,8 @@ class DHFSCF:
                           "s": time.perf_counter() - ti})
             if verbose:
                 print(iters[-1], flush=True)
-            if last is not None and abs(de) < etol:
+            if (last is not None and abs(de) < etol
+                    and (dtol is None or iters[-1]["err"] < dtol)):
                 break
             last = energy
         if wfn_out:
@@ -234,13 +239,27 @@ class DHFSCF:
             wfn.write_wfn(wfn_out, eign, coef)
         out = {"energy": energy, "enuc": enuc, "iterations": len(iters),
                "converged": bool(iters and iters[-1]["de"] is not None
-                                 and abs(iters[-1]["de"]) < etol),
+                                 and abs(iters[-1]["de"]) < etol
+                                 and (dtol is None or iters[-1]["err"] < dtol)),
+               "gradient": iters[-1]["err"] if iters else None,
                "oneel_s": t_one, "fock_s": t_fock, "linalg_s": t_lin,
                "wall_s": t_one + t_fock + t_lin, "history": iters,
                "orbital_energies": eps[nneg:nneg + self.nocc].cpu().numpy().tolist()}
         if return_density:
             out["density"] = D
         return out
+
+    def energy_at(self, D):
+        """ENRGIES' total energy of the density D (NDIM x NDIM, device) with
+        this backend's Fock build: one build, no iteration.  Two precisions'
+        energies at one converged density measure the precision's effect on
+        the energy apart from where each SCF stops."""
+        t = self.torch
+        S, V, T = self.backend.oneel()
+        H1 = V + T
+        G = self.backend.fock(D)
+        self.backend.sync()
+        return nuclear_repulsion(self.basis) + float(t.sum(D * (H1 + 0.5 * G)).real.item())
 
     def close(self):
         self.backend.close()

@@ -81,6 +81,26 @@ def quartet_flops(basis, quart, t1, t2):
     return float(np.sum(fr + f1 + f2))
 
 
+def contraction_flops(basis, quart, t1, t2):
+    """Dense Hermite-contraction flops of a quartet list (the tensor-core
+    work): first contraction 2*(4P_ab)*N_ab*N_cd and second 2*(4P_ab)*(4P_cd)*N_cd
+    per quartet (the R recursion excluded)."""
+    sh = basis.shells()
+    l = np.array([s[1] for s in sh])
+    la, lb, lc, ld = (l[quart[:, j]] for j in range(4))
+
+    def nt(L):
+        return (L + 1) * (L + 2) * (L + 3) // 6
+
+    degab = la + lb + 2 * t1
+    degcd = lc + ld + 2 * t2
+    pab = (2 * la + 1) * (2 * lb + 1)
+    pcd = (2 * lc + 1) * (2 * ld + 1)
+    f1 = 2 * (4 * pab) * nt(degab) * nt(degcd)
+    f2 = 2 * (4 * pab) * (4 * pcd) * nt(degcd)
+    return float(np.sum(f1 + f2))
+
+
 def breit_quartets(basis, ilev=3, racah1=True):
     """Shell quartets of the Breit build as the library lists them
     (BRTFAST centre and stage rules): (LS|LS) with pair index ab >= cd and
@@ -128,3 +148,21 @@ def breit_flops(basis, quart, gaunt=False):
     f1 = 2 * (4 * pab) * nt(degab) * nt(degcd) * (3 if gaunt else 9)
     f2 = 2 * (4 * pab) * (4 * pcd) * nt(degcd) * 3
     return float(np.sum(fr + f1 + f2))
+
+
+def group_by_class(basis, quart):
+    """A quartet list reordered by angular class (l_a,l_b,l_c,l_d), highest
+    first (the order in which CLMFAST visits its L blocks), with its segment
+    table: returns (quartets, seg, lclass) where entries seg[i]..seg[i+1]-1
+    have angular momenta lclass[i] (the arguments of
+    bertha_gpu_quartets_segments)."""
+    l = np.array([s[1] for s in basis.shells()])
+    ls = np.stack([l[quart[:, j]] for j in range(4)], 1)
+    key = ((ls[:, 0] * 4 + ls[:, 1]) * 4 + ls[:, 2]) * 4 + ls[:, 3]
+    order = np.argsort(-key, kind="stable")
+    q = np.ascontiguousarray(quart[order])
+    ks = key[order]
+    starts = np.flatnonzero(np.r_[True, ks[1:] != ks[:-1]]) if len(ks) else np.zeros(0, int)
+    seg = np.r_[starts, len(ks)].astype(np.int64)
+    lclass = ls[order][starts].astype(np.int32)
+    return q, seg, lclass

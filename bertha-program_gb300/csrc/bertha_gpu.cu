@@ -19,6 +19,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -2245,17 +2246,51 @@ size_t quartet_smem() {
 
 }  // namespace
 
+namespace {
+#include "tc_quartet.cuh"
+
+// Launch geometry of k_quartet_tc for classes needing at most n1 + n2 TMEM
+// columns: the allocation (a power of two, 32..512), the CTAs that share an
+// SM's 512 columns, and a dynamic shared-memory request large enough that
+// no more CTAs than that are resident on one SM (a surplus CTA would block
+// in tcgen05.alloc until a neighbour exits).
+struct TcGeom {
+  int cols, ctas_per_sm;
+  size_t smem;
+};
+constexpr size_t SM_SMEM = 233472;  // 228 KB of shared memory per SM
+constexpr size_t TC_SMEM_MAX = 122880;
+
+TcGeom tc_geom(int n1, int n2) {
+  TcGeom g;
+  int need = n1 + n2, cols = 32;
+  while (cols < need) cols *= 2;
+  g.cols = cols;
+  size_t s = (size_t)tcq::layout(n1, n2).total;
+  int ctas = std::min(4, 512 / cols);
+  while (ctas > 1 && (s + 1024) * ctas > SM_SMEM) --ctas;
+  // smallest request that still keeps ctas + 1 CTAs off one SM
+  size_t floor_req = SM_SMEM / (ctas + 1) - 1024 + 64;
+  g.smem = std::max(s, floor_req);
+  g.ctas_per_sm = ctas;
+  return g;
+}
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // Context and C ABI
 // ---------------------------------------------------------------------------
 // A run of consecutive entries of a quartet list and the kernel that
 // digests it under BG_PREC_AUTO (df: the split-precision kernel).
+enum { KIND_FP64 = 0, KIND_DF32 = 1, KIND_TC = 2 };
 struct Run {
   long long start, count;
-  int df;
+  int kind;    // KIND_*: the kernel that digests this run
+  int n1, n2;  // KIND_TC: largest TMEM column needs (D1, D2) of the run's classes
 };
 
 struct bg_ctx {
+  int dev = -1;  // device the context was made on
   int ncnt = 0, ndim = 0, nskp = 0, hmlt = 0, isym = 0, racah1 = 1;
   std::vector<double> cxyz;  // BXYZ of the centres
   int ns = 0, ncomp = 1;
@@ -2284,11 +2319,13 @@ struct bg_ctx {
   // BG_PREC_AUTO: angular-class segments of the cached lists and the tuned
   // kernel of each run of them (see tune_runs)
   std::vector<long long> seg[4];
+  std::vector<int> segkey[4];  // angular class (la,lb,lc,ld) of each segment, base 4
   std::vector<Run> runs[4];
   bool tuned = false;
   // split-precision copies
   float4 *d_Edf = nullptr, *d_Ddf = nullptr;
   int prec = BG_PREC_FP64;
+  double err_budget = 1e-7;  // BG_PREC_AUTO: estimated energy error allowed per build (Eh)
   // Breit: sigma-coupled LS/SL E-coefficients (generated on first use) and
   // quartet lists of the classes (LS|LS) and (LS|SL)
   int gaunt = 0;
@@ -2312,7 +2349,9 @@ struct bg_ctx {
 // device, quartet lists of every instance merged per component class and
 // grouped by angular class, one kernel launch per class for all instances.
 struct bg_batch {
+  int dev = -1;  // device of its instances
   int n = 0, ncomp = 1, hmlt = 0, isym = 0, racah1 = 1, prec = BG_PREC_FP64;
+  double err_budget = 1e-7;  // BG_PREC_AUTO: estimated energy error allowed per build (Eh)
   std::vector<bg_ctx *> shadow;  // host copies of the instances' shells, bounds and rules
   std::vector<int> sbase;        // first batch shell of each instance
   std::vector<int> ndim;
@@ -2329,6 +2368,7 @@ struct bg_batch {
   long long nquart[4] = {0, 0, 0, 0};
   int quart_ilev = -1;
   std::vector<long long> seg[4];  // BG_PREC_AUTO, as in bg_ctx
+  std::vector<int> segkey[4];
   std::vector<Run> runs[4];
   bool tuned = false;
   long long launches = 0;
@@ -2361,9 +2401,20 @@ inline int kappa_of(int ka) {
   return (ka % 2 == 0) ? ka / 2 : -(ka / 2) - 1;
 }
 
-int upload_tables() {
-  static bool done = false;
-  if (done) return 0;
+// One-time set-up of a device, done with that device current and recorded
+// per device ordinal: the __constant__ Hermite and reciprocal tables, the
+// split path's Boys table, and the >48 KB dynamic shared-memory opt-in of
+// every quartet kernel.  All of them are properties of a device (a context on
+// a second device gets its own), and none may be issued inside a stream
+// capture, so the launchers never touch them.
+constexpr int MAXDEV = 64;
+std::mutex g_dev_mu;
+bool g_dev_ready[MAXDEV] = {false};
+
+int device_setup(int dev) {
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if (dev < 0 || dev >= MAXDEV) return 1;
+  if (g_dev_ready[dev]) return 0;
   signed char t[NTR], u[NTR], v[NTR];
   int n = 0;
   for (int L = 0; L <= MAXLAM; ++L)
@@ -2378,8 +2429,35 @@ int upload_tables() {
   double rinv[NRINV];
   for (int k = 0; k < NRINV; ++k) rinv[k] = 1.0 / double(2 * k + 1);
   if (cudaMemcpyToSymbol(c_rinv, rinv, sizeof(rinv)) != cudaSuccess) return 1;
-  done = true;
+  k_boys_table<<<(NBGRID + 127) / 128, 128>>>();
+  if (cudaFuncSetAttribute(k_quartet_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)TC_SMEM_MAX) != cudaSuccess ||
+      cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)quartet_smem()) != cudaSuccess ||
+      cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)quartet_smem_df_max()) != cudaSuccess ||
+      cudaFuncSetAttribute(k_breit, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)breit_smem()) != cudaSuccess)
+    return 1;
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return 1;
+  g_dev_ready[dev] = true;
   return 0;
+}
+
+// Every context and batch remembers the device it was made on; calls made
+// while another device is current are refused (BG_ERR_STATE).
+int current_device() {
+  int d = -1;
+  if (cudaGetDevice(&d) != cudaSuccess) return -1;
+  return d;
+}
+
+int wrong_device(bg_ctx *c) {
+  int d = current_device();
+  if (d == c->dev) return 0;
+  c->err = "context was made on device " + std::to_string(c->dev) + ", device " +
+           std::to_string(d) + " is current";
+  return BG_ERR_STATE;
 }
 
 // Ordered shell quartets of the multi-centre build for one component class,
@@ -2496,17 +2574,15 @@ int compute_bounds(bg_ctx *c, cudaStream_t st) {
 
 int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                        const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
-                       cudaStream_t st, float4 *ddf, int sym = 0) {
+                       cudaStream_t st, float4 *ddf, int sym = 0, bool convert = true) {
   if (nq <= 0) return 0;
-  static bool attr_df = false;
   size_t smem = quartet_smem_df(sym ? 1 : 0);
-  if (!attr_df) {
-    CK(c, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)quartet_smem_df_max()));
-    attr_df = true;
-  }
   int n = c->ndim;
-  k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, ddf);
+  // convert = false: ddf already holds this density (one conversion per build)
+  if (convert) {
+    k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, ddf);
+    c->launches++;
+  }
   QArgsDF a;
   a.inst = nullptr;
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = ddf; a.Eci = c->d_Eci;
@@ -2515,7 +2591,7 @@ int launch_quartets_df(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   long long grid = std::min<long long>(nq, 152LL * 128);
   k_quartet_df<<<(unsigned)grid, DFTHREADS, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
-  c->launches += 2;
+  c->launches++;
   return 0;
 }
 
@@ -2546,9 +2622,36 @@ int launch_quartets_fp64(bg_ctx *c, const int *d_q, long long nq, int t1, int t2
                          const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
                          cudaStream_t st, int sym, double *bound);
 
-// FP64 or split-precision launch as the context's precision says
-// (BG_PREC_AUTO takes the split kernel here: explicit and streamed lists
-// are not tuned per class); bound mode is always FP64.
+// Tensor-core launch over list entries whose classes need at most n1 (D1)
+// and n2 (D2) TMEM columns (tcq::N1MAX, tcq::N2MAX cover every class).  The
+// double-float density copy ddf is made here unless convert is false.
+int launch_quartets_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
+                       const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
+                       cudaStream_t st, float4 *ddf, int sym, int n1, int n2,
+                       bool convert = true) {
+  if (nq <= 0) return 0;
+  int n = c->ndim;
+  if (convert) {
+    k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, ddf);
+    c->launches++;
+  }
+  TcGeom g = tc_geom(n1, n2);
+  tcq::Args a;
+  a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = ddf;
+  a.GD = d_GD; a.GX = d_GX; a.ldd = n; a.ldf = ldf; a.nskp = c->nskp;
+  a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym; a.inst = nullptr;
+  a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2;
+  long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
+  k_quartet_tc<<<(unsigned)grid, tcq::TCT, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  CK(c, cudaGetLastError());
+  c->launches++;
+  return 0;
+}
+
+// FP64, split-precision or tensor-core launch as the context's precision
+// says (BG_PREC_AUTO takes the split kernel here: explicit and streamed
+// lists are not tuned per class; the tensor-core kernel is sized for every
+// class); bound mode is always FP64.
 int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                     const double2 *d_D, int ldd, double *d_GD, double *d_GX,
                     int ldf, cudaStream_t st, int sym = 0, double *bound = nullptr) {
@@ -2556,6 +2659,9 @@ int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   if (c->prec != BG_PREC_FP64 && !bound) {
     int n = c->ndim;
     if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
+    if (c->prec == BG_PREC_TC32)
+      return launch_quartets_tc(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, c->d_Ddf, sym,
+                                tcq::N1MAX, tcq::N2MAX);
     return launch_quartets_df(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, c->d_Ddf, sym);
   }
   return launch_quartets_fp64(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, sym, bound);
@@ -2565,13 +2671,7 @@ int launch_quartets_fp64(bg_ctx *c, const int *d_q, long long nq, int t1, int t2
                          const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
                          cudaStream_t st, int sym, double *bound) {
   if (nq <= 0) return 0;
-  static bool attr = false;
   size_t smem = quartet_smem();
-
-  if (!attr) {
-    CK(c, cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
   QArgs a;
   a.inst = nullptr;
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_E; a.D = d_D;
@@ -2710,12 +2810,7 @@ int launch_breit(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const 
                  int ldd, double *d_BX, int ldf, cudaStream_t st, int dual,
                  double *bound = nullptr) {
   if (nq <= 0) return 0;
-  static bool attr = false;
   size_t smem = breit_smem();
-  if (!attr) {
-    CK(c, cudaFuncSetAttribute(k_breit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
   BArgs a;
   a.sh = c->d_sh; a.offq = c->d_offq; a.E = c->d_EB; a.D = d_D; a.BX = d_BX;
   a.Ecv = c->d_EBcv; a.Eci = c->d_EBci;
@@ -2761,90 +2856,227 @@ constexpr long long CHUNK_Q = 1LL << 23;  // 8M quartets, 128 MB per buffer (def
 
 // Autotuner of BG_PREC_AUTO.  A list sorted by angular class has segments
 // seg[i]..seg[i+1] of one class (l_a,l_b,l_c,l_d) each.  For every segment
-// of at least TUNE_MIN quartets the FP64 and the split-precision kernels
-// are timed on its first min(size, TUNE_SAMPLE) quartets (CUDA events on
-// `st`, the second of two runs, into scratch outputs) and the faster is
-// kept; smaller segments take the FP64 kernel (their cost is launch- and
-// latency-bound either way).  Neighbouring segments with the same choice
-// merge into one run, so a build issues one launch per run.
-// launch(df, start, count) issues one kernel over list entries
-// [start, start + count).
+// of at least TUNE_MIN quartets, each candidate kernel (FP64, the
+// double-float split path, the 3xTF32 tensor-core path) digests the first
+// min(size, TUNE_SAMPLE) quartets into zeroed scratch outputs; its energy
+// terms sum_ij Re D_ij G_ij (J and K) are compared with the FP64 kernel's,
+// and a second, event-timed run gives its time.  The sample's energy error
+// scaled by size/sample (a bound for errors of random sign) estimates the
+// segment's error.  Every segment first takes the faster of the two kernels
+// with FP64-level accuracy (FP64, split); then segments switch to the
+// tensor-core kernel in order of time saved per unit of estimated error
+// while the summed estimates stay within the error budget (Eh).  Smaller
+// segments take the FP64 kernel (launch- and latency-bound either way).
+// Neighbouring segments with the same choice merge into one run (tensor-core
+// runs only when they share a TMEM allocation size).
+// launch(kind, start, count, n1, n2) issues one kernel over list entries
+// [start, start + count); energy(eJ, eK) reduces the scratch outputs.
 constexpr long long TUNE_MIN = 2048, TUNE_SAMPLE = 16384;
 
-template <class Launch>
-int tune_runs(const std::vector<long long> &seg, cudaStream_t st, Launch &&launch,
+struct SegDims {
+  int n1, n2;
+};
+
+SegDims seg_dims(int key, int t1, int t2) {
+  int la = (key >> 6) & 3, lb = (key >> 4) & 3, lc = (key >> 2) & 3, ld = key & 3;
+  SegDims d;
+  bool swp;
+  tcq::tc_dims(la, lb, lc, ld, t1, t2, d.n1, d.n2, swp);
+  return d;
+}
+
+// Runs of one kernel kind over all segments (BG_PREC_TC32 on cached lists:
+// tensor-core runs sized per class).
+std::vector<Run> uniform_runs(const std::vector<long long> &seg, const std::vector<int> &key,
+                              int t1, int t2, int kind) {
+  std::vector<Run> runs;
+  for (size_t i = 0; i + 1 < seg.size(); ++i) {
+    long long n = seg[i + 1] - seg[i];
+    if (n <= 0) continue;
+    SegDims d = seg_dims(key[i], t1, t2);
+    if (!runs.empty() && runs.back().start + runs.back().count == seg[i] &&
+        (kind != KIND_TC || tc_geom(d.n1, d.n2).cols ==
+                                tc_geom(runs.back().n1, runs.back().n2).cols)) {
+      runs.back().count += n;
+      runs.back().n1 = std::max(runs.back().n1, d.n1);
+      runs.back().n2 = std::max(runs.back().n2, d.n2);
+    } else {
+      runs.push_back({seg[i], n, kind, d.n1, d.n2});
+    }
+  }
+  return runs;
+}
+
+struct SegTune {
+  long long start, n;
+  int n1, n2;
+  float t[3];     // ms on the sample per kind (0: untimed)
+  double err[3];  // estimated segment energy error per kind (Eh)
+  int kind;
+};
+
+template <class Launch, class Zero, class Energy>
+int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, int t1, int t2,
+              cudaStream_t st, double budget, Launch &&launch, Zero &&zero, Energy &&energy,
               std::vector<Run> &runs) {
   runs.clear();
   if (seg.size() < 2) return 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -1;
   int rc = 0;
+  std::vector<SegTune> tv;
   for (size_t i = 0; i + 1 < seg.size() && !rc; ++i) {
     long long n = seg[i + 1] - seg[i];
     if (n <= 0) continue;
-    int df = 0;
+    SegDims d = seg_dims(key[i], t1, t2);
+    SegTune x = {seg[i], n, d.n1, d.n2, {0.f, 0.f, 0.f}, {0.0, 0.0, 0.0}, KIND_FP64};
     if (n >= TUNE_MIN) {
       long long m = std::min(n, TUNE_SAMPLE);
-      float t[2] = {0.f, 0.f};
-      for (int k = 0; k < 2 && !rc; ++k)
-        for (int rep = 0; rep < 2 && !rc; ++rep) {
-          cudaEventRecord(e0, st);
-          rc = launch(k, seg[i], m);
-          cudaEventRecord(e1, st);
-          if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = -1;
-          if (!rc) cudaEventElapsedTime(&t[k], e0, e1);
-        }
-      df = t[1] < t[0];
+      double ej[3] = {0, 0, 0}, ek[3] = {0, 0, 0};
+      for (int k = 0; k < 3 && !rc; ++k) {
+        rc = zero();
+        if (!rc) rc = launch(k, seg[i], m, d.n1, d.n2);
+        if (!rc) rc = energy(ej[k], ek[k]);
+        if (rc) break;
+        cudaEventRecord(e0, st);
+        rc = launch(k, seg[i], m, d.n1, d.n2);
+        cudaEventRecord(e1, st);
+        if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = -1;
+        if (!rc) cudaEventElapsedTime(&x.t[k], e0, e1);
+      }
+      for (int k = 0; k < 3; ++k)
+        x.err[k] = (fabs(ej[k] - ej[0]) + fabs(ek[k] - ek[0])) * (double)n / (double)m;
+      x.kind = x.t[1] < x.t[0] ? KIND_DF32 : KIND_FP64;
     }
-    if (!runs.empty() && runs.back().df == df && runs.back().start + runs.back().count == seg[i])
-      runs.back().count += n;
-    else
-      runs.push_back({seg[i], n, df});
+    tv.push_back(x);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  return rc;
+  if (rc) return rc;
+  // tensor-core switches by time saved per error, within the budget
+  std::vector<int> cand;
+  for (size_t i = 0; i < tv.size(); ++i)
+    if (tv[i].n >= TUNE_MIN && tv[i].t[2] > 0.f && tv[i].t[2] < tv[i].t[tv[i].kind]) cand.push_back((int)i);
+  auto gain = [&](int i) {
+    const SegTune &x = tv[i];
+    double saved = (x.t[x.kind] - x.t[2]) * (double)x.n / (double)std::min(x.n, TUNE_SAMPLE);
+    return saved / (x.err[2] + 1e-300);
+  };
+  std::sort(cand.begin(), cand.end(), [&](int a, int b) { return gain(a) > gain(b); });
+  double used = 0.0;
+  for (int i : cand)
+    if (used + tv[i].err[2] <= budget) {
+      used += tv[i].err[2];
+      tv[i].kind = KIND_TC;
+    }
+  for (const SegTune &x : tv) {
+    if (!runs.empty() && runs.back().kind == x.kind &&
+        runs.back().start + runs.back().count == x.start &&
+        (x.kind != KIND_TC ||
+         tc_geom(x.n1, x.n2).cols == tc_geom(runs.back().n1, runs.back().n2).cols)) {
+      runs.back().count += x.n;
+      runs.back().n1 = std::max(runs.back().n1, x.n1);
+      runs.back().n2 = std::max(runs.back().n2, x.n2);
+    } else {
+      runs.push_back({x.start, x.n, x.kind, x.n1, x.n2});
+    }
+  }
+  return 0;
 }
 
 // Angular-class segment boundaries of a quartet list (entries grouped by
-// class): start of every class, then the list size.
+// class): start of every class, then the list size; keys[i] is segment i's
+// class (l_a,l_b,l_c,l_d) in base 4.
 std::vector<long long> class_segments(const std::vector<Shell> &sh, const std::vector<int> &q,
-                                      int sbase = 0) {
+                                      std::vector<int> &keys, int sbase = 0) {
   std::vector<long long> seg;
+  keys.clear();
   long long n = (long long)q.size() / 4;
   int last = -1;
   for (long long i = 0; i < n; ++i) {
     const int *e = &q[4 * i];
     int key = ((sh[e[0] - sbase].l * 4 + sh[e[1] - sbase].l) * 4 + sh[e[2] - sbase].l) * 4 +
               sh[e[3] - sbase].l;
-    if (key != last) { seg.push_back(i); last = key; }
+    if (key != last) { seg.push_back(i); keys.push_back(key); last = key; }
   }
   seg.push_back(n);
   return seg;
+}
+
+// sum_ij Re(D_ij G_ij) over an n x n block (leading dimensions ldd, ldg) or,
+// with inst, over every instance's block; added to *out.
+__global__ void k_edot(const double2 *D, long long ldd, const double2 *G, long long ldg, int n,
+                       const Inst *inst, const int *ndim, int ninst, double *out) {
+  double acc = 0.0;
+  for (int k = 0; k < ninst; ++k) {
+    const double2 *Dk = D, *Gk = G;
+    long long m = n, ld1 = ldd, ld2 = ldg;
+    if (inst) {
+      Dk = D + inst[k].off;
+      Gk = G + inst[k].off;
+      m = ndim[k];
+      ld1 = ld2 = inst[k].ld;
+    }
+    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < m * m;
+         w += (long long)gridDim.x * blockDim.x) {
+      long long i = w % m, j = w / m;
+      double2 d = Dk[i + ld1 * j], g = Gk[i + ld2 * j];
+      acc += d.x * g.x - d.y * g.y;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
 }
 
 // Tunes the cached lists of a context (first BG_PREC_AUTO build after the
 // lists were made), with scratch outputs of NDIM^2.
 int tune_ctx(bg_ctx *c, const double2 *d_D, int ldd, cudaStream_t st) {
   int n = c->ndim;
-  double *gd = nullptr, *gx = nullptr;
+  double *gd = nullptr, *gx = nullptr, *d_e = nullptr;
   CK(c, cudaMalloc(&gd, sizeof(double2) * (size_t)n * n));
   CK(c, cudaMalloc(&gx, sizeof(double2) * (size_t)n * n));
+  CK(c, cudaMalloc(&d_e, sizeof(double) * 2));
   if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
+  k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, c->d_Ddf);
   int rc = 0;
+  auto zero = [&]() {
+    if (cudaMemsetAsync(gd, 0, sizeof(double2) * (size_t)n * n, st) != cudaSuccess ||
+        cudaMemsetAsync(gx, 0, sizeof(double2) * (size_t)n * n, st) != cudaSuccess)
+      return -1;
+    return 0;
+  };
+  auto energy = [&](double &ej, double &ek) {
+    if (cudaMemsetAsync(d_e, 0, sizeof(double) * 2, st) != cudaSuccess) return -1;
+    k_edot<<<256, 256, 0, st>>>(d_D, ldd, (const double2 *)gd, n, n, nullptr, nullptr, 1, d_e);
+    k_edot<<<256, 256, 0, st>>>(d_D, ldd, (const double2 *)gx, n, n, nullptr, nullptr, 1, d_e + 1);
+    double h[2];
+    if (cudaMemcpyAsync(h, d_e, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return -1;
+    ej = h[0];
+    ek = h[1];
+    return 0;
+  };
   for (int t1 = 0; t1 < c->ncomp && !rc; ++t1)
     for (int t2 = 0; t2 < c->ncomp && !rc; ++t2) {
       int k = 2 * t1 + t2;
       const int *q = c->d_quart[k];
-      rc = tune_runs(c->seg[k], st, [&](int df, long long start, long long m) {
-        return df ? launch_quartets_df(c, q + 4 * start, m, t1, t2, d_D, ldd, gd, gx, n, st,
-                                       c->d_Ddf, 2)
-                  : launch_quartets_fp64(c, q + 4 * start, m, t1, t2, d_D, ldd, gd, gx, n, st,
-                                         2, nullptr);
-      }, c->runs[k]);
+      // the budget is shared by the component classes
+      double budget = c->err_budget / (c->ncomp * c->ncomp);
+      rc = tune_runs(c->seg[k], c->segkey[k], t1, t2, st, budget,
+                     [&](int kind, long long start, long long m, int n1, int n2) {
+        const int *qq = q + 4 * start;
+        if (kind == KIND_DF32)
+          return launch_quartets_df(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, c->d_Ddf, 2, false);
+        if (kind == KIND_TC)
+          return launch_quartets_tc(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, c->d_Ddf, 2, n1, n2,
+                                    false);
+        return launch_quartets_fp64(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, 2, nullptr);
+      }, zero, energy, c->runs[k]);
     }
   cudaFree(gd);
   cudaFree(gx);
+  cudaFree(d_e);
   if (rc) return rc > 0 ? rc : cuda_fail(c, cudaGetLastError(), "autotuning");
   c->tuned = true;
   return 0;
@@ -2932,6 +3164,7 @@ int batch_lists(bg_batch *b, int ilev) {
       int k = 2 * t1 + t2;
       b->nquart[k] = (long long)tot / 4;
       b->seg[k].clear();
+      b->segkey[k].clear();
       b->runs[k].clear();
       if (!tot) continue;
       BK(b, cudaMalloc(&b->d_quart[k], sizeof(int) * tot));
@@ -2939,6 +3172,7 @@ int batch_lists(bg_batch *b, int ilev) {
       for (auto &v : bucket) {
         if (v.empty()) continue;
         b->seg[k].push_back((long long)pos / 4);  // one angular class per bucket
+        b->segkey[k].push_back(NKEY - 1 - (int)(&v - &bucket[0]));
         BK(b, cudaMemcpy(b->d_quart[k] + pos, v.data(), sizeof(int) * v.size(),
                          cudaMemcpyHostToDevice));
         pos += v.size();
@@ -2951,34 +3185,33 @@ int batch_lists(bg_batch *b, int ilev) {
   return 0;
 }
 
-// One launch of the FP64 (df = 0) or split-precision (df = 1) quartet
-// kernel over entries [start, start + nq) of a batch's list of one
-// component class, both orders of each listed quartet digested.
-int batch_launch(bg_batch *b, int t1, int t2, int df, long long start, long long nq,
-                 const double2 *d_D, double *d_GD, double *d_GX, cudaStream_t st) {
+// One launch of the FP64, split-precision or tensor-core quartet kernel
+// (KIND_*) over entries [start, start + nq) of a batch's list of one
+// component class, both orders of each listed quartet digested; n1, n2 size
+// the tensor-core launch.
+int batch_launch(bg_batch *b, int t1, int t2, int kind, long long start, long long nq,
+                 const double2 *d_D, double *d_GD, double *d_GX, cudaStream_t st, int n1 = 0,
+                 int n2 = 0) {
   int k = 2 * t1 + t2;
   if (nq <= 0) return 0;
   const int4 *quart = (const int4 *)b->d_quart[k] + start;
-  if (df) {
-    static bool attr_df = false;  // set once: no attribute call inside a graph capture
-    if (!attr_df) {
-      BK(b, cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)quartet_smem_df_max()));
-      attr_df = true;
-    }
+  if (kind == KIND_DF32) {
     QArgsDF a;
     a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_Edf; a.D = b->d_Ddf; a.Eci = b->d_Eci;
     a.GD = d_GD; a.GX = d_GX; a.ns = 0; a.ldd = 0; a.ldf = 0; a.nskp = 0;
     a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.inst = b->d_inst;
     long long grid = std::min<long long>(nq, 152LL * 128);
     k_quartet_df<<<(unsigned)grid, DFTHREADS, quartet_smem_df(1), st>>>(a, quart, nq, t1, t2);
+  } else if (kind == KIND_TC) {
+    TcGeom g = tc_geom(n1, n2);
+    tcq::Args a;
+    a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_Edf; a.D = b->d_Ddf;
+    a.GD = d_GD; a.GX = d_GX; a.ldd = 0; a.ldf = 0; a.nskp = 0;
+    a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.inst = b->d_inst;
+    a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2;
+    long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
+    k_quartet_tc<<<(unsigned)grid, tcq::TCT, g.smem, st>>>(a, quart, nq, t1, t2);
   } else {
-    static bool attr = false;
-    if (!attr) {
-      BK(b, cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)quartet_smem()));
-      attr = true;
-    }
     QArgs a;
     a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_E; a.D = d_D; a.Ecv = b->d_Ecv; a.Eci = b->d_Eci;
     a.GD = d_GD; a.GX = d_GX; a.ns = 0; a.ldd = 0; a.ldf = 0; a.nskp = 0;
@@ -3074,8 +3307,12 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
     c->shells[a].inst = 0;
     c->shells[a].prow = a * c->ns;
   }
-  if (upload_tables()) { g_init_err = "constant table upload failed"; delete c; return BG_ERR_CUDA; }
-  k_boys_table<<<(NBGRID + 127) / 128, 128>>>();
+  c->dev = current_device();
+  if (device_setup(c->dev)) {
+    g_init_err = "device set-up failed (constant tables, Boys table, kernel attributes)";
+    delete c;
+    return BG_ERR_CUDA;
+  }
   // E-coefficient storage for every ordered shell pair and component
   int ns = c->ns, ncomp = c->ncomp;
   std::vector<PairE> pe((size_t)ns * ns);
@@ -3175,7 +3412,9 @@ int bertha_gpu_set_screening(bg_ctx *c, double threshold) {
 
 int bertha_gpu_set_precision(bg_ctx *c, int prec) {
   if (!c) return BG_ERR_ARG;
-  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32 && prec != BG_PREC_AUTO) return BG_ERR_ARG;
+  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32 && prec != BG_PREC_AUTO &&
+      prec != BG_PREC_TC32)
+    return BG_ERR_ARG;
   if (prec != c->prec) c->tuned = false;
   c->prec = prec;
   return BG_OK;
@@ -3217,30 +3456,71 @@ int bertha_gpu_layout(const bg_ctx *c, int *lrge) {
 long long bertha_gpu_launches(const bg_ctx *c) { return c ? c->launches : 0; }
 
 namespace {
-void auto_stats(const std::vector<Run> (&runs)[4], long long *nf, long long *nd, int *nr) {
-  long long f = 0, d = 0;
+void auto_stats(const std::vector<Run> (&runs)[4], long long *nq, int *nr) {
+  nq[0] = nq[1] = nq[2] = 0;
   int r = 0;
   for (int k = 0; k < 4; ++k)
     for (const Run &x : runs[k]) {
-      (x.df ? d : f) += x.count;
+      nq[x.kind] += x.count;
       ++r;
     }
-  if (nf) *nf = f;
-  if (nd) *nd = d;
   if (nr) *nr = r;
 }
 }  // namespace
 
 int bertha_gpu_auto_stats(const bg_ctx *c, long long *nq_fp64, long long *nq_df32, int *nruns) {
   if (!c) return BG_ERR_ARG;
-  auto_stats(c->runs, nq_fp64, nq_df32, nruns);
+  long long nq[3];
+  auto_stats(c->runs, nq, nruns);
+  if (nq_fp64) *nq_fp64 = nq[0];
+  if (nq_df32) *nq_df32 = nq[1];
+  return BG_OK;
+}
+
+int bertha_gpu_kernel_stats(const bg_ctx *c, long long *nq, int *nruns) {
+  if (!c || !nq) return BG_ERR_ARG;
+  auto_stats(c->runs, nq, nruns);
   return BG_OK;
 }
 
 int bertha_gpu_batch_auto_stats(const bg_batch *b, long long *nq_fp64, long long *nq_df32,
                                 int *nruns) {
   if (!b) return BG_ERR_ARG;
-  auto_stats(b->runs, nq_fp64, nq_df32, nruns);
+  long long nq[3];
+  auto_stats(b->runs, nq, nruns);
+  if (nq_fp64) *nq_fp64 = nq[0];
+  if (nq_df32) *nq_df32 = nq[1];
+  return BG_OK;
+}
+
+int bertha_gpu_batch_kernel_stats(const bg_batch *b, long long *nq, int *nruns) {
+  if (!b || !nq) return BG_ERR_ARG;
+  auto_stats(b->runs, nq, nruns);
+  return BG_OK;
+}
+
+int bertha_gpu_set_error_budget(bg_ctx *c, double eh) {
+  if (!c || !(eh >= 0.0)) return BG_ERR_ARG;
+  if (eh != c->err_budget) c->tuned = false;
+  c->err_budget = eh;
+  return BG_OK;
+}
+
+int bertha_gpu_batch_set_error_budget(bg_batch *b, double eh) {
+  if (!b || !(eh >= 0.0)) return BG_ERR_ARG;
+  if (eh != b->err_budget) b->tuned = false;
+  b->err_budget = eh;
+  return BG_OK;
+}
+
+int bertha_gpu_device_status(int *status) {
+  if (!status) return BG_ERR_ARG;
+  int v = 0;
+  if (cudaDeviceSynchronize() != cudaSuccess) return BG_ERR_CUDA;
+  if (cudaMemcpyFromSymbol(&v, tcq::g_tc_status, sizeof(int)) != cudaSuccess) return BG_ERR_CUDA;
+  int z = 0;
+  if (cudaMemcpyToSymbol(tcq::g_tc_status, &z, sizeof(int)) != cudaSuccess) return BG_ERR_CUDA;
+  *status = v;
   return BG_OK;
 }
 
@@ -3253,10 +3533,56 @@ int bertha_gpu_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                         int ldf, void *stream) {
   if (!c) return BG_ERR_ARG;
   if (c->bad) return BG_ERR_STATE;
-  if (t1 < 0 || t1 >= c->ncomp || t2 < 0 || t2 >= c->ncomp || nq < 0) return BG_ERR_ARG;
+  if (int rd = wrong_device(c)) return rd;
+  if (t1 < 0 || t1 >= c->ncomp || t2 < 0 || t2 >= c->ncomp || nq < 0 || ldd < c->ndim ||
+      ldf < c->ndim || (nq > 0 && (!d_q || !d_dent || !d_gdir || !d_gxch)))
+    return BG_ERR_ARG;
   c->launches = 0;
   return launch_quartets(c, d_q, nq, t1, t2, (const double2 *)d_dent, ldd, d_gdir, d_gxch,
                          ldf, (cudaStream_t)stream);
+}
+
+int bertha_gpu_quartets_segments(bg_ctx *c, const int *d_q, int nseg, const long long *seg,
+                                 const int *lclass, int t1, int t2, const double *d_dent,
+                                 int ldd, double *d_gdir, double *d_gxch, int ldf, void *stream) {
+  if (!c) return BG_ERR_ARG;
+  if (c->bad) return BG_ERR_STATE;
+  if (int rd = wrong_device(c)) return rd;
+  if (t1 < 0 || t1 >= c->ncomp || t2 < 0 || t2 >= c->ncomp || nseg < 0 || !seg || !lclass ||
+      ldd < c->ndim || ldf < c->ndim)
+    return BG_ERR_ARG;
+  std::vector<long long> sv(seg, seg + nseg + 1);
+  std::vector<int> keys(nseg);
+  for (int i = 0; i < nseg; ++i) {
+    if (sv[i] < 0 || sv[i + 1] < sv[i]) return BG_ERR_ARG;
+    int key = 0;
+    for (int j = 0; j < 4; ++j) {
+      int l = lclass[4 * i + j];
+      if (l < 0 || l > MAXLB) return BG_ERR_ARG;
+      key = key * 4 + l;
+    }
+    keys[i] = key;
+  }
+  long long nq = nseg ? sv[nseg] - sv[0] : 0;
+  if (nq > 0 && (!d_q || !d_dent || !d_gdir || !d_gxch)) return BG_ERR_ARG;
+  c->launches = 0;
+  if (nq <= 0) return BG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const double2 *D = (const double2 *)d_dent;
+  if (c->prec != BG_PREC_TC32)
+    return launch_quartets(c, d_q + 4 * sv[0], nq, t1, t2, D, ldd, d_gdir, d_gxch, ldf, st);
+  // tensor cores: launches sized per class (runs of classes sharing a TMEM
+  // allocation size); one double-float density copy for all of them
+  int n = c->ndim;
+  if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
+  k_dconv<<<1024, 256, 0, st>>>(D, ldd, n, c->d_Ddf);
+  c->launches++;
+  for (const Run &r : uniform_runs(sv, keys, t1, t2, KIND_TC)) {
+    int rc = launch_quartets_tc(c, d_q + 4 * r.start, r.count, t1, t2, D, ldd, d_gdir, d_gxch,
+                                ldf, st, c->d_Ddf, 0, r.n1, r.n2, false);
+    if (rc) return rc;
+  }
+  return BG_OK;
 }
 
 int bertha_gpu_quartets_noalloc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
@@ -3264,7 +3590,9 @@ int bertha_gpu_quartets_noalloc(bg_ctx *c, const int *d_q, long long nq, int t1,
                                 double *d_gxch, int ldf, void *stream) {
   if (!c) return BG_ERR_ARG;
   if (c->bad) return BG_ERR_STATE;
-  if (t1 < 0 || t1 >= c->ncomp || t2 < 0 || t2 >= c->ncomp || nq < 0 || ldd < c->ndim)
+  if (int rd = wrong_device(c)) return rd;
+  if (t1 < 0 || t1 >= c->ncomp || t2 < 0 || t2 >= c->ncomp || nq < 0 || ldd < c->ndim ||
+      ldf < c->ndim || (nq > 0 && (!d_q || !d_dent || !d_gdir || !d_gxch)))
     return BG_ERR_ARG;
   if (c->ndim > BG_NOALLOC_MAX_NDIM) {
     c->err = "bertha_gpu_quartets_noalloc: NDIM " + std::to_string(c->ndim) +
@@ -3283,6 +3611,7 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
                               double *d_gdir, double *d_gxch, int ldf, void *stream) {
   if (!c) return BG_ERR_ARG;
   if (c->bad) return BG_ERR_STATE;
+  if (int rd = wrong_device(c)) return rd;
   if (ilev < 1 || ilev > 4 || ldd < c->ndim || ldf < c->ndim) return BG_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   c->launches = 0;
@@ -3316,7 +3645,7 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
     c->tuned = false;
     if (!c->stream_lists)
       for (int k = 0; k < 4; ++k) {
-        c->seg[k] = class_segments(c->shells, q[k]);
+        c->seg[k] = class_segments(c->shells, q[k], c->segkey[k]);
         c->runs[k].clear();
         c->nquart[k] = (long long)q[k].size() / 4;
         if (!q[k].empty()) {
@@ -3327,23 +3656,53 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
       }
     c->quart_ilev = ilev;
   }
-  bool autoprec = c->prec == BG_PREC_AUTO && !c->stream_lists;
-  if (autoprec && !c->tuned) {
-    int rc = tune_ctx(c, (const double2 *)d_dent, ldd, st);
-    if (rc) return rc;
+  // per-run kernels: tuned (BG_PREC_AUTO) or the tensor-core kernel sized
+  // per class (BG_PREC_TC32) on cached lists
+  bool byrun = (c->prec == BG_PREC_AUTO || c->prec == BG_PREC_TC32) && !c->stream_lists;
+  if (byrun && !c->tuned) {
+    if (c->prec == BG_PREC_AUTO) {
+      int rc = tune_ctx(c, (const double2 *)d_dent, ldd, st);
+      if (rc) return rc;
+    } else {
+      for (int t1 = 0; t1 < c->ncomp; ++t1)
+        for (int t2 = 0; t2 < c->ncomp; ++t2) {
+          int k = 2 * t1 + t2;
+          c->runs[k] = uniform_runs(c->seg[k], c->segkey[k], t1, t2, KIND_TC);
+        }
+      c->tuned = true;
+    }
+  }
+  if (byrun) {
+    // one double-float copy of the density for all split-precision and
+    // tensor-core runs
+    bool any_f = false;
+    for (int k = 0; k < 4; ++k)
+      for (const Run &r : c->runs[k]) any_f |= r.kind != KIND_FP64;
+    if (any_f) {
+      if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)c->ndim * c->ndim));
+      k_dconv<<<1024, 256, 0, st>>>((const double2 *)d_dent, ldd, c->ndim, c->d_Ddf);
+      CK(c, cudaGetLastError());
+      c->launches++;
+    }
   }
   for (int t1 = c->ncomp - 1; t1 >= 0; --t1)
     for (int t2 = c->ncomp - 1; t2 >= 0; --t2) {
       int k = 2 * t1 + t2, rc = 0;
       if (c->stream_lists)
         rc = stream_class(c, t1, t2, ilev, (const double2 *)d_dent, ldd, d_gdir, d_gxch, ldf, st);
-      else if (autoprec)
+      else if (byrun)
         for (const Run &r : c->runs[k]) {
           const int *q = c->d_quart[k] + 4 * r.start;
-          rc = r.df ? launch_quartets_df(c, q, r.count, t1, t2, (const double2 *)d_dent, ldd,
-                                         d_gdir, d_gxch, ldf, st, c->d_Ddf, 2)
-                    : launch_quartets_fp64(c, q, r.count, t1, t2, (const double2 *)d_dent, ldd,
-                                           d_gdir, d_gxch, ldf, st, 2, nullptr);
+          const double2 *D = (const double2 *)d_dent;
+          if (r.kind == KIND_DF32)
+            rc = launch_quartets_df(c, q, r.count, t1, t2, D, ldd, d_gdir, d_gxch, ldf, st,
+                                    c->d_Ddf, 2, false);
+          else if (r.kind == KIND_TC)
+            rc = launch_quartets_tc(c, q, r.count, t1, t2, D, ldd, d_gdir, d_gxch, ldf, st,
+                                    c->d_Ddf, 2, r.n1, r.n2, false);
+          else
+            rc = launch_quartets_fp64(c, q, r.count, t1, t2, D, ldd, d_gdir, d_gxch, ldf, st, 2,
+                                      nullptr);
           if (rc) break;
         }
       else
@@ -3364,6 +3723,7 @@ int bertha_gpu_clmfast(bg_ctx *c, const double *dent, int ldd, int ilev, double 
                        double *gxch, int ldf) {
   if (!c || !dent || !gdir || !gxch) return BG_ERR_ARG;
   if (c->bad) return BG_ERR_STATE;
+  if (int rd = wrong_device(c)) return rd;
   if (ilev < 1 || ilev > 4 || ldd < c->ndim || ldf < c->ndim) return BG_ERR_ARG;
   if (c->hmlt == BG_HMLT_BARE) return BG_OK;
   int n = c->ndim;
@@ -3389,6 +3749,7 @@ int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
                               double *d_bxch, int ldf, void *stream) {
   if (!c) return BG_ERR_ARG;
   if (c->bad) return BG_ERR_STATE;
+  if (int rd = wrong_device(c)) return rd;
   if (ilev < 1 || ilev > 4 || ldd < c->ndim || ldf < c->ndim) return BG_ERR_ARG;
   if (c->hmlt == BG_HMLT_NORL || c->hmlt == BG_HMLT_BARE) {
     c->err = "bertha_gpu_brtfast: the Breit interaction needs a four-component Hamiltonian";
@@ -3441,6 +3802,7 @@ int bertha_gpu_brtfast(bg_ctx *c, const double *dent, int ldd, int ilev, double 
                        int ldf) {
   if (!c || !dent || !bxch) return BG_ERR_ARG;
   if (c->bad) return BG_ERR_STATE;
+  if (int rd = wrong_device(c)) return rd;
   if (ilev < 1 || ilev > 4 || ldd < c->ndim || ldf < c->ndim) return BG_ERR_ARG;
   if (c->hmlt == BG_HMLT_NORL || c->hmlt == BG_HMLT_BARE) {
     c->err = "bertha_gpu_brtfast: the Breit interaction needs a four-component Hamiltonian";
@@ -3468,6 +3830,7 @@ int bertha_gpu_oneel_device(bg_ctx *c, const double *znuc, const double *xi, dou
                              double *d_hnuc, double *d_hkin, int ldf, void *stream) {
   if (!c || !znuc || !xi || !d_ovlp || !d_hnuc || !d_hkin) return BG_ERR_ARG;
   if (c->bad) return BG_ERR_STATE;
+  if (int rd = wrong_device(c)) return rd;
   if (ldf < c->ndim) return BG_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   std::vector<double> nuc((size_t)c->ncnt * 5);
@@ -3499,6 +3862,7 @@ int bertha_gpu_oneel(bg_ctx *c, const double *znuc, const double *xi, double *ov
                      double *hnuc, double *hkin, int ldf) {
   if (!c || !ovlp || !hnuc || !hkin) return BG_ERR_ARG;
   if (c->bad) return BG_ERR_STATE;
+  if (int rd = wrong_device(c)) return rd;
   if (ldf < c->ndim) return BG_ERR_ARG;
   int n = c->ndim;
   size_t bytes = sizeof(double2) * (size_t)n * n;
@@ -3557,6 +3921,10 @@ int bertha_gpu_batch_create(bg_batch **out, int n, bg_ctx *const *ctxs,
     if (!ctxs[i]) { g_init_err = "null context"; return BG_ERR_ARG; }
     if (ctxs[i]->bad) { g_init_err = "context failed earlier"; return BG_ERR_STATE; }
     const bg_ctx *c = ctxs[i], *c0 = ctxs[0];
+    if (c->dev != c0->dev || c->dev != current_device()) {
+      g_init_err = "batched instances must live on the current device";
+      return BG_ERR_STATE;
+    }
     if (c->hmlt != c0->hmlt || c->isym != c0->isym || c->racah1 != c0->racah1) {
       g_init_err = "batched instances must share hmlt, shape and the RACAH1 flag";
       return BG_ERR_ARG;
@@ -3570,9 +3938,10 @@ int bertha_gpu_batch_create(bg_batch **out, int n, bg_ctx *const *ctxs,
     }
   }
   bg_batch *b = new bg_batch();
+  b->dev = ctxs[0]->dev;
   b->n = n;
   b->ncomp = ctxs[0]->ncomp; b->hmlt = ctxs[0]->hmlt; b->isym = ctxs[0]->isym;
-  b->racah1 = ctxs[0]->racah1; b->prec = ctxs[0]->prec;
+  b->racah1 = ctxs[0]->racah1; b->prec = ctxs[0]->prec; b->err_budget = ctxs[0]->err_budget;
   std::vector<long long> pbase(n), ebase(n);
   long long nst = 0, npt = 0, net = 0, packed = 0;
   std::vector<Shell> sh;
@@ -3658,7 +4027,9 @@ int bertha_gpu_batch_create(bg_batch **out, int n, bg_ctx *const *ctxs,
 
 int bertha_gpu_batch_set_precision(bg_batch *b, int prec) {
   if (!b) return BG_ERR_ARG;
-  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32 && prec != BG_PREC_AUTO) return BG_ERR_ARG;
+  if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32 && prec != BG_PREC_AUTO &&
+      prec != BG_PREC_TC32)
+    return BG_ERR_ARG;
   if (prec != b->prec) b->tuned = false;
   b->prec = prec;
   return BG_OK;
@@ -3668,6 +4039,10 @@ int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
                                     double *d_gxch, void *stream) {
   if (!b) return BG_ERR_ARG;
   if (b->bad) return BG_ERR_STATE;
+  if (current_device() != b->dev) {
+    b->err = "batch was made on device " + std::to_string(b->dev) + ", another device is current";
+    return BG_ERR_STATE;
+  }
   if (ilev < 1 || ilev > 4 || !d_dent || !d_gdir || !d_gxch) return BG_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   b->launches = 0;
@@ -3689,35 +4064,68 @@ int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
   }
   const double2 *D = (const double2 *)d_dent;
   if (b->prec == BG_PREC_AUTO && !b->tuned) {
-    // kernel choice per angular class, timed into scratch outputs
-    double *gd = nullptr, *gx = nullptr;
+    // kernel choice per angular class, timed and checked into scratch outputs
+    double *gd = nullptr, *gx = nullptr, *d_e = nullptr;
     size_t bytes = sizeof(double2) * std::max<long long>(b->span, 1);
     BK(b, cudaMalloc(&gd, bytes));
     BK(b, cudaMalloc(&gx, bytes));
+    BK(b, cudaMalloc(&d_e, 2 * sizeof(double)));
+    auto zero = [&]() {
+      if (cudaMemsetAsync(gd, 0, bytes, st) != cudaSuccess ||
+          cudaMemsetAsync(gx, 0, bytes, st) != cudaSuccess)
+        return -1;
+      return 0;
+    };
+    auto energy = [&](double &ej, double &ek) {
+      if (cudaMemsetAsync(d_e, 0, 2 * sizeof(double), st) != cudaSuccess) return -1;
+      k_edot<<<256, 256, 0, st>>>(D, 0, (const double2 *)gd, 0, 0, b->d_inst, b->d_ndim, b->n,
+                                  d_e);
+      k_edot<<<256, 256, 0, st>>>(D, 0, (const double2 *)gx, 0, 0, b->d_inst, b->d_ndim, b->n,
+                                  d_e + 1);
+      double h[2];
+      if (cudaMemcpyAsync(h, d_e, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return -1;
+      ej = h[0];
+      ek = h[1];
+      return 0;
+    };
     int rc = 0;
     for (int t1 = 0; t1 < b->ncomp && !rc; ++t1)
       for (int t2 = 0; t2 < b->ncomp && !rc; ++t2) {
         int k = 2 * t1 + t2;
-        rc = tune_runs(b->seg[k], st, [&](int df, long long start, long long m) {
-          return batch_launch(b, t1, t2, df, start, m, D, gd, gx, st);
-        }, b->runs[k]);
+        double budget = b->err_budget / (b->ncomp * b->ncomp);
+        rc = tune_runs(b->seg[k], b->segkey[k], t1, t2, st, budget,
+                       [&](int kind, long long start, long long m, int n1, int n2) {
+          return batch_launch(b, t1, t2, kind, start, m, D, gd, gx, st, n1, n2);
+        }, zero, energy, b->runs[k]);
       }
     cudaFree(gd);
     cudaFree(gx);
+    cudaFree(d_e);
     if (rc) return rc > 0 ? rc : batch_fail(b, cudaGetLastError(), "autotuning");
+    b->tuned = true;
+  }
+  if (b->prec == BG_PREC_TC32 && !b->tuned) {
+    for (int t1 = 0; t1 < b->ncomp; ++t1)
+      for (int t2 = 0; t2 < b->ncomp; ++t2) {
+        int k = 2 * t1 + t2;
+        b->runs[k] = uniform_runs(b->seg[k], b->segkey[k], t1, t2, KIND_TC);
+      }
     b->tuned = true;
   }
   for (int t1 = b->ncomp - 1; t1 >= 0; --t1)
     for (int t2 = b->ncomp - 1; t2 >= 0; --t2) {
       int k = 2 * t1 + t2, rc = 0;
-      if (b->prec == BG_PREC_AUTO)
+      if (b->prec == BG_PREC_AUTO || b->prec == BG_PREC_TC32)
         for (const Run &r : b->runs[k]) {
-          rc = batch_launch(b, t1, t2, r.df, r.start, r.count, D, d_gdir, d_gxch, st);
+          rc = batch_launch(b, t1, t2, r.kind, r.start, r.count, D, d_gdir, d_gxch, st, r.n1,
+                            r.n2);
           if (rc) break;
         }
       else
-        rc = batch_launch(b, t1, t2, b->prec == BG_PREC_DF32, 0, b->nquart[k], D, d_gdir,
-                          d_gxch, st);
+        rc = batch_launch(b, t1, t2, b->prec == BG_PREC_DF32 ? KIND_DF32 : KIND_FP64, 0,
+                          b->nquart[k], D, d_gdir, d_gxch, st);
       if (rc) return rc;
     }
   k_herm_complete<<<dim3(gx, 16), 256, 0, st>>>((double2 *)d_gdir, 0, 0, b->d_inst, b->d_ndim,

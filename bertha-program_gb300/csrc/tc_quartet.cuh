@@ -1,0 +1,632 @@
+// Tensor-core quartet kernel: the two Hermite contractions of ERIFAST
+// (bertha-scf.f:12676-12799 first, :12802-13126 second) as GEMMs on the
+// 5th-generation tensor cores (tcgen05.mma kind::tf32, accumulators in
+// tensor memory), each product in three TF32 passes hi*hi + hi*lo + lo*hi
+// (3xTF32, about 22 significant bits per operand, FP32 accumulation).
+// Boys values and the R recursion stay FP64 (as in k_quartet_df), the
+// per-quartet J/K sums are FP32 and every J/K element is accumulated in FP64
+// in global memory.  Included inside the anonymous namespace of
+// bertha_gpu.cu.
+//
+// One 128-thread CTA per shell quartet (grid-stride).  With the left pair
+// (labels L, Hermite terms s) and the right pair (labels R, terms q):
+//   GEMM 1  D1[row][q]   = sum_s  E_L[row][s] * R[s+q]        rows (L, set, re/im)
+//   GEMM 2  D2[row][col] = sum_q  G[row][q] * E_R[col][q]     cols (R, set, re/im)
+// with G = D1 times (-1)^|q| and the exponent balancing of the split path.
+// M = 128 rows per tile (32 left labels), K in chunks of 32, B operands K-major.
+// D2 holds, per label pair, the 16 real products that ERIFAST's second
+// contraction forms (:12809-13119); the 16 m-sign combinations and the
+// CLMMTG/CLMMTZ digestion (batch types 1 and 5) follow in FP32.
+
+namespace tcq {
+
+constexpr int TCT = 128;        // threads per CTA (4 warps, one per TMEM lane quarter)
+constexpr int KC = 32;          // K elements per staged chunk (4 MMAs of K = 8)
+constexpr int MROWS = 128;      // rows per M tile
+constexpr int MLAB = MROWS / 4; // left labels per M tile
+constexpr int N1MAX = 192;      // roundup(165, 32): R columns of the right pair
+constexpr int N2MAX = 208;      // roundup(4 * 49, 16): E columns of the right pair
+constexpr int PSTR = 65;        // row stride (floats) of the D2 slab in shared memory
+constexpr int SLAB = 64;        // D2 columns per epilogue slab (16 right labels)
+constexpr long long WAIT_LIMIT = 1LL << 24;  // mbarrier polls before giving up
+
+__device__ int g_tc_status;  // nonzero: a tensor-core wait timed out or a class did not fit
+
+__device__ __forceinline__ uint32_t saddr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor of a K-major operand without swizzling:
+// core matrices of 8 rows x 16 bytes, stored contiguously (128 B); the two
+// core matrices of one MMA's K = 8 extent 128 B apart (leading byte offset),
+// 8-row groups 1024 B apart (stride byte offset: a 32-element chunk holds 8
+// core matrices per row group); bits 46-48 carry the fixed value 0b001.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) |
+         ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor, kind::tf32: FP32 accumulator, TF32 A and B,
+// both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__device__ __forceinline__ uint32_t idesc(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+// Float offset of element (row, k) of a staged K chunk: [row/8][k/4][row%8][k%4].
+__device__ __forceinline__ int kmaj(int row, int k) {
+  return (((row >> 3) * (KC / 4) + (k >> 2)) * 8 + (row & 7)) * 4 + (k & 3);
+}
+
+// x = hi + lo with hi carrying the 10 explicit mantissa bits a TF32 operand
+// keeps; the tensor core reads lo as TF32 again, ~22 bits in all.
+__device__ __forceinline__ void tsplit(float x, float &h, float &l) {
+  h = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+  l = x - h;
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id,
+                                    uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred pa;\n\t"
+      "setp.ne.b32 pa, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, pa;\n\t}"
+      :: "r"(d), "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+
+__device__ __forceinline__ void commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               :: "r"(saddr(bar)) : "memory");
+}
+
+// Waits for completion of the phase with the given parity; false after
+// WAIT_LIMIT polls.
+__device__ __forceinline__ bool wait(uint64_t *bar, uint32_t parity) {
+  uint32_t done = 0;
+  for (long long it = 0; it < WAIT_LIMIT && !done; ++it)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done) : "r"(saddr(bar)), "r"(parity) : "memory");
+  return done != 0;
+}
+
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tld16(uint32_t ta, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(ta));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__host__ __device__ inline int rup(int x, int m) { return (x + m - 1) / m * m; }
+
+// Tensor-core cost (MMA columns x K, per 128-row tile) of an orientation:
+// left pair nlL labels / nL terms, right pair nlR / nR.
+__host__ __device__ inline long long tc_cost(int nlL, int nL, int nlR, int nR) {
+  long long tiles = (4 * nlL + MROWS - 1) / MROWS;
+  int n1 = rup(nR, KC), n2 = rup(4 * nlR, 16);
+  return tiles * ((long long)rup(nL, KC) * n1 + (long long)n1 * n2) + 64LL * nlL * nlR;
+}
+
+// TMEM columns (D1 + D2) a class needs in the orientation the kernel takes.
+__host__ __device__ inline void tc_dims(int la, int lb, int lc, int ld, int t1, int t2, int &n1,
+                                        int &n2, bool &swp) {
+  int nab = ntuv(la + lb + 2 * t1), ncd = ntuv(lc + ld + 2 * t2);
+  int nlab = (2 * la + 1) * (2 * lb + 1), nlcd = (2 * lc + 1) * (2 * ld + 1);
+  swp = tc_cost(nlcd, ncd, nlab, nab) < tc_cost(nlab, nab, nlcd, ncd);
+  int nR = swp ? nab : ncd, nlR = swp ? nlab : nlcd;
+  n1 = rup(nR, KC);
+  n2 = rup(4 * nlR, 16);
+}
+
+// Shared-memory layout (bytes from a 128-byte aligned base).
+struct Layout {
+  int stage, rf, dsm, acc, fb, total;
+};
+__host__ __device__ inline Layout layout(int n1max, int n2max) {
+  Layout L;
+  int g1 = 2 * MROWS * KC * 4 + 2 * n1max * KC * 4;       // A1 and B1, hi and lo
+  int g2 = 2 * MROWS * KC * 4 + 2 * n2max * KC * 4;       // A2 and B2
+  int pslab = MROWS * PSTR * 4;                            // D2 slab
+  int rrec = 2 * NTR * 8;                                  // FP64 R recursion buffers
+  int st = g1 > g2 ? g1 : g2;
+  st = st > pslab ? st : pslab;
+  st = st > rrec ? st : rrec;
+  L.stage = 0;
+  L.rf = rup(st, 128);                                     // float R (balanced)
+  L.dsm = L.rf + rup(NTR * 4, 128);                        // density blocks, 4 x MAXSP^2 float2
+  L.acc = L.dsm + 4 * MAXSP * MAXSP * 8;                   // J, K, J2, K2 accumulators (float2)
+  L.fb = L.acc + 4 * MAXSP * MAXSP * 8;                    // Boys values (double)
+  L.total = L.fb + (MAXLAM + 2) * 8 + 128;                 // + alignment slack
+  return L;
+}
+
+struct Args {
+  const Shell *sh;
+  const PairE *pe;
+  const float4 *E;   // double-float E copy (k_econv): hi parts used
+  const float4 *D;   // double-float density, n x n (batched: Inst placement)
+  double *GD, *GX;
+  int ldd, ldf, nskp, isym, racah1;
+  int sym;           // as QArgsDF
+  const Inst *inst;
+  int tmem_cols, n1max, n2max;
+};
+
+__device__ inline float fsgn(float x, float s) { return s < 0.f ? -x : x; }
+
+// (ab|cd) m-sign combination from the (left|right) products (the same table
+// as rv_sign of the split path), complex value as float2.
+template <bool SWP>
+__device__ inline float2 rvc(const float2 (&sv)[8], int sa, int sb, int sc, int sd, float sl,
+                             float slr) {
+  int idx = SWP ? 8 * sc + 4 * sd + 2 * sa + sb : 8 * sa + 4 * sb + 2 * sc + sd;
+  const int src[16] = {0, 3, 2, 1, 5, 6, 7, 4, 4, 7, 6, 5, 1, 2, 3, 0};
+  const int kind[16] = {0, -3, 0, 3, -1, 2, -1, -2, 0, -3, 0, 3, 1, -2, 1, 2};
+  int kd = kind[idx];
+  float f = 1.f;
+  int ak = kd < 0 ? -kd : kd;
+  if (ak == 1) f = sl;
+  else if (ak == 2) f = slr;
+  else if (ak == 3) f = sl * slr;
+  if (kd < 0) f = -f;
+  float2 v = sv[src[idx]];
+  if (idx & 1) return make_float2(f * v.x, -f * v.y);
+  return make_float2(f * v.x, f * v.y);
+}
+
+__device__ __forceinline__ void cmac(float2 &acc, float2 u, float2 d) {
+  acc.x = fmaf(u.x, d.x, fmaf(-u.y, d.y, acc.x));
+  acc.y = fmaf(u.x, d.y, fmaf(u.y, d.x, acc.y));
+}
+
+__device__ __forceinline__ void sadd(float2 *p, float2 v) {
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+
+}  // namespace tcq
+
+__global__ void __launch_bounds__(tcq::TCT)
+k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
+  using namespace tcq;
+  extern __shared__ unsigned char tc_smem_raw[];
+  unsigned char *base =
+      (unsigned char *)(((uintptr_t)tc_smem_raw + 127) & ~(uintptr_t)127);
+  const Layout LY = layout(q.n1max, q.n2max);
+  float *A1h = (float *)(base + LY.stage);
+  float *A1l = A1h + MROWS * KC;
+  float *B1h = A1l + MROWS * KC;
+  float *B1l = B1h + q.n1max * KC;
+  float *B2h = A1l + MROWS * KC;  // GEMM 2 staging reuses the GEMM 1 space
+  float *B2l = B2h + q.n2max * KC;
+  float *P = (float *)(base + LY.stage);          // D2 slab (epilogue)
+  double *R = (double *)(base + LY.stage);        // FP64 recursion (before the GEMMs)
+  double *R2 = R + NTR;
+  float *Rf = (float *)(base + LY.rf);
+  float2 *Dsm = (float2 *)(base + LY.dsm);        // D(c,d), D(c,b), D(a,b), D(a,d)
+  float2 *Acc = (float2 *)(base + LY.acc);        // J(a,b), K(a,d), J2(c,d), K2(c,b)
+  double *F = (double *)(base + LY.fb);
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tslot;
+  __shared__ double sgeo[8];
+  __shared__ int sk;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(saddr(&tslot)), "r"(q.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar)));
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tslot;
+  uint32_t phase = 0;
+  bool abort = false;
+
+  for (long long qi = blockIdx.x; qi < nq && !abort; qi += gridDim.x) {
+    int4 Q4 = quart[qi];
+    const Shell &A = q.sh[Q4.x], &B = q.sh[Q4.y], &C = q.sh[Q4.z], &Dd = q.sh[Q4.w];
+    int la = A.l, lb = B.l, lc = C.l, ld = Dd.l;
+    int degab = la + lb + 2 * t1, degcd = lc + ld + 2 * t2;
+    int lam = degab + degcd;
+    int nla = 2 * la + 1, nlb = 2 * lb + 1, nlc = 2 * lc + 1, nld = 2 * ld + 1;
+    int nab = ntuv(degab), ncd = ntuv(degcd);
+    int n1, n2;
+    bool swp;
+    tc_dims(la, lb, lc, ld, t1, t2, n1, n2, swp);
+    if (n1 + n2 > q.tmem_cols || n1 > q.n1max || n2 > q.n2max) {
+      if (tid == 0) atomicOr(&g_tc_status, 2);  // launch sized for other classes
+      continue;
+    }
+    int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
+    const float4 *Dm = q.D;
+    double *GDm = q.GD, *GXm = q.GX;
+    size_t lddm = q.ldd, ldfm = q.ldf;
+    int nskpm = q.nskp;
+    if (q.inst) {
+      const Inst I = q.inst[A.inst];
+      Dm += I.off;
+      GDm += 2 * I.off;
+      GXm += 2 * I.off;
+      lddm = ldfm = (size_t)I.ld;
+      nskpm = I.nskp;
+    }
+    const PairE &pab_e = q.pe[A.prow + Q4.y], &pcd_e = q.pe[C.prow + Q4.w];
+    if (tid == 0) {
+      double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
+      double Px = (A.alpha * A.x + B.alpha * B.x) / p;
+      double Py = (A.alpha * A.y + B.alpha * B.y) / p;
+      double Pz = (A.alpha * A.z + B.alpha * B.z) / p;
+      double Qx = (C.alpha * C.x + Dd.alpha * Dd.x) / qq;
+      double Qy = (C.alpha * C.y + Dd.alpha * Dd.y) / qq;
+      double Qz = (C.alpha * C.z + Dd.alpha * Dd.z) / qq;
+      double aph = p * qq / (p + qq);
+      double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
+      double sg = swp ? -1.0 : 1.0;
+      sgeo[0] = sg * (Px - Qx); sgeo[1] = sg * (Py - Qy); sgeo[2] = sg * (Pz - Qz);
+      sgeo[3] = -2.0 * aph;
+      sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
+      sgeo[5] = T;
+      sk = half_floor_log2(2.0 * aph);
+    }
+    // the previous quartet's TMEM reads and shared-memory use end here
+    fence_before();
+    __syncthreads();
+    fence_after();
+    boys_block(sgeo[5], lam, F);
+    __syncthreads();
+    {
+      double X = sgeo[0], Y = sgeo[1], Z = sgeo[2], m2a = sgeo[3];
+      double *cur = R, *nxt = R2;
+      for (int n = lam; n >= 0; --n) {
+        int cnt = ntuv(lam - n);
+        for (int k = tid; k < cnt; k += TCT) {
+          double val;
+          if (k == 0) {
+            double pw = 1.0;
+            for (int i = 0; i < n; ++i) pw *= m2a;
+            val = pw * F[n];
+          } else {
+            int t = c_t[k], u = c_u[k], v = c_v[k];
+            if (t > 0) {
+              val = X * cur[hidx(t - 1, u, v)];
+              if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
+            } else if (u > 0) {
+              val = Y * cur[hidx(t, u - 1, v)];
+              if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
+            } else {
+              val = Z * cur[hidx(t, u, v - 1)];
+              if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
+            }
+          }
+          nxt[k] = val;
+        }
+        __syncthreads();
+        double *tmp = cur; cur = nxt; nxt = tmp;
+      }
+      // PRE * R scaled by 2^(-k lambda) (exponent balancing), in FP32
+      double pre = sgeo[4];
+      int k = sk;
+      for (int i = tid; i < ntuv(lam); i += TCT) {
+        int L = c_t[i] + c_u[i] + c_v[i];
+        Rf[i] = __double2float_rn(ldexp(cur[i] * pre, -k * L));
+      }
+    }
+    // roles
+    const float4 *Eab = q.E + pab_e.off[t1];
+    const float4 *Ecd = q.E + pcd_e.off[t2];
+    const float4 *EL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
+    int kL = swp ? pcd_e.kexp : pab_e.kexp, kR = swp ? pab_e.kexp : pcd_e.kexp;
+    int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
+    int nlab = nla * nlb, nlcd = nlc * nld;
+    int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
+    int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;
+    int lq[4] = {la, lb, lc, ld};
+    int oab = t1 ? nskpm : 0, ocd = t2 ? nskpm : 0;
+    int kq0 = sk;
+    bool dual = q.sym && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
+    // density blocks of this quartet: D(c,d), D(c,b), and for (cd|ab) D(a,b), D(a,d)
+    {
+      int sizes[4][2] = {{2 * nlc, 2 * nld}, {2 * nlc, 2 * nlb}, {2 * nla, 2 * nlb},
+                         {2 * nla, 2 * nld}};
+      const Shell *rs[4] = {&C, &C, &A, &A}, *cs[4] = {&Dd, &B, &B, &Dd};
+      int ro[4] = {ocd, ocd, oab, oab}, co[4] = {ocd, oab, oab, ocd};
+      for (int blk = 0; blk < (dual ? 4 : 2); ++blk) {
+        int nr = sizes[blk][0], nc = sizes[blk][1];
+        for (int w = tid; w < nr * nc; w += TCT) {
+          int r = w / nc, c = w % nc;
+          int fr = rs[blk]->fock[r >> 1][r & 1] + ro[blk];
+          int fc = cs[blk]->fock[c >> 1][c & 1] + co[blk];
+          float4 v = Dm[(size_t)fr + lddm * fc];
+          Dsm[blk * MAXSP * MAXSP + r * MAXSP + c] = make_float2(v.x, v.z);
+        }
+      }
+    }
+    for (int i = tid; i < 4 * MAXSP * MAXSP; i += TCT) Acc[i] = make_float2(0.f, 0.f);
+    __syncthreads();  // R (FP64) is dead: the staging buffers may overwrite it
+
+    const uint32_t tD1 = tmem, tD2 = tmem + (uint32_t)n1;
+    const uint32_t id1 = idesc(MROWS, n1), id2 = idesc(MROWS, n2);
+    for (int l0 = 0; l0 < nlL && !abort; l0 += MLAB) {
+      int ntl = min(MLAB, nlL - l0);
+      // ---- GEMM 1: D1 = E_L (rows) x Hankel R (columns q), K = s ----
+      for (int kc = 0; kc < nL && !abort; kc += KC) {
+        for (int w = tid; w < MLAB * 2 * KC; w += TCT) {
+          int lab = w / (2 * KC), set = (w / KC) & 1, kk = w % KC;
+          int s = kc + kk;
+          float vr = 0.f, vi = 0.f;
+          if (lab < ntl && s < nL) {
+            float4 e = EL[((long long)(l0 + lab) * 2 + set) * nL + s];
+            int L = c_t[s] + c_u[s] + c_v[s];
+            float f = ldexpf(1.0f, (kq0 - kL) * L);
+            vr = e.x * f;
+            vi = e.z * f;
+          }
+          int row = lab * 4 + set * 2;
+          float h, l;
+          tsplit(vr, h, l);
+          A1h[kmaj(row, kk)] = h; A1l[kmaj(row, kk)] = l;
+          tsplit(vi, h, l);
+          A1h[kmaj(row + 1, kk)] = h; A1l[kmaj(row + 1, kk)] = l;
+        }
+        for (int w = tid; w < n1 * KC; w += TCT) {
+          int n = w / KC, kk = w % KC, s = kc + kk;
+          float v = 0.f;
+          if (n < nR && s < nL) v = Rf[hidx(c_t[s] + c_t[n], c_u[s] + c_u[n], c_v[s] + c_v[n])];
+          float h, l;
+          tsplit(v, h, l);
+          B1h[kmaj(n, kk)] = h; B1l[kmaj(n, kk)] = l;
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        if (tid == 0) {
+          fence_after();
+#pragma unroll
+          for (int ks = 0; ks < KC / 8; ++ks) {
+            uint32_t off = ks * 256;
+            uint64_t ah = sdesc(saddr(A1h) + off), al = sdesc(saddr(A1l) + off);
+            uint64_t bh = sdesc(saddr(B1h) + off), bl = sdesc(saddr(B1l) + off);
+            uint32_t acc0 = (kc > 0 || ks > 0) ? 1u : 0u;
+            mma(tD1, ah, bh, id1, acc0);
+            mma(tD1, ah, bl, id1, 1u);
+            mma(tD1, al, bh, id1, 1u);
+          }
+          commit(&mbar);
+        }
+        bool ok = wait(&mbar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) abort = true;
+        fence_after();
+      }
+      // ---- GEMM 2: D2 = G (rows, K = q) x E_R (columns) ----
+      for (int kc = 0; kc < n1 && !abort; kc += KC) {
+        {
+          // this warp's 32 rows of D1, columns kc..kc+31: sign (-1)^|q| and
+          // the right pair's balancing 2^((k - kR)|q|), then TF32 split
+          int row = warp * 32 + lane;
+          float v[32];
+          uint32_t ta = tD1 + ((uint32_t)(warp * 32) << 16) + (uint32_t)kc;
+          tld16(ta, v);
+          tld16(ta + 16, v + 16);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            int qq = kc + j;
+            float x = 0.f;
+            if (qq < nR) {
+              int L = c_t[qq] + c_u[qq] + c_v[qq];
+              x = v[j] * ldexpf((L & 1) ? -1.0f : 1.0f, (kq0 - kR) * L);
+            }
+            float h, l;
+            tsplit(x, h, l);
+            A1h[kmaj(row, j)] = h;
+            A1l[kmaj(row, j)] = l;
+          }
+        }
+        for (int w = tid; w < n2 * KC; w += TCT) {
+          int n = w / KC, kk = w % KC, qq = kc + kk;
+          float v = 0.f;
+          if (n < 4 * nlR && qq < nR) {
+            int labR = n >> 2, set = (n >> 1) & 1;
+            float4 e = ER[((long long)labR * 2 + set) * nR + qq];
+            v = (n & 1) ? e.z : e.x;
+          }
+          float h, l;
+          tsplit(v, h, l);
+          B2h[kmaj(n, kk)] = h; B2l[kmaj(n, kk)] = l;
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        if (tid == 0) {
+          fence_after();
+#pragma unroll
+          for (int ks = 0; ks < KC / 8; ++ks) {
+            uint32_t off = ks * 256;
+            uint64_t ah = sdesc(saddr(A1h) + off), al = sdesc(saddr(A1l) + off);
+            uint64_t bh = sdesc(saddr(B2h) + off), bl = sdesc(saddr(B2l) + off);
+            uint32_t acc0 = (kc > 0 || ks > 0) ? 1u : 0u;
+            mma(tD2, ah, bh, id2, acc0);
+            mma(tD2, ah, bl, id2, 1u);
+            mma(tD2, al, bh, id2, 1u);
+          }
+          commit(&mbar);
+        }
+        bool ok = wait(&mbar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) abort = true;
+        fence_after();
+      }
+      if (abort) break;
+      // ---- epilogue: 16 products per label pair -> m-sign combinations ->
+      //      J/K digestion (FP32 products, per-quartet FP32 sums) ----
+      for (int c0 = 0; c0 < 4 * nlR; c0 += SLAB) {
+        int ncol = min(SLAB, n2 - c0);
+        {
+          int row = warp * 32 + lane;
+          for (int j0 = 0; j0 < ncol; j0 += 16) {
+            float v[16];
+            tld16(tD2 + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c0 + j0), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) P[row * PSTR + j0 + j] = v[j];
+          }
+        }
+        fence_before();
+        __syncthreads();
+        int r0 = c0 / 4, nrl = min(SLAB / 4, nlR - r0);
+        for (int w = tid; w < ntl * nrl; w += TCT) {
+          int lab = w % ntl;
+          int lr = r0 + (w / ntl + lab) % nrl;  // skewed: lanes hit different targets
+          int labL = l0 + lab;
+          int l1 = labL / nl2L, l2 = labL % nl2L, r1 = lr / nl2R, r2 = lr % nl2R;
+          int ia = swp ? r1 : l1, ib = swp ? r2 : l2, ic = swp ? l1 : r1, id = swp ? l2 : r2;
+          int kq[4], mq[4], mm[4];
+          label_of(la, ia, kq[0], mm[0]);
+          label_of(lb, ib, kq[1], mm[1]);
+          label_of(lc, ic, kq[2], mm[2]);
+          label_of(ld, id, kq[3], mm[3]);
+          for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
+          if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
+          // products: rows (lab, set L, re/im), columns (lr, set R, re/im)
+          const float *pr0 = P + (lab * 4) * PSTR + (lr - r0) * 4;
+          // pp = 2*setL + setR: a = re.re, b = im.im, c = G.im*E.re, d = G.re*E.im
+          float2 sv[8];
+#pragma unroll
+          for (int sL = 0; sL < 2; ++sL)
+#pragma unroll
+            for (int sR = 0; sR < 2; ++sR) {
+              const float *pre_ = pr0 + (sL * 2) * PSTR + sR * 2;
+              float a = pre_[0], d = pre_[1];            // G.re x (E.re, E.im)
+              float c = pre_[PSTR], b = pre_[PSTR + 1];  // G.im x (E.re, E.im)
+              int pp = sL * 2 + sR;                      // s1: (0,0) s2: (0,1) s3: (1,0) s4: (1,1)
+              sv[2 * pp] = make_float2(a - b, c + d);
+              sv[2 * pp + 1] = make_float2(a + b, d - c);
+            }
+          double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
+          double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
+          double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
+          float sl = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
+          const float2 *Dcd = Dsm, *Dcb = Dsm + MAXSP * MAXSP;
+          const float2 *Dab = Dsm + 2 * MAXSP * MAXSP, *Dad = Dsm + 3 * MAXSP * MAXSP;
+          float2 *Jl = Acc, *Kl = Acc + MAXSP * MAXSP, *J2 = Acc + 2 * MAXSP * MAXSP,
+                 *K2 = Acc + 3 * MAXSP * MAXSP;
+#define TCV(sa, sb, sc, sd) (swp ? rvc<true>(sv, sa, sb, sc, sd, sl, slr) \
+                                 : rvc<false>(sv, sa, sb, sc, sd, sl, slr))
+          if (q.isym == 0) {
+            for (int sa = 0; sa < 2; ++sa)
+              for (int sb = 0; sb < 2; ++sb) {
+                float2 j = make_float2(0.f, 0.f);
+                for (int sc = 0; sc < 2; ++sc)
+                  for (int sd = 0; sd < 2; ++sd)
+                    cmac(j, TCV(sa, sb, sc, sd), Dcd[(ic * 2 + sc) * MAXSP + id * 2 + sd]);
+                sadd(&Jl[(ia * 2 + sa) * MAXSP + ib * 2 + sb], j);
+              }
+            for (int sa = 0; sa < 2; ++sa)
+              for (int sd = 0; sd < 2; ++sd) {
+                float2 k = make_float2(0.f, 0.f);
+                for (int sb = 0; sb < 2; ++sb)
+                  for (int sc = 0; sc < 2; ++sc)
+                    cmac(k, TCV(sa, sb, sc, sd), Dcb[(ic * 2 + sc) * MAXSP + ib * 2 + sb]);
+                sadd(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], k);
+              }
+            if (dual) {
+              for (int sc = 0; sc < 2; ++sc)
+                for (int sd = 0; sd < 2; ++sd) {
+                  float2 j = make_float2(0.f, 0.f);
+                  for (int sa = 0; sa < 2; ++sa)
+                    for (int sb = 0; sb < 2; ++sb)
+                      cmac(j, TCV(sa, sb, sc, sd), Dab[(ia * 2 + sa) * MAXSP + ib * 2 + sb]);
+                  sadd(&J2[(ic * 2 + sc) * MAXSP + id * 2 + sd], j);
+                }
+              for (int sc = 0; sc < 2; ++sc)
+                for (int sb = 0; sb < 2; ++sb) {
+                  float2 k = make_float2(0.f, 0.f);
+                  for (int sa = 0; sa < 2; ++sa)
+                    for (int sd = 0; sd < 2; ++sd)
+                      cmac(k, TCV(sa, sb, sc, sd), Dad[(ia * 2 + sa) * MAXSP + id * 2 + sd]);
+                  sadd(&K2[(ic * 2 + sc) * MAXSP + ib * 2 + sb], k);
+                }
+            }
+          } else {
+            // CLMMTZ: real parts, equal-sign direct blocks, crossed exchange
+            for (int s = 0; s < 2; ++s) {
+              float jv = 0.f, kv = 0.f;
+              for (int t = 0; t < 2; ++t) {
+                jv = fmaf(TCV(s, s, t, t).x, Dcd[(ic * 2 + t) * MAXSP + id * 2 + t].x, jv);
+                kv = fmaf(TCV(s, t, t, s).x, Dcb[(ic * 2 + t) * MAXSP + ib * 2 + t].x, kv);
+              }
+              atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, jv);
+              atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
+            }
+            if (dual)
+              for (int s = 0; s < 2; ++s) {
+                float jv = 0.f, kv = 0.f;
+                for (int t = 0; t < 2; ++t) {
+                  jv = fmaf(TCV(t, t, s, s).x, Dab[(ia * 2 + t) * MAXSP + ib * 2 + t].x, jv);
+                  kv = fmaf(TCV(t, s, s, t).x, Dad[(ia * 2 + t) * MAXSP + id * 2 + t].x, kv);
+                }
+                atomicAdd(&J2[(ic * 2 + s) * MAXSP + id * 2 + s].x, jv);
+                atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
+              }
+          }
+#undef TCV
+        }
+        __syncthreads();  // the slab buffer is rewritten next
+      }
+    }
+    if (abort) break;
+    // flush: weight 1/2 for a quartet equal to its (ba|dc) image, or to its
+    // (dc|ba) image within one class; FP64 accumulation in global memory
+    const double wq = (q.sym == 2 && ((Q4.x == Q4.y && Q4.z == Q4.w) ||
+                                      (t1 == t2 && Q4.x == Q4.w && Q4.y == Q4.z))) ? 0.5 : 1.0;
+    const int rr[4][2] = {{0, 1}, {0, 3}, {2, 3}, {2, 1}};  // roles (row, column) per target
+    const Shell *sh4[4] = {&A, &B, &C, &Dd};
+    const int nl4[4] = {nla, nlb, nlc, nld}, off4[4] = {oab, oab, ocd, ocd};
+    for (int f = 0; f < (dual ? 4 : 2); ++f) {
+      int ra = rr[f][0], ca = rr[f][1];
+      int nr = 2 * nl4[ra], nc = 2 * nl4[ca];
+      double *G = (f == 0 || f == 2) ? GDm : GXm;
+      for (int w = tid; w < nr * nc; w += TCT) {
+        int a = w / nc, b = w % nc;
+        float2 v = Acc[f * MAXSP * MAXSP + a * MAXSP + b];
+        if (v.x == 0.f && v.y == 0.f) continue;
+        int fa = sh4[ra]->fock[a >> 1][a & 1] + off4[ra];
+        int fb = sh4[ca]->fock[b >> 1][b & 1] + off4[ca];
+        double *dst = G + 2 * ((size_t)fa + ldfm * fb);
+        atomicAdd(dst, wq * (double)v.x);
+        atomicAdd(dst + 1, wq * (double)v.y);
+      }
+    }
+  }
+  if (abort && tid == 0) atomicOr(&g_tc_status, 1);
+  // release: every TMEM read and MMA of this CTA has completed (waited above;
+  // after a timeout, wait once more, bounded, for the MMAs in flight)
+  if (abort) wait(&mbar, phase ^ 1);
+  fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 :: "r"(tmem), "r"(q.tmem_cols));
+}

@@ -51,8 +51,11 @@ extern "C" {
 #define BG_PREC_FP64 0 /* all FP64: the drop-in path */
 #define BG_PREC_DF32 1 /* split precision: FP32 double-float contractions and
                           digestion products, FP64 Boys/R and J/K sums */
-#define BG_PREC_AUTO 2 /* per angular class the faster of the two kernels,
-                          chosen by timing both on the first build */
+#define BG_PREC_AUTO 2 /* per angular class the fastest kernel within an
+                          energy-error budget, chosen on the first build */
+#define BG_PREC_TC32 3 /* tensor cores: both Hermite contractions as 3xTF32
+                          tcgen05 GEMMs (FP32 accumulation), FP32 digestion
+                          products, FP64 Boys/R and J/K sums */
 
 /* compiled limits */
 #define BG_MAX_L 3 /* highest orbital angular momentum of a basis shell */
@@ -80,15 +83,36 @@ int bertha_gpu_init(bg_ctx **ctx, int ncnt, const double *bxyz,
 int bertha_gpu_set_precision(bg_ctx *ctx, int prec);
 
 /* BG_PREC_AUTO is the autotuned mixed mode: the first build after the
- * quartet lists are made times the FP64 and the split-precision kernels on
- * a sample of every angular class (l_a,l_b,l_c,l_d) of every component
- * class (classes under 2048 quartets take FP64) and later builds launch the
- * faster kernel per run of classes.  Its results carry at most the split
- * path's error.  Streamed lists and bertha_gpu_quartets take the split
- * kernel.  After a build, the quartets each kernel digests and the number
- * of runs (launches per build): */
+ * quartet lists are made runs the FP64, the split-precision and the
+ * tensor-core kernels on a sample of every angular class (l_a,l_b,l_c,l_d)
+ * of every component class (classes under 2048 quartets take FP64), timing
+ * each and comparing the sample's energy terms sum_ij Re D_ij G_ij (J and
+ * K) with the FP64 kernel's.  Each class takes the faster of FP64 and the
+ * split path (both FP64-accurate); classes then move to the tensor-core
+ * kernel, largest time saved per estimated error first, while the summed
+ * estimates (sample error x class size / sample size) stay within the
+ * error budget (bertha_gpu_set_error_budget).  Later builds launch the
+ * chosen kernel per run of classes.  Streamed lists and bertha_gpu_quartets
+ * take the split kernel.  After a build, the quartets each kernel digests
+ * and the number of runs (launches per build): */
 int bertha_gpu_auto_stats(const bg_ctx *ctx, long long *nq_fp64, long long *nq_df32,
                           int *nruns);
+
+/* The same with the tensor-core kernel: nq[0] FP64, nq[1] split, nq[2]
+ * tensor-core quartets of the last tuned (or BG_PREC_TC32) build. */
+int bertha_gpu_kernel_stats(const bg_ctx *ctx, long long nq[3], int *nruns);
+
+/* Energy error (Eh) the BG_PREC_AUTO tuner may spend on tensor-core classes
+ * per Coulomb build, shared equally by the component classes (default
+ * 1e-7; 0 keeps every class FP64-accurate).  Changing it retunes. */
+int bertha_gpu_set_error_budget(bg_ctx *ctx, double eh);
+
+/* Status of the tensor-core kernels since the last call (synchronises the
+ * device): bit 0 set when an mbarrier wait gave up (the kernel skipped the
+ * rest of its work, freed its tensor memory and returned), bit 1 when a
+ * quartet's class needed more tensor memory than its launch allocated (the
+ * quartet was skipped).  0 when every quartet was digested. */
+int bertha_gpu_device_status(int *status);
 
 /* Schwarz screening of the Fock build (SCHWARZ/CLMDIAG, bertha-scf.f:37889,
  * :38126; off by default there, SCHWRZ=.FALSE. :5257).  With threshold > 0,
@@ -177,6 +201,19 @@ int bertha_gpu_quartets(bg_ctx *ctx, const int *d_quartets, long long nq,
                         int t1, int t2, const double *d_dent, int ldd,
                         double *d_gdir, double *d_gxch, int ldf, void *stream);
 
+/* bertha_gpu_quartets over a list the caller has grouped by angular class:
+ * nseg segments, entries seg[i]..seg[i+1]-1 (host array of nseg+1 offsets
+ * into d_quartets) all of class lclass[4i..4i+3] = (l_a, l_b, l_c, l_d)
+ * (host array).  Under BG_PREC_TC32 each run of classes gets a launch sized
+ * for its tensor-memory need (more CTAs per SM for small classes); other
+ * precisions digest the whole range in one launch as bertha_gpu_quartets
+ * does.  A quartet whose class needs more tensor memory than its segment's
+ * class is skipped and flagged (bertha_gpu_device_status). */
+int bertha_gpu_quartets_segments(bg_ctx *ctx, const int *d_quartets, int nseg,
+                                 const long long *seg, const int *lclass, int t1, int t2,
+                                 const double *d_dent, int ldd, double *d_gdir,
+                                 double *d_gxch, int ldf, void *stream);
+
 /* Largest NDIM bertha_gpu_quartets_noalloc accepts. */
 #define BG_NOALLOC_MAX_NDIM 1024
 
@@ -220,9 +257,13 @@ int bertha_gpu_batch_create(bg_batch **b, int n, bg_ctx *const *ctxs,
  * first build, as for a context). */
 int bertha_gpu_batch_set_precision(bg_batch *b, int prec);
 
-/* bertha_gpu_auto_stats of a batch. */
+/* bertha_gpu_auto_stats, bertha_gpu_kernel_stats and
+ * bertha_gpu_set_error_budget of a batch (the budget covers the whole
+ * batch's build). */
 int bertha_gpu_batch_auto_stats(const bg_batch *b, long long *nq_fp64, long long *nq_df32,
                                 int *nruns);
+int bertha_gpu_batch_kernel_stats(const bg_batch *b, long long nq[3], int *nruns);
+int bertha_gpu_batch_set_error_budget(bg_batch *b, double eh);
 
 /* CLMFAST of every instance at stage ilev on device arrays in the batch's
  * placement: d_dent holds all densities; d_gdir, d_gxch get all GDIR and

@@ -207,7 +207,7 @@ class QuartetOracle:
         xyz, lmax, nfn, ex = _basis_arrays(basis)
         self._keep = (xyz, lmax, nfn, ex)
         self.h = L.orc_ctx_new(basis.ncnt, _p(xyz), _p(lmax), _p(nfn), _p(ex),
-                               ex.shape[1], ex.shape[2], int(basis.hmlt == 0))
+                               ex.shape[1], ex.shape[2], int(basis.hmlt))
         ns = ctypes.c_int()
         self.ndim = L.orc_ndim(self.h, ctypes.byref(ns))
         self.nskp = ns.value

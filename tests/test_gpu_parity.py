@@ -180,3 +180,98 @@ def test_streamed_quartet_lists(prec):
     tol = (TOL if prec == "fp64" else DF_TOL) * scale + 1e-9
     for g, r in ((gd, rd), (gx, rx), (gd2, rd), (gx2, rx)):
         assert np.abs(g - r).max() <= tol
+
+
+def test_h2o_stage3_fp64():
+    """The H2O configuration at ILEV 3 (all four component classes), FP64,
+    against the oracle."""
+    b = deck.h2o_basis()
+    _cmp(b, deck.density(b, seed=2), 3)
+
+
+def _explicit(fb, q, cls, dent):
+    import torch
+    n = fb.ndim
+    D = torch.from_numpy(np.ascontiguousarray(dent.T).view(np.float64).reshape(n, 2 * n)).cuda()
+    GD = torch.zeros(n, 2 * n, dtype=torch.float64, device="cuda")
+    GX = torch.zeros_like(GD)
+    dq = torch.from_numpy(np.ascontiguousarray(q, dtype=np.int32)).cuda()
+    fb.quartets(dq.data_ptr(), q.shape[0], cls[0], cls[1], D.data_ptr(), GD.data_ptr(),
+                GX.data_ptr(), n, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return (GD.cpu().numpy().view(np.complex128).reshape(n, n).T,
+            GX.cpu().numpy().view(np.complex128).reshape(n, n).T)
+
+
+def _oracle_explicit(b, q, cls, dent):
+    n = b.ndim
+    rd = np.zeros((n, n), complex, order="F")
+    rx = np.zeros((n, n), complex, order="F")
+    O = orc.QuartetOracle(b)
+    O.prepare(q, *cls)
+    O.digest(q, *cls, dent, rd, rx, nthreads=16)
+    O.close()
+    return rd, rx
+
+
+def _class_sample(b, per_class, seed):
+    """Seeded quartets of every angular class (l_a,l_b,l_c,l_d) of a basis,
+    shells drawn at random among those of each l (every centre)."""
+    rng = np.random.default_rng(seed)
+    sh = b.shells()
+    byl = {}
+    for s, (c, l, i, _) in enumerate(sh):
+        byl.setdefault(l, []).append(s)
+    out = []
+    ls = sorted(byl)
+    for la in ls:
+        for lb in ls:
+            for lc in ls:
+                for ld in ls:
+                    for _ in range(per_class):
+                        out.append([rng.choice(byl[x]) for x in (la, lb, lc, ld)])
+    return np.array(out, dtype=np.int32)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "df32", "auto", "tc32"])
+def test_tlf_full_basis_class_sample(prec):
+    """The full TlF basis (Tl exponents up to 0.02 * 2.2^27, about 3.6e7) on
+    a seeded sample of every angular class of every component class, through
+    explicit lists against the oracle.  The shape is taken as GENERAL so that
+    both sides use the complex digestion (the oracle's explicit-list path has
+    no real-digestion mode); the integrals are those of the linear molecule."""
+    b0 = deck.tlf_basis()
+    b = deck.Basis(xyz=b0.xyz, lmax=b0.lmax, nfn=b0.nfn, ex=b0.ex, hmlt=deck.HMLT["DHFR"],
+                   isym=0, name="TlF")
+    q = _class_sample(b, 2, seed=17)
+    dent = deck.density(b, seed=4)
+    fb = berthagpu.FockBuilder(b)
+    fb.set_precision(prec)
+    tol = {"fp64": TOL, "df32": DF_TOL, "auto": DF_TOL, "tc32": 2e-5}[prec]
+    for cls in ((0, 0), (0, 1), (1, 0), (1, 1)):
+        gd, gx = _explicit(fb, q, cls, dent)
+        rd, rx = _oracle_explicit(b, q, cls, dent)
+        scale = max(np.abs(rd).max(), np.abs(rx).max())
+        assert np.abs(gd - rd).max() <= tol * scale, cls
+        assert np.abs(gx - rx).max() <= tol * scale, cls
+    fb.close()
+
+
+def test_microbench_quartets_vs_oracle():
+    """4096 quartets of the ERI microbenchmark's distribution (l <= 3,
+    exponents 0.05..1e6, 20 % overlapping pairs) against the oracle, FP64
+    and split precision."""
+    from berthagpu import workloads
+    b = workloads.microbench_pool(seed=5, ncentres=12)
+    quarts = workloads.microbench_quartets(b, 4096, seed=5)
+    dent = deck.density(b, seed=5)
+    for prec, tol in (("fp64", TOL), ("df32", DF_TOL)):
+        fb = berthagpu.FockBuilder(b)
+        fb.set_precision(prec)
+        for cls, q in quarts.items():
+            gd, gx = _explicit(fb, q, cls, dent)
+            rd, rx = _oracle_explicit(b, q, cls, dent)
+            scale = max(np.abs(rd).max(), np.abs(rx).max())
+            assert np.abs(gd - rd).max() <= tol * scale, (prec, cls)
+            assert np.abs(gx - rx).max() <= tol * scale, (prec, cls)
+        fb.close()

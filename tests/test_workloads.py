@@ -47,3 +47,31 @@ def test_breit_ls_sl_halving_covers_every_quartet():
         assert ((w, x, y, z) in listed) != (img in listed) or img == (w, x, y, z)
     assert listed <= allq
     assert len(q_lsls) > 0
+
+
+def test_quartet_oracle_layout_matches_basis():
+    """The oracle's explicit-list context uses the basis's own Fock layout:
+    a four-component basis has its small component at NSKP = NDIM/2 (the
+    layout the library and the oracle's CLMFAST use), a NORL basis none."""
+    from oracle import oracle as orc
+    b = deck.make_basis([((0, 0, 0), {0: [0.4, 2.0], 1: [0.9]}),
+                         ((0.0, 0.6, 1.1), {0: [0.7]})], hmlt="DHFR")
+    O = orc.QuartetOracle(b)
+    assert O.ndim == b.ndim and O.nskp == b.ndim // 2
+    O.close()
+    bn = deck.make_basis([((0, 0, 0), {0: [0.4, 2.0], 1: [0.9]})], hmlt="NORL")
+    O = orc.QuartetOracle(bn)
+    assert O.ndim == bn.ndim and O.nskp == 0
+    O.close()
+
+
+def test_group_by_class_segments():
+    b = workloads.microbench_pool(seed=3, ncentres=4)
+    q = workloads.microbench_quartets(b, 2000, seed=3)[(0, 1)]
+    qq, seg, lcl = workloads.group_by_class(b, q)
+    l = np.array([s[1] for s in b.shells()])
+    assert sorted(map(tuple, qq)) == sorted(map(tuple, q))
+    assert seg[0] == 0 and seg[-1] == len(q)
+    for i in range(len(seg) - 1):
+        part = qq[seg[i]:seg[i + 1]]
+        assert (np.stack([l[part[:, j]] for j in range(4)], 1) == lcl[i]).all()
