@@ -60,6 +60,8 @@ def lib():
         L.bertha_gpu_auto_stats.argtypes = [P, P, P, P]
         L.bertha_gpu_batch_auto_stats.argtypes = [P, P, P, P]
         L.bertha_gpu_kernel_stats.argtypes = [P, P, P]
+        L.bertha_gpu_breit_kernel_stats.argtypes = [P, P, P]
+        L.bertha_gpu_tuning_record.argtypes = [P, i, i, P, P, P]
         L.bertha_gpu_batch_kernel_stats.argtypes = [P, P, P]
         L.bertha_gpu_set_error_budget.argtypes = [P, ctypes.c_double]
         L.bertha_gpu_batch_set_error_budget.argtypes = [P, ctypes.c_double]
@@ -93,7 +95,8 @@ EXPORTED = [
     "bertha_gpu_batch_clmfast_device", "bertha_gpu_batch_quartets",
     "bertha_gpu_batch_launches", "bertha_gpu_batch_last_error", "bertha_gpu_batch_free",
     "bertha_gpu_auto_stats", "bertha_gpu_batch_auto_stats",
-    "bertha_gpu_kernel_stats", "bertha_gpu_batch_kernel_stats",
+    "bertha_gpu_kernel_stats", "bertha_gpu_batch_kernel_stats", "bertha_gpu_breit_kernel_stats",
+    "bertha_gpu_tuning_record",
     "bertha_gpu_set_error_budget", "bertha_gpu_batch_set_error_budget",
     "bertha_gpu_device_status",
 ]

@@ -158,6 +158,34 @@ class FockBuilder:
             ctypes.c_void_p(d_dent), ld, ctypes.c_void_p(d_gdir), ctypes.c_void_p(d_gxch), ld,
             ctypes.c_void_p(stream)), self._ctx)
 
+    def tuning_record(self, breit=False):
+        """The autotuner's last record, one dict per segment (class and
+        bound decade): comp, class (l_a, l_b, l_c, l_d), quartets, kernel
+        chosen, sample ms and estimated energy error per kernel."""
+        n = ctypes.c_int()
+        check(lib().bertha_gpu_tuning_record(self._ctx, int(breit), 0, None, None,
+                                             ctypes.byref(n)), self._ctx)
+        info = np.zeros(4 * max(n.value, 1), np.int32)
+        vals = np.zeros(6 * max(n.value, 1), np.float64)
+        check(lib().bertha_gpu_tuning_record(self._ctx, int(breit), n.value, _p(info), _p(vals),
+                                             ctypes.byref(n)), self._ctx)
+        rows = []
+        for i in range(n.value):
+            k = int(info[4 * i + 1])
+            rows.append({"comp": int(info[4 * i]),
+                         "class": ((k >> 6) & 3, (k >> 4) & 3, (k >> 2) & 3, k & 3),
+                         "quartets": int(info[4 * i + 2]), "kind": int(info[4 * i + 3]),
+                         "ms": [float(x) for x in vals[6 * i:6 * i + 3]],
+                         "err": [float(x) for x in vals[6 * i + 3:6 * i + 6]]})
+        return rows
+
+    def breit_stats(self):
+        """Kernel use of the last Breit build: FP64 and tensor-core quartets, runs."""
+        nq = (ctypes.c_longlong * 3)()
+        r = ctypes.c_int()
+        check(lib().bertha_gpu_breit_kernel_stats(self._ctx, nq, ctypes.byref(r)), self._ctx)
+        return {"fp64_quartets": nq[0], "tc32_quartets": nq[2], "runs": r.value}
+
     def launches(self):
         return int(lib().bertha_gpu_launches(self._ctx))
 

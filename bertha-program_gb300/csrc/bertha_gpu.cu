@@ -1569,6 +1569,37 @@ __global__ void k_econv(const double2 *E, float4 *Edf, const PairE *pe, const Sh
   }
 }
 
+// FP32 (re, im) copy of the double-float E copy (its high words): the
+// tensor-core kernel's operand source, half the bytes.
+__global__ void k_ef(const float4 *Edf, float2 *Ef, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float4 v = Edf[i];
+    Ef[i] = make_float2(v.x, v.z);
+  }
+}
+
+// FP32 copy of the sigma-coupled LS/SL E-coefficients, one block per (pair,
+// component), each coefficient times 2^(kexp lambda) (layout
+// [lab_a][lab_b][set][x,y,z][tuv], degree l_a + l_b + 1).
+__global__ void k_ebf(const double2 *EB, float2 *EBf, const long long *offq, const PairE *pe,
+                      const Shell *sh, int ns) {
+  long long pc = blockIdx.x;
+  if (pc >= (long long)ns * ns * 2) return;
+  long long pair = pc / 2;
+  const Shell &A = sh[pair / ns], &B = sh[pair % ns];
+  int k = pe[pair].kexp;
+  int nt = ntuv(A.l + B.l + 1);
+  long long n = (long long)(2 * A.l + 1) * (2 * B.l + 1) * 6 * nt, off = offq[pc];
+  for (long long w = threadIdx.x; w < n; w += blockDim.x) {
+    int t = (int)(w % nt);
+    int lam = c_t[t] + c_u[t] + c_v[t];
+    double2 v = EB[off + w];
+    EBf[off + w] = make_float2(__double2float_rn(ldexp(v.x, k * lam)),
+                               __double2float_rn(ldexp(v.y, k * lam)));
+  }
+}
+
 // Double-float copy of the density (column-major, leading dimension ld).
 __global__ void k_dconv(const double2 *D, int ld, int n, float4 *Ddf) {
   long long tot = (long long)n * n;
@@ -2255,20 +2286,29 @@ namespace {
 // no more CTAs than that are resident on one SM (a surplus CTA would block
 // in tcgen05.alloc until a neighbour exits).
 struct TcGeom {
-  int cols, ctas_per_sm;
+  int cols, ctas_per_sm, nbuf;
   size_t smem;
 };
 constexpr size_t SM_SMEM = 233472;  // 228 KB of shared memory per SM
-constexpr size_t TC_SMEM_MAX = 122880;
+constexpr size_t TC_SMEM_MAX = 232448;  // 227 KB, the per-CTA opt-in limit
 
-TcGeom tc_geom(int n1, int n2) {
+TcGeom tc_geom(int n1, int n2, bool breit = false) {
   TcGeom g;
   int need = n1 + n2, cols = 32;
   while (cols < need) cols *= 2;
   g.cols = cols;
-  size_t s = (size_t)tcq::layout(n1, n2).total;
-  int ctas = std::min(4, 512 / cols);
-  while (ctas > 1 && (s + 1024) * ctas > SM_SMEM) --ctas;
+  auto total = [&](int nb) {
+    return breit ? (size_t)tcq::layout_b(n1, n2).total : (size_t)tcq::layout(n1, n2, nb).total;
+  };
+  size_t s = total(1);
+  int ctas = std::min(2, 512 / cols);  // k_quartet_tc: at most 2 CTAs of 256 threads
+  while (ctas > 1 && (s + 1024 + 4096) * ctas > SM_SMEM) --ctas;  // + static shared memory
+  // one CTA per SM: double-buffered K chunks when they fit
+  g.nbuf = 1;
+  if (ctas == 1 && !breit && total(2) + 4096 <= TC_SMEM_MAX) {
+    g.nbuf = 2;
+    s = total(2);
+  }
   // smallest request that still keeps ctas + 1 CTAs off one SM
   size_t floor_req = SM_SMEM / (ctas + 1) - 1024 + 64;
   g.smem = std::max(s, floor_req);
@@ -2283,6 +2323,16 @@ TcGeom tc_geom(int n1, int n2) {
 // A run of consecutive entries of a quartet list and the kernel that
 // digests it under BG_PREC_AUTO (df: the split-precision kernel).
 enum { KIND_FP64 = 0, KIND_DF32 = 1, KIND_TC = 2 };
+
+// One row of the tuner's record: segment, class, sample time per kernel,
+// estimated error per kernel, choice.
+struct TuneRow {
+  int comp, key;
+  long long start, n;
+  float t[3];
+  double err[3];
+  int kind;
+};
 struct Run {
   long long start, count;
   int kind;    // KIND_*: the kernel that digests this run
@@ -2322,8 +2372,10 @@ struct bg_ctx {
   std::vector<int> segkey[4];  // angular class (la,lb,lc,ld) of each segment, base 4
   std::vector<Run> runs[4];
   bool tuned = false;
-  // split-precision copies
+  // split-precision copies: double-float E (and density), FP32 E (re, im) for
+  // the tensor-core kernel, both scaled by 2^(kexp lambda)
   float4 *d_Edf = nullptr, *d_Ddf = nullptr;
+  float2 *d_Ef = nullptr;
   int prec = BG_PREC_FP64;
   double err_budget = 1e-7;  // BG_PREC_AUTO: estimated energy error allowed per build (Eh)
   // Breit: sigma-coupled LS/SL E-coefficients (generated on first use) and
@@ -2338,6 +2390,12 @@ struct bg_ctx {
   long long nbquart[2] = {0, 0};
   int bquart_ilev = -1;
   std::vector<double> bqbound;  // [pair] sqrt max |(ab|ab)| of the LS pair, Breit
+  float2 *d_EBf = nullptr;      // FP32 copy of d_EB scaled by 2^(kexp lambda) (tensor cores)
+  std::vector<long long> bseg[2];  // Breit lists: class / bound-decade segments
+  std::vector<int> bsegkey[2];
+  std::vector<Run> bruns[2];
+  bool btuned = false;
+  std::vector<TuneRow> tune_rec, btune_rec;  // the tuner's last records (Coulomb, Breit)
   double2 *d_BX = nullptr;
   long long launches = 0;
   std::string err;
@@ -2362,6 +2420,7 @@ struct bg_batch {
   double2 *d_E = nullptr, *d_Ecv = nullptr;
   unsigned char *d_Eci = nullptr;
   float4 *d_Edf = nullptr, *d_Ddf = nullptr;
+  float2 *d_Ef = nullptr;
   Inst *d_inst = nullptr;
   int *d_ndim = nullptr;
   int *d_quart[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -2432,6 +2491,8 @@ int device_setup(int dev) {
   k_boys_table<<<(NBGRID + 127) / 128, 128>>>();
   if (cudaFuncSetAttribute(k_quartet_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)TC_SMEM_MAX) != cudaSuccess ||
+      cudaFuncSetAttribute(k_breit_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)TC_SMEM_MAX) != cudaSuccess ||
       cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)quartet_smem()) != cudaSuccess ||
       cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2458,6 +2519,16 @@ int wrong_device(bg_ctx *c) {
   c->err = "context was made on device " + std::to_string(c->dev) + ", device " +
            std::to_string(d) + " is current";
   return BG_ERR_STATE;
+}
+
+// Decades of the Schwarz bound Q_ab Q_cd that split an angular class into
+// segments: >= 1e1, [1, 1e1), ..., < 1e-5 (everything in one segment when
+// no bounds exist).
+constexpr int NBND = 8;
+inline int bound_bucket(double b, bool have) {
+  if (!have || !(b > 0.0)) return 0;
+  int e = (int)std::floor(std::log10(b));
+  return std::min(NBND - 1, std::max(0, 1 - e));
 }
 
 // Ordered shell quartets of the multi-centre build for one component class,
@@ -2488,7 +2559,8 @@ void pair_lists(const bg_ctx *c, int t, bool scr, std::vector<PairRec> (&pl)[MAX
   for (int a = 0; a < c->ns; ++a)
     for (int b = 0; b < c->ns; ++b) {
       long long idx = (long long)a * c->ns + b;
-      pl[c->shells[a].l][c->shells[b].l].push_back({a, b, scr ? c->qbound[idx * 2 + t] : 1.0, idx});
+      pl[c->shells[a].l][c->shells[b].l].push_back(
+          {a, b, c->qbound.empty() ? 1.0 : c->qbound[idx * 2 + t], idx});
     }
   if (scr)
     for (auto &row : pl)
@@ -2534,7 +2606,7 @@ void gen_quartets(const bg_ctx *c, int t1, int t2, int ilev, bool sym, Sink &&si
         if (ilev == 1 && itt > 1 && mcnt != 1) continue;
         if (ilev == 2 && itt > 3 && mcnt != 1) continue;
         if (mcnt == 1 && par) continue;
-        sink(x.a, x.b, y.a, y.b);
+        sink(x.a, x.b, y.a, y.b, x.q * y.q);
       }
     }
   }
@@ -2637,10 +2709,10 @@ int launch_quartets_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   }
   TcGeom g = tc_geom(n1, n2);
   tcq::Args a;
-  a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Edf; a.D = ddf;
+  a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Ef; a.D = ddf;
   a.GD = d_GD; a.GX = d_GX; a.ldd = n; a.ldf = ldf; a.nskp = c->nskp;
   a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym; a.inst = nullptr;
-  a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2;
+  a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2; a.nbuf = g.nbuf;
   long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
   k_quartet_tc<<<(unsigned)grid, tcq::TCT, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
@@ -2753,7 +2825,17 @@ int breit_prepare(bg_ctx *c) {
           bnt.push_back(nt);
         }
     }
-  return compact_e(c, c->d_EB, off, boff, bnt, &c->d_EBcv, &c->d_EBci);
+  int rc = compact_e(c, c->d_EB, off, boff, bnt, &c->d_EBcv, &c->d_EBci);
+  if (rc) return rc;
+  // FP32 copy for the tensor-core kernel, scaled per pair like the
+  // double-float Coulomb copy (2^(kexp lambda), kexp of the pair's exponent sum)
+  CK(c, cudaMalloc(&c->d_EBf, sizeof(float2) * std::max<long long>(off, 1)));
+  k_ebf<<<(unsigned)((long long)ns * ns * 2), 128>>>(c->d_EB, c->d_EBf, c->d_offq, c->d_pe,
+                                                     c->d_sh, ns);
+  cudaError_t e2 = cudaDeviceSynchronize();
+  if (e2 == cudaSuccess) e2 = cudaGetLastError();
+  if (e2 != cudaSuccess) return cuda_fail(c, e2, "k_ebf");
+  return 0;
 }
 
 // Shell quartets of the Breit classes with BRTFAST's centre and stage rules
@@ -2770,15 +2852,20 @@ int breit_prepare(bg_ctx *c) {
 // the LL and SS blocks it feeds being completed as Hermitian matrices
 // afterwards (Hermitian density).  The (SL|SL) class only feeds the SL
 // block, which BRTFAST overwrites by conjugation of the LS block.
-std::vector<int> build_breit_quartets(const bg_ctx *c, int t2, int ilev) {
+std::vector<int> build_breit_quartets(const bg_ctx *c, int t2, int ilev,
+                                      std::vector<long long> *seg = nullptr,
+                                      std::vector<int> *segkey = nullptr) {
   std::vector<int> out;
   bool scr = c->screen > 0.0 && !c->bqbound.empty();
+  bool bnds = !c->bqbound.empty();
   std::vector<int> byl[MAXLB + 1];
   for (int s = 0; s < c->ns; ++s) byl[c->shells[s].l].push_back(s);
+  if (seg) { seg->clear(); segkey->clear(); }
+  std::vector<int> cls[NBND];
   for (int la = MAXLB; la >= 0; --la)
   for (int lb = MAXLB; lb >= 0; --lb)
   for (int lc = MAXLB; lc >= 0; --lc)
-  for (int ld = MAXLB; ld >= 0; --ld)
+  for (int ld = MAXLB; ld >= 0; --ld) {
     for (int a : byl[la])
     for (int b : byl[lb])
       for (int cc : byl[lc])
@@ -2798,11 +2885,25 @@ std::vector<int> build_breit_quartets(const bg_ctx *c, int t2, int ilev) {
         if (mcnt != 1 && ilev < 3) continue;
         if (mcnt == 1 && ((la + lb) & 1) != ((lc + ld) & 1)) continue;
         // Schwarz: Q(LS pair ab) Q(cd as LS pair for t2 = 0, dc for SL)
-        if (scr && c->bqbound[pab] *
-                       c->bqbound[t2 == 0 ? pcd : (long long)d * c->ns + cc] < c->screen)
-          continue;
-        out.push_back(a); out.push_back(b); out.push_back(cc); out.push_back(d);
+        double bnd = bnds ? c->bqbound[pab] *
+                                c->bqbound[t2 == 0 ? pcd : (long long)d * c->ns + cc]
+                          : 1.0;
+        if (scr && bnd < c->screen) continue;
+        std::vector<int> &v = cls[bound_bucket(bnd, bnds)];
+        v.push_back(a); v.push_back(b); v.push_back(cc); v.push_back(d);
       }
+    // this class's quartets, largest bound decade first
+    for (int bk = 0; bk < NBND; ++bk) {
+      if (cls[bk].empty()) continue;
+      if (seg) {
+        seg->push_back((long long)out.size() / 4);
+        segkey->push_back(((la * 4 + lb) * 4 + lc) * 4 + ld);
+      }
+      out.insert(out.end(), cls[bk].begin(), cls[bk].end());
+      cls[bk].clear();
+    }
+  }
+  if (seg) seg->push_back((long long)out.size() / 4);
   return out;
 }
 
@@ -2818,6 +2919,24 @@ int launch_breit(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const 
   a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual; a.bound = bound;
   long long grid = std::min<long long>(nq, 152LL * 64);
   k_breit<<<(unsigned)grid, QT64, smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  CK(c, cudaGetLastError());
+  c->launches++;
+  return 0;
+}
+
+// Tensor-core Breit launch over list entries whose classes need at most
+// n1 + n2 TMEM columns; ddf holds the double-float density copy.
+int launch_breit_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const float4 *ddf,
+                    double *d_BX, int ldf, cudaStream_t st, int dual, int n1, int n2) {
+  if (nq <= 0) return 0;
+  TcGeom g = tc_geom(n1, n2, true);
+  tcq::ArgsB a;
+  a.sh = c->d_sh; a.pe = c->d_pe; a.offq = c->d_offq; a.E = c->d_EBf; a.D = ddf; a.BX = d_BX;
+  a.ns = c->ns; a.ldd = c->ndim; a.ldf = ldf; a.nskp = c->nskp; a.isym = c->isym;
+  a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual;
+  a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2;
+  long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
+  k_breit_tc<<<(unsigned)grid, tcq::TCT, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
   c->launches++;
   return 0;
@@ -2852,6 +2971,7 @@ int compute_breit_bounds(bg_ctx *c, cudaStream_t st) {
 // lists are streamed (regenerated on the host every build, CHUNK_Q at a
 // time, overlapping the kernels of the previous chunk).
 constexpr long long CACHE_Q = 1LL << 28;  // 268M quartets, 4.3 GB (default)
+
 constexpr long long CHUNK_Q = 1LL << 23;  // 8M quartets, 128 MB per buffer (default)
 
 // Autotuner of BG_PREC_AUTO.  A list sorted by angular class has segments
@@ -2885,15 +3005,25 @@ SegDims seg_dims(int key, int t1, int t2) {
   return d;
 }
 
+int g_gaunt_dims = 0;  // set by the Breit tuner: Gaunt-only kernel tables
+
+SegDims seg_dims_breit(int key) {
+  int la = (key >> 6) & 3, lb = (key >> 4) & 3, lc = (key >> 2) & 3, ld = key & 3;
+  SegDims d;
+  bool swp;
+  tcq::tcb_dims(la, lb, lc, ld, g_gaunt_dims, d.n1, d.n2, swp);
+  return d;
+}
+
 // Runs of one kernel kind over all segments (BG_PREC_TC32 on cached lists:
 // tensor-core runs sized per class).
 std::vector<Run> uniform_runs(const std::vector<long long> &seg, const std::vector<int> &key,
-                              int t1, int t2, int kind) {
+                              int t1, int t2, int kind, bool breit = false) {
   std::vector<Run> runs;
   for (size_t i = 0; i + 1 < seg.size(); ++i) {
     long long n = seg[i + 1] - seg[i];
     if (n <= 0) continue;
-    SegDims d = seg_dims(key[i], t1, t2);
+    SegDims d = breit ? seg_dims_breit(key[i]) : seg_dims(key[i], t1, t2);
     if (!runs.empty() && runs.back().start + runs.back().count == seg[i] &&
         (kind != KIND_TC || tc_geom(d.n1, d.n2).cols ==
                                 tc_geom(runs.back().n1, runs.back().n2).cols)) {
@@ -2918,7 +3048,7 @@ struct SegTune {
 template <class Launch, class Zero, class Energy>
 int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, int t1, int t2,
               cudaStream_t st, double budget, Launch &&launch, Zero &&zero, Energy &&energy,
-              std::vector<Run> &runs) {
+              std::vector<Run> &runs, bool breit = false, std::vector<TuneRow> *rec = nullptr) {
   runs.clear();
   if (seg.size() < 2) return 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -2928,12 +3058,13 @@ int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, in
   for (size_t i = 0; i + 1 < seg.size() && !rc; ++i) {
     long long n = seg[i + 1] - seg[i];
     if (n <= 0) continue;
-    SegDims d = seg_dims(key[i], t1, t2);
+    SegDims d = breit ? seg_dims_breit(key[i]) : seg_dims(key[i], t1, t2);
     SegTune x = {seg[i], n, d.n1, d.n2, {0.f, 0.f, 0.f}, {0.0, 0.0, 0.0}, KIND_FP64};
     if (n >= TUNE_MIN) {
       long long m = std::min(n, TUNE_SAMPLE);
       double ej[3] = {0, 0, 0}, ek[3] = {0, 0, 0};
       for (int k = 0; k < 3 && !rc; ++k) {
+        if (breit && k == KIND_DF32) continue;  // the Breit build has no split-precision kernel
         rc = zero();
         if (!rc) rc = launch(k, seg[i], m, d.n1, d.n2);
         if (!rc) rc = energy(ej[k], ek[k]);
@@ -2946,7 +3077,7 @@ int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, in
       }
       for (int k = 0; k < 3; ++k)
         x.err[k] = (fabs(ej[k] - ej[0]) + fabs(ek[k] - ek[0])) * (double)n / (double)m;
-      x.kind = x.t[1] < x.t[0] ? KIND_DF32 : KIND_FP64;
+      x.kind = (!breit && x.t[1] < x.t[0]) ? KIND_DF32 : KIND_FP64;
     }
     tv.push_back(x);
   }
@@ -2968,6 +3099,13 @@ int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, in
     if (used + tv[i].err[2] <= budget) {
       used += tv[i].err[2];
       tv[i].kind = KIND_TC;
+    }
+  if (rec)
+    for (size_t i = 0, j = 0; i + 1 < seg.size(); ++i) {
+      if (seg[i + 1] - seg[i] <= 0) continue;
+      const SegTune &x = tv[j++];
+      rec->push_back({2 * t1 + t2, key[i], x.start, x.n, {x.t[0], x.t[1], x.t[2]},
+                      {x.err[0], x.err[1], x.err[2]}, x.kind});
     }
   for (const SegTune &x : tv) {
     if (!runs.empty() && runs.back().kind == x.kind &&
@@ -3063,6 +3201,7 @@ int tune_ctx(bg_ctx *c, const double2 *d_D, int ldd, cudaStream_t st) {
       const int *q = c->d_quart[k];
       // the budget is shared by the component classes
       double budget = c->err_budget / (c->ncomp * c->ncomp);
+      if (k == 0) c->tune_rec.clear();
       rc = tune_runs(c->seg[k], c->segkey[k], t1, t2, st, budget,
                      [&](int kind, long long start, long long m, int n1, int n2) {
         const int *qq = q + 4 * start;
@@ -3072,7 +3211,7 @@ int tune_ctx(bg_ctx *c, const double2 *d_D, int ldd, cudaStream_t st) {
           return launch_quartets_tc(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, c->d_Ddf, 2, n1, n2,
                                     false);
         return launch_quartets_fp64(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, 2, nullptr);
-      }, zero, energy, c->runs[k]);
+      }, zero, energy, c->runs[k], false, &c->tune_rec);
     }
   cudaFree(gd);
   cudaFree(gx);
@@ -3113,7 +3252,7 @@ int stream_class(bg_ctx *c, int t1, int t2, int ilev, const double2 *d_D, int ld
     if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaEventSynchronize");
     fill = 0;
   };
-  gen_quartets(c, t1, t2, ilev, true, [&](int a, int b, int cc, int d) {
+  gen_quartets(c, t1, t2, ilev, true, [&](int a, int b, int cc, int d, double) {
     if (rc) return;
     int *h = c->h_chunk[cur] + 4 * fill;
     h[0] = a; h[1] = b; h[2] = cc; h[3] = d;
@@ -3148,14 +3287,14 @@ int batch_lists(bg_batch *b, int ilev) {
   constexpr int NKEY = (MAXLB + 1) * (MAXLB + 1) * (MAXLB + 1) * (MAXLB + 1);
   for (int t1 = 0; t1 < b->ncomp; ++t1)
     for (int t2 = 0; t2 < b->ncomp; ++t2) {
-      std::vector<std::vector<int>> bucket(NKEY);
+      std::vector<std::vector<int>> bucket(NKEY * NBND);
       for (int i = 0; i < b->n; ++i) {
         const bg_ctx *c = b->shadow[i];
         int s0 = b->sbase[i];
-        gen_quartets(c, t1, t2, ilev, true, [&](int a, int bb, int cc, int d) {
+        gen_quartets(c, t1, t2, ilev, true, [&](int a, int bb, int cc, int d, double bnd) {
           int key = ((c->shells[a].l * (MAXLB + 1) + c->shells[bb].l) * (MAXLB + 1) +
                      c->shells[cc].l) * (MAXLB + 1) + c->shells[d].l;
-          std::vector<int> &v = bucket[NKEY - 1 - key];
+          std::vector<int> &v = bucket[(NKEY - 1 - key) * NBND + bound_bucket(bnd, !c->qbound.empty())];
           v.push_back(a + s0); v.push_back(bb + s0); v.push_back(cc + s0); v.push_back(d + s0);
         });
       }
@@ -3171,8 +3310,8 @@ int batch_lists(bg_batch *b, int ilev) {
       size_t pos = 0;
       for (auto &v : bucket) {
         if (v.empty()) continue;
-        b->seg[k].push_back((long long)pos / 4);  // one angular class per bucket
-        b->segkey[k].push_back(NKEY - 1 - (int)(&v - &bucket[0]));
+        b->seg[k].push_back((long long)pos / 4);  // one angular class and bound decade per bucket
+        b->segkey[k].push_back(NKEY - 1 - (int)(&v - &bucket[0]) / NBND);
         BK(b, cudaMemcpy(b->d_quart[k] + pos, v.data(), sizeof(int) * v.size(),
                          cudaMemcpyHostToDevice));
         pos += v.size();
@@ -3205,10 +3344,10 @@ int batch_launch(bg_batch *b, int t1, int t2, int kind, long long start, long lo
   } else if (kind == KIND_TC) {
     TcGeom g = tc_geom(n1, n2);
     tcq::Args a;
-    a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_Edf; a.D = b->d_Ddf;
+    a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_Ef; a.D = b->d_Ddf;
     a.GD = d_GD; a.GX = d_GX; a.ldd = 0; a.ldf = 0; a.nskp = 0;
     a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.inst = b->d_inst;
-    a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2;
+    a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2; a.nbuf = g.nbuf;
     long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
     k_quartet_tc<<<(unsigned)grid, tcq::TCT, g.smem, st>>>(a, quart, nq, t1, t2);
   } else {
@@ -3371,6 +3510,12 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
     return BG_ERR_CUDA;
   }
   k_econv<<<(unsigned)((long long)ns * ns), 128>>>(c->d_E, c->d_Edf, c->d_pe, c->d_sh, ns, ncomp);
+  if ((e = cudaMalloc(&c->d_Ef, sizeof(float2) * std::max<long long>(off, 1))) != cudaSuccess) {
+    cuda_fail(nullptr, e, "cudaMalloc");
+    bertha_gpu_free(c);
+    return BG_ERR_CUDA;
+  }
+  k_ef<<<1024, 256>>>(c->d_Edf, c->d_Ef, off);
   e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -3415,7 +3560,7 @@ int bertha_gpu_set_precision(bg_ctx *c, int prec) {
   if (prec != BG_PREC_FP64 && prec != BG_PREC_DF32 && prec != BG_PREC_AUTO &&
       prec != BG_PREC_TC32)
     return BG_ERR_ARG;
-  if (prec != c->prec) c->tuned = false;
+  if (prec != c->prec) c->tuned = c->btuned = false;
   c->prec = prec;
   return BG_OK;
 }
@@ -3483,6 +3628,19 @@ int bertha_gpu_kernel_stats(const bg_ctx *c, long long *nq, int *nruns) {
   return BG_OK;
 }
 
+int bertha_gpu_breit_kernel_stats(const bg_ctx *c, long long *nq, int *nruns) {
+  if (!c || !nq) return BG_ERR_ARG;
+  nq[0] = nq[1] = nq[2] = 0;
+  int r = 0;
+  for (int k = 0; k < 2; ++k)
+    for (const Run &x : c->bruns[k]) {
+      nq[x.kind] += x.count;
+      ++r;
+    }
+  if (nruns) *nruns = r;
+  return BG_OK;
+}
+
 int bertha_gpu_batch_auto_stats(const bg_batch *b, long long *nq_fp64, long long *nq_df32,
                                 int *nruns) {
   if (!b) return BG_ERR_ARG;
@@ -3499,9 +3657,28 @@ int bertha_gpu_batch_kernel_stats(const bg_batch *b, long long *nq, int *nruns) 
   return BG_OK;
 }
 
+int bertha_gpu_tuning_record(const bg_ctx *c, int breit, int cap, int *info,
+                             double *vals, int *nrows) {
+  if (!c || !nrows) return BG_ERR_ARG;
+  const std::vector<TuneRow> &r = breit ? c->btune_rec : c->tune_rec;
+  *nrows = (int)r.size();
+  if (!info || !vals) return BG_OK;
+  for (int i = 0; i < (int)r.size() && i < cap; ++i) {
+    info[4 * i] = r[i].comp;
+    info[4 * i + 1] = r[i].key;
+    info[4 * i + 2] = (int)std::min<long long>(r[i].n, 0x7fffffff);
+    info[4 * i + 3] = r[i].kind;
+    for (int k = 0; k < 3; ++k) {
+      vals[6 * i + k] = r[i].t[k];
+      vals[6 * i + 3 + k] = r[i].err[k];
+    }
+  }
+  return BG_OK;
+}
+
 int bertha_gpu_set_error_budget(bg_ctx *c, double eh) {
   if (!c || !(eh >= 0.0)) return BG_ERR_ARG;
-  if (eh != c->err_budget) c->tuned = false;
+  if (eh != c->err_budget) c->tuned = c->btuned = false;
   c->err_budget = eh;
   return BG_OK;
 }
@@ -3620,9 +3797,11 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
   k_zero2d<<<1024, 256, 0, st>>>(d_gxch, c->ndim, ldf);
   CK(c, cudaGetLastError());
   c->launches += 2;
-  if (c->screen > 0.0 && c->qbound.empty()) {
+  // bounds for screening and, under BG_PREC_AUTO, for the bound decades
+  if ((c->screen > 0.0 || c->prec == BG_PREC_AUTO) && c->qbound.empty()) {
     int rc = compute_bounds(c, st);
     if (rc) return rc;
+    c->quart_ilev = -1;
   }
   if (c->quart_ilev != ilev) {
     for (int k = 0; k < 4; ++k) {
@@ -3633,19 +3812,45 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
     c->stream_lists = false;
     long long total = 0;
     std::vector<int> q[4];
+    // each angular class's quartets grouped by the decade of their Schwarz
+    // bound (largest first): segments of one class and bound decade, so that
+    // the autotuner can give the small-magnitude part of a class another
+    // kernel than its large part
+    bool bnds = !c->qbound.empty();
     for (int t1 = 0; t1 < c->ncomp && !c->stream_lists; ++t1)
       for (int t2 = 0; t2 < c->ncomp && !c->stream_lists; ++t2) {
         int k = 2 * t1 + t2;
-        gen_quartets(c, t1, t2, ilev, true, [&](int a, int b, int cc, int d) {
+        std::vector<int> cls[NBND];
+        int curkey = -1;
+        c->seg[k].clear();
+        c->segkey[k].clear();
+        auto flush = [&]() {
+          for (int bk = 0; bk < NBND; ++bk) {
+            if (cls[bk].empty()) continue;
+            c->seg[k].push_back((long long)q[k].size() / 4);
+            c->segkey[k].push_back(curkey);
+            q[k].insert(q[k].end(), cls[bk].begin(), cls[bk].end());
+            cls[bk].clear();
+          }
+        };
+        gen_quartets(c, t1, t2, ilev, true, [&](int a, int b, int cc, int d, double bnd) {
           if (c->stream_lists) return;
-          q[k].push_back(a); q[k].push_back(b); q[k].push_back(cc); q[k].push_back(d);
+          int key = ((c->shells[a].l * 4 + c->shells[b].l) * 4 + c->shells[cc].l) * 4 +
+                    c->shells[d].l;
+          if (key != curkey) {
+            flush();
+            curkey = key;
+          }
+          std::vector<int> &v = cls[bound_bucket(bnd, bnds)];
+          v.push_back(a); v.push_back(b); v.push_back(cc); v.push_back(d);
           if (++total > (c->cache_q > 0 ? c->cache_q : CACHE_Q)) c->stream_lists = true;
         });
+        flush();
+        c->seg[k].push_back((long long)q[k].size() / 4);
       }
     c->tuned = false;
     if (!c->stream_lists)
       for (int k = 0; k < 4; ++k) {
-        c->seg[k] = class_segments(c->shells, q[k], c->segkey[k]);
         c->runs[k].clear();
         c->nquart[k] = (long long)q[k].size() / 4;
         if (!q[k].empty()) {
@@ -3762,28 +3967,91 @@ int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
   k_zero2d<<<1024, 256, 0, st>>>(d_bxch, c->ndim, ldf);
   CK(c, cudaGetLastError());
   c->launches++;
-  if (c->screen > 0.0 && c->bqbound.empty()) {
+  // bounds for screening and, under BG_PREC_AUTO, for the bound decades
+  if ((c->screen > 0.0 || c->prec == BG_PREC_AUTO) && c->bqbound.empty()) {
     rc = compute_breit_bounds(c, st);
     if (rc) return rc;
+    c->bquart_ilev = -1;
   }
   if (c->bquart_ilev != ilev) {
     for (int k = 0; k < 2; ++k) {
       if (c->d_bquart[k]) cudaFree(c->d_bquart[k]);
       c->d_bquart[k] = nullptr;
       c->nbquart[k] = 0;
-      std::vector<int> q = build_breit_quartets(c, k, ilev);
+      std::vector<int> q = build_breit_quartets(c, k, ilev, &c->bseg[k], &c->bsegkey[k]);
       c->nbquart[k] = (long long)q.size() / 4;
+      c->bruns[k].clear();
       if (!q.empty()) {
         CK(c, cudaMalloc(&c->d_bquart[k], sizeof(int) * q.size()));
         CK(c, cudaMemcpy(c->d_bquart[k], q.data(), sizeof(int) * q.size(), cudaMemcpyHostToDevice));
       }
     }
     c->bquart_ilev = ilev;
+    c->btuned = false;
+  }
+  const double2 *D = (const double2 *)d_dent;
+  bool byrun = c->prec == BG_PREC_AUTO || c->prec == BG_PREC_TC32;
+  if (byrun) {
+    int n = c->ndim;
+    if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
+    k_dconv<<<1024, 256, 0, st>>>(D, ldd, n, c->d_Ddf);
+    CK(c, cudaGetLastError());
+    c->launches++;
+    g_gaunt_dims = c->gaunt;
+    if (!c->btuned && c->prec == BG_PREC_TC32) {
+      for (int k = 0; k < 2; ++k)
+        c->bruns[k] = uniform_runs(c->bseg[k], c->bsegkey[k], 0, k, KIND_TC, true);
+      c->btuned = true;
+    }
+    if (!c->btuned) {
+      // per class and bound decade: FP64 or tensor cores within the error
+      // budget, timed and checked into a scratch output
+      double *bx = nullptr, *d_e = nullptr;
+      CK(c, cudaMalloc(&bx, sizeof(double2) * (size_t)n * n));
+      CK(c, cudaMalloc(&d_e, 2 * sizeof(double)));
+      auto zero = [&]() {
+        return cudaMemsetAsync(bx, 0, sizeof(double2) * (size_t)n * n, st) == cudaSuccess ? 0 : -1;
+      };
+      auto energy = [&](double &ej, double &ek) {
+        if (cudaMemsetAsync(d_e, 0, 2 * sizeof(double), st) != cudaSuccess) return -1;
+        k_edot<<<256, 256, 0, st>>>(D, ldd, (const double2 *)bx, n, n, nullptr, nullptr, 1, d_e);
+        double h[2];
+        if (cudaMemcpyAsync(h, d_e, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+          return -1;
+        ej = 0.0;
+        ek = h[0];
+        return 0;
+      };
+      c->btune_rec.clear();
+      for (int k = 0; k < 2 && !rc; ++k) {
+        const int *q = c->d_bquart[k];
+        rc = tune_runs(c->bseg[k], c->bsegkey[k], 0, k, st, c->err_budget,
+                       [&](int kind, long long start, long long m, int n1, int n2) {
+          if (kind == KIND_TC)
+            return launch_breit_tc(c, q + 4 * start, m, 0, k, c->d_Ddf, bx, n, st, 2, n1, n2);
+          return launch_breit(c, q + 4 * start, m, 0, k, D, ldd, bx, n, st, 2);
+        }, zero, energy, c->bruns[k], true, &c->btune_rec);
+      }
+      cudaFree(bx);
+      cudaFree(d_e);
+      if (rc) return rc > 0 ? rc : cuda_fail(c, cudaGetLastError(), "Breit autotuning");
+      c->btuned = true;
+    }
   }
   for (int k = 0; k < 2; ++k) {
-    rc = launch_breit(c, c->d_bquart[k], c->nbquart[k], 0, k, (const double2 *)d_dent, ldd,
-                      d_bxch, ldf, st, 2);
-    if (rc) return rc;
+    if (byrun) {
+      for (const Run &r : c->bruns[k]) {
+        const int *q = c->d_bquart[k] + 4 * r.start;
+        rc = r.kind == KIND_TC
+                 ? launch_breit_tc(c, q, r.count, 0, k, c->d_Ddf, d_bxch, ldf, st, 2, r.n1, r.n2)
+                 : launch_breit(c, q, r.count, 0, k, D, ldd, d_bxch, ldf, st, 2);
+        if (rc) return rc;
+      }
+    } else {
+      rc = launch_breit(c, c->d_bquart[k], c->nbquart[k], 0, k, D, ldd, d_bxch, ldf, st, 2);
+      if (rc) return rc;
+    }
   }
   int n = c->nskp;
   // LL and SS blocks: add the (dc|ba) images of the halved (LS|SL) list
@@ -3892,11 +4160,13 @@ void bertha_gpu_free(bg_ctx *c) {
   cudaFree(c->d_E);
   for (int k = 0; k < 4; ++k) cudaFree(c->d_quart[k]);
   cudaFree(c->d_Edf);
+  cudaFree(c->d_Ef);
   cudaFree(c->d_Ddf);
   cudaFree(c->d_D);
   cudaFree(c->d_GD);
   cudaFree(c->d_GX);
   cudaFree(c->d_EB);
+  cudaFree(c->d_EBf);
   cudaFree(c->d_offq);
   for (int k = 0; k < 2; ++k) {
     if (c->h_chunk[k]) cudaFreeHost(c->h_chunk[k]);
@@ -3995,6 +4265,7 @@ int bertha_gpu_batch_create(bg_batch **out, int n, bg_ctx *const *ctxs,
       (e = cudaMalloc(&b->d_Ecv, sizeof(double2) * std::max<long long>(net, 1))) ||
       (e = cudaMalloc(&b->d_Eci, std::max<long long>(net, 1))) ||
       (e = cudaMalloc(&b->d_Edf, sizeof(float4) * std::max<long long>(net, 1))) ||
+      (e = cudaMalloc(&b->d_Ef, sizeof(float2) * std::max<long long>(net, 1))) ||
       (e = cudaMalloc(&b->d_inst, sizeof(Inst) * n)) ||
       (e = cudaMalloc(&b->d_ndim, sizeof(int) * n)))
     return fail("cudaMalloc");
@@ -4018,7 +4289,8 @@ int bertha_gpu_batch_create(bg_batch **out, int n, bg_ctx *const *ctxs,
         ((e = cudaMemcpy(b->d_E + ebase[i], c->d_E, sizeof(double2) * ne, cudaMemcpyDeviceToDevice)) ||
          (e = cudaMemcpy(b->d_Ecv + ebase[i], c->d_Ecv, sizeof(double2) * ne, cudaMemcpyDeviceToDevice)) ||
          (e = cudaMemcpy(b->d_Eci + ebase[i], c->d_Eci, ne, cudaMemcpyDeviceToDevice)) ||
-         (e = cudaMemcpy(b->d_Edf + ebase[i], c->d_Edf, sizeof(float4) * ne, cudaMemcpyDeviceToDevice))))
+         (e = cudaMemcpy(b->d_Edf + ebase[i], c->d_Edf, sizeof(float4) * ne, cudaMemcpyDeviceToDevice)) ||
+         (e = cudaMemcpy(b->d_Ef + ebase[i], c->d_Ef, sizeof(float2) * ne, cudaMemcpyDeviceToDevice))))
       return fail("cudaMemcpy");
   }
   *out = b;
@@ -4157,6 +4429,7 @@ void bertha_gpu_batch_free(bg_batch *b) {
   cudaFree(b->d_Ecv);
   cudaFree(b->d_Eci);
   cudaFree(b->d_Edf);
+  cudaFree(b->d_Ef);
   cudaFree(b->d_Ddf);
   cudaFree(b->d_inst);
   cudaFree(b->d_ndim);

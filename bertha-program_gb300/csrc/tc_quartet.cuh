@@ -8,7 +8,7 @@
 // in global memory.  Included inside the anonymous namespace of
 // bertha_gpu.cu.
 //
-// One 128-thread CTA per shell quartet (grid-stride).  With the left pair
+// One 256-thread CTA per shell quartet (grid-stride).  With the left pair
 // (labels L, Hermite terms s) and the right pair (labels R, terms q):
 //   GEMM 1  D1[row][q]   = sum_s  E_L[row][s] * R[s+q]        rows (L, set, re/im)
 //   GEMM 2  D2[row][col] = sum_q  G[row][q] * E_R[col][q]     cols (R, set, re/im)
@@ -20,7 +20,7 @@
 
 namespace tcq {
 
-constexpr int TCT = 128;        // threads per CTA (4 warps, one per TMEM lane quarter)
+constexpr int TCT = 256;        // threads per CTA (8 warps; warps w and w+4 share TMEM lane quarter w%4)
 constexpr int KC = 32;          // K elements per staged chunk (4 MMAs of K = 8)
 constexpr int MROWS = 128;      // rows per M tile
 constexpr int MLAB = MROWS / 4; // left labels per M tile
@@ -58,11 +58,28 @@ __device__ __forceinline__ int kmaj(int row, int k) {
   return (((row >> 3) * (KC / 4) + (k >> 2)) * 8 + (row & 7)) * 4 + (k & 3);
 }
 
-// x = hi + lo with hi carrying the 10 explicit mantissa bits a TF32 operand
-// keeps; the tensor core reads lo as TF32 again, ~22 bits in all.
+// TF32 value of x rounded to nearest (ties away from zero).
+__device__ __forceinline__ float tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// x = hi + lo, both TF32 and rounded to nearest, ~22 significant bits in
+// all: rounding (not truncation) keeps the dropped parts of unbiased sign,
+// so the products' errors average out in the J/K sums instead of drifting.
 __device__ __forceinline__ void tsplit(float x, float &h, float &l) {
-  h = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
-  l = x - h;
+  h = tf32(x);
+  l = tf32(x - h);
+}
+
+// Hermite index tables in shared memory: t | u << 8 | v << 16 | lambda << 24
+// (a lane-divergent __constant__ read would be serialised).
+__device__ __forceinline__ int tuvL(uint32_t w) { return (int)(w >> 24); }
+__device__ __forceinline__ int hsum(uint32_t a, uint32_t b) {
+  int t = (int)(a & 255) + (int)(b & 255), u = (int)((a >> 8) & 255) + (int)((b >> 8) & 255);
+  int v = (int)((a >> 16) & 255) + (int)((b >> 16) & 255);
+  return hidx(t, u, v);
 }
 
 __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id,
@@ -138,17 +155,21 @@ __host__ __device__ inline void tc_dims(int la, int lb, int lc, int ld, int t1, 
   n2 = rup(4 * nlR, 16);
 }
 
-// Shared-memory layout (bytes from a 128-byte aligned base).
+// Shared-memory layout (bytes from a 128-byte aligned base).  The staging
+// region holds nbuf buffers of gsz bytes (double buffering lets the next K
+// chunk be staged while the tensor cores work on the current one); the D2
+// slab and the FP64 R recursion reuse it when no GEMM is in flight.
 struct Layout {
-  int stage, rf, dsm, acc, fb, total;
+  int stage, gsz, rf, dsm, acc, fb, total;
 };
-__host__ __device__ inline Layout layout(int n1max, int n2max) {
+__host__ __device__ inline Layout layout(int n1max, int n2max, int nbuf = 1) {
   Layout L;
   int g1 = 2 * MROWS * KC * 4 + 2 * n1max * KC * 4;       // A1 and B1, hi and lo
   int g2 = 2 * MROWS * KC * 4 + 2 * n2max * KC * 4;       // A2 and B2
   int pslab = MROWS * PSTR * 4;                            // D2 slab
   int rrec = 2 * NTR * 8;                                  // FP64 R recursion buffers
-  int st = g1 > g2 ? g1 : g2;
+  L.gsz = rup(g1 > g2 ? g1 : g2, 128);
+  int st = nbuf * L.gsz;
   st = st > pslab ? st : pslab;
   st = st > rrec ? st : rrec;
   L.stage = 0;
@@ -160,16 +181,33 @@ __host__ __device__ inline Layout layout(int n1max, int n2max) {
   return L;
 }
 
+// MMA completion tracking of up to two staging buffers: one mbarrier per
+// buffer, its phase parity, and whether a commit on it is outstanding.
+struct Pipe {
+  uint64_t *bar;
+  uint32_t ph[2];
+  bool pend[2];
+};
+
+// Waits for the outstanding commit on buffer b (if any); false on timeout.
+__device__ __forceinline__ bool pipe_wait(Pipe &p, int b) {
+  if (!p.pend[b]) return true;
+  bool ok = wait(&p.bar[b], p.ph[b]);
+  p.ph[b] ^= 1;
+  p.pend[b] = false;
+  return ok;
+}
+
 struct Args {
   const Shell *sh;
   const PairE *pe;
-  const float4 *E;   // double-float E copy (k_econv): hi parts used
+  const float2 *E;   // FP32 E copy (re, im), scaled like the double-float copy
   const float4 *D;   // double-float density, n x n (batched: Inst placement)
   double *GD, *GX;
   int ldd, ldf, nskp, isym, racah1;
   int sym;           // as QArgsDF
   const Inst *inst;
-  int tmem_cols, n1max, n2max;
+  int tmem_cols, n1max, n2max, nbuf;
 };
 
 __device__ inline float fsgn(float x, float s) { return s < 0.f ? -x : x; }
@@ -206,19 +244,16 @@ __device__ __forceinline__ void sadd(float2 *p, float2 v) {
 
 }  // namespace tcq
 
-__global__ void __launch_bounds__(tcq::TCT)
+__global__ void __launch_bounds__(tcq::TCT, 2)
 k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   using namespace tcq;
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char *base =
       (unsigned char *)(((uintptr_t)tc_smem_raw + 127) & ~(uintptr_t)127);
-  const Layout LY = layout(q.n1max, q.n2max);
-  float *A1h = (float *)(base + LY.stage);
-  float *A1l = A1h + MROWS * KC;
-  float *B1h = A1l + MROWS * KC;
-  float *B1l = B1h + q.n1max * KC;
-  float *B2h = A1l + MROWS * KC;  // GEMM 2 staging reuses the GEMM 1 space
-  float *B2l = B2h + q.n2max * KC;
+  const Layout LY = layout(q.n1max, q.n2max, q.nbuf);
+  // staging buffer b: A hi, A lo (MROWS x KC each), then B hi, B lo (GEMM 1:
+  // n1max rows each; GEMM 2 reuses the space with n2max rows)
+  auto bufA = [&](int b) { return (float *)(base + LY.stage + b * LY.gsz); };
   float *P = (float *)(base + LY.stage);          // D2 slab (epilogue)
   double *R = (double *)(base + LY.stage);        // FP64 recursion (before the GEMMs)
   double *R2 = R + NTR;
@@ -226,23 +261,32 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   float2 *Dsm = (float2 *)(base + LY.dsm);        // D(c,d), D(c,b), D(a,b), D(a,d)
   float2 *Acc = (float2 *)(base + LY.acc);        // J(a,b), K(a,d), J2(c,d), K2(c,b)
   double *F = (double *)(base + LY.fb);
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
   __shared__ double sgeo[8];
   __shared__ int sk;
+  __shared__ uint32_t stuv[NTR];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quad = warp & 3, half = warp >> 2;  // TMEM lane quarter, column half
 
+  for (int i = tid; i < NTR; i += TCT)
+    stuv[i] = (uint32_t)c_t[i] | ((uint32_t)c_u[i] << 8) | ((uint32_t)c_v[i] << 16) |
+              ((uint32_t)(c_t[i] + c_u[i] + c_v[i]) << 24);
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                  :: "r"(saddr(&tslot)), "r"(q.tmem_cols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar)));
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar[1])));
+  }
   fence_before();
   __syncthreads();
   fence_after();
   const uint32_t tmem = tslot;
-  uint32_t phase = 0;
+  Pipe pp = {mbar, {0u, 0u}, {false, false}};
+  const int nbuf = q.nbuf;
   bool abort = false;
 
   for (long long qi = blockIdx.x; qi < nq && !abort; qi += gridDim.x) {
@@ -309,7 +353,8 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
             for (int i = 0; i < n; ++i) pw *= m2a;
             val = pw * F[n];
           } else {
-            int t = c_t[k], u = c_u[k], v = c_v[k];
+            uint32_t w = stuv[k];
+            int t = w & 255, u = (w >> 8) & 255, v = (w >> 16) & 255;
             if (t > 0) {
               val = X * cur[hidx(t - 1, u, v)];
               if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
@@ -329,15 +374,13 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
       // PRE * R scaled by 2^(-k lambda) (exponent balancing), in FP32
       double pre = sgeo[4];
       int k = sk;
-      for (int i = tid; i < ntuv(lam); i += TCT) {
-        int L = c_t[i] + c_u[i] + c_v[i];
-        Rf[i] = __double2float_rn(ldexp(cur[i] * pre, -k * L));
-      }
+      for (int i = tid; i < ntuv(lam); i += TCT)
+        Rf[i] = __double2float_rn(ldexp(cur[i] * pre, -k * tuvL(stuv[i])));
     }
     // roles
-    const float4 *Eab = q.E + pab_e.off[t1];
-    const float4 *Ecd = q.E + pcd_e.off[t2];
-    const float4 *EL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
+    const float2 *Eab = q.E + pab_e.off[t1];
+    const float2 *Ecd = q.E + pcd_e.off[t2];
+    const float2 *EL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
     int kL = swp ? pcd_e.kexp : pab_e.kexp, kR = swp ? pab_e.kexp : pcd_e.kexp;
     int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
     int nlab = nla * nlb, nlcd = nlc * nld;
@@ -369,32 +412,47 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
 
     const uint32_t tD1 = tmem, tD2 = tmem + (uint32_t)n1;
     const uint32_t id1 = idesc(MROWS, n1), id2 = idesc(MROWS, n2);
+    const uint32_t lanebase = (uint32_t)(quad * 32) << 16;
     for (int l0 = 0; l0 < nlL && !abort; l0 += MLAB) {
       int ntl = min(MLAB, nlL - l0);
       // ---- GEMM 1: D1 = E_L (rows) x Hankel R (columns q), K = s ----
-      for (int kc = 0; kc < nL && !abort; kc += KC) {
-        for (int w = tid; w < MLAB * 2 * KC; w += TCT) {
-          int lab = w / (2 * KC), set = (w / KC) & 1, kk = w % KC;
-          int s = kc + kk;
-          float vr = 0.f, vi = 0.f;
-          if (lab < ntl && s < nL) {
-            float4 e = EL[((long long)(l0 + lab) * 2 + set) * nL + s];
-            int L = c_t[s] + c_u[s] + c_v[s];
-            float f = ldexpf(1.0f, (kq0 - kL) * L);
-            vr = e.x * f;
-            vi = e.z * f;
+      // K chunk c is staged into buffer c % nbuf while the MMAs of chunk
+      // c - 1 run; a buffer is rewritten once its previous MMAs completed
+      for (int c = 0, kc = 0; kc < nL && !abort; ++c, kc += KC) {
+        int bsel = c % nbuf;
+        if (__syncthreads_or(!pipe_wait(pp, bsel))) { abort = true; break; }
+        fence_after();
+        float *A1h = bufA(bsel), *A1l = A1h + MROWS * KC;
+        float *B1h = A1l + MROWS * KC, *B1l = B1h + q.n1max * KC;
+        {
+          // E_L chunk: (label, set, s) items, each filling a re and an im
+          // row; the loads are issued together, then split and stored
+          constexpr int AIT = MLAB * 2 * KC / TCT;
+          float2 ev[AIT];
+#pragma unroll
+          for (int j = 0; j < AIT; ++j) {
+            int w = tid + j * TCT;
+            int lab = w / (2 * KC), set = (w / KC) & 1, s = kc + (w % KC);
+            ev[j] = (lab < ntl && s < nL) ? EL[((long long)(l0 + lab) * 2 + set) * nL + s]
+                                          : make_float2(0.f, 0.f);
           }
-          int row = lab * 4 + set * 2;
-          float h, l;
-          tsplit(vr, h, l);
-          A1h[kmaj(row, kk)] = h; A1l[kmaj(row, kk)] = l;
-          tsplit(vi, h, l);
-          A1h[kmaj(row + 1, kk)] = h; A1l[kmaj(row + 1, kk)] = l;
+#pragma unroll
+          for (int j = 0; j < AIT; ++j) {
+            int w = tid + j * TCT;
+            int lab = w / (2 * KC), set = (w / KC) & 1, kk = w % KC, s = kc + kk;
+            float f = s < nL ? ldexpf(1.0f, (kq0 - kL) * tuvL(stuv[s])) : 0.f;
+            int row = lab * 4 + set * 2;
+            float h, l;
+            tsplit(ev[j].x * f, h, l);
+            A1h[kmaj(row, kk)] = h; A1l[kmaj(row, kk)] = l;
+            tsplit(ev[j].y * f, h, l);
+            A1h[kmaj(row + 1, kk)] = h; A1l[kmaj(row + 1, kk)] = l;
+          }
         }
         for (int w = tid; w < n1 * KC; w += TCT) {
           int n = w / KC, kk = w % KC, s = kc + kk;
           float v = 0.f;
-          if (n < nR && s < nL) v = Rf[hidx(c_t[s] + c_t[n], c_u[s] + c_u[n], c_v[s] + c_v[n])];
+          if (n < nR && s < nL) v = Rf[hsum(stuv[s], stuv[n])];
           float h, l;
           tsplit(v, h, l);
           B1h[kmaj(n, kk)] = h; B1l[kmaj(n, kk)] = l;
@@ -414,48 +472,75 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
             mma(tD1, ah, bl, id1, 1u);
             mma(tD1, al, bh, id1, 1u);
           }
-          commit(&mbar);
+          commit(&pp.bar[bsel]);
         }
-        bool ok = wait(&mbar, phase);
-        phase ^= 1;
+        pp.pend[bsel] = true;
+      }
+      // D1 complete before its columns are read
+      {
+        bool ok = pipe_wait(pp, 0);
+        ok = pipe_wait(pp, 1) && ok;
         if (__syncthreads_or(!ok)) abort = true;
         fence_after();
       }
       // ---- GEMM 2: D2 = G (rows, K = q) x E_R (columns) ----
-      for (int kc = 0; kc < n1 && !abort; kc += KC) {
+      for (int c = 0, kc = 0; kc < n1 && !abort; ++c, kc += KC) {
+        int bsel = c % nbuf;
+        if (__syncthreads_or(!pipe_wait(pp, bsel))) { abort = true; break; }
+        fence_after();
+        float *A1h = bufA(bsel), *A1l = A1h + MROWS * KC;
+        float *B2h = A1l + MROWS * KC, *B2l = B2h + q.n2max * KC;
         {
-          // this warp's 32 rows of D1, columns kc..kc+31: sign (-1)^|q| and
-          // the right pair's balancing 2^((k - kR)|q|), then TF32 split
-          int row = warp * 32 + lane;
-          float v[32];
-          uint32_t ta = tD1 + ((uint32_t)(warp * 32) << 16) + (uint32_t)kc;
-          tld16(ta, v);
-          tld16(ta + 16, v + 16);
+          // D1 rows of this warp's lane quarter, 16 of the chunk's 32
+          // columns: sign (-1)^|q| and the right pair's balancing
+          // 2^((k - kR)|q|), then the TF32 split
+          int row = quad * 32 + lane, c0 = 16 * half;
+          float v[16];
+          tld16(tD1 + lanebase + (uint32_t)(kc + c0), v);
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            int qq = kc + j;
+          for (int j = 0; j < 16; ++j) {
+            int qq = kc + c0 + j;
             float x = 0.f;
             if (qq < nR) {
-              int L = c_t[qq] + c_u[qq] + c_v[qq];
+              int L = tuvL(stuv[qq]);
               x = v[j] * ldexpf((L & 1) ? -1.0f : 1.0f, (kq0 - kR) * L);
             }
             float h, l;
             tsplit(x, h, l);
-            A1h[kmaj(row, j)] = h;
-            A1l[kmaj(row, j)] = l;
+            A1h[kmaj(row, c0 + j)] = h;
+            A1l[kmaj(row, c0 + j)] = l;
           }
         }
-        for (int w = tid; w < n2 * KC; w += TCT) {
-          int n = w / KC, kk = w % KC, qq = kc + kk;
-          float v = 0.f;
-          if (n < 4 * nlR && qq < nR) {
-            int labR = n >> 2, set = (n >> 1) & 1;
-            float4 e = ER[((long long)labR * 2 + set) * nR + qq];
-            v = (n & 1) ? e.z : e.x;
+        {
+          // E_R chunk: (label, set, q) items, each filling a re and an im
+          // row; zero rows above 4 nlR
+          int nit = nlR * 2 * KC;
+          for (int b0 = 0; b0 < nit; b0 += 4 * TCT) {
+            float2 ev[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              int w = b0 + tid + j * TCT;
+              int lr = w / (2 * KC), set = (w / KC) & 1, qq = kc + (w % KC);
+              ev[j] = (w < nit && qq < nR) ? ER[((long long)lr * 2 + set) * nR + qq]
+                                          : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              int w = b0 + tid + j * TCT;
+              if (w >= nit) continue;
+              int lr = w / (2 * KC), set = (w / KC) & 1, kk = w % KC;
+              int row = lr * 4 + set * 2;
+              float h, l;
+              tsplit(ev[j].x, h, l);
+              B2h[kmaj(row, kk)] = h; B2l[kmaj(row, kk)] = l;
+              tsplit(ev[j].y, h, l);
+              B2h[kmaj(row + 1, kk)] = h; B2l[kmaj(row + 1, kk)] = l;
+            }
           }
-          float h, l;
-          tsplit(v, h, l);
-          B2h[kmaj(n, kk)] = h; B2l[kmaj(n, kk)] = l;
+          for (int w = 4 * nlR * KC + tid; w < n2 * KC; w += TCT) {
+            int n = w / KC, kk = w % KC;
+            B2h[kmaj(n, kk)] = 0.f; B2l[kmaj(n, kk)] = 0.f;
+          }
         }
         fence_async_smem();
         fence_before();
@@ -472,10 +557,13 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
             mma(tD2, ah, bl, id2, 1u);
             mma(tD2, al, bh, id2, 1u);
           }
-          commit(&mbar);
+          commit(&pp.bar[bsel]);
         }
-        bool ok = wait(&mbar, phase);
-        phase ^= 1;
+        pp.pend[bsel] = true;
+      }
+      {
+        bool ok = pipe_wait(pp, 0);
+        ok = pipe_wait(pp, 1) && ok;
         if (__syncthreads_or(!ok)) abort = true;
         fence_after();
       }
@@ -485,10 +573,10 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
       for (int c0 = 0; c0 < 4 * nlR; c0 += SLAB) {
         int ncol = min(SLAB, n2 - c0);
         {
-          int row = warp * 32 + lane;
-          for (int j0 = 0; j0 < ncol; j0 += 16) {
+          int row = quad * 32 + lane;
+          for (int j0 = 16 * half; j0 < ncol; j0 += 32) {
             float v[16];
-            tld16(tD2 + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c0 + j0), v);
+            tld16(tD2 + lanebase + (uint32_t)(c0 + j0), v);
 #pragma unroll
             for (int j = 0; j < 16; ++j) P[row * PSTR + j0 + j] = v[j];
           }
@@ -511,7 +599,6 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
           if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
           // products: rows (lab, set L, re/im), columns (lr, set R, re/im)
           const float *pr0 = P + (lab * 4) * PSTR + (lr - r0) * 4;
-          // pp = 2*setL + setR: a = re.re, b = im.im, c = G.im*E.re, d = G.re*E.im
           float2 sv[8];
 #pragma unroll
           for (int sL = 0; sL < 2; ++sL)
@@ -623,6 +710,512 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   if (abort && tid == 0) atomicOr(&g_tc_status, 1);
   // release: every TMEM read and MMA of this CTA has completed (waited above;
   // after a timeout, wait once more, bounded, for the MMAs in flight)
+  if (abort) {
+    pipe_wait(pp, 0);
+    pipe_wait(pp, 1);
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 :: "r"(tmem), "r"(q.tmem_cols));
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core Breit kernel: BIIFAST's contractions (bertha-scf.f:18337-19171)
+// on tcgen05 in the same 3xTF32 form.  With the 3x3 Breit kernel table
+// W_ij(N) (Gaunt and gauge terms, :18655-18880; symmetric, 6 entries per N),
+// per Cartesian component i of the right electron:
+//   GEMM 1  D1[row][q]   = sum_j sum_s E_L[row][j][s] W_ij(s+q)
+//   GEMM 2  D2[row][col] += sum_q G_i[row][q] E_R[col][i][q]
+// D2 summed over i holds the 16 products per label pair; exchange digestion
+// (BRTMTG/BRTMTZ batch type 5) with the Breit phases follows in FP32.
+// ---------------------------------------------------------------------------
+namespace tcq {
+
+// Tensor-core cost of a Breit orientation (as tc_cost, three components i,
+// each contracting three components j, or one for the Gaunt term alone).
+__host__ __device__ inline long long tcb_cost(int nlL, int nL, int nlR, int nR, int gaunt) {
+  long long tiles = (4 * nlL + MROWS - 1) / MROWS;
+  int n1 = rup(nR, KC), n2 = rup(4 * nlR, 16);
+  int nj = gaunt ? 1 : 3;
+  return tiles * 3 * ((long long)nj * rup(nL, KC) * n1 + (long long)n1 * n2) + 64LL * nlL * nlR;
+}
+
+__host__ __device__ inline void tcb_dims(int la, int lb, int lc, int ld, int gaunt, int &n1,
+                                         int &n2, bool &swp) {
+  int nab = ntuv(la + lb + 1), ncd = ntuv(lc + ld + 1);
+  int nlab = (2 * la + 1) * (2 * lb + 1), nlcd = (2 * lc + 1) * (2 * ld + 1);
+  swp = tcb_cost(nlcd, ncd, nlab, nab, gaunt) < tcb_cost(nlab, nab, nlcd, ncd, gaunt);
+  int nR = swp ? nab : ncd, nlR = swp ? nlab : nlcd;
+  n1 = rup(nR, KC);
+  n2 = rup(4 * nlR, 16);
+}
+
+constexpr int NWT = ntuv(4 * BG_MAX_L + 2);  // kernel-table entries (degree la+lb+lc+ld+2)
+
+struct LayoutB {
+  int stage, wf, dsm, acc, fb, total;
+};
+__host__ __device__ inline LayoutB layout_b(int n1max, int n2max) {
+  LayoutB L;
+  Layout c = layout(n1max, n2max);
+  L.stage = 0;
+  L.wf = c.rf;                                   // W table, 6 floats per entry
+  L.dsm = L.wf + rup(NWT * 6 * 4, 128);          // D(c,b), D(a,d)
+  L.acc = L.dsm + 2 * MAXSP * MAXSP * 8;         // K(a,d), K2(c,b)
+  L.fb = L.acc + 2 * MAXSP * MAXSP * 8;
+  L.total = L.fb + (MAXLAM + 4) * 8 + 128;
+  return L;
+}
+
+struct ArgsB {
+  const Shell *sh;
+  const PairE *pe;        // kexp of each ordered pair (row prow of the first shell)
+  const long long *offq;  // sigma-coupled E offsets [pair][LS/SL]
+  const float2 *E;        // their FP32 copy, scaled by 2^(kexp lambda)
+  const float4 *D;        // double-float density (hi words used), n x n
+  double *BX;
+  int ns, ldd, ldf, nskp, isym, racah1, gaunt;
+  int dual;               // as BArgs
+  int tmem_cols, n1max, n2max;
+};
+
+}  // namespace tcq
+
+__global__ void __launch_bounds__(tcq::TCT, 2)
+k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
+  using namespace tcq;
+  extern __shared__ unsigned char tc_smem_raw[];
+  unsigned char *base =
+      (unsigned char *)(((uintptr_t)tc_smem_raw + 127) & ~(uintptr_t)127);
+  const LayoutB LY = layout_b(q.n1max, q.n2max);
+  float *A1h = (float *)(base + LY.stage);
+  float *A1l = A1h + MROWS * KC;
+  float *B1h = A1l + MROWS * KC;
+  float *B1l = B1h + q.n1max * KC;
+  float *B2h = A1l + MROWS * KC;
+  float *B2l = B2h + q.n2max * KC;
+  float *P = (float *)(base + LY.stage);
+  double *R = (double *)(base + LY.stage);
+  double *R2 = R + NTR;
+  float *Wf = (float *)(base + LY.wf);
+  float2 *Dsm = (float2 *)(base + LY.dsm);   // D(c,b), D(a,d)
+  float2 *Acc = (float2 *)(base + LY.acc);   // K(a,d), K2(c,b)
+  double *F = (double *)(base + LY.fb);
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tslot;
+  __shared__ double sgeo[10];
+  __shared__ int sk;
+  __shared__ uint32_t stuv[NTR];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quad = warp & 3, half = warp >> 2;
+
+  for (int i = tid; i < NTR; i += TCT)
+    stuv[i] = (uint32_t)c_t[i] | ((uint32_t)c_u[i] << 8) | ((uint32_t)c_v[i] << 16) |
+              ((uint32_t)(c_t[i] + c_u[i] + c_v[i]) << 24);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(saddr(&tslot)), "r"(q.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar)));
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tslot;
+  uint32_t phase = 0;
+  bool abort = false;
+
+  for (long long qi = blockIdx.x; qi < nq && !abort; qi += gridDim.x) {
+    int4 Q4 = quart[qi];
+    const Shell &A = q.sh[Q4.x], &B = q.sh[Q4.y], &C = q.sh[Q4.z], &Dd = q.sh[Q4.w];
+    int la = A.l, lb = B.l, lc = C.l, ld = Dd.l;
+    int degab = la + lb + 1, degcd = lc + ld + 1;
+    int lamn = degab + degcd, lam = lamn + (q.gaunt ? 0 : 2);
+    int nla = 2 * la + 1, nlb = 2 * lb + 1, nlc = 2 * lc + 1, nld = 2 * ld + 1;
+    int nab = ntuv(degab), ncd = ntuv(degcd);
+    int n1, n2;
+    bool swp;
+    tcb_dims(la, lb, lc, ld, q.gaunt, n1, n2, swp);
+    if (n1 + n2 > q.tmem_cols || n1 > q.n1max || n2 > q.n2max) {
+      if (tid == 0) atomicOr(&g_tc_status, 2);
+      continue;
+    }
+    int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
+    bool dual = q.dual && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
+    if (tid == 0) {
+      double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
+      double Px = (A.alpha * A.x + B.alpha * B.x) / p;
+      double Py = (A.alpha * A.y + B.alpha * B.y) / p;
+      double Pz = (A.alpha * A.z + B.alpha * B.z) / p;
+      double Qx = (C.alpha * C.x + Dd.alpha * Dd.x) / qq;
+      double Qy = (C.alpha * C.y + Dd.alpha * Dd.y) / qq;
+      double Qz = (C.alpha * C.z + Dd.alpha * Dd.z) / qq;
+      double aph = p * qq / (p + qq);
+      double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
+      // R and the kernel table for the left pair's centre minus the right's
+      double sg = swp ? -1.0 : 1.0;
+      sgeo[0] = sg * (Px - Qx); sgeo[1] = sg * (Py - Qy); sgeo[2] = sg * (Pz - Qz);
+      sgeo[3] = -2.0 * aph;
+      sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
+      sgeo[5] = 0.5 / aph;
+      sgeo[6] = sg * (Qx - Px); sgeo[7] = sg * (Qy - Py); sgeo[8] = sg * (Qz - Pz);
+      sgeo[9] = T;
+      sk = half_floor_log2(2.0 * aph);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    boys_block(sgeo[9], lam, F);
+    __syncthreads();
+    {
+      double X = sgeo[0], Y = sgeo[1], Z = sgeo[2], m2a = sgeo[3];
+      double *cur = R, *nxt = R2;
+      for (int n = lam; n >= 0; --n) {
+        int cnt = ntuv(lam - n);
+        for (int k = tid; k < cnt; k += TCT) {
+          double val;
+          if (k == 0) {
+            double pw = 1.0;
+            for (int i = 0; i < n; ++i) pw *= m2a;
+            val = pw * F[n];
+          } else {
+            uint32_t w = stuv[k];
+            int t = w & 255, u = (w >> 8) & 255, v = (w >> 16) & 255;
+            if (t > 0) {
+              val = X * cur[hidx(t - 1, u, v)];
+              if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
+            } else if (u > 0) {
+              val = Y * cur[hidx(t, u - 1, v)];
+              if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
+            } else {
+              val = Z * cur[hidx(t, u, v - 1)];
+              if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
+            }
+          }
+          nxt[k] = val;
+        }
+        __syncthreads();
+        double *tmp = cur; cur = nxt; nxt = tmp;
+      }
+      // kernel table W_ij(N) = BFAC (delta_ij R_N - T_ij(N)) from PRE * R,
+      // scaled by 2^(-k lambda_N), FP32 (6 symmetric entries per N)
+      double pre = sgeo[4], h2a = sgeo[5];
+      double pq[3] = {sgeo[6], sgeo[7], sgeo[8]};
+      double bfac = q.gaunt ? -1.0 : -0.5;
+      int k = sk;
+      for (int w = tid; w < ntuv(lamn) * 6; w += TCT) {
+        int n = w / 6, e = w % 6;
+        int i = e < 3 ? e : (e == 5 ? 1 : 0), j = e < 3 ? e : (e == 3 ? 1 : 2);
+        uint32_t tw = stuv[n];
+        int N[3] = {(int)(tw & 255), (int)((tw >> 8) & 255), (int)((tw >> 16) & 255)};
+        double rn = cur[n] * pre;
+        double val;
+        if (q.gaunt) {
+          val = i == j ? -rn : 0.0;
+        } else {
+          int a[3] = {N[0], N[1], N[2]};
+          a[i] += 1;
+          a[j] += 1;
+          double tt = cur[hidx(a[0], a[1], a[2])] * h2a;
+          a[j] -= 1;
+          tt -= cur[hidx(a[0], a[1], a[2])] * pq[j];
+          a[j] -= 1;
+          if (a[j] >= 0) tt += cur[hidx(a[0], a[1], a[2])] * double(N[j]);
+          val = bfac * ((i == j ? rn : 0.0) - tt * pre);
+        }
+        Wf[w] = __double2float_rn(ldexp(val, -k * tuvL(tw)));
+      }
+    }
+    const PairE &pab_e = q.pe[A.prow + Q4.y], &pcd_e = q.pe[C.prow + Q4.w];
+    const float2 *Eab = q.E + q.offq[((size_t)Q4.x * q.ns + Q4.y) * 2 + t1];
+    const float2 *Ecd = q.E + q.offq[((size_t)Q4.z * q.ns + Q4.w) * 2 + t2];
+    const float2 *EL = swp ? Ecd : Eab, *ER = swp ? Eab : Ecd;
+    int kL = swp ? pcd_e.kexp : pab_e.kexp, kR = swp ? pab_e.kexp : pcd_e.kexp;
+    int nL = swp ? ncd : nab, nR = swp ? nab : ncd;
+    int nlab = nla * nlb, nlcd = nlc * nld;
+    int nlL = swp ? nlcd : nlab, nlR = swp ? nlab : nlcd;
+    int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;
+    int lq[4] = {la, lb, lc, ld};
+    // Fock offsets: an LS pair has its first function large, second small
+    int oa = t1 ? q.nskp : 0, ob = t1 ? 0 : q.nskp;
+    int oc = t2 ? q.nskp : 0, od = t2 ? 0 : q.nskp;
+    int kq0 = sk;
+    {
+      // D(c,b) and, for (cd|ab), D(a,d)
+      int sizes[2][2] = {{2 * nlc, 2 * nlb}, {2 * nla, 2 * nld}};
+      const Shell *rs[2] = {&C, &A}, *cs[2] = {&B, &Dd};
+      int ro[2] = {oc, oa}, co[2] = {ob, od};
+      for (int blk = 0; blk < (dual ? 2 : 1); ++blk) {
+        int nr = sizes[blk][0], nc = sizes[blk][1];
+        for (int w = tid; w < nr * nc; w += TCT) {
+          int r = w / nc, c = w % nc;
+          int fr = rs[blk]->fock[r >> 1][r & 1] + ro[blk];
+          int fc = cs[blk]->fock[c >> 1][c & 1] + co[blk];
+          float4 v = q.D[(size_t)fr + (size_t)q.ldd * fc];
+          Dsm[blk * MAXSP * MAXSP + r * MAXSP + c] = make_float2(v.x, v.z);
+        }
+      }
+    }
+    for (int i = tid; i < 2 * MAXSP * MAXSP; i += TCT) Acc[i] = make_float2(0.f, 0.f);
+    __syncthreads();
+
+    const uint32_t tD1 = tmem, tD2 = tmem + (uint32_t)n1;
+    const uint32_t id1 = idesc(MROWS, n1), id2 = idesc(MROWS, n2);
+    const uint32_t lanebase = (uint32_t)(quad * 32) << 16;
+    for (int l0 = 0; l0 < nlL && !abort; l0 += MLAB) {
+      int ntl = min(MLAB, nlL - l0);
+      for (int ci = 0; ci < 3 && !abort; ++ci) {
+        // ---- GEMM 1 for component i: K over (j, s) ----
+        int j0 = q.gaunt ? ci : 0, j1 = q.gaunt ? ci + 1 : 3;
+        bool first = true;
+        for (int cj = j0; cj < j1 && !abort; ++cj) {
+          int sw = cj == ci ? ci : ci + cj + 2;  // symmetric table entry (i, j)
+          for (int kc = 0; kc < nL && !abort; kc += KC) {
+            {
+              constexpr int AIT = MLAB * 2 * KC / TCT;
+              float2 ev[AIT];
+#pragma unroll
+              for (int j = 0; j < AIT; ++j) {
+                int w = tid + j * TCT;
+                int lab = w / (2 * KC), set = (w / KC) & 1, s = kc + (w % KC);
+                ev[j] = (lab < ntl && s < nL)
+                            ? EL[(((long long)(l0 + lab) * 2 + set) * 3 + cj) * nL + s]
+                            : make_float2(0.f, 0.f);
+              }
+#pragma unroll
+              for (int j = 0; j < AIT; ++j) {
+                int w = tid + j * TCT;
+                int lab = w / (2 * KC), set = (w / KC) & 1, kk = w % KC, s = kc + kk;
+                float f = s < nL ? ldexpf(1.0f, (kq0 - kL) * tuvL(stuv[s])) : 0.f;
+                int row = lab * 4 + set * 2;
+                float h, l;
+                tsplit(ev[j].x * f, h, l);
+                A1h[kmaj(row, kk)] = h; A1l[kmaj(row, kk)] = l;
+                tsplit(ev[j].y * f, h, l);
+                A1h[kmaj(row + 1, kk)] = h; A1l[kmaj(row + 1, kk)] = l;
+              }
+            }
+            for (int w = tid; w < n1 * KC; w += TCT) {
+              int n = w / KC, kk = w % KC, s = kc + kk;
+              float v = 0.f;
+              if (n < nR && s < nL) v = Wf[hsum(stuv[s], stuv[n]) * 6 + sw];
+              float h, l;
+              tsplit(v, h, l);
+              B1h[kmaj(n, kk)] = h; B1l[kmaj(n, kk)] = l;
+            }
+            fence_async_smem();
+            fence_before();
+            __syncthreads();
+            if (tid == 0) {
+              fence_after();
+#pragma unroll
+              for (int ks = 0; ks < KC / 8; ++ks) {
+                uint32_t off = ks * 256;
+                uint64_t ah = sdesc(saddr(A1h) + off), al = sdesc(saddr(A1l) + off);
+                uint64_t bh = sdesc(saddr(B1h) + off), bl = sdesc(saddr(B1l) + off);
+                uint32_t acc0 = (!first || ks > 0) ? 1u : 0u;
+                mma(tD1, ah, bh, id1, acc0);
+                mma(tD1, ah, bl, id1, 1u);
+                mma(tD1, al, bh, id1, 1u);
+              }
+              commit(&mbar);
+            }
+            first = false;
+            bool ok = wait(&mbar, phase);
+            phase ^= 1;
+            if (__syncthreads_or(!ok)) abort = true;
+            fence_after();
+          }
+        }
+        // ---- GEMM 2 for component i, accumulated over i ----
+        for (int kc = 0; kc < n1 && !abort; kc += KC) {
+          {
+            int row = quad * 32 + lane, c0 = 16 * half;
+            float v[16];
+            tld16(tD1 + lanebase + (uint32_t)(kc + c0), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              int qq = kc + c0 + j;
+              float x = 0.f;
+              if (qq < nR) {
+                int L = tuvL(stuv[qq]);
+                x = v[j] * ldexpf((L & 1) ? -1.0f : 1.0f, (kq0 - kR) * L);
+              }
+              float h, l;
+              tsplit(x, h, l);
+              A1h[kmaj(row, c0 + j)] = h;
+              A1l[kmaj(row, c0 + j)] = l;
+            }
+          }
+          {
+            int nit = nlR * 2 * KC;
+            for (int b0 = 0; b0 < nit; b0 += 4 * TCT) {
+              float2 ev[4];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                int w = b0 + tid + j * TCT;
+                int lr = w / (2 * KC), set = (w / KC) & 1, qq = kc + (w % KC);
+                ev[j] = (w < nit && qq < nR) ? ER[(((long long)lr * 2 + set) * 3 + ci) * nR + qq]
+                                            : make_float2(0.f, 0.f);
+              }
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                int w = b0 + tid + j * TCT;
+                if (w >= nit) continue;
+                int lr = w / (2 * KC), set = (w / KC) & 1, kk = w % KC;
+                int row = lr * 4 + set * 2;
+                float h, l;
+                tsplit(ev[j].x, h, l);
+                B2h[kmaj(row, kk)] = h; B2l[kmaj(row, kk)] = l;
+                tsplit(ev[j].y, h, l);
+                B2h[kmaj(row + 1, kk)] = h; B2l[kmaj(row + 1, kk)] = l;
+              }
+            }
+            for (int w = 4 * nlR * KC + tid; w < n2 * KC; w += TCT) {
+              int n = w / KC, kk = w % KC;
+              B2h[kmaj(n, kk)] = 0.f; B2l[kmaj(n, kk)] = 0.f;
+            }
+          }
+          fence_async_smem();
+          fence_before();
+          __syncthreads();
+          if (tid == 0) {
+            fence_after();
+#pragma unroll
+            for (int ks = 0; ks < KC / 8; ++ks) {
+              uint32_t off = ks * 256;
+              uint64_t ah = sdesc(saddr(A1h) + off), al = sdesc(saddr(A1l) + off);
+              uint64_t bh = sdesc(saddr(B2h) + off), bl = sdesc(saddr(B2l) + off);
+              uint32_t acc0 = (ci > 0 || kc > 0 || ks > 0) ? 1u : 0u;
+              mma(tD2, ah, bh, id2, acc0);
+              mma(tD2, ah, bl, id2, 1u);
+              mma(tD2, al, bh, id2, 1u);
+            }
+            commit(&mbar);
+          }
+          bool ok = wait(&mbar, phase);
+          phase ^= 1;
+          if (__syncthreads_or(!ok)) abort = true;
+          fence_after();
+        }
+      }
+      if (abort) break;
+      // ---- epilogue: exchange digestion with the Breit phases ----
+      for (int c0 = 0; c0 < 4 * nlR; c0 += SLAB) {
+        int ncol = min(SLAB, n2 - c0);
+        {
+          int row = quad * 32 + lane;
+          for (int jj = 16 * half; jj < ncol; jj += 32) {
+            float v[16];
+            tld16(tD2 + lanebase + (uint32_t)(c0 + jj), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) P[row * PSTR + jj + j] = v[j];
+          }
+        }
+        fence_before();
+        __syncthreads();
+        int r0 = c0 / 4, nrl = min(SLAB / 4, nlR - r0);
+        for (int w = tid; w < ntl * nrl; w += TCT) {
+          int lab = w % ntl;
+          int lr = r0 + (w / ntl + lab) % nrl;
+          int labL = l0 + lab;
+          int l1 = labL / nl2L, l2 = labL % nl2L, r1 = lr / nl2R, r2 = lr % nl2R;
+          int ia = swp ? r1 : l1, ib = swp ? r2 : l2, ic = swp ? l1 : r1, id = swp ? l2 : r2;
+          int kq[4], mq[4], mm[4];
+          label_of(la, ia, kq[0], mm[0]);
+          label_of(lb, ib, kq[1], mm[1]);
+          label_of(lc, ic, kq[2], mm[2]);
+          label_of(ld, id, kq[3], mm[3]);
+          for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
+          if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
+          const float *pr0 = P + (lab * 4) * PSTR + (lr - r0) * 4;
+          float2 sv[8];
+#pragma unroll
+          for (int sL = 0; sL < 2; ++sL)
+#pragma unroll
+            for (int sR = 0; sR < 2; ++sR) {
+              const float *pre_ = pr0 + (sL * 2) * PSTR + sR * 2;
+              float a = pre_[0], d = pre_[1];
+              float c = pre_[PSTR], b = pre_[PSTR + 1];
+              int pp = sL * 2 + sR;
+              sv[2 * pp] = make_float2(a - b, c + d);
+              sv[2 * pp + 1] = make_float2(a + b, d - c);
+            }
+          // Breit phases: the Coulomb pair phases negated (BRTFAST :17528-17533)
+          double pab = -pair_phase(kq[0], mm[0], kq[1], mm[1]);
+          double pcd = -pair_phase(kq[2], mm[2], kq[3], mm[3]);
+          double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
+          float sl = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
+          const float2 *Dcb = Dsm, *Dad = Dsm + MAXSP * MAXSP;
+          float2 *Kl = Acc, *K2 = Acc + MAXSP * MAXSP;
+#define TCV(sa, sb, sc, sd) (swp ? rvc<true>(sv, sa, sb, sc, sd, sl, slr) \
+                                 : rvc<false>(sv, sa, sb, sc, sd, sl, slr))
+          if (q.isym == 0) {
+            for (int sa = 0; sa < 2; ++sa)
+              for (int sd = 0; sd < 2; ++sd) {
+                float2 k = make_float2(0.f, 0.f);
+                for (int sb = 0; sb < 2; ++sb)
+                  for (int sc = 0; sc < 2; ++sc)
+                    cmac(k, TCV(sa, sb, sc, sd), Dcb[(ic * 2 + sc) * MAXSP + ib * 2 + sb]);
+                sadd(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], k);
+              }
+            if (dual)
+              for (int sc = 0; sc < 2; ++sc)
+                for (int sb = 0; sb < 2; ++sb) {
+                  float2 k = make_float2(0.f, 0.f);
+                  for (int sa = 0; sa < 2; ++sa)
+                    for (int sd = 0; sd < 2; ++sd)
+                      cmac(k, TCV(sa, sb, sc, sd), Dad[(ia * 2 + sa) * MAXSP + id * 2 + sd]);
+                  sadd(&K2[(ic * 2 + sc) * MAXSP + ib * 2 + sb], k);
+                }
+          } else {
+            // BRTMTZ: real parts, crossed exchange blocks
+            for (int s = 0; s < 2; ++s) {
+              float kv = 0.f;
+              for (int t = 0; t < 2; ++t)
+                kv = fmaf(TCV(s, t, t, s).x, Dcb[(ic * 2 + t) * MAXSP + ib * 2 + t].x, kv);
+              atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
+            }
+            if (dual)
+              for (int s = 0; s < 2; ++s) {
+                float kv = 0.f;
+                for (int t = 0; t < 2; ++t)
+                  kv = fmaf(TCV(t, s, s, t).x, Dad[(ia * 2 + t) * MAXSP + id * 2 + t].x, kv);
+                atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
+              }
+          }
+#undef TCV
+        }
+        __syncthreads();
+      }
+    }
+    if (abort) break;
+    // flush; in a halved (LS|SL) list a quartet equal to its (dc|ba) image
+    // counts 1/2 (the completion adds it again)
+    const double wq = (q.dual == 2 && t2 == 1 && Q4.x == Q4.w && Q4.y == Q4.z) ? 0.5 : 1.0;
+    for (int w = tid; w < 2 * nla * 2 * nld; w += TCT) {
+      int a = w / (2 * nld), d = w % (2 * nld);
+      float2 v = Acc[a * MAXSP + d];
+      if (v.x == 0.f && v.y == 0.f) continue;
+      int fa = A.fock[a >> 1][a & 1] + oa, fdd = Dd.fock[d >> 1][d & 1] + od;
+      double *dst = q.BX + 2 * ((size_t)fa + (size_t)q.ldf * fdd);
+      atomicAdd(dst, wq * (double)v.x);
+      atomicAdd(dst + 1, wq * (double)v.y);
+    }
+    if (dual)
+      for (int w = tid; w < 2 * nlc * 2 * nlb; w += TCT) {
+        int cc = w / (2 * nlb), b = w % (2 * nlb);
+        float2 v = Acc[MAXSP * MAXSP + cc * MAXSP + b];
+        if (v.x == 0.f && v.y == 0.f) continue;
+        int fcc = C.fock[cc >> 1][cc & 1] + oc, fbb = B.fock[b >> 1][b & 1] + ob;
+        double *dst = q.BX + 2 * ((size_t)fcc + (size_t)q.ldf * fbb);
+        atomicAdd(dst, wq * (double)v.x);
+        atomicAdd(dst + 1, wq * (double)v.y);
+      }
+  }
+  if (abort && tid == 0) atomicOr(&g_tc_status, 1);
   if (abort) wait(&mbar, phase ^ 1);
   fence_before();
   __syncthreads();

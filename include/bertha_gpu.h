@@ -103,9 +103,28 @@ int bertha_gpu_auto_stats(const bg_ctx *ctx, long long *nq_fp64, long long *nq_d
 int bertha_gpu_kernel_stats(const bg_ctx *ctx, long long nq[3], int *nruns);
 
 /* Energy error (Eh) the BG_PREC_AUTO tuner may spend on tensor-core classes
- * per Coulomb build, shared equally by the component classes (default
- * 1e-7; 0 keeps every class FP64-accurate).  Changing it retunes. */
+ * per Coulomb build (shared equally by the component classes) and, apart,
+ * per Breit build (default 1e-7 each; 0 keeps every class FP64-accurate).
+ * Within a class, quartets are grouped by the decade of their Schwarz bound
+ * Q_ab Q_cd, so that the small-magnitude part of a class can take the
+ * tensor cores while its large part stays FP64.  Changing it retunes. */
 int bertha_gpu_set_error_budget(bg_ctx *ctx, double eh);
+
+/* The BG_PREC_AUTO tuner's record of the last tuning of the Coulomb
+ * (breit = 0) or Breit (breit = 1) lists, one row per segment (angular
+ * class and Schwarz-bound decade): info[4i..4i+3] = component class
+ * (2*t1 + t2; Breit: 0 (LS|LS), 1 (LS|SL)), angular class
+ * ((l_a*4 + l_b)*4 + l_c)*4 + l_d, quartets, chosen kernel (0 FP64,
+ * 1 split, 2 tensor cores); vals[6i..6i+5] = sample time (ms) of the three
+ * kernels (0 when not run) and their estimated energy errors (Eh).  At most
+ * cap rows are written; *nrows gets the record's length. */
+int bertha_gpu_tuning_record(const bg_ctx *ctx, int breit, int cap, int *info, double *vals,
+                             int *nrows);
+
+/* Kernel use of the last Breit build (BG_PREC_AUTO or BG_PREC_TC32):
+ * nq[0] FP64, nq[2] tensor-core quartets (nq[1] is 0: the Breit build has
+ * no split-precision kernel). */
+int bertha_gpu_breit_kernel_stats(const bg_ctx *ctx, long long nq[3], int *nruns);
 
 /* Status of the tensor-core kernels since the last call (synchronises the
  * device): bit 0 set when an mbarrier wait gave up (the kernel skipped the
@@ -155,6 +174,9 @@ int bertha_gpu_clmfast_device(bg_ctx *ctx, const double *d_dent, int ldd,
 
 /* Closed-shell multi-centre Breit exchange matrix, replacing CALL BRTFAST
  * (bertha-scf.f:17060-17670; BIIFAST :18337, BRTMTG :19815, BRTMTZ :19172).
+ * Precision: FP64 by default; BG_PREC_TC32 runs every class on the tensor
+ * cores (k_breit_tc, 3xTF32), BG_PREC_AUTO tunes per class and bound decade
+ * within the error budget; BG_PREC_DF32 leaves the Breit build FP64.
  *   dent[ldd*ndim]  total density DENT
  *   ilev            ILEV: multi-centre quartets from stage 3 on (:17230-17231)
  *   bxch[ldf*ndim]  output BXCH, overwritten

@@ -177,3 +177,76 @@ def test_auto_error_budget():
         assert abs(aj - ej) + abs(ak - ek) <= budget + 1e-11 * (abs(ej) + abs(ek))
         if budget == 0.0:
             assert st["tc32_quartets"] == 0
+
+
+# ---- Breit on the tensor cores ----
+
+def _breit_basis(lmax=1):
+    cent = [((0.0, 0.0, 0.0), {0: [0.3, 2.5], 1: [0.7]}),
+            ((0.3, -0.8, 1.3), {0: [0.45], 1: [1.1]}),
+            ((-1.0, 0.5, 0.4), {0: [0.9, 0.2]})]
+    if lmax >= 2:
+        cent[0][1][2] = [0.8]
+    if lmax >= 3:
+        cent[1][1][3] = [0.6]
+        cent[2][1][3] = [1.3]
+    return deck.make_basis(cent, hmlt="DHFB")
+
+
+def _cmp_breit_tc(b, dent, racah1=True, gaunt=False):
+    fb = berthagpu.FockBuilder(b, racah1=racah1, gaunt=gaunt)
+    fb.set_precision("tc32")
+    bx = fb.brtfast(dent, 3)
+    st = fb.breit_stats()
+    fb.close()
+    assert _lib.device_status() == 0
+    ref = orc.brtfast(b, dent, 3, racah1=racah1, gaunt=gaunt)
+    scale = max(np.abs(ref).max(), 1e-300)
+    err = np.abs(bx - ref).max() / scale
+    assert err <= TC_TOL, err
+    assert st["tc32_quartets"] > 0
+    return bx, ref
+
+
+@pytest.mark.parametrize("gaunt", [False, True])
+def test_breit_tc_general(gaunt):
+    b = _breit_basis()
+    _cmp_breit_tc(b, deck.density(b, seed=31), gaunt=gaunt)
+
+
+@pytest.mark.parametrize("lmax", [2, 3])
+def test_breit_tc_high_l(lmax):
+    b = _breit_basis(lmax=lmax)
+    _cmp_breit_tc(b, deck.density(b, seed=32))
+
+
+def test_breit_tc_linear_real_digestion():
+    b = deck.make_basis([((0, 0, 0), {0: [0.4, 1.9], 1: [0.8], 2: [1.2], 3: [0.9]}),
+                         ((0, 0, 2.1), {0: [0.6], 1: [0.5]})], hmlt="DHFB")
+    assert b.isym == 1
+    _cmp_breit_tc(b, deck.density(b, seed=33, real=True))
+
+
+def test_breit_tc_one_centre_by_md():
+    b = _breit_basis(lmax=2)
+    _cmp_breit_tc(b, deck.density(b, seed=34), racah1=False)
+
+
+def test_breit_auto_error_budget():
+    """BG_PREC_AUTO on the Breit build: energy within the budget of FP64's."""
+    b = _breit_basis(lmax=3)
+    dent = deck.density(b, seed=35)
+
+    def energy(prec, budget=None):
+        fb = berthagpu.FockBuilder(b)
+        fb.set_precision(prec)
+        if budget is not None:
+            fb.set_error_budget(budget)
+        fb.brtfast(dent, 3)
+        bx = fb.brtfast(dent, 3)
+        fb.close()
+        return 0.5 * np.sum(dent * bx).real
+
+    e64 = energy("fp64")
+    for budget in (0.0, 1e-6):
+        assert abs(energy("auto", budget) - e64) <= budget + 1e-12 * abs(e64)
