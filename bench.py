@@ -219,9 +219,10 @@ def h2o_fock_build(torch, with_cpu):
     out = {"ndim": b.ndim, "shells": len(b.shells()), "ilev": 3,
            "density": "seeded random Hermitian PSD (DENSTY form)"}
     res = {}
-    for prec in ("fp64", "df32"):
+    for prec in ("fp64", "df32", "tc32", "auto"):
         fb = berthagpu.FockBuilder(b)
         fb.set_precision(prec)
+        fb.set_screening(1e-12)
         fb.clmfast(dent, 3)
         ts = []
         for _ in range(3):
@@ -235,10 +236,16 @@ def h2o_fock_build(torch, with_cpu):
     for prec, (gd, gx) in res.items():
         e[prec] = (0.5 * np.sum(dent * gd).real, 0.5 * np.sum(dent * gx).real)
     out["energy_j_eh"], out["energy_k_eh"] = e["fp64"]
-    out["split_energy_err_eh"] = float(max(abs(e["df32"][0] - e["fp64"][0]),
-                                           abs(e["df32"][1] - e["fp64"][1])))
+    out["screen"] = 1e-12
+    for prec in ("df32", "tc32", "auto"):
+        out[prec + "_energy_err_eh"] = float(max(abs(e[prec][0] - e["fp64"][0]),
+                                                 abs(e[prec][1] - e["fp64"][1])))
     if with_cpu:
         from oracle import oracle as orc
+        # the oracle is unscreened: compare the GPU's unscreened FP64 build
+        fb = berthagpu.FockBuilder(b)
+        res["fp64"] = fb.clmfast(dent, 3)
+        fb.close()
         t0 = time.perf_counter()
         rd, rx = orc.clmfast(b, dent, 3)
         out["cpu_port_1core_s"] = time.perf_counter() - t0
@@ -312,14 +319,16 @@ def h2o_scf(torch):
     warm.run(max_iter=1)
     warm.close()
     torch.cuda.synchronize()
-    out = {"molecule": "H2O", "ndim": b.ndim, "nocc": 10, "screen": 1e-12, "etol_eh": 1e-9}
-    for prec in ("fp64", "df32"):
+    out = {"molecule": "H2O", "ndim": b.ndim, "nocc": 10, "screen": 1e-12, "etol_eh": 1e-10,
+           "gradient_tol": 1e-7}
+    for prec in ("fp64", "df32", "auto"):
         scf = DHFSCF(b, nocc=10, precision=prec, screen=1e-12, torch=torch)
-        r = scf.run(max_iter=60, etol=1e-9)
+        r = scf.run(max_iter=60, etol=1e-10, dtol=1e-7)
         scf.close()
-        out[prec] = {k: r[k] for k in ("energy", "iterations", "converged", "wall_s", "fock_s",
-                                       "linalg_s", "oneel_s")}
-    out["energy_diff_split_vs_fp64_eh"] = abs(out["df32"]["energy"] - out["fp64"]["energy"])
+        out[prec] = {k: r[k] for k in ("energy", "iterations", "converged", "gradient", "wall_s",
+                                       "fock_s", "linalg_s", "oneel_s")}
+    for prec in ("df32", "auto"):
+        out[f"energy_{prec}_vs_fp64_eh"] = out[prec]["energy"] - out["fp64"]["energy"]
     return out
 
 
@@ -340,10 +349,11 @@ def _device_time(torch, fn, reps=1):
 def tlf_builds(torch):
     """The TlF Dirac-Coulomb-Breit configuration (R = 3.94 bohr on z, Tl
     28s24p16d12f and F 14s9p3d even-tempered, Schwarz 1e-12, DIATOM: real
-    digestion): one stage-3 Coulomb build in FP64 and in the autotuned mixed
-    mode, and the Breit build in FP64, on device arrays (seeded Hermitian
-    density), each timed with CUDA events after a first call that builds
-    the lists (and, for the mixed mode, tunes the kernel per class)."""
+    digestion): the stage-3 Coulomb and Breit builds in FP64, in the
+    tensor-core precision and in the autotuned mixed mode (per angular class
+    and Schwarz-bound decade the fastest kernel within a 1e-7 Eh budget per
+    build), on device arrays (seeded Hermitian density), each timed with
+    CUDA events after a first call that builds the lists (and tunes)."""
     import berthagpu
     from berthagpu import deck
     b = deck.tlf_basis()
@@ -351,8 +361,9 @@ def tlf_builds(torch):
     n = b.ndim
     d_D = torch.from_numpy(np.ascontiguousarray(dent.T)).cuda()
     J, K, B = (torch.zeros((n, n), dtype=torch.complex128, device="cuda") for _ in range(3))
-    out = {"ndim": n, "shells": len(b.shells()), "hmlt": "DHFB", "screen": 1e-12, "ilev": 3}
-    for prec in ("fp64", "auto"):
+    out = {"ndim": n, "shells": len(b.shells()), "hmlt": "DHFB", "screen": 1e-12, "ilev": 3,
+           "error_budget_eh_per_build": 1e-7}
+    for prec in ("fp64", "tc32", "auto"):
         fb = berthagpu.FockBuilder(b)
         fb.set_precision(prec)
         fb.set_screening(1e-12)
@@ -362,38 +373,59 @@ def tlf_builds(torch):
         first = time.perf_counter() - t0
         t = _device_time(torch, lambda s: fb.clmfast_device(d_D.data_ptr(), J.data_ptr(),
                                                            K.data_ptr(), 3, n, s))
-        r = {"first_call_s": first, "device_s": t,
+        r = {"coulomb_first_call_s": first, "coulomb_device_s": t,
              "energy_j_eh": float(0.5 * torch.sum(d_D * J).real),
              "energy_k_eh": float(0.5 * torch.sum(d_D * K).real)}
-        if prec == "auto":
-            r["auto"] = fb.auto_stats()
-        else:
-            fb.brtfast_device(d_D.data_ptr(), B.data_ptr(), 3, n)
-            torch.cuda.synchronize()
-            out["breit_fp64"] = {
-                "device_s": _device_time(torch, lambda s: fb.brtfast_device(
-                    d_D.data_ptr(), B.data_ptr(), 3, n, s)),
-                "energy_bx_eh": float(0.5 * torch.sum(d_D * B).real)}
+        t0 = time.perf_counter()
+        fb.brtfast_device(d_D.data_ptr(), B.data_ptr(), 3, n)
+        torch.cuda.synchronize()
+        r["breit_first_call_s"] = time.perf_counter() - t0
+        r["breit_device_s"] = _device_time(torch, lambda s: fb.brtfast_device(
+            d_D.data_ptr(), B.data_ptr(), 3, n, s))
+        r["energy_bx_eh"] = float(0.5 * torch.sum(d_D * B).real)
+        r["dcb_build_s"] = r["coulomb_device_s"] + r["breit_device_s"]
+        if prec != "fp64":
+            r["coulomb_kernels"] = fb.auto_stats()
+            r["breit_kernels"] = fb.breit_stats()
         fb.close()
-        out["coulomb_" + prec] = r
-    out["auto_vs_fp64_energy_abs_eh"] = max(
-        abs(out["coulomb_auto"]["energy_j_eh"] - out["coulomb_fp64"]["energy_j_eh"]),
-        abs(out["coulomb_auto"]["energy_k_eh"] - out["coulomb_fp64"]["energy_k_eh"]))
-    out["dcb_fock_build_fp64_s"] = out["coulomb_fp64"]["device_s"] + out["breit_fp64"]["device_s"]
+        out[prec] = r
+    f = out["fp64"]
+    for prec in ("tc32", "auto"):
+        r = out[prec]
+        r["speedup_vs_fp64"] = {"coulomb": f["coulomb_device_s"] / r["coulomb_device_s"],
+                                "breit": f["breit_device_s"] / r["breit_device_s"],
+                                "dcb": f["dcb_build_s"] / r["dcb_build_s"]}
+        r["energy_error_vs_fp64_eh"] = {
+            "j": r["energy_j_eh"] - f["energy_j_eh"], "k": r["energy_k_eh"] - f["energy_k_eh"],
+            "bx": r["energy_bx_eh"] - f["energy_bx_eh"],
+            "total_two_electron": (r["energy_j_eh"] - r["energy_k_eh"] - r["energy_bx_eh"])
+            - (f["energy_j_eh"] - f["energy_k_eh"] - f["energy_bx_eh"])}
     # the precision's effect on a converged DCB total energy: the small TlF
-    # case (same geometry, angular momenta and exponent range) from the
-    # bare-nucleus start with maximum-overlap occupation from iteration 3,
-    # FP64 and autotuned mixed precision
+    # case (same geometry, angular momenta and exponent range), both SCFs
+    # converged in energy and orbital gradient, and both precisions' total
+    # energies at the FP64 SCF's converged density
     from berthagpu.scf import DHFSCF
     bs = deck.tlf_small_basis()
     scf = {"case": "TlF, Tl 7s6p4d3f / F 4s3p1d, DHFB", "ndim": bs.ndim, "nocc": 90,
-           "guess": "bare nucleus, maximum overlap from iteration 3", "etol_eh": 1e-8}
+           "guess": "bare nucleus, maximum overlap from iteration 3",
+           "etol_eh": 1e-10, "gradient_tol": 1e-6}
+    dens = {}
     for prec in ("fp64", "auto"):
-        s = DHFSCF(bs, nocc=90, precision=prec, screen=1e-12, torch=torch)
-        r = s.run(max_iter=120, etol=1e-8, mom=3)
-        s.close()
-        scf[prec] = {k: r[k] for k in ("energy", "iterations", "converged", "wall_s", "fock_s")}
-    scf["energy_auto_vs_fp64_eh"] = abs(scf["auto"]["energy"] - scf["fp64"]["energy"])
+        s_ = DHFSCF(bs, nocc=90, precision=prec, screen=1e-12, torch=torch)
+        r = s_.run(max_iter=200, etol=1e-10, dtol=1e-6, mom=3, return_density=True)
+        dens[prec] = r["density"]
+        scf[prec] = {k: r[k] for k in ("energy", "iterations", "converged", "gradient", "wall_s",
+                                       "fock_s")}
+        s_.close()
+    scf["energy_auto_vs_fp64_eh"] = scf["auto"]["energy"] - scf["fp64"]["energy"]
+    at = {}
+    for prec in ("fp64", "auto"):
+        s_ = DHFSCF(bs, nocc=90, precision=prec, screen=1e-12, torch=torch)
+        s_.energy_at(dens["fp64"])  # first build: lists and tuning
+        at[prec] = s_.energy_at(dens["fp64"])
+        s_.close()
+    scf["energy_at_fp64_density"] = at
+    scf["energy_auto_vs_fp64_at_shared_density_eh"] = at["auto"] - at["fp64"]
     out["scf_tlf_small"] = scf
     return out
 

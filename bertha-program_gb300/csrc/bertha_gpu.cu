@@ -2291,6 +2291,7 @@ struct TcGeom {
 };
 constexpr size_t SM_SMEM = 233472;  // 228 KB of shared memory per SM
 constexpr size_t TC_SMEM_MAX = 232448;  // 227 KB, the per-CTA opt-in limit
+size_t g_tc_smem_max = 122880;  // dynamic shared memory the tensor-core kernels may ask for
 
 TcGeom tc_geom(int n1, int n2, bool breit = false) {
   TcGeom g;
@@ -2305,7 +2306,7 @@ TcGeom tc_geom(int n1, int n2, bool breit = false) {
   while (ctas > 1 && (s + 1024 + 4096) * ctas > SM_SMEM) --ctas;  // + static shared memory
   // one CTA per SM: double-buffered K chunks when they fit
   g.nbuf = 1;
-  if (ctas == 1 && !breit && total(2) + 4096 <= TC_SMEM_MAX) {
+  if (ctas == 1 && !breit && total(2) <= g_tc_smem_max) {
     g.nbuf = 2;
     s = total(2);
   }
@@ -2470,10 +2471,10 @@ constexpr int MAXDEV = 64;
 std::mutex g_dev_mu;
 bool g_dev_ready[MAXDEV] = {false};
 
-int device_setup(int dev) {
+const char *device_setup(int dev) {
   std::lock_guard<std::mutex> lk(g_dev_mu);
-  if (dev < 0 || dev >= MAXDEV) return 1;
-  if (g_dev_ready[dev]) return 0;
+  if (dev < 0 || dev >= MAXDEV) return "device ordinal out of range";
+  if (g_dev_ready[dev]) return nullptr;
   signed char t[NTR], u[NTR], v[NTR];
   int n = 0;
   for (int L = 0; L <= MAXLAM; ++L)
@@ -2482,27 +2483,42 @@ int device_setup(int dev) {
         t[n] = (signed char)a; u[n] = (signed char)b; v[n] = (signed char)(L - a - b);
         ++n;
       }
-  if (cudaMemcpyToSymbol(c_t, t, sizeof(t)) != cudaSuccess) return 1;
-  if (cudaMemcpyToSymbol(c_u, u, sizeof(u)) != cudaSuccess) return 1;
-  if (cudaMemcpyToSymbol(c_v, v, sizeof(v)) != cudaSuccess) return 1;
+  if (cudaMemcpyToSymbol(c_t, t, sizeof(t)) != cudaSuccess ||
+      cudaMemcpyToSymbol(c_u, u, sizeof(u)) != cudaSuccess ||
+      cudaMemcpyToSymbol(c_v, v, sizeof(v)) != cudaSuccess)
+    return "Hermite index table upload failed";
   double rinv[NRINV];
   for (int k = 0; k < NRINV; ++k) rinv[k] = 1.0 / double(2 * k + 1);
-  if (cudaMemcpyToSymbol(c_rinv, rinv, sizeof(rinv)) != cudaSuccess) return 1;
+  if (cudaMemcpyToSymbol(c_rinv, rinv, sizeof(rinv)) != cudaSuccess)
+    return "reciprocal table upload failed";
   k_boys_table<<<(NBGRID + 127) / 128, 128>>>();
+  // the tensor-core kernels: the per-block opt-in limit less their static
+  // shared memory (the launches never ask for more than g_tc_smem_max)
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return "shared-memory opt-in query failed";
+  cudaFuncAttributes fq, fbr;
+  if (cudaFuncGetAttributes(&fq, k_quartet_tc) != cudaSuccess ||
+      cudaFuncGetAttributes(&fbr, k_breit_tc) != cudaSuccess)
+    return "kernel attribute query failed";
+  size_t stat = std::max(fq.sharedSizeBytes, fbr.sharedSizeBytes);
+  g_tc_smem_max = std::min(TC_SMEM_MAX, (size_t)optin - stat);
   if (cudaFuncSetAttribute(k_quartet_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)TC_SMEM_MAX) != cudaSuccess ||
+                           (int)g_tc_smem_max) != cudaSuccess ||
       cudaFuncSetAttribute(k_breit_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)TC_SMEM_MAX) != cudaSuccess ||
-      cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)g_tc_smem_max) != cudaSuccess)
+    return "tensor-core kernel shared-memory opt-in failed";
+  if (cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)quartet_smem()) != cudaSuccess ||
       cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)quartet_smem_df_max()) != cudaSuccess ||
       cudaFuncSetAttribute(k_breit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)breit_smem()) != cudaSuccess)
-    return 1;
-  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return 1;
+    return "quartet kernel shared-memory opt-in failed";
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return "Boys table kernel failed";
   g_dev_ready[dev] = true;
-  return 0;
+  return nullptr;
 }
 
 // Every context and batch remembers the device it was made on; calls made
@@ -3122,25 +3138,6 @@ int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, in
   return 0;
 }
 
-// Angular-class segment boundaries of a quartet list (entries grouped by
-// class): start of every class, then the list size; keys[i] is segment i's
-// class (l_a,l_b,l_c,l_d) in base 4.
-std::vector<long long> class_segments(const std::vector<Shell> &sh, const std::vector<int> &q,
-                                      std::vector<int> &keys, int sbase = 0) {
-  std::vector<long long> seg;
-  keys.clear();
-  long long n = (long long)q.size() / 4;
-  int last = -1;
-  for (long long i = 0; i < n; ++i) {
-    const int *e = &q[4 * i];
-    int key = ((sh[e[0] - sbase].l * 4 + sh[e[1] - sbase].l) * 4 + sh[e[2] - sbase].l) * 4 +
-              sh[e[3] - sbase].l;
-    if (key != last) { seg.push_back(i); keys.push_back(key); last = key; }
-  }
-  seg.push_back(n);
-  return seg;
-}
-
 // sum_ij Re(D_ij G_ij) over an n x n block (leading dimensions ldd, ldg) or,
 // with inst, over every instance's block; added to *out.
 __global__ void k_edot(const double2 *D, long long ldd, const double2 *G, long long ldg, int n,
@@ -3447,8 +3444,9 @@ int bertha_gpu_init(bg_ctx **out, int ncnt, const double *bxyz, const int *nkap,
     c->shells[a].prow = a * c->ns;
   }
   c->dev = current_device();
-  if (device_setup(c->dev)) {
-    g_init_err = "device set-up failed (constant tables, Boys table, kernel attributes)";
+  if (const char *why = device_setup(c->dev)) {
+    g_init_err = std::string("device set-up failed: ") + why + " (" +
+                 cudaGetErrorString(cudaGetLastError()) + ")";
     delete c;
     return BG_ERR_CUDA;
   }

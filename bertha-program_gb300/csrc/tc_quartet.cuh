@@ -212,24 +212,29 @@ struct Args {
 
 __device__ inline float fsgn(float x, float s) { return s < 0.f ? -x : x; }
 
-// (ab|cd) m-sign combination from the (left|right) products (the same table
-// as rv_sign of the split path), complex value as float2.
-template <bool SWP>
-__device__ inline float2 rvc(const float2 (&sv)[8], int sa, int sb, int sc, int sd, float sl,
-                             float slr) {
-  int idx = SWP ? 8 * sc + 4 * sd + 2 * sa + sb : 8 * sa + 4 * sb + 2 * sc + sd;
-  const int src[16] = {0, 3, 2, 1, 5, 6, 7, 4, 4, 7, 6, 5, 1, 2, 3, 0};
-  const int kind[16] = {0, -3, 0, 3, -1, 2, -1, -2, 0, -3, 0, 3, 1, -2, 1, 2};
-  int kd = kind[idx];
-  float f = 1.f;
-  int ak = kd < 0 ? -kd : kd;
-  if (ak == 1) f = sl;
-  else if (ak == 2) f = slr;
-  else if (ak == 3) f = sl * slr;
-  if (kd < 0) f = -f;
-  float2 v = sv[src[idx]];
-  if (idx & 1) return make_float2(f * v.x, -f * v.y);
-  return make_float2(f * v.x, f * v.y);
+// The 16 m-sign combinations of (left|right) from the four complex products
+// s_p = u*x and their conjugate-side forms sc_p = u*conj(x) (sv = s1, s1c,
+// ..., s4, s4c) with the left pair phase sl and the product phase slr
+// (ERIFAST :12861-12864, :13013-13016: the time-reversal relations), index
+// 8a+4b+2c+d of (left|right).
+__device__ __forceinline__ void combos16(const float2 (&sv)[8], float sl, float slr,
+                                         float2 (&r)[16]) {
+  r[0] = sv[0];
+  r[12] = make_float2(sv[1].x * sl, sv[1].y * sl);
+  r[15] = make_float2(r[0].x * slr, -r[0].y * slr);
+  r[3] = make_float2(r[12].x * slr, -r[12].y * slr);
+  r[2] = sv[2];
+  r[14] = make_float2(sv[3].x * sl, sv[3].y * sl);
+  r[13] = make_float2(-r[2].x * slr, r[2].y * slr);
+  r[1] = make_float2(-r[14].x * slr, r[14].y * slr);
+  r[8] = sv[4];
+  r[4] = make_float2(-sv[5].x * sl, -sv[5].y * sl);
+  r[7] = make_float2(-r[8].x * slr, r[8].y * slr);
+  r[11] = make_float2(-r[4].x * slr, r[4].y * slr);
+  r[10] = sv[6];
+  r[6] = make_float2(-sv[7].x * sl, -sv[7].y * sl);
+  r[5] = make_float2(r[10].x * slr, -r[10].y * slr);
+  r[9] = make_float2(r[6].x * slr, -r[6].y * slr);
 }
 
 __device__ __forceinline__ void cmac(float2 &acc, float2 u, float2 d) {
@@ -619,38 +624,58 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
           const float2 *Dab = Dsm + 2 * MAXSP * MAXSP, *Dad = Dsm + 3 * MAXSP * MAXSP;
           float2 *Jl = Acc, *Kl = Acc + MAXSP * MAXSP, *J2 = Acc + 2 * MAXSP * MAXSP,
                  *K2 = Acc + 3 * MAXSP * MAXSP;
-#define TCV(sa, sb, sc, sd) (swp ? rvc<true>(sv, sa, sb, sc, sd, sl, slr) \
-                                 : rvc<false>(sv, sa, sb, sc, sd, sl, slr))
+          float2 r16[16];
+          combos16(sv, sl, slr, r16);
+          // (ab|cd) m-sign combination from the (left|right) one; every index
+          // is a compile-time constant once the loops are unrolled
+#define TCV(sa, sb, sc, sd) (swp ? r16[8 * (sc) + 4 * (sd) + 2 * (sa) + (sb)] \
+                                 : r16[8 * (sa) + 4 * (sb) + 2 * (sc) + (sd)])
           if (q.isym == 0) {
+#pragma unroll
             for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
               for (int sb = 0; sb < 2; ++sb) {
                 float2 j = make_float2(0.f, 0.f);
+#pragma unroll
                 for (int sc = 0; sc < 2; ++sc)
+#pragma unroll
                   for (int sd = 0; sd < 2; ++sd)
                     cmac(j, TCV(sa, sb, sc, sd), Dcd[(ic * 2 + sc) * MAXSP + id * 2 + sd]);
                 sadd(&Jl[(ia * 2 + sa) * MAXSP + ib * 2 + sb], j);
               }
+#pragma unroll
             for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
               for (int sd = 0; sd < 2; ++sd) {
                 float2 k = make_float2(0.f, 0.f);
+#pragma unroll
                 for (int sb = 0; sb < 2; ++sb)
+#pragma unroll
                   for (int sc = 0; sc < 2; ++sc)
                     cmac(k, TCV(sa, sb, sc, sd), Dcb[(ic * 2 + sc) * MAXSP + ib * 2 + sb]);
                 sadd(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], k);
               }
             if (dual) {
+#pragma unroll
               for (int sc = 0; sc < 2; ++sc)
+#pragma unroll
                 for (int sd = 0; sd < 2; ++sd) {
                   float2 j = make_float2(0.f, 0.f);
+#pragma unroll
                   for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
                     for (int sb = 0; sb < 2; ++sb)
                       cmac(j, TCV(sa, sb, sc, sd), Dab[(ia * 2 + sa) * MAXSP + ib * 2 + sb]);
                   sadd(&J2[(ic * 2 + sc) * MAXSP + id * 2 + sd], j);
                 }
+#pragma unroll
               for (int sc = 0; sc < 2; ++sc)
+#pragma unroll
                 for (int sb = 0; sb < 2; ++sb) {
                   float2 k = make_float2(0.f, 0.f);
+#pragma unroll
                   for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
                     for (int sd = 0; sd < 2; ++sd)
                       cmac(k, TCV(sa, sb, sc, sd), Dad[(ia * 2 + sa) * MAXSP + id * 2 + sd]);
                   sadd(&K2[(ic * 2 + sc) * MAXSP + ib * 2 + sb], k);
@@ -658,8 +683,10 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
             }
           } else {
             // CLMMTZ: real parts, equal-sign direct blocks, crossed exchange
+#pragma unroll
             for (int s = 0; s < 2; ++s) {
               float jv = 0.f, kv = 0.f;
+#pragma unroll
               for (int t = 0; t < 2; ++t) {
                 jv = fmaf(TCV(s, s, t, t).x, Dcd[(ic * 2 + t) * MAXSP + id * 2 + t].x, jv);
                 kv = fmaf(TCV(s, t, t, s).x, Dcb[(ic * 2 + t) * MAXSP + ib * 2 + t].x, kv);
@@ -668,8 +695,10 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
               atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
             }
             if (dual)
+#pragma unroll
               for (int s = 0; s < 2; ++s) {
                 float jv = 0.f, kv = 0.f;
+#pragma unroll
                 for (int t = 0; t < 2; ++t) {
                   jv = fmaf(TCV(t, t, s, s).x, Dab[(ia * 2 + t) * MAXSP + ib * 2 + t].x, jv);
                   kv = fmaf(TCV(t, s, s, t).x, Dad[(ia * 2 + t) * MAXSP + id * 2 + t].x, kv);
@@ -1150,37 +1179,53 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
           float sl = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
           const float2 *Dcb = Dsm, *Dad = Dsm + MAXSP * MAXSP;
           float2 *Kl = Acc, *K2 = Acc + MAXSP * MAXSP;
-#define TCV(sa, sb, sc, sd) (swp ? rvc<true>(sv, sa, sb, sc, sd, sl, slr) \
-                                 : rvc<false>(sv, sa, sb, sc, sd, sl, slr))
+          float2 r16[16];
+          combos16(sv, sl, slr, r16);
+          // (ab|cd) m-sign combination from the (left|right) one; every index
+          // is a compile-time constant once the loops are unrolled
+#define TCV(sa, sb, sc, sd) (swp ? r16[8 * (sc) + 4 * (sd) + 2 * (sa) + (sb)] \
+                                 : r16[8 * (sa) + 4 * (sb) + 2 * (sc) + (sd)])
           if (q.isym == 0) {
+#pragma unroll
             for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
               for (int sd = 0; sd < 2; ++sd) {
                 float2 k = make_float2(0.f, 0.f);
+#pragma unroll
                 for (int sb = 0; sb < 2; ++sb)
+#pragma unroll
                   for (int sc = 0; sc < 2; ++sc)
                     cmac(k, TCV(sa, sb, sc, sd), Dcb[(ic * 2 + sc) * MAXSP + ib * 2 + sb]);
                 sadd(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], k);
               }
             if (dual)
+#pragma unroll
               for (int sc = 0; sc < 2; ++sc)
+#pragma unroll
                 for (int sb = 0; sb < 2; ++sb) {
                   float2 k = make_float2(0.f, 0.f);
+#pragma unroll
                   for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
                     for (int sd = 0; sd < 2; ++sd)
                       cmac(k, TCV(sa, sb, sc, sd), Dad[(ia * 2 + sa) * MAXSP + id * 2 + sd]);
                   sadd(&K2[(ic * 2 + sc) * MAXSP + ib * 2 + sb], k);
                 }
           } else {
             // BRTMTZ: real parts, crossed exchange blocks
+#pragma unroll
             for (int s = 0; s < 2; ++s) {
               float kv = 0.f;
+#pragma unroll
               for (int t = 0; t < 2; ++t)
                 kv = fmaf(TCV(s, t, t, s).x, Dcb[(ic * 2 + t) * MAXSP + ib * 2 + t].x, kv);
               atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
             }
             if (dual)
+#pragma unroll
               for (int s = 0; s < 2; ++s) {
                 float kv = 0.f;
+#pragma unroll
                 for (int t = 0; t < 2; ++t)
                   kv = fmaf(TCV(t, s, s, t).x, Dad[(ia * 2 + t) * MAXSP + id * 2 + t].x, kv);
                 atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
