@@ -2280,13 +2280,16 @@ size_t quartet_smem() {
 namespace {
 #include "tc_quartet.cuh"
 
-// Launch geometry of k_quartet_tc for classes needing at most n1 + n2 TMEM
-// columns: the allocation (a power of two, 32..512), the CTAs that share an
-// SM's 512 columns, and a dynamic shared-memory request large enough that
-// no more CTAs than that are resident on one SM (a surplus CTA would block
-// in tcgen05.alloc until a neighbour exits).
+// Launch geometry of the tensor-core kernels for classes needing at most
+// (n1, n2) TMEM columns for D1 and D2: the allocation (a power of two,
+// 32..512; the Breit kernel keeps three D1 side by side when they fit, tri),
+// the CTAs that share an SM's 512 columns (256 threads each, or one CTA of
+// 512 threads), double buffering for a lone CTA when its shared memory
+// fits, and a dynamic shared-memory request large enough that no more CTAs
+// than that are resident on one SM (a surplus CTA would block in
+// tcgen05.alloc until a neighbour exits).
 struct TcGeom {
-  int cols, ctas_per_sm, nbuf;
+  int cols, ctas_per_sm, nbuf, nt, tri;
   size_t smem;
 };
 constexpr size_t SM_SMEM = 233472;  // 228 KB of shared memory per SM
@@ -2295,21 +2298,23 @@ size_t g_tc_smem_max = 122880;  // dynamic shared memory the tensor-core kernels
 
 TcGeom tc_geom(int n1, int n2, bool breit = false) {
   TcGeom g;
-  int need = n1 + n2, cols = 32;
+  g.tri = breit && 3 * n1 + n2 <= 512 ? 1 : 0;
+  int need = (g.tri ? 3 * n1 : n1) + n2, cols = 32;
   while (cols < need) cols *= 2;
   g.cols = cols;
   auto total = [&](int nb) {
-    return breit ? (size_t)tcq::layout_b(n1, n2).total : (size_t)tcq::layout(n1, n2, nb).total;
+    return breit ? (size_t)tcq::layout_b(n1, n2, nb, g.tri).total
+                 : (size_t)tcq::layout_c(n1, n2, nb).total;
   };
   size_t s = total(1);
-  int ctas = std::min(2, 512 / cols);  // k_quartet_tc: at most 2 CTAs of 256 threads
+  int ctas = std::min(2, 512 / cols);
   while (ctas > 1 && (s + 1024 + 4096) * ctas > SM_SMEM) --ctas;  // + static shared memory
-  // one CTA per SM: double-buffered K chunks when they fit
   g.nbuf = 1;
-  if (ctas == 1 && !breit && total(2) <= g_tc_smem_max) {
+  if (ctas == 1 && total(2) <= g_tc_smem_max) {
     g.nbuf = 2;
     s = total(2);
   }
+  g.nt = ctas == 1 ? 512 : 256;
   // smallest request that still keeps ctas + 1 CTAs off one SM
   size_t floor_req = SM_SMEM / (ctas + 1) - 1024 + 64;
   g.smem = std::max(s, floor_req);
@@ -2497,17 +2502,19 @@ const char *device_setup(int dev) {
   int optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return "shared-memory opt-in query failed";
-  cudaFuncAttributes fq, fbr;
-  if (cudaFuncGetAttributes(&fq, k_quartet_tc) != cudaSuccess ||
-      cudaFuncGetAttributes(&fbr, k_breit_tc) != cudaSuccess)
-    return "kernel attribute query failed";
-  size_t stat = std::max(fq.sharedSizeBytes, fbr.sharedSizeBytes);
+  const void *tck[4] = {(const void *)k_quartet_tc<256>, (const void *)k_quartet_tc<512>,
+                        (const void *)k_breit_tc<256>, (const void *)k_breit_tc<512>};
+  size_t stat = 0;
+  for (const void *f : tck) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, f) != cudaSuccess) return "kernel attribute query failed";
+    stat = std::max(stat, fa.sharedSizeBytes);
+  }
   g_tc_smem_max = std::min(TC_SMEM_MAX, (size_t)optin - stat);
-  if (cudaFuncSetAttribute(k_quartet_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)g_tc_smem_max) != cudaSuccess ||
-      cudaFuncSetAttribute(k_breit_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)g_tc_smem_max) != cudaSuccess)
-    return "tensor-core kernel shared-memory opt-in failed";
+  for (const void *f : tck)
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)g_tc_smem_max) != cudaSuccess)
+      return "tensor-core kernel shared-memory opt-in failed";
   if (cudaFuncSetAttribute(k_quartet, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)quartet_smem()) != cudaSuccess ||
       cudaFuncSetAttribute(k_quartet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2730,7 +2737,10 @@ int launch_quartets_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
   a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym; a.inst = nullptr;
   a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2; a.nbuf = g.nbuf;
   long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
-  k_quartet_tc<<<(unsigned)grid, tcq::TCT, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  if (g.nt == 512)
+    k_quartet_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  else
+    k_quartet_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
   c->launches++;
   return 0;
@@ -2950,9 +2960,12 @@ int launch_breit_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, con
   a.sh = c->d_sh; a.pe = c->d_pe; a.offq = c->d_offq; a.E = c->d_EBf; a.D = ddf; a.BX = d_BX;
   a.ns = c->ns; a.ldd = c->ndim; a.ldf = ldf; a.nskp = c->nskp; a.isym = c->isym;
   a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual;
-  a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2;
+  a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2; a.nbuf = g.nbuf; a.tri = g.tri;
   long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
-  k_breit_tc<<<(unsigned)grid, tcq::TCT, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  if (g.nt == 512)
+    k_breit_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
+  else
+    k_breit_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
   CK(c, cudaGetLastError());
   c->launches++;
   return 0;
@@ -3041,8 +3054,8 @@ std::vector<Run> uniform_runs(const std::vector<long long> &seg, const std::vect
     if (n <= 0) continue;
     SegDims d = breit ? seg_dims_breit(key[i]) : seg_dims(key[i], t1, t2);
     if (!runs.empty() && runs.back().start + runs.back().count == seg[i] &&
-        (kind != KIND_TC || tc_geom(d.n1, d.n2).cols ==
-                                tc_geom(runs.back().n1, runs.back().n2).cols)) {
+        (kind != KIND_TC || tc_geom(d.n1, d.n2, breit).cols ==
+                                tc_geom(runs.back().n1, runs.back().n2, breit).cols)) {
       runs.back().count += n;
       runs.back().n1 = std::max(runs.back().n1, d.n1);
       runs.back().n2 = std::max(runs.back().n2, d.n2);
@@ -3127,7 +3140,7 @@ int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, in
     if (!runs.empty() && runs.back().kind == x.kind &&
         runs.back().start + runs.back().count == x.start &&
         (x.kind != KIND_TC ||
-         tc_geom(x.n1, x.n2).cols == tc_geom(runs.back().n1, runs.back().n2).cols)) {
+         tc_geom(x.n1, x.n2, breit).cols == tc_geom(runs.back().n1, runs.back().n2, breit).cols)) {
       runs.back().count += x.n;
       runs.back().n1 = std::max(runs.back().n1, x.n1);
       runs.back().n2 = std::max(runs.back().n2, x.n2);
@@ -3346,7 +3359,10 @@ int batch_launch(bg_batch *b, int t1, int t2, int kind, long long start, long lo
     a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.inst = b->d_inst;
     a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2; a.nbuf = g.nbuf;
     long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
-    k_quartet_tc<<<(unsigned)grid, tcq::TCT, g.smem, st>>>(a, quart, nq, t1, t2);
+    if (g.nt == 512)
+      k_quartet_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, quart, nq, t1, t2);
+    else
+      k_quartet_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, quart, nq, t1, t2);
   } else {
     QArgs a;
     a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_E; a.D = d_D; a.Ecv = b->d_Ecv; a.Eci = b->d_Eci;

@@ -8,7 +8,8 @@
 // in global memory.  Included inside the anonymous namespace of
 // bertha_gpu.cu.
 //
-// One 256-thread CTA per shell quartet (grid-stride).  With the left pair
+// One CTA (256 threads, or 512 for classes that take a whole SM's tensor
+// memory) per shell quartet (grid-stride).  With the left pair
 // (labels L, Hermite terms s) and the right pair (labels R, terms q):
 //   GEMM 1  D1[row][q]   = sum_s  E_L[row][s] * R[s+q]        rows (L, set, re/im)
 //   GEMM 2  D2[row][col] = sum_q  G[row][q] * E_R[col][q]     cols (R, set, re/im)
@@ -20,7 +21,6 @@
 
 namespace tcq {
 
-constexpr int TCT = 256;        // threads per CTA (8 warps; warps w and w+4 share TMEM lane quarter w%4)
 constexpr int KC = 32;          // K elements per staged chunk (4 MMAs of K = 8)
 constexpr int MROWS = 128;      // rows per M tile
 constexpr int MLAB = MROWS / 4; // left labels per M tile
@@ -119,6 +119,19 @@ __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// 8 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tld8(uint32_t ta, float *v) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(ta));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
 // 16 consecutive FP32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tld16(uint32_t ta, float *v) {
   uint32_t r[16];
@@ -134,6 +147,7 @@ __device__ __forceinline__ void tld16(uint32_t ta, float *v) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+
 __host__ __device__ inline int rup(int x, int m) { return (x + m - 1) / m * m; }
 
 // Tensor-core cost (MMA columns x K, per 128-row tile) of an orientation:
@@ -144,7 +158,7 @@ __host__ __device__ inline long long tc_cost(int nlL, int nL, int nlR, int nR) {
   return tiles * ((long long)rup(nL, KC) * n1 + (long long)n1 * n2) + 64LL * nlL * nlR;
 }
 
-// TMEM columns (D1 + D2) a class needs in the orientation the kernel takes.
+// TMEM columns (D1, D2) a class needs in the orientation the kernel takes.
 __host__ __device__ inline void tc_dims(int la, int lb, int lc, int ld, int t1, int t2, int &n1,
                                         int &n2, bool &swp) {
   int nab = ntuv(la + lb + 2 * t1), ncd = ntuv(lc + ld + 2 * t2);
@@ -155,30 +169,71 @@ __host__ __device__ inline void tc_dims(int la, int lb, int lc, int ld, int t1, 
   n2 = rup(4 * nlR, 16);
 }
 
-// Shared-memory layout (bytes from a 128-byte aligned base).  The staging
-// region holds nbuf buffers of gsz bytes (double buffering lets the next K
-// chunk be staged while the tensor cores work on the current one); the D2
-// slab and the FP64 R recursion reuse it when no GEMM is in flight.
+// Tensor-core cost of a Breit orientation (as tc_cost, three components i,
+// each contracting three components j, or one for the Gaunt term alone).
+__host__ __device__ inline long long tcb_cost(int nlL, int nL, int nlR, int nR, int gaunt) {
+  long long tiles = (4 * nlL + MROWS - 1) / MROWS;
+  int n1 = rup(nR, KC), n2 = rup(4 * nlR, 16);
+  int nj = gaunt ? 1 : 3;
+  return tiles * 3 * ((long long)nj * rup(nL, KC) * n1 + (long long)n1 * n2) + 64LL * nlL * nlR;
+}
+
+__host__ __device__ inline void tcb_dims(int la, int lb, int lc, int ld, int gaunt, int &n1,
+                                         int &n2, bool &swp) {
+  int nab = ntuv(la + lb + 1), ncd = ntuv(lc + ld + 1);
+  int nlab = (2 * la + 1) * (2 * lb + 1), nlcd = (2 * lc + 1) * (2 * ld + 1);
+  swp = tcb_cost(nlcd, ncd, nlab, nab, gaunt) < tcb_cost(nlab, nab, nlcd, ncd, gaunt);
+  int nR = swp ? nab : ncd, nlR = swp ? nlab : nlcd;
+  n1 = rup(nR, KC);
+  n2 = rup(4 * nlR, 16);
+}
+
+constexpr int NWT = ntuv(4 * BG_MAX_L + 2);  // Breit kernel-table entries (degree la+lb+lc+ld+2)
+constexpr int ABYTES = 2 * MROWS * KC * 4;    // one A staging buffer (hi and lo)
+
+// Shared-memory layout (bytes from a 128-byte aligned base):
+//   nbuf A buffers (MROWS x KC, hi and lo; their padding rows stay zero, so
+//   that a staging pass only writes the rows that carry data),
+//   nbuf B buffers of bbytes each, whose space the FP64 R recursion (before
+//   the GEMMs) and the D2 slab (after them) reuse,
+//   the table the B operand is read from (R, or the Breit kernel table),
+//   nblk density blocks and nblk J/K accumulators, the Boys values.
+// Double buffering (nbuf = 2) lets the next K chunk be staged while the
+// tensor cores work on the current one.
 struct Layout {
-  int stage, gsz, rf, dsm, acc, fb, total;
+  int abuf, bbuf, bsz, rf, dsm, acc, fb, total;
 };
-__host__ __device__ inline Layout layout(int n1max, int n2max, int nbuf = 1) {
+__host__ __device__ inline Layout layout(int bbytes, int nbuf, int rfbytes, int nblk) {
   Layout L;
-  int g1 = 2 * MROWS * KC * 4 + 2 * n1max * KC * 4;       // A1 and B1, hi and lo
-  int g2 = 2 * MROWS * KC * 4 + 2 * n2max * KC * 4;       // A2 and B2
-  int pslab = MROWS * PSTR * 4;                            // D2 slab
-  int rrec = 2 * NTR * 8;                                  // FP64 R recursion buffers
-  L.gsz = rup(g1 > g2 ? g1 : g2, 128);
-  int st = nbuf * L.gsz;
-  st = st > pslab ? st : pslab;
-  st = st > rrec ? st : rrec;
-  L.stage = 0;
-  L.rf = rup(st, 128);                                     // float R (balanced)
-  L.dsm = L.rf + rup(NTR * 4, 128);                        // density blocks, 4 x MAXSP^2 float2
-  L.acc = L.dsm + 4 * MAXSP * MAXSP * 8;                   // J, K, J2, K2 accumulators (float2)
-  L.fb = L.acc + 4 * MAXSP * MAXSP * 8;                    // Boys values (double)
-  L.total = L.fb + (MAXLAM + 2) * 8 + 128;                 // + alignment slack
+  L.abuf = 0;
+  L.bsz = rup(bbytes, 128);
+  int breg = nbuf * L.bsz;
+  breg = breg > MROWS * PSTR * 4 ? breg : MROWS * PSTR * 4;  // D2 slab
+  breg = breg > 2 * NTR * 8 ? breg : 2 * NTR * 8;            // FP64 R recursion
+  L.bbuf = nbuf * ABYTES;
+  L.rf = rup(L.bbuf + breg, 128);
+  L.dsm = L.rf + rup(rfbytes, 128);
+  L.acc = L.dsm + nblk * MAXSP * MAXSP * 8;
+  L.fb = L.acc + nblk * MAXSP * MAXSP * 8;
+  L.total = L.fb + (MAXLAM + 4) * 8 + 128;  // + alignment slack
   return L;
+}
+
+// B-buffer bytes of the Coulomb kernel (one operand of up to max(n1, n2)
+// rows) and of the Breit kernel (three GEMM-1 operands of n1 rows when the
+// three Cartesian components run together, else one).
+__host__ __device__ inline int bbytes_c(int n1, int n2) {
+  return 2 * (n1 > n2 ? n1 : n2) * KC * 4;
+}
+__host__ __device__ inline int bbytes_b(int n1, int n2, int tri) {
+  int b1 = (tri ? 3 : 1) * 2 * n1 * KC * 4, b2 = 2 * n2 * KC * 4;
+  return b1 > b2 ? b1 : b2;
+}
+__host__ __device__ inline Layout layout_c(int n1, int n2, int nbuf) {
+  return layout(bbytes_c(n1, n2), nbuf, NTR * 4, 4);
+}
+__host__ __device__ inline Layout layout_b(int n1, int n2, int nbuf, int tri) {
+  return layout(bbytes_b(n1, n2, tri), nbuf, NWT * 6 * 4, 2);
 }
 
 // MMA completion tracking of up to two staging buffers: one mbarrier per
@@ -210,7 +265,18 @@ struct Args {
   int tmem_cols, n1max, n2max, nbuf;
 };
 
-__device__ inline float fsgn(float x, float s) { return s < 0.f ? -x : x; }
+struct ArgsB {
+  const Shell *sh;
+  const PairE *pe;        // kexp of each ordered pair (row prow of the first shell)
+  const long long *offq;  // sigma-coupled E offsets [pair][LS/SL]
+  const float2 *E;        // their FP32 copy, scaled by 2^(kexp lambda)
+  const float4 *D;        // double-float density (hi words used), n x n
+  double *BX;
+  int ns, ldd, ldf, nskp, isym, racah1, gaunt;
+  int dual;               // as BArgs
+  int tmem_cols, n1max, n2max, nbuf;
+  int tri;                // the three Cartesian components' D1 side by side in TMEM
+};
 
 // The 16 m-sign combinations of (left|right) from the four complex products
 // s_p = u*x and their conjugate-side forms sc_p = u*conj(x) (sv = s1, s1c,
@@ -237,6 +303,23 @@ __device__ __forceinline__ void combos16(const float2 (&sv)[8], float sl, float 
   r[9] = make_float2(r[6].x * slr, -r[6].y * slr);
 }
 
+// The 8 complex products of a label pair from the D2 slab: rows (left label,
+// set, re/im), columns (right label, set, re/im); pp = 2 setL + setR,
+// s_p = u*x = (a-b, c+d), sc_p = u*conj(x) = (a+b, d-c) with a = re.re,
+// b = im.im, c = G.im E.re, d = G.re E.im.
+__device__ __forceinline__ void products8(const float *pr0, float2 (&sv)[8]) {
+#pragma unroll
+  for (int sL = 0; sL < 2; ++sL)
+#pragma unroll
+    for (int sR = 0; sR < 2; ++sR) {
+      const float *p = pr0 + (sL * 2) * PSTR + sR * 2;
+      float a = p[0], d = p[1], c = p[PSTR], b = p[PSTR + 1];
+      int pp = sL * 2 + sR;
+      sv[2 * pp] = make_float2(a - b, c + d);
+      sv[2 * pp + 1] = make_float2(a + b, d - c);
+    }
+}
+
 __device__ __forceinline__ void cmac(float2 &acc, float2 u, float2 d) {
   acc.x = fmaf(u.x, d.x, fmaf(-u.y, d.y, acc.x));
   acc.y = fmaf(u.x, d.y, fmaf(u.y, d.x, acc.y));
@@ -247,20 +330,225 @@ __device__ __forceinline__ void sadd(float2 *p, float2 v) {
   atomicAdd(&p->y, v.y);
 }
 
+// ---- staging of one K chunk into the canonical K-major layout ----
+
+// A rows from E-coefficients: row (label, set, re/im) = 4 label + 2 set + ri
+// for ntl labels; src is label 0 set 0 term 0, rows of (label, set) rstride
+// apart; each term s scaled by 2^(kdiff lambda_s).  Rows from 4 ntl up to
+// the buffer's previous row count are cleared (the rest are zero already).
+template <int NT>
+__device__ __forceinline__ void stage_e_rows(float *Ah, float *Al, const float2 *src,
+                                             long long rstride, int ntl, int kc, int nK,
+                                             int kdiff, const uint32_t *stuv, int &arows,
+                                             int tid) {
+  int nit = ntl * 2 * KC;
+  for (int b0 = 0; b0 < nit; b0 += 4 * NT) {
+    float2 ev[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int w = b0 + tid + j * NT;
+      int ls = w / KC, s = kc + (w % KC);
+      ev[j] = (w < nit && s < nK) ? src[(long long)ls * rstride + s] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int w = b0 + tid + j * NT;
+      if (w >= nit) break;
+      int ls = w / KC, kk = w % KC, s = kc + kk;
+      float f = s < nK ? ldexpf(1.0f, kdiff * tuvL(stuv[s])) : 0.f;
+      int row = ls * 2;
+      float h, l;
+      tsplit(ev[j].x * f, h, l);
+      Ah[kmaj(row, kk)] = h; Al[kmaj(row, kk)] = l;
+      tsplit(ev[j].y * f, h, l);
+      Ah[kmaj(row + 1, kk)] = h; Al[kmaj(row + 1, kk)] = l;
+    }
+  }
+  int r = 4 * ntl;
+  for (int w = r * KC + tid; w < arows * KC; w += NT) {
+    int row = w / KC, kk = w % KC;
+    Ah[kmaj(row, kk)] = 0.f; Al[kmaj(row, kk)] = 0.f;
+  }
+  arows = r;
+}
+
+// B rows of a Hankel matrix: row q < n1, term s of the chunk: tab[(s+q) *
+// tstride + toff] (zero beyond nR rows or nK terms).
+template <int NT>
+__device__ __forceinline__ void stage_hankel(float *Bh, float *Bl, const float *tab, int tstride,
+                                             int toff, int n1, int nR, int kc, int nK,
+                                             const uint32_t *stuv, int tid) {
+  for (int w = tid; w < n1 * KC; w += NT) {
+    int n = w / KC, kk = w % KC, s = kc + kk;
+    float v = 0.f;
+    if (n < nR && s < nK) v = tab[hsum(stuv[s], stuv[n]) * tstride + toff];
+    float h, l;
+    tsplit(v, h, l);
+    Bh[kmaj(n, kk)] = h; Bl[kmaj(n, kk)] = l;
+  }
+}
+
+// A rows of GEMM 2 from D1 in tensor memory (TMEM address ta of column kc at
+// lane 0): rows below `rows` only (D1's other rows are zero), each column q
+// times (-1)^|q| 2^(kdiff |q|); warps sharing a lane quarter split the 32
+// columns.
+template <int NT>
+__device__ __forceinline__ void stage_g(float *Ah, float *Al, uint32_t ta, int kc, int nR,
+                                        int rows, int kdiff, const uint32_t *stuv, int &arows,
+                                        int warp, int lane, int tid) {
+  constexpr int NQ = NT / 128, CW = KC / NQ;
+  int quad = warp & 3, c0 = CW * (warp >> 2);
+  int row = quad * 32 + lane;
+  if (quad * 32 < rows) {  // warp-uniform: the TMEM load is warp-collective
+    float v[CW];
+    uint32_t a = ta + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
+    if (CW == 16) tld16(a, v); else tld8(a, v);
+    if (row < rows) {
+#pragma unroll
+      for (int j = 0; j < CW; ++j) {
+        int qq = kc + c0 + j;
+        float x = 0.f;
+        if (qq < nR) {
+          int L = tuvL(stuv[qq]);
+          x = v[j] * ldexpf((L & 1) ? -1.0f : 1.0f, kdiff * L);
+        }
+        float h, l;
+        tsplit(x, h, l);
+        Ah[kmaj(row, c0 + j)] = h;
+        Al[kmaj(row, c0 + j)] = l;
+      }
+    }
+  }
+  for (int w = rows * KC + tid; w < arows * KC; w += NT) {
+    int rw = w / KC, kk = w % KC;
+    Ah[kmaj(rw, kk)] = 0.f; Al[kmaj(rw, kk)] = 0.f;
+  }
+  arows = rows;
+}
+
+// B rows of GEMM 2 from the right pair's E-coefficients: row (label, set,
+// re/im) for nlR labels, rows of (label, set) rstride apart; zero rows up
+// to n2.
+template <int NT>
+__device__ __forceinline__ void stage_er(float *Bh, float *Bl, const float2 *src,
+                                         long long rstride, int nlR, int n2, int kc, int nR,
+                                         int tid) {
+  int nit = nlR * 2 * KC;
+  for (int b0 = 0; b0 < nit; b0 += 4 * NT) {
+    float2 ev[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int w = b0 + tid + j * NT;
+      int ls = w / KC, qq = kc + (w % KC);
+      ev[j] = (w < nit && qq < nR) ? src[(long long)ls * rstride + qq] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int w = b0 + tid + j * NT;
+      if (w >= nit) break;
+      int ls = w / KC, kk = w % KC;
+      int row = ls * 2;
+      float h, l;
+      tsplit(ev[j].x, h, l);
+      Bh[kmaj(row, kk)] = h; Bl[kmaj(row, kk)] = l;
+      tsplit(ev[j].y, h, l);
+      Bh[kmaj(row + 1, kk)] = h; Bl[kmaj(row + 1, kk)] = l;
+    }
+  }
+  for (int w = 4 * nlR * KC + tid; w < n2 * KC; w += NT) {
+    int n = w / KC, kk = w % KC;
+    Bh[kmaj(n, kk)] = 0.f; Bl[kmaj(n, kk)] = 0.f;
+  }
+}
+
+// The 12 MMAs of one staged K chunk (4 steps of K = 8, three TF32 passes
+// each) into the accumulator at TMEM address d; acc0 = 0 starts it.
+__device__ __forceinline__ void issue_chunk(uint32_t d, const float *Ah, const float *Al,
+                                            const float *Bh, const float *Bl, uint32_t id,
+                                            bool acc0) {
+#pragma unroll
+  for (int ks = 0; ks < KC / 8; ++ks) {
+    uint32_t off = ks * 256;
+    uint64_t ah = sdesc(saddr(Ah) + off), al = sdesc(saddr(Al) + off);
+    uint64_t bh = sdesc(saddr(Bh) + off), bl = sdesc(saddr(Bl) + off);
+    mma(d, ah, bh, id, (acc0 || ks > 0) ? 1u : 0u);
+    mma(d, ah, bl, id, 1u);
+    mma(d, al, bh, id, 1u);
+  }
+}
+
+// D2 columns c0 .. c0+ncol-1 of this thread's lane into the slab P (row
+// stride PSTR), warps sharing a lane quarter taking 16-column pieces in turn.
+template <int NT>
+__device__ __forceinline__ void load_slab(float *P, uint32_t tD2, int c0, int ncol, int rows,
+                                          int warp, int lane) {
+  constexpr int NQ = NT / 128;
+  int quad = warp & 3, row = quad * 32 + lane;
+  if (quad * 32 >= rows) return;
+  for (int j0 = 16 * (warp >> 2); j0 < ncol; j0 += 16 * NQ) {
+    float v[16];
+    tld16(tD2 + ((uint32_t)(quad * 32) << 16) + (uint32_t)(c0 + j0), v);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) P[row * PSTR + j0 + j] = v[j];
+  }
+}
+
+// FP64 R recursion (RMAKE's MD recursion, :31900) for one quartet into R/R2
+// (level by level, one barrier per level); returns the buffer holding
+// R^{(0)}.  F holds F_0..F_lam; g = (X, Y, Z, -2 alpha).
+template <int NT>
+__device__ __forceinline__ double *r_recursion(double *R, double *R2, const double *F, int lam,
+                                               const double *g, const uint32_t *stuv, int tid) {
+  double X = g[0], Y = g[1], Z = g[2], m2a = g[3];
+  double *cur = R, *nxt = R2;
+  for (int n = lam; n >= 0; --n) {
+    int cnt = ntuv(lam - n);
+    for (int k = tid; k < cnt; k += NT) {
+      double val;
+      if (k == 0) {
+        double pw = 1.0;
+        for (int i = 0; i < n; ++i) pw *= m2a;
+        val = pw * F[n];
+      } else {
+        uint32_t w = stuv[k];
+        int t = w & 255, u = (w >> 8) & 255, v = (w >> 16) & 255;
+        if (t > 0) {
+          val = X * cur[hidx(t - 1, u, v)];
+          if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
+        } else if (u > 0) {
+          val = Y * cur[hidx(t, u - 1, v)];
+          if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
+        } else {
+          val = Z * cur[hidx(t, u, v - 1)];
+          if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
+        }
+      }
+      nxt[k] = val;
+    }
+    __syncthreads();
+    double *tmp = cur; cur = nxt; nxt = tmp;
+  }
+  return cur;
+}
+
 }  // namespace tcq
 
-__global__ void __launch_bounds__(tcq::TCT, 2)
+// ---------------------------------------------------------------------------
+// Coulomb kernel
+// ---------------------------------------------------------------------------
+template <int NT>
+__global__ void __launch_bounds__(NT, NT >= 512 ? 1 : 2)
 k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   using namespace tcq;
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char *base =
       (unsigned char *)(((uintptr_t)tc_smem_raw + 127) & ~(uintptr_t)127);
-  const Layout LY = layout(q.n1max, q.n2max, q.nbuf);
-  // staging buffer b: A hi, A lo (MROWS x KC each), then B hi, B lo (GEMM 1:
-  // n1max rows each; GEMM 2 reuses the space with n2max rows)
-  auto bufA = [&](int b) { return (float *)(base + LY.stage + b * LY.gsz); };
-  float *P = (float *)(base + LY.stage);          // D2 slab (epilogue)
-  double *R = (double *)(base + LY.stage);        // FP64 recursion (before the GEMMs)
+  const Layout LY = layout_c(q.n1max, q.n2max, q.nbuf);
+  const int bmax = q.n1max > q.n2max ? q.n1max : q.n2max;
+  auto bufA = [&](int b) { return (float *)(base + LY.abuf + b * ABYTES); };
+  auto bufB = [&](int b) { return (float *)(base + LY.bbuf + b * LY.bsz); };
+  float *P = (float *)(base + LY.bbuf);           // D2 slab (epilogue)
+  double *R = (double *)(base + LY.bbuf);         // FP64 recursion (before the GEMMs)
   double *R2 = R + NTR;
   float *Rf = (float *)(base + LY.rf);
   float2 *Dsm = (float2 *)(base + LY.dsm);        // D(c,d), D(c,b), D(a,b), D(a,d)
@@ -272,11 +560,12 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   __shared__ int sk;
   __shared__ uint32_t stuv[NTR];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quad = warp & 3, half = warp >> 2;  // TMEM lane quarter, column half
+  const int nbuf = q.nbuf;
 
-  for (int i = tid; i < NTR; i += TCT)
+  for (int i = tid; i < NTR; i += NT)
     stuv[i] = (uint32_t)c_t[i] | ((uint32_t)c_u[i] << 8) | ((uint32_t)c_v[i] << 16) |
               ((uint32_t)(c_t[i] + c_u[i] + c_v[i]) << 24);
+  for (int i = tid; i < nbuf * 2 * MROWS * KC; i += NT) bufA(0)[i] = 0.f;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                  :: "r"(saddr(&tslot)), "r"(q.tmem_cols));
@@ -291,7 +580,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   fence_after();
   const uint32_t tmem = tslot;
   Pipe pp = {mbar, {0u, 0u}, {false, false}};
-  const int nbuf = q.nbuf;
+  int arows[2] = {0, 0};  // rows of each A buffer that may be nonzero
   bool abort = false;
 
   for (long long qi = blockIdx.x; qi < nq && !abort; qi += gridDim.x) {
@@ -347,39 +636,11 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
     boys_block(sgeo[5], lam, F);
     __syncthreads();
     {
-      double X = sgeo[0], Y = sgeo[1], Z = sgeo[2], m2a = sgeo[3];
-      double *cur = R, *nxt = R2;
-      for (int n = lam; n >= 0; --n) {
-        int cnt = ntuv(lam - n);
-        for (int k = tid; k < cnt; k += TCT) {
-          double val;
-          if (k == 0) {
-            double pw = 1.0;
-            for (int i = 0; i < n; ++i) pw *= m2a;
-            val = pw * F[n];
-          } else {
-            uint32_t w = stuv[k];
-            int t = w & 255, u = (w >> 8) & 255, v = (w >> 16) & 255;
-            if (t > 0) {
-              val = X * cur[hidx(t - 1, u, v)];
-              if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
-            } else if (u > 0) {
-              val = Y * cur[hidx(t, u - 1, v)];
-              if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
-            } else {
-              val = Z * cur[hidx(t, u, v - 1)];
-              if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
-            }
-          }
-          nxt[k] = val;
-        }
-        __syncthreads();
-        double *tmp = cur; cur = nxt; nxt = tmp;
-      }
+      const double *cur = r_recursion<NT>(R, R2, F, lam, sgeo, stuv, tid);
       // PRE * R scaled by 2^(-k lambda) (exponent balancing), in FP32
       double pre = sgeo[4];
       int k = sk;
-      for (int i = tid; i < ntuv(lam); i += TCT)
+      for (int i = tid; i < ntuv(lam); i += NT)
         Rf[i] = __double2float_rn(ldexp(cur[i] * pre, -k * tuvL(stuv[i])));
     }
     // roles
@@ -403,7 +664,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
       int ro[4] = {ocd, ocd, oab, oab}, co[4] = {ocd, oab, oab, ocd};
       for (int blk = 0; blk < (dual ? 4 : 2); ++blk) {
         int nr = sizes[blk][0], nc = sizes[blk][1];
-        for (int w = tid; w < nr * nc; w += TCT) {
+        for (int w = tid; w < nr * nc; w += NT) {
           int r = w / nc, c = w % nc;
           int fr = rs[blk]->fock[r >> 1][r & 1] + ro[blk];
           int fc = cs[blk]->fock[c >> 1][c & 1] + co[blk];
@@ -412,14 +673,13 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
         }
       }
     }
-    for (int i = tid; i < 4 * MAXSP * MAXSP; i += TCT) Acc[i] = make_float2(0.f, 0.f);
-    __syncthreads();  // R (FP64) is dead: the staging buffers may overwrite it
+    for (int i = tid; i < 4 * MAXSP * MAXSP; i += NT) Acc[i] = make_float2(0.f, 0.f);
+    __syncthreads();  // R (FP64) is dead: the B buffers may overwrite it
 
     const uint32_t tD1 = tmem, tD2 = tmem + (uint32_t)n1;
     const uint32_t id1 = idesc(MROWS, n1), id2 = idesc(MROWS, n2);
-    const uint32_t lanebase = (uint32_t)(quad * 32) << 16;
     for (int l0 = 0; l0 < nlL && !abort; l0 += MLAB) {
-      int ntl = min(MLAB, nlL - l0);
+      int ntl = min(MLAB, nlL - l0), rows = 4 * ntl;
       // ---- GEMM 1: D1 = E_L (rows) x Hankel R (columns q), K = s ----
       // K chunk c is staged into buffer c % nbuf while the MMAs of chunk
       // c - 1 run; a buffer is rewritten once its previous MMAs completed
@@ -427,56 +687,17 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
         int bsel = c % nbuf;
         if (__syncthreads_or(!pipe_wait(pp, bsel))) { abort = true; break; }
         fence_after();
-        float *A1h = bufA(bsel), *A1l = A1h + MROWS * KC;
-        float *B1h = A1l + MROWS * KC, *B1l = B1h + q.n1max * KC;
-        {
-          // E_L chunk: (label, set, s) items, each filling a re and an im
-          // row; the loads are issued together, then split and stored
-          constexpr int AIT = MLAB * 2 * KC / TCT;
-          float2 ev[AIT];
-#pragma unroll
-          for (int j = 0; j < AIT; ++j) {
-            int w = tid + j * TCT;
-            int lab = w / (2 * KC), set = (w / KC) & 1, s = kc + (w % KC);
-            ev[j] = (lab < ntl && s < nL) ? EL[((long long)(l0 + lab) * 2 + set) * nL + s]
-                                          : make_float2(0.f, 0.f);
-          }
-#pragma unroll
-          for (int j = 0; j < AIT; ++j) {
-            int w = tid + j * TCT;
-            int lab = w / (2 * KC), set = (w / KC) & 1, kk = w % KC, s = kc + kk;
-            float f = s < nL ? ldexpf(1.0f, (kq0 - kL) * tuvL(stuv[s])) : 0.f;
-            int row = lab * 4 + set * 2;
-            float h, l;
-            tsplit(ev[j].x * f, h, l);
-            A1h[kmaj(row, kk)] = h; A1l[kmaj(row, kk)] = l;
-            tsplit(ev[j].y * f, h, l);
-            A1h[kmaj(row + 1, kk)] = h; A1l[kmaj(row + 1, kk)] = l;
-          }
-        }
-        for (int w = tid; w < n1 * KC; w += TCT) {
-          int n = w / KC, kk = w % KC, s = kc + kk;
-          float v = 0.f;
-          if (n < nR && s < nL) v = Rf[hsum(stuv[s], stuv[n])];
-          float h, l;
-          tsplit(v, h, l);
-          B1h[kmaj(n, kk)] = h; B1l[kmaj(n, kk)] = l;
-        }
+        float *Ah = bufA(bsel), *Al = Ah + MROWS * KC;
+        float *Bh = bufB(bsel), *Bl = Bh + bmax * KC;
+        stage_e_rows<NT>(Ah, Al, EL + (long long)l0 * 2 * nL, nL, ntl, kc, nL, kq0 - kL, stuv,
+                         arows[bsel], tid);
+        stage_hankel<NT>(Bh, Bl, Rf, 1, 0, n1, nR, kc, nL, stuv, tid);
         fence_async_smem();
         fence_before();
         __syncthreads();
         if (tid == 0) {
           fence_after();
-#pragma unroll
-          for (int ks = 0; ks < KC / 8; ++ks) {
-            uint32_t off = ks * 256;
-            uint64_t ah = sdesc(saddr(A1h) + off), al = sdesc(saddr(A1l) + off);
-            uint64_t bh = sdesc(saddr(B1h) + off), bl = sdesc(saddr(B1l) + off);
-            uint32_t acc0 = (kc > 0 || ks > 0) ? 1u : 0u;
-            mma(tD1, ah, bh, id1, acc0);
-            mma(tD1, ah, bl, id1, 1u);
-            mma(tD1, al, bh, id1, 1u);
-          }
+          issue_chunk(tD1, Ah, Al, Bh, Bl, id1, kc > 0);
           commit(&pp.bar[bsel]);
         }
         pp.pend[bsel] = true;
@@ -493,75 +714,17 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
         int bsel = c % nbuf;
         if (__syncthreads_or(!pipe_wait(pp, bsel))) { abort = true; break; }
         fence_after();
-        float *A1h = bufA(bsel), *A1l = A1h + MROWS * KC;
-        float *B2h = A1l + MROWS * KC, *B2l = B2h + q.n2max * KC;
-        {
-          // D1 rows of this warp's lane quarter, 16 of the chunk's 32
-          // columns: sign (-1)^|q| and the right pair's balancing
-          // 2^((k - kR)|q|), then the TF32 split
-          int row = quad * 32 + lane, c0 = 16 * half;
-          float v[16];
-          tld16(tD1 + lanebase + (uint32_t)(kc + c0), v);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            int qq = kc + c0 + j;
-            float x = 0.f;
-            if (qq < nR) {
-              int L = tuvL(stuv[qq]);
-              x = v[j] * ldexpf((L & 1) ? -1.0f : 1.0f, (kq0 - kR) * L);
-            }
-            float h, l;
-            tsplit(x, h, l);
-            A1h[kmaj(row, c0 + j)] = h;
-            A1l[kmaj(row, c0 + j)] = l;
-          }
-        }
-        {
-          // E_R chunk: (label, set, q) items, each filling a re and an im
-          // row; zero rows above 4 nlR
-          int nit = nlR * 2 * KC;
-          for (int b0 = 0; b0 < nit; b0 += 4 * TCT) {
-            float2 ev[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              int w = b0 + tid + j * TCT;
-              int lr = w / (2 * KC), set = (w / KC) & 1, qq = kc + (w % KC);
-              ev[j] = (w < nit && qq < nR) ? ER[((long long)lr * 2 + set) * nR + qq]
-                                          : make_float2(0.f, 0.f);
-            }
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              int w = b0 + tid + j * TCT;
-              if (w >= nit) continue;
-              int lr = w / (2 * KC), set = (w / KC) & 1, kk = w % KC;
-              int row = lr * 4 + set * 2;
-              float h, l;
-              tsplit(ev[j].x, h, l);
-              B2h[kmaj(row, kk)] = h; B2l[kmaj(row, kk)] = l;
-              tsplit(ev[j].y, h, l);
-              B2h[kmaj(row + 1, kk)] = h; B2l[kmaj(row + 1, kk)] = l;
-            }
-          }
-          for (int w = 4 * nlR * KC + tid; w < n2 * KC; w += TCT) {
-            int n = w / KC, kk = w % KC;
-            B2h[kmaj(n, kk)] = 0.f; B2l[kmaj(n, kk)] = 0.f;
-          }
-        }
+        float *Ah = bufA(bsel), *Al = Ah + MROWS * KC;
+        float *Bh = bufB(bsel), *Bl = Bh + bmax * KC;
+        stage_g<NT>(Ah, Al, tD1 + (uint32_t)kc, kc, nR, rows, kq0 - kR, stuv, arows[bsel], warp,
+                    lane, tid);
+        stage_er<NT>(Bh, Bl, ER, nR, nlR, n2, kc, nR, tid);
         fence_async_smem();
         fence_before();
         __syncthreads();
         if (tid == 0) {
           fence_after();
-#pragma unroll
-          for (int ks = 0; ks < KC / 8; ++ks) {
-            uint32_t off = ks * 256;
-            uint64_t ah = sdesc(saddr(A1h) + off), al = sdesc(saddr(A1l) + off);
-            uint64_t bh = sdesc(saddr(B2h) + off), bl = sdesc(saddr(B2l) + off);
-            uint32_t acc0 = (kc > 0 || ks > 0) ? 1u : 0u;
-            mma(tD2, ah, bh, id2, acc0);
-            mma(tD2, ah, bl, id2, 1u);
-            mma(tD2, al, bh, id2, 1u);
-          }
+          issue_chunk(tD2, Ah, Al, Bh, Bl, id2, kc > 0);
           commit(&pp.bar[bsel]);
         }
         pp.pend[bsel] = true;
@@ -577,19 +740,11 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
       //      J/K digestion (FP32 products, per-quartet FP32 sums) ----
       for (int c0 = 0; c0 < 4 * nlR; c0 += SLAB) {
         int ncol = min(SLAB, n2 - c0);
-        {
-          int row = quad * 32 + lane;
-          for (int j0 = 16 * half; j0 < ncol; j0 += 32) {
-            float v[16];
-            tld16(tD2 + lanebase + (uint32_t)(c0 + j0), v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) P[row * PSTR + j0 + j] = v[j];
-          }
-        }
+        load_slab<NT>(P, tD2, c0, ncol, rows, warp, lane);
         fence_before();
         __syncthreads();
         int r0 = c0 / 4, nrl = min(SLAB / 4, nlR - r0);
-        for (int w = tid; w < ntl * nrl; w += TCT) {
+        for (int w = tid; w < ntl * nrl; w += NT) {
           int lab = w % ntl;
           int lr = r0 + (w / ntl + lab) % nrl;  // skewed: lanes hit different targets
           int labL = l0 + lab;
@@ -602,20 +757,8 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
           label_of(ld, id, kq[3], mm[3]);
           for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
           if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
-          // products: rows (lab, set L, re/im), columns (lr, set R, re/im)
-          const float *pr0 = P + (lab * 4) * PSTR + (lr - r0) * 4;
           float2 sv[8];
-#pragma unroll
-          for (int sL = 0; sL < 2; ++sL)
-#pragma unroll
-            for (int sR = 0; sR < 2; ++sR) {
-              const float *pre_ = pr0 + (sL * 2) * PSTR + sR * 2;
-              float a = pre_[0], d = pre_[1];            // G.re x (E.re, E.im)
-              float c = pre_[PSTR], b = pre_[PSTR + 1];  // G.im x (E.re, E.im)
-              int pp = sL * 2 + sR;                      // s1: (0,0) s2: (0,1) s3: (1,0) s4: (1,1)
-              sv[2 * pp] = make_float2(a - b, c + d);
-              sv[2 * pp + 1] = make_float2(a + b, d - c);
-            }
+          products8(P + (lab * 4) * PSTR + (lr - r0) * 4, sv);
           double pab = pair_phase(kq[0], mm[0], kq[1], mm[1]);
           double pcd = pair_phase(kq[2], mm[2], kq[3], mm[3]);
           double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
@@ -694,7 +837,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
               atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, jv);
               atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
             }
-            if (dual)
+            if (dual) {
 #pragma unroll
               for (int s = 0; s < 2; ++s) {
                 float jv = 0.f, kv = 0.f;
@@ -706,6 +849,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
                 atomicAdd(&J2[(ic * 2 + s) * MAXSP + id * 2 + s].x, jv);
                 atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
               }
+            }
           }
 #undef TCV
         }
@@ -724,7 +868,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
       int ra = rr[f][0], ca = rr[f][1];
       int nr = 2 * nl4[ra], nc = 2 * nl4[ca];
       double *G = (f == 0 || f == 2) ? GDm : GXm;
-      for (int w = tid; w < nr * nc; w += TCT) {
+      for (int w = tid; w < nr * nc; w += NT) {
         int a = w / nc, b = w % nc;
         float2 v = Acc[f * MAXSP * MAXSP + a * MAXSP + b];
         if (v.x == 0.f && v.y == 0.f) continue;
@@ -755,105 +899,58 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
 // on tcgen05 in the same 3xTF32 form.  With the 3x3 Breit kernel table
 // W_ij(N) (Gaunt and gauge terms, :18655-18880; symmetric, 6 entries per N),
 // per Cartesian component i of the right electron:
-//   GEMM 1  D1[row][q]   = sum_j sum_s E_L[row][j][s] W_ij(s+q)
+//   GEMM 1  D1_i[row][q]  = sum_j sum_s E_L[row][j][s] W_ij(s+q)
 //   GEMM 2  D2[row][col] += sum_q G_i[row][q] E_R[col][i][q]
 // D2 summed over i holds the 16 products per label pair; exchange digestion
-// (BRTMTG/BRTMTZ batch type 5) with the Breit phases follows in FP32.
+// (BRTMTG/BRTMTZ batch type 5) with the Breit phases follows in FP32.  When
+// three D1 fit in tensor memory beside D2 (tri), each staged E_L chunk feeds
+// all three components at once; otherwise the components run one after the
+// other.
 // ---------------------------------------------------------------------------
-namespace tcq {
-
-// Tensor-core cost of a Breit orientation (as tc_cost, three components i,
-// each contracting three components j, or one for the Gaunt term alone).
-__host__ __device__ inline long long tcb_cost(int nlL, int nL, int nlR, int nR, int gaunt) {
-  long long tiles = (4 * nlL + MROWS - 1) / MROWS;
-  int n1 = rup(nR, KC), n2 = rup(4 * nlR, 16);
-  int nj = gaunt ? 1 : 3;
-  return tiles * 3 * ((long long)nj * rup(nL, KC) * n1 + (long long)n1 * n2) + 64LL * nlL * nlR;
-}
-
-__host__ __device__ inline void tcb_dims(int la, int lb, int lc, int ld, int gaunt, int &n1,
-                                         int &n2, bool &swp) {
-  int nab = ntuv(la + lb + 1), ncd = ntuv(lc + ld + 1);
-  int nlab = (2 * la + 1) * (2 * lb + 1), nlcd = (2 * lc + 1) * (2 * ld + 1);
-  swp = tcb_cost(nlcd, ncd, nlab, nab, gaunt) < tcb_cost(nlab, nab, nlcd, ncd, gaunt);
-  int nR = swp ? nab : ncd, nlR = swp ? nlab : nlcd;
-  n1 = rup(nR, KC);
-  n2 = rup(4 * nlR, 16);
-}
-
-constexpr int NWT = ntuv(4 * BG_MAX_L + 2);  // kernel-table entries (degree la+lb+lc+ld+2)
-
-struct LayoutB {
-  int stage, wf, dsm, acc, fb, total;
-};
-__host__ __device__ inline LayoutB layout_b(int n1max, int n2max) {
-  LayoutB L;
-  Layout c = layout(n1max, n2max);
-  L.stage = 0;
-  L.wf = c.rf;                                   // W table, 6 floats per entry
-  L.dsm = L.wf + rup(NWT * 6 * 4, 128);          // D(c,b), D(a,d)
-  L.acc = L.dsm + 2 * MAXSP * MAXSP * 8;         // K(a,d), K2(c,b)
-  L.fb = L.acc + 2 * MAXSP * MAXSP * 8;
-  L.total = L.fb + (MAXLAM + 4) * 8 + 128;
-  return L;
-}
-
-struct ArgsB {
-  const Shell *sh;
-  const PairE *pe;        // kexp of each ordered pair (row prow of the first shell)
-  const long long *offq;  // sigma-coupled E offsets [pair][LS/SL]
-  const float2 *E;        // their FP32 copy, scaled by 2^(kexp lambda)
-  const float4 *D;        // double-float density (hi words used), n x n
-  double *BX;
-  int ns, ldd, ldf, nskp, isym, racah1, gaunt;
-  int dual;               // as BArgs
-  int tmem_cols, n1max, n2max;
-};
-
-}  // namespace tcq
-
-__global__ void __launch_bounds__(tcq::TCT, 2)
+template <int NT>
+__global__ void __launch_bounds__(NT, NT >= 512 ? 1 : 2)
 k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
   using namespace tcq;
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char *base =
       (unsigned char *)(((uintptr_t)tc_smem_raw + 127) & ~(uintptr_t)127);
-  const LayoutB LY = layout_b(q.n1max, q.n2max);
-  float *A1h = (float *)(base + LY.stage);
-  float *A1l = A1h + MROWS * KC;
-  float *B1h = A1l + MROWS * KC;
-  float *B1l = B1h + q.n1max * KC;
-  float *B2h = A1l + MROWS * KC;
-  float *B2l = B2h + q.n2max * KC;
-  float *P = (float *)(base + LY.stage);
-  double *R = (double *)(base + LY.stage);
+  const Layout LY = layout_b(q.n1max, q.n2max, q.nbuf, q.tri);
+  auto bufA = [&](int b) { return (float *)(base + LY.abuf + b * ABYTES); };
+  auto bufB = [&](int b) { return (float *)(base + LY.bbuf + b * LY.bsz); };
+  float *P = (float *)(base + LY.bbuf);
+  double *R = (double *)(base + LY.bbuf);
   double *R2 = R + NTR;
-  float *Wf = (float *)(base + LY.wf);
+  float *Wf = (float *)(base + LY.rf);
   float2 *Dsm = (float2 *)(base + LY.dsm);   // D(c,b), D(a,d)
   float2 *Acc = (float2 *)(base + LY.acc);   // K(a,d), K2(c,b)
   double *F = (double *)(base + LY.fb);
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
   __shared__ double sgeo[10];
   __shared__ int sk;
   __shared__ uint32_t stuv[NTR];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quad = warp & 3, half = warp >> 2;
+  const int nbuf = q.nbuf;
 
-  for (int i = tid; i < NTR; i += TCT)
+  for (int i = tid; i < NTR; i += NT)
     stuv[i] = (uint32_t)c_t[i] | ((uint32_t)c_u[i] << 8) | ((uint32_t)c_v[i] << 16) |
               ((uint32_t)(c_t[i] + c_u[i] + c_v[i]) << 24);
+  for (int i = tid; i < nbuf * 2 * MROWS * KC; i += NT) bufA(0)[i] = 0.f;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                  :: "r"(saddr(&tslot)), "r"(q.tmem_cols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar)));
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar[1])));
+  }
   fence_before();
   __syncthreads();
   fence_after();
   const uint32_t tmem = tslot;
-  uint32_t phase = 0;
+  Pipe pp = {mbar, {0u, 0u}, {false, false}};
+  int arows[2] = {0, 0};
   bool abort = false;
 
   for (long long qi = blockIdx.x; qi < nq && !abort; qi += gridDim.x) {
@@ -867,7 +964,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
     int n1, n2;
     bool swp;
     tcb_dims(la, lb, lc, ld, q.gaunt, n1, n2, swp);
-    if (n1 + n2 > q.tmem_cols || n1 > q.n1max || n2 > q.n2max) {
+    if ((q.tri ? 3 * n1 : n1) + n2 > q.tmem_cols || n1 > q.n1max || n2 > q.n2max) {
       if (tid == 0) atomicOr(&g_tc_status, 2);
       continue;
     }
@@ -899,42 +996,14 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
     boys_block(sgeo[9], lam, F);
     __syncthreads();
     {
-      double X = sgeo[0], Y = sgeo[1], Z = sgeo[2], m2a = sgeo[3];
-      double *cur = R, *nxt = R2;
-      for (int n = lam; n >= 0; --n) {
-        int cnt = ntuv(lam - n);
-        for (int k = tid; k < cnt; k += TCT) {
-          double val;
-          if (k == 0) {
-            double pw = 1.0;
-            for (int i = 0; i < n; ++i) pw *= m2a;
-            val = pw * F[n];
-          } else {
-            uint32_t w = stuv[k];
-            int t = w & 255, u = (w >> 8) & 255, v = (w >> 16) & 255;
-            if (t > 0) {
-              val = X * cur[hidx(t - 1, u, v)];
-              if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
-            } else if (u > 0) {
-              val = Y * cur[hidx(t, u - 1, v)];
-              if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
-            } else {
-              val = Z * cur[hidx(t, u, v - 1)];
-              if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
-            }
-          }
-          nxt[k] = val;
-        }
-        __syncthreads();
-        double *tmp = cur; cur = nxt; nxt = tmp;
-      }
+      const double *cur = r_recursion<NT>(R, R2, F, lam, sgeo, stuv, tid);
       // kernel table W_ij(N) = BFAC (delta_ij R_N - T_ij(N)) from PRE * R,
       // scaled by 2^(-k lambda_N), FP32 (6 symmetric entries per N)
       double pre = sgeo[4], h2a = sgeo[5];
       double pq[3] = {sgeo[6], sgeo[7], sgeo[8]};
       double bfac = q.gaunt ? -1.0 : -0.5;
       int k = sk;
-      for (int w = tid; w < ntuv(lamn) * 6; w += TCT) {
+      for (int w = tid; w < ntuv(lamn) * 6; w += NT) {
         int n = w / 6, e = w % 6;
         int i = e < 3 ? e : (e == 5 ? 1 : 0), j = e < 3 ? e : (e == 3 ? 1 : 2);
         uint32_t tw = stuv[n];
@@ -978,7 +1047,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
       int ro[2] = {oc, oa}, co[2] = {ob, od};
       for (int blk = 0; blk < (dual ? 2 : 1); ++blk) {
         int nr = sizes[blk][0], nc = sizes[blk][1];
-        for (int w = tid; w < nr * nc; w += TCT) {
+        for (int w = tid; w < nr * nc; w += NT) {
           int r = w / nc, c = w % nc;
           int fr = rs[blk]->fock[r >> 1][r & 1] + ro[blk];
           int fc = cs[blk]->fock[c >> 1][c & 1] + co[blk];
@@ -987,145 +1056,89 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
         }
       }
     }
-    for (int i = tid; i < 2 * MAXSP * MAXSP; i += TCT) Acc[i] = make_float2(0.f, 0.f);
+    for (int i = tid; i < 2 * MAXSP * MAXSP; i += NT) Acc[i] = make_float2(0.f, 0.f);
     __syncthreads();
 
-    const uint32_t tD1 = tmem, tD2 = tmem + (uint32_t)n1;
+    const int nslot = q.tri ? 3 : 1;  // D1 accumulators side by side
+    const uint32_t tD2 = tmem + (uint32_t)(nslot * n1);
     const uint32_t id1 = idesc(MROWS, n1), id2 = idesc(MROWS, n2);
-    const uint32_t lanebase = (uint32_t)(quad * 32) << 16;
+    const long long rsL = 3LL * nL, rsR = 3LL * nR;  // (label, set) strides of the E blocks
     for (int l0 = 0; l0 < nlL && !abort; l0 += MLAB) {
-      int ntl = min(MLAB, nlL - l0);
-      for (int ci = 0; ci < 3 && !abort; ++ci) {
-        // ---- GEMM 1 for component i: K over (j, s) ----
-        int j0 = q.gaunt ? ci : 0, j1 = q.gaunt ? ci + 1 : 3;
-        bool first = true;
-        for (int cj = j0; cj < j1 && !abort; ++cj) {
-          int sw = cj == ci ? ci : ci + cj + 2;  // symmetric table entry (i, j)
-          for (int kc = 0; kc < nL && !abort; kc += KC) {
-            {
-              constexpr int AIT = MLAB * 2 * KC / TCT;
-              float2 ev[AIT];
-#pragma unroll
-              for (int j = 0; j < AIT; ++j) {
-                int w = tid + j * TCT;
-                int lab = w / (2 * KC), set = (w / KC) & 1, s = kc + (w % KC);
-                ev[j] = (lab < ntl && s < nL)
-                            ? EL[(((long long)(l0 + lab) * 2 + set) * 3 + cj) * nL + s]
-                            : make_float2(0.f, 0.f);
-              }
-#pragma unroll
-              for (int j = 0; j < AIT; ++j) {
-                int w = tid + j * TCT;
-                int lab = w / (2 * KC), set = (w / KC) & 1, kk = w % KC, s = kc + kk;
-                float f = s < nL ? ldexpf(1.0f, (kq0 - kL) * tuvL(stuv[s])) : 0.f;
-                int row = lab * 4 + set * 2;
-                float h, l;
-                tsplit(ev[j].x * f, h, l);
-                A1h[kmaj(row, kk)] = h; A1l[kmaj(row, kk)] = l;
-                tsplit(ev[j].y * f, h, l);
-                A1h[kmaj(row + 1, kk)] = h; A1l[kmaj(row + 1, kk)] = l;
-              }
-            }
-            for (int w = tid; w < n1 * KC; w += TCT) {
-              int n = w / KC, kk = w % KC, s = kc + kk;
-              float v = 0.f;
-              if (n < nR && s < nL) v = Wf[hsum(stuv[s], stuv[n]) * 6 + sw];
-              float h, l;
-              tsplit(v, h, l);
-              B1h[kmaj(n, kk)] = h; B1l[kmaj(n, kk)] = l;
+      int ntl = min(MLAB, nlL - l0), rows = 4 * ntl;
+      const float2 *ELt = EL + (long long)l0 * 2 * rsL;
+      int c = 0;  // chunk counter (buffer selection) across the passes
+      // passes: all three components at once (tri), or one after the other
+      for (int i0 = 0; i0 < 3 && !abort; i0 += nslot) {
+        int i1 = i0 + nslot;
+        // ---- GEMM 1: D1_i for i0 <= i < i1, K over (j, s) ----
+        for (int cj = 0; cj < 3 && !abort; ++cj) {
+          // components i of this pass that couple to j (Gaunt: i = j only)
+          int ilo = q.gaunt ? cj : i0, ihi = q.gaunt ? cj + 1 : i1;
+          if (ilo < i0) ilo = i0;
+          if (ihi > i1) ihi = i1;
+          if (ilo >= ihi) continue;
+          for (int kc = 0; kc < nL && !abort; kc += KC, ++c) {
+            int bsel = c % nbuf;
+            if (__syncthreads_or(!pipe_wait(pp, bsel))) { abort = true; break; }
+            fence_after();
+            float *Ah = bufA(bsel), *Al = Ah + MROWS * KC;
+            float *Bb = bufB(bsel);
+            stage_e_rows<NT>(Ah, Al, ELt + (long long)cj * nL, rsL, ntl, kc, nL, kq0 - kL, stuv,
+                             arows[bsel], tid);
+            for (int ci = ilo; ci < ihi; ++ci) {
+              float *Bh = Bb + (ci - i0) * 2 * q.n1max * KC, *Bl = Bh + q.n1max * KC;
+              int sw = cj == ci ? ci : ci + cj + 2;  // symmetric table entry (i, j)
+              stage_hankel<NT>(Bh, Bl, Wf, 6, sw, n1, nR, kc, nL, stuv, tid);
             }
             fence_async_smem();
             fence_before();
             __syncthreads();
             if (tid == 0) {
               fence_after();
-#pragma unroll
-              for (int ks = 0; ks < KC / 8; ++ks) {
-                uint32_t off = ks * 256;
-                uint64_t ah = sdesc(saddr(A1h) + off), al = sdesc(saddr(A1l) + off);
-                uint64_t bh = sdesc(saddr(B1h) + off), bl = sdesc(saddr(B1l) + off);
-                uint32_t acc0 = (!first || ks > 0) ? 1u : 0u;
-                mma(tD1, ah, bh, id1, acc0);
-                mma(tD1, ah, bl, id1, 1u);
-                mma(tD1, al, bh, id1, 1u);
+              for (int ci = ilo; ci < ihi; ++ci) {
+                float *Bh = Bb + (ci - i0) * 2 * q.n1max * KC, *Bl = Bh + q.n1max * KC;
+                // first contribution to D1_i: j = 0 (Gaunt: j = i) at kc = 0
+                bool acc0 = kc > 0 || (!q.gaunt && cj > 0);
+                issue_chunk(tmem + (uint32_t)((ci - i0) * n1), Ah, Al, Bh, Bl, id1, acc0);
               }
-              commit(&mbar);
+              commit(&pp.bar[bsel]);
             }
-            first = false;
-            bool ok = wait(&mbar, phase);
-            phase ^= 1;
-            if (__syncthreads_or(!ok)) abort = true;
-            fence_after();
+            pp.pend[bsel] = true;
           }
         }
-        // ---- GEMM 2 for component i, accumulated over i ----
-        for (int kc = 0; kc < n1 && !abort; kc += KC) {
-          {
-            int row = quad * 32 + lane, c0 = 16 * half;
-            float v[16];
-            tld16(tD1 + lanebase + (uint32_t)(kc + c0), v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              int qq = kc + c0 + j;
-              float x = 0.f;
-              if (qq < nR) {
-                int L = tuvL(stuv[qq]);
-                x = v[j] * ldexpf((L & 1) ? -1.0f : 1.0f, (kq0 - kR) * L);
-              }
-              float h, l;
-              tsplit(x, h, l);
-              A1h[kmaj(row, c0 + j)] = h;
-              A1l[kmaj(row, c0 + j)] = l;
-            }
-          }
-          {
-            int nit = nlR * 2 * KC;
-            for (int b0 = 0; b0 < nit; b0 += 4 * TCT) {
-              float2 ev[4];
-#pragma unroll
-              for (int j = 0; j < 4; ++j) {
-                int w = b0 + tid + j * TCT;
-                int lr = w / (2 * KC), set = (w / KC) & 1, qq = kc + (w % KC);
-                ev[j] = (w < nit && qq < nR) ? ER[(((long long)lr * 2 + set) * 3 + ci) * nR + qq]
-                                            : make_float2(0.f, 0.f);
-              }
-#pragma unroll
-              for (int j = 0; j < 4; ++j) {
-                int w = b0 + tid + j * TCT;
-                if (w >= nit) continue;
-                int lr = w / (2 * KC), set = (w / KC) & 1, kk = w % KC;
-                int row = lr * 4 + set * 2;
-                float h, l;
-                tsplit(ev[j].x, h, l);
-                B2h[kmaj(row, kk)] = h; B2l[kmaj(row, kk)] = l;
-                tsplit(ev[j].y, h, l);
-                B2h[kmaj(row + 1, kk)] = h; B2l[kmaj(row + 1, kk)] = l;
-              }
-            }
-            for (int w = 4 * nlR * KC + tid; w < n2 * KC; w += TCT) {
-              int n = w / KC, kk = w % KC;
-              B2h[kmaj(n, kk)] = 0.f; B2l[kmaj(n, kk)] = 0.f;
-            }
-          }
-          fence_async_smem();
-          fence_before();
-          __syncthreads();
-          if (tid == 0) {
+        {
+          bool ok = pipe_wait(pp, 0);
+          ok = pipe_wait(pp, 1) && ok;
+          if (__syncthreads_or(!ok)) abort = true;
+          fence_after();
+        }
+        // ---- GEMM 2 for the pass's components, accumulated over i ----
+        for (int ci = i0; ci < i1 && !abort; ++ci) {
+          uint32_t tD1 = tmem + (uint32_t)((ci - i0) * n1);
+          for (int kc = 0; kc < n1 && !abort; kc += KC, ++c) {
+            int bsel = c % nbuf;
+            if (__syncthreads_or(!pipe_wait(pp, bsel))) { abort = true; break; }
             fence_after();
-#pragma unroll
-            for (int ks = 0; ks < KC / 8; ++ks) {
-              uint32_t off = ks * 256;
-              uint64_t ah = sdesc(saddr(A1h) + off), al = sdesc(saddr(A1l) + off);
-              uint64_t bh = sdesc(saddr(B2h) + off), bl = sdesc(saddr(B2l) + off);
-              uint32_t acc0 = (ci > 0 || kc > 0 || ks > 0) ? 1u : 0u;
-              mma(tD2, ah, bh, id2, acc0);
-              mma(tD2, ah, bl, id2, 1u);
-              mma(tD2, al, bh, id2, 1u);
+            float *Ah = bufA(bsel), *Al = Ah + MROWS * KC;
+            float *Bh = bufB(bsel), *Bl = Bh + q.n2max * KC;
+            stage_g<NT>(Ah, Al, tD1 + (uint32_t)kc, kc, nR, rows, kq0 - kR, stuv, arows[bsel],
+                        warp, lane, tid);
+            stage_er<NT>(Bh, Bl, ER + (long long)ci * nR, rsR, nlR, n2, kc, nR, tid);
+            fence_async_smem();
+            fence_before();
+            __syncthreads();
+            if (tid == 0) {
+              fence_after();
+              issue_chunk(tD2, Ah, Al, Bh, Bl, id2, ci > 0 || kc > 0);
+              commit(&pp.bar[bsel]);
             }
-            commit(&mbar);
+            pp.pend[bsel] = true;
           }
-          bool ok = wait(&mbar, phase);
-          phase ^= 1;
+        }
+        {
+          // D1 is rewritten by the next pass, D2 read by the epilogue
+          bool ok = pipe_wait(pp, 0);
+          ok = pipe_wait(pp, 1) && ok;
           if (__syncthreads_or(!ok)) abort = true;
           fence_after();
         }
@@ -1134,19 +1147,11 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
       // ---- epilogue: exchange digestion with the Breit phases ----
       for (int c0 = 0; c0 < 4 * nlR; c0 += SLAB) {
         int ncol = min(SLAB, n2 - c0);
-        {
-          int row = quad * 32 + lane;
-          for (int jj = 16 * half; jj < ncol; jj += 32) {
-            float v[16];
-            tld16(tD2 + lanebase + (uint32_t)(c0 + jj), v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) P[row * PSTR + jj + j] = v[j];
-          }
-        }
+        load_slab<NT>(P, tD2, c0, ncol, rows, warp, lane);
         fence_before();
         __syncthreads();
         int r0 = c0 / 4, nrl = min(SLAB / 4, nlR - r0);
-        for (int w = tid; w < ntl * nrl; w += TCT) {
+        for (int w = tid; w < ntl * nrl; w += NT) {
           int lab = w % ntl;
           int lr = r0 + (w / ntl + lab) % nrl;
           int labL = l0 + lab;
@@ -1159,19 +1164,8 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
           label_of(ld, id, kq[3], mm[3]);
           for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
           if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
-          const float *pr0 = P + (lab * 4) * PSTR + (lr - r0) * 4;
           float2 sv[8];
-#pragma unroll
-          for (int sL = 0; sL < 2; ++sL)
-#pragma unroll
-            for (int sR = 0; sR < 2; ++sR) {
-              const float *pre_ = pr0 + (sL * 2) * PSTR + sR * 2;
-              float a = pre_[0], d = pre_[1];
-              float c = pre_[PSTR], b = pre_[PSTR + 1];
-              int pp = sL * 2 + sR;
-              sv[2 * pp] = make_float2(a - b, c + d);
-              sv[2 * pp + 1] = make_float2(a + b, d - c);
-            }
+          products8(P + (lab * 4) * PSTR + (lr - r0) * 4, sv);
           // Breit phases: the Coulomb pair phases negated (BRTFAST :17528-17533)
           double pab = -pair_phase(kq[0], mm[0], kq[1], mm[1]);
           double pcd = -pair_phase(kq[2], mm[2], kq[3], mm[3]);
@@ -1181,8 +1175,6 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
           float2 *Kl = Acc, *K2 = Acc + MAXSP * MAXSP;
           float2 r16[16];
           combos16(sv, sl, slr, r16);
-          // (ab|cd) m-sign combination from the (left|right) one; every index
-          // is a compile-time constant once the loops are unrolled
 #define TCV(sa, sb, sc, sd) (swp ? r16[8 * (sc) + 4 * (sd) + 2 * (sa) + (sb)] \
                                  : r16[8 * (sa) + 4 * (sb) + 2 * (sc) + (sd)])
           if (q.isym == 0) {
@@ -1198,7 +1190,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
                     cmac(k, TCV(sa, sb, sc, sd), Dcb[(ic * 2 + sc) * MAXSP + ib * 2 + sb]);
                 sadd(&Kl[(ia * 2 + sa) * MAXSP + id * 2 + sd], k);
               }
-            if (dual)
+            if (dual) {
 #pragma unroll
               for (int sc = 0; sc < 2; ++sc)
 #pragma unroll
@@ -1211,6 +1203,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
                       cmac(k, TCV(sa, sb, sc, sd), Dad[(ia * 2 + sa) * MAXSP + id * 2 + sd]);
                   sadd(&K2[(ic * 2 + sc) * MAXSP + ib * 2 + sb], k);
                 }
+            }
           } else {
             // BRTMTZ: real parts, crossed exchange blocks
 #pragma unroll
@@ -1221,7 +1214,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
                 kv = fmaf(TCV(s, t, t, s).x, Dcb[(ic * 2 + t) * MAXSP + ib * 2 + t].x, kv);
               atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
             }
-            if (dual)
+            if (dual) {
 #pragma unroll
               for (int s = 0; s < 2; ++s) {
                 float kv = 0.f;
@@ -1230,6 +1223,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
                   kv = fmaf(TCV(t, s, s, t).x, Dad[(ia * 2 + t) * MAXSP + id * 2 + t].x, kv);
                 atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
               }
+            }
           }
 #undef TCV
         }
@@ -1240,7 +1234,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
     // flush; in a halved (LS|SL) list a quartet equal to its (dc|ba) image
     // counts 1/2 (the completion adds it again)
     const double wq = (q.dual == 2 && t2 == 1 && Q4.x == Q4.w && Q4.y == Q4.z) ? 0.5 : 1.0;
-    for (int w = tid; w < 2 * nla * 2 * nld; w += TCT) {
+    for (int w = tid; w < 2 * nla * 2 * nld; w += NT) {
       int a = w / (2 * nld), d = w % (2 * nld);
       float2 v = Acc[a * MAXSP + d];
       if (v.x == 0.f && v.y == 0.f) continue;
@@ -1250,7 +1244,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
       atomicAdd(dst + 1, wq * (double)v.y);
     }
     if (dual)
-      for (int w = tid; w < 2 * nlc * 2 * nlb; w += TCT) {
+      for (int w = tid; w < 2 * nlc * 2 * nlb; w += NT) {
         int cc = w / (2 * nlb), b = w % (2 * nlb);
         float2 v = Acc[MAXSP * MAXSP + cc * MAXSP + b];
         if (v.x == 0.f && v.y == 0.f) continue;
@@ -1261,7 +1255,10 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
       }
   }
   if (abort && tid == 0) atomicOr(&g_tc_status, 1);
-  if (abort) wait(&mbar, phase ^ 1);
+  if (abort) {
+    pipe_wait(pp, 0);
+    pipe_wait(pp, 1);
+  }
   fence_before();
   __syncthreads();
   if (warp == 0)
