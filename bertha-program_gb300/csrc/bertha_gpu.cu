@@ -1637,38 +1637,108 @@ __global__ void k_boys_table() {
   for (int m = 0; m < NBORD; ++m) g_boys_tab[i * NBORD + m] = F[m];
 }
 
+// F_m(T) for T <= 17 from the table (7-term Taylor expansion about the
+// nearest grid point).
+__device__ __forceinline__ double boys_tab_m(double T, int m) {
+  int i = __double2int_rn(T * 32.0);
+  double d = i / 32.0 - T;  // -(T - T_i)
+  const double *f = g_boys_tab + i * NBORD + m;
+  double v = f[6] * (1.0 / 720.0);
+  v = fma(v, d, f[5] * (1.0 / 120.0));
+  v = fma(v, d, f[4] * (1.0 / 24.0));
+  v = fma(v, d, f[3] * (1.0 / 6.0));
+  v = fma(v, d, f[2] * 0.5);
+  v = fma(v, d, f[1]);
+  return fma(v, d, f[0]);
+}
+
+// F_0 .. F_lam for T > 17 by upward recursion: the reference's rational
+// seed up to 30, asymptotic beyond (FUNFM's regimes).
+__device__ __forceinline__ void boys_large(double T, int lam, double *F) {
+  const double A0 = 4.994501191201870e-1, B0 = 4.551838436668326e-1;
+  const double PI12 = 1.7724538509055160;
+  if (T <= 30.0) {
+    double txp = exp(-T), r2 = 0.5 / T;
+    F[0] = 0.5 * PI12 / sqrt(T) - txp * (A0 / (B0 + T));
+    for (int k = 0; k < lam; ++k) F[k + 1] = (double(2 * k + 1) * F[k] - txp) * r2;
+  } else {
+    double r2 = 0.5 / T;
+    F[0] = 0.5 * PI12 / sqrt(T);
+    for (int k = 0; k < lam; ++k) F[k + 1] = double(2 * k + 1) * F[k] * r2;
+  }
+}
+
 // F_m(T) for m = threadIdx.x <= lam, all threads of the block take part
 // (regimes as in FUNFM: exact at T=0, table below 17, the reference's
 // rational seed up to 30, asymptotic beyond).
 __device__ void boys_block(double T, int lam, double *F) {
-  const double A0 = 4.994501191201870e-1, B0 = 4.551838436668326e-1;
-  const double PI12 = 1.7724538509055160;
   int m = threadIdx.x;
   if (T <= 1.0e-11) {
     if (m <= lam) F[m] = c_rinv[m];
   } else if (T <= 17.0) {
-    if (m <= lam) {
-      int i = __double2int_rn(T * 32.0);
-      double d = i / 32.0 - T;  // -(T - T_i)
-      const double *f = g_boys_tab + i * NBORD + m;
-      double v = f[6] * (1.0 / 720.0);
-      v = fma(v, d, f[5] * (1.0 / 120.0));
-      v = fma(v, d, f[4] * (1.0 / 24.0));
-      v = fma(v, d, f[3] * (1.0 / 6.0));
-      v = fma(v, d, f[2] * 0.5);
-      v = fma(v, d, f[1]);
-      v = fma(v, d, f[0]);
-      F[m] = v;
-    }
+    if (m <= lam) F[m] = boys_tab_m(T, m);
   } else if (m == 0) {
-    if (T <= 30.0) {
-      double txp = exp(-T), r2 = 0.5 / T;
-      F[0] = 0.5 * PI12 / sqrt(T) - txp * (A0 / (B0 + T));
-      for (int k = 0; k < lam; ++k) F[k + 1] = (double(2 * k + 1) * F[k] - txp) * r2;
+    boys_large(T, lam, F);
+  }
+}
+
+// Per-quartet scalars of a tensor-core launch, one thread per quartet for
+// all quartets of the launch at once: the quartet geometry and Boys values
+// are long dependent FP64 chains, which on one thread of each CTA would
+// hold the whole CTA; here they run at full occupancy.  Record i of qp
+// (QPW doubles):
+//   [0..2] P - Q, [3] -2 alpha, [4] PRE = 2 pi^(5/2) / (p q sqrt(p + q)),
+//   [5] T = alpha |P - Q|^2, [6] 1 / (2 alpha), [7] floor(log2(2 alpha) / 2)
+//   (the exponent-balancing shift), [8 + n] (-2 alpha)^n F_n(T) for
+//   n <= lam (RMAKE's R^(n)_000 before the PRE factor),
+// with alpha = p q / (p + q) and lam = la + lb + lc + ld + lextra.  The
+// arithmetic is that of the per-CTA code it replaces, value for value.
+constexpr int QPW = 8 + MAXLAM + 1;
+// Tensor-core launches take their lists in pieces of at most QP_CHUNK
+// quartets, the size of the record scratch (200 MB).
+constexpr long long QP_CHUNK = 1LL << 20;
+
+// Hermite index of the sum of two Hermite terms, hidx(t_s + t_n, u_s + u_n,
+// v_s + v_n), for n, s < NTE (row n holds NHS entries, the last ones
+// unused): the gather table of the tensor-core kernels' Hankel operands.
+constexpr int NHS = 192;
+__device__ unsigned short g_hx[NTE * NHS];
+__global__ void k_qprep(const Shell *sh, const int4 *quart, long long nq, int lextra,
+                        double *qp) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nq;
+       i += (long long)gridDim.x * blockDim.x) {
+    int4 Q4 = quart[i];
+    const Shell &A = sh[Q4.x], &B = sh[Q4.y], &C = sh[Q4.z], &Dd = sh[Q4.w];
+    int lam = A.l + B.l + C.l + Dd.l + lextra;
+    double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
+    double Px = (A.alpha * A.x + B.alpha * B.x) / p;
+    double Py = (A.alpha * A.y + B.alpha * B.y) / p;
+    double Pz = (A.alpha * A.z + B.alpha * B.z) / p;
+    double Qx = (C.alpha * C.x + Dd.alpha * Dd.x) / qq;
+    double Qy = (C.alpha * C.y + Dd.alpha * Dd.y) / qq;
+    double Qz = (C.alpha * C.z + Dd.alpha * Dd.z) / qq;
+    double aph = p * qq / (p + qq);
+    double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
+    double *o = qp + i * QPW;
+    o[0] = Px - Qx; o[1] = Py - Qy; o[2] = Pz - Qz;
+    double m2a = -2.0 * aph;
+    o[3] = m2a;
+    o[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
+    o[5] = T;
+    o[6] = 0.5 / aph;
+    o[7] = (double)half_floor_log2(2.0 * aph);
+    double F[MAXLAM + 1];
+    if (T <= 1.0e-11) {
+      for (int m = 0; m <= lam; ++m) F[m] = c_rinv[m];
+    } else if (T <= 17.0) {
+      for (int m = 0; m <= lam; ++m) F[m] = boys_tab_m(T, m);
     } else {
-      double r2 = 0.5 / T;
-      F[0] = 0.5 * PI12 / sqrt(T);
-      for (int k = 0; k < lam; ++k) F[k + 1] = double(2 * k + 1) * F[k] * r2;
+      boys_large(T, lam, F);
+    }
+    double pw = 1.0;
+    for (int n = 0; n <= lam; ++n) {
+      o[8 + n] = pw * F[n];
+      pw *= m2a;
     }
   }
 }
@@ -2381,6 +2451,7 @@ struct bg_ctx {
   // split-precision copies: double-float E (and density), FP32 E (re, im) for
   // the tensor-core kernel, both scaled by 2^(kexp lambda)
   float4 *d_Edf = nullptr, *d_Ddf = nullptr;
+  double *d_qp = nullptr;  // k_qprep records of tensor-core launches (QP_CHUNK of them)
   float2 *d_Ef = nullptr;
   int prec = BG_PREC_FP64;
   double err_budget = 1e-7;  // BG_PREC_AUTO: estimated energy error allowed per build (Eh)
@@ -2426,6 +2497,7 @@ struct bg_batch {
   double2 *d_E = nullptr, *d_Ecv = nullptr;
   unsigned char *d_Eci = nullptr;
   float4 *d_Edf = nullptr, *d_Ddf = nullptr;
+  double *d_qp = nullptr;  // k_qprep records of tensor-core launches (QP_CHUNK of them)
   float2 *d_Ef = nullptr;
   Inst *d_inst = nullptr;
   int *d_ndim = nullptr;
@@ -2497,6 +2569,15 @@ const char *device_setup(int dev) {
   if (cudaMemcpyToSymbol(c_rinv, rinv, sizeof(rinv)) != cudaSuccess)
     return "reciprocal table upload failed";
   k_boys_table<<<(NBGRID + 127) / 128, 128>>>();
+  {
+    std::vector<unsigned short> hx((size_t)NTE * NHS, 0);
+    for (int nn = 0; nn < NTE; ++nn)
+      for (int ss = 0; ss < NTE; ++ss)
+        hx[(size_t)nn * NHS + ss] =
+            (unsigned short)hidx(t[nn] + t[ss], u[nn] + u[ss], v[nn] + v[ss]);
+    if (cudaMemcpyToSymbol(g_hx, hx.data(), sizeof(unsigned short) * hx.size()) != cudaSuccess)
+      return "Hankel index table upload failed";
+  }
   // the tensor-core kernels: the per-block opt-in limit less their static
   // shared memory (the launches never ask for more than g_tc_smem_max)
   int optin = 0;
@@ -2722,27 +2803,28 @@ int launch_quartets_fp64(bg_ctx *c, const int *d_q, long long nq, int t1, int t2
 // double-float density copy ddf is made here unless convert is false.
 int launch_quartets_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                        const double2 *d_D, int ldd, double *d_GD, double *d_GX, int ldf,
-                       cudaStream_t st, float4 *ddf, int sym, int n1, int n2,
-                       bool convert = true) {
+                       cudaStream_t st, int sym, int n1, int n2) {
   if (nq <= 0) return 0;
-  int n = c->ndim;
-  if (convert) {
-    k_dconv<<<1024, 256, 0, st>>>(d_D, ldd, n, ddf);
-    c->launches++;
-  }
+  if (!c->d_qp) CK(c, cudaMalloc(&c->d_qp, sizeof(double) * QPW * QP_CHUNK));
   TcGeom g = tc_geom(n1, n2);
   tcq::Args a;
-  a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Ef; a.D = ddf;
-  a.GD = d_GD; a.GX = d_GX; a.ldd = n; a.ldf = ldf; a.nskp = c->nskp;
-  a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym; a.inst = nullptr;
+  a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Ef; a.D = d_D;
+  a.GD = d_GD; a.GX = d_GX; a.ldd = ldd; a.ldf = ldf; a.nskp = c->nskp;
+  a.isym = c->isym; a.racah1 = c->racah1; a.sym = sym; a.inst = nullptr; a.qp = c->d_qp;
   a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2; a.nbuf = g.nbuf;
-  long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
-  if (g.nt == 512)
-    k_quartet_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
-  else
-    k_quartet_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
-  CK(c, cudaGetLastError());
-  c->launches++;
+  for (long long s0 = 0; s0 < nq; s0 += QP_CHUNK) {
+    long long m = std::min(QP_CHUNK, nq - s0);
+    const int4 *qq = (const int4 *)d_q + s0;
+    k_qprep<<<(unsigned)std::min<long long>((m + 127) / 128, 152LL * 16), 128, 0, st>>>(
+        c->d_sh, qq, m, 2 * t1 + 2 * t2, c->d_qp);
+    long long grid = std::min<long long>(m, 152LL * g.ctas_per_sm);
+    if (g.nt == 512)
+      k_quartet_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, qq, m, t1, t2);
+    else
+      k_quartet_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, qq, m, t1, t2);
+    CK(c, cudaGetLastError());
+    c->launches += 2;
+  }
   return 0;
 }
 
@@ -2754,12 +2836,12 @@ int launch_quartets(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                     const double2 *d_D, int ldd, double *d_GD, double *d_GX,
                     int ldf, cudaStream_t st, int sym = 0, double *bound = nullptr) {
   if (nq <= 0) return 0;
+  if (c->prec == BG_PREC_TC32 && !bound)
+    return launch_quartets_tc(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, sym, tcq::N1MAX,
+                              tcq::N2MAX);
   if (c->prec != BG_PREC_FP64 && !bound) {
     int n = c->ndim;
     if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
-    if (c->prec == BG_PREC_TC32)
-      return launch_quartets_tc(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, c->d_Ddf, sym,
-                                tcq::N1MAX, tcq::N2MAX);
     return launch_quartets_df(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, c->d_Ddf, sym);
   }
   return launch_quartets_fp64(c, d_q, nq, t1, t2, d_D, ldd, d_GD, d_GX, ldf, st, sym, bound);
@@ -2951,23 +3033,32 @@ int launch_breit(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const 
 }
 
 // Tensor-core Breit launch over list entries whose classes need at most
-// n1 + n2 TMEM columns; ddf holds the double-float density copy.
-int launch_breit_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const float4 *ddf,
-                    double *d_BX, int ldf, cudaStream_t st, int dual, int n1, int n2) {
+// n1 + n2 TMEM columns; D is the FP64 density (leading dimension ldd).
+int launch_breit_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2, const double2 *D,
+                    int ldd, double *d_BX, int ldf, cudaStream_t st, int dual, int n1, int n2) {
   if (nq <= 0) return 0;
+  if (!c->d_qp) CK(c, cudaMalloc(&c->d_qp, sizeof(double) * QPW * QP_CHUNK));
   TcGeom g = tc_geom(n1, n2, true);
   tcq::ArgsB a;
-  a.sh = c->d_sh; a.pe = c->d_pe; a.offq = c->d_offq; a.E = c->d_EBf; a.D = ddf; a.BX = d_BX;
-  a.ns = c->ns; a.ldd = c->ndim; a.ldf = ldf; a.nskp = c->nskp; a.isym = c->isym;
-  a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual;
+  a.sh = c->d_sh; a.pe = c->d_pe; a.offq = c->d_offq; a.E = c->d_EBf; a.D = D; a.BX = d_BX;
+  a.ns = c->ns; a.ldd = ldd; a.ldf = ldf; a.nskp = c->nskp; a.isym = c->isym;
+  a.racah1 = c->racah1; a.gaunt = c->gaunt; a.dual = dual; a.qp = c->d_qp;
   a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2; a.nbuf = g.nbuf; a.tri = g.tri;
-  long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
-  if (g.nt == 512)
-    k_breit_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
-  else
-    k_breit_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, (const int4 *)d_q, nq, t1, t2);
-  CK(c, cudaGetLastError());
-  c->launches++;
+  // R to order la+lb+lc+ld+2, +2 more for the gauge term's derivatives
+  int lextra = 2 + (c->gaunt ? 0 : 2);
+  for (long long s0 = 0; s0 < nq; s0 += QP_CHUNK) {
+    long long m = std::min(QP_CHUNK, nq - s0);
+    const int4 *qq = (const int4 *)d_q + s0;
+    k_qprep<<<(unsigned)std::min<long long>((m + 127) / 128, 152LL * 16), 128, 0, st>>>(
+        c->d_sh, qq, m, lextra, c->d_qp);
+    long long grid = std::min<long long>(m, 152LL * g.ctas_per_sm);
+    if (g.nt == 512)
+      k_breit_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, qq, m, t1, t2);
+    else
+      k_breit_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, qq, m, t1, t2);
+    CK(c, cudaGetLastError());
+    c->launches += 2;
+  }
   return 0;
 }
 
@@ -3151,6 +3242,86 @@ int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, in
   return 0;
 }
 
+// Reorders a cached quartet list so that the segments digested by one kind
+// of launch (the FP64 kernel, the split kernel, or the tensor-core kernel
+// at one launch shape: TMEM columns, CTAs per SM, threads) are contiguous, and rebuilds seg, key and runs over the
+// new order.  A build then makes one launch per kind and shape instead
+// of one per stretch of neighbouring segments with the same choice (each
+// launch ends with a partly idle GPU).  The segments and the kernel chosen
+// for each are unchanged.  Returns nonzero on a CUDA failure.
+int regroup_list(int *&d_list, std::vector<long long> &seg, std::vector<int> &key,
+                 std::vector<Run> &runs, int t1, int t2, bool breit, cudaStream_t st) {
+  if (seg.size() < 2 || seg.front() != 0 || runs.size() < 2) return 0;
+  // launch shape of the tensor-core kernel (runs merge only within one)
+  auto shape = [&](int n1, int n2) {
+    TcGeom g = tc_geom(n1, n2, breit);
+    return ((g.cols * 4 + g.ctas_per_sm) * 1024 + g.nt) * 4 + g.nbuf * 2 + g.tri;
+  };
+  struct S {
+    long long start, n;
+    int key, kind, shp, n1, n2;  // shp: launch shape (tensor cores)
+  };
+  std::vector<S> ss;
+  size_t r = 0;
+  for (size_t i = 0; i + 1 < seg.size(); ++i) {
+    long long n = seg[i + 1] - seg[i];
+    if (n <= 0) continue;
+    while (r < runs.size() && runs[r].start + runs[r].count <= seg[i]) ++r;
+    if (r == runs.size() || runs[r].start > seg[i]) return 0;  // not covered: keep the order
+    SegDims d = breit ? seg_dims_breit(key[i]) : seg_dims(key[i], t1, t2);
+    int kind = runs[r].kind;
+    ss.push_back({seg[i], n, key[i], kind, kind == KIND_TC ? shape(d.n1, d.n2) : 0, d.n1, d.n2});
+  }
+  std::vector<int> ord(ss.size());
+  for (size_t i = 0; i < ord.size(); ++i) ord[i] = (int)i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+    const S &x = ss[a], &y = ss[b];
+    if (x.kind != y.kind) return x.kind < y.kind;
+    if (x.shp != y.shp) return x.shp < y.shp;
+    return x.kind == KIND_TC && (x.n1 != y.n1 ? x.n1 < y.n1 : x.n2 < y.n2);
+  });
+  long long tot = seg.back();
+  int *nl = nullptr;
+  if (cudaMalloc(&nl, sizeof(int4) * (size_t)tot) != cudaSuccess) return -1;
+  std::vector<long long> nseg;
+  std::vector<int> nkey;
+  std::vector<Run> nruns;
+  long long pos = 0;
+  for (int o : ord) {
+    const S &x = ss[o];
+    if (cudaMemcpyAsync(nl + 4 * pos, d_list + 4 * x.start, sizeof(int4) * (size_t)x.n,
+                        cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+      cudaFree(nl);
+      return -1;
+    }
+    nseg.push_back(pos);
+    nkey.push_back(x.key);
+    Run *b = nruns.empty() ? nullptr : &nruns.back();
+    if (b && b->kind == x.kind &&
+        (x.kind != KIND_TC ||
+         (shape(b->n1, b->n2) == x.shp &&
+          shape(std::max(b->n1, x.n1), std::max(b->n2, x.n2)) == x.shp))) {
+      b->count += x.n;
+      b->n1 = std::max(b->n1, x.n1);
+      b->n2 = std::max(b->n2, x.n2);
+    } else {
+      nruns.push_back({pos, x.n, x.kind, x.n1, x.n2});
+    }
+    pos += x.n;
+  }
+  nseg.push_back(pos);
+  if (cudaStreamSynchronize(st) != cudaSuccess) {
+    cudaFree(nl);
+    return -1;
+  }
+  cudaFree(d_list);
+  d_list = nl;
+  seg.swap(nseg);
+  key.swap(nkey);
+  runs.swap(nruns);
+  return 0;
+}
+
 // sum_ij Re(D_ij G_ij) over an n x n block (leading dimensions ldd, ldg) or,
 // with inst, over every instance's block; added to *out.
 __global__ void k_edot(const double2 *D, long long ldd, const double2 *G, long long ldg, int n,
@@ -3218,8 +3389,7 @@ int tune_ctx(bg_ctx *c, const double2 *d_D, int ldd, cudaStream_t st) {
         if (kind == KIND_DF32)
           return launch_quartets_df(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, c->d_Ddf, 2, false);
         if (kind == KIND_TC)
-          return launch_quartets_tc(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, c->d_Ddf, 2, n1, n2,
-                                    false);
+          return launch_quartets_tc(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, 2, n1, n2);
         return launch_quartets_fp64(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, 2, nullptr);
       }, zero, energy, c->runs[k], false, &c->tune_rec);
     }
@@ -3227,6 +3397,12 @@ int tune_ctx(bg_ctx *c, const double2 *d_D, int ldd, cudaStream_t st) {
   cudaFree(gx);
   cudaFree(d_e);
   if (rc) return rc > 0 ? rc : cuda_fail(c, cudaGetLastError(), "autotuning");
+  for (int t1 = 0; t1 < c->ncomp; ++t1)
+    for (int t2 = 0; t2 < c->ncomp; ++t2) {
+      int k = 2 * t1 + t2;
+      if (regroup_list(c->d_quart[k], c->seg[k], c->segkey[k], c->runs[k], t1, t2, false, st))
+        return cuda_fail(c, cudaGetLastError(), "list regrouping");
+    }
   c->tuned = true;
   return 0;
 }
@@ -3352,17 +3528,25 @@ int batch_launch(bg_batch *b, int t1, int t2, int kind, long long start, long lo
     long long grid = std::min<long long>(nq, 152LL * 128);
     k_quartet_df<<<(unsigned)grid, DFTHREADS, quartet_smem_df(1), st>>>(a, quart, nq, t1, t2);
   } else if (kind == KIND_TC) {
+    if (!b->d_qp) BK(b, cudaMalloc(&b->d_qp, sizeof(double) * QPW * QP_CHUNK));
     TcGeom g = tc_geom(n1, n2);
     tcq::Args a;
-    a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_Ef; a.D = b->d_Ddf;
+    a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_Ef; a.D = d_D;
     a.GD = d_GD; a.GX = d_GX; a.ldd = 0; a.ldf = 0; a.nskp = 0;
-    a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.inst = b->d_inst;
+    a.isym = b->isym; a.racah1 = b->racah1; a.sym = 2; a.inst = b->d_inst; a.qp = b->d_qp;
     a.tmem_cols = g.cols; a.n1max = n1; a.n2max = n2; a.nbuf = g.nbuf;
-    long long grid = std::min<long long>(nq, 152LL * g.ctas_per_sm);
-    if (g.nt == 512)
-      k_quartet_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, quart, nq, t1, t2);
-    else
-      k_quartet_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, quart, nq, t1, t2);
+    for (long long s0 = 0; s0 < nq; s0 += QP_CHUNK) {
+      long long m = std::min(QP_CHUNK, nq - s0);
+      k_qprep<<<(unsigned)std::min<long long>((m + 127) / 128, 152LL * 16), 128, 0, st>>>(
+          b->d_sh, quart + s0, m, 2 * t1 + 2 * t2, b->d_qp);
+      long long grid = std::min<long long>(m, 152LL * g.ctas_per_sm);
+      if (g.nt == 512)
+        k_quartet_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, quart + s0, m, t1, t2);
+      else
+        k_quartet_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, quart + s0, m, t1, t2);
+      b->launches += 2;
+    }
+    b->launches--;  // counted once more below
   } else {
     QArgs a;
     a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_E; a.D = d_D; a.Ecv = b->d_Ecv; a.Eci = b->d_Eci;
@@ -3763,14 +3947,10 @@ int bertha_gpu_quartets_segments(bg_ctx *c, const int *d_q, int nseg, const long
   if (c->prec != BG_PREC_TC32)
     return launch_quartets(c, d_q + 4 * sv[0], nq, t1, t2, D, ldd, d_gdir, d_gxch, ldf, st);
   // tensor cores: launches sized per class (runs of classes sharing a TMEM
-  // allocation size); one double-float density copy for all of them
-  int n = c->ndim;
-  if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
-  k_dconv<<<1024, 256, 0, st>>>(D, ldd, n, c->d_Ddf);
-  c->launches++;
+  // allocation size), each reading the FP64 density
   for (const Run &r : uniform_runs(sv, keys, t1, t2, KIND_TC)) {
     int rc = launch_quartets_tc(c, d_q + 4 * r.start, r.count, t1, t2, D, ldd, d_gdir, d_gxch,
-                                ldf, st, c->d_Ddf, 0, r.n1, r.n2, false);
+                                ldf, st, 0, r.n1, r.n2);
     if (rc) return rc;
   }
   return BG_OK;
@@ -3887,16 +4067,18 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
         for (int t2 = 0; t2 < c->ncomp; ++t2) {
           int k = 2 * t1 + t2;
           c->runs[k] = uniform_runs(c->seg[k], c->segkey[k], t1, t2, KIND_TC);
+          if (regroup_list(c->d_quart[k], c->seg[k], c->segkey[k], c->runs[k], t1, t2, false, st))
+            return cuda_fail(c, cudaGetLastError(), "list regrouping");
         }
       c->tuned = true;
     }
   }
   if (byrun) {
-    // one double-float copy of the density for all split-precision and
-    // tensor-core runs
+    // one double-float copy of the density for all split-precision runs
+    // (the tensor-core kernels read the FP64 density)
     bool any_f = false;
     for (int k = 0; k < 4; ++k)
-      for (const Run &r : c->runs[k]) any_f |= r.kind != KIND_FP64;
+      for (const Run &r : c->runs[k]) any_f |= r.kind == KIND_DF32;
     if (any_f) {
       if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)c->ndim * c->ndim));
       k_dconv<<<1024, 256, 0, st>>>((const double2 *)d_dent, ldd, c->ndim, c->d_Ddf);
@@ -3917,8 +4099,8 @@ int bertha_gpu_clmfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
             rc = launch_quartets_df(c, q, r.count, t1, t2, D, ldd, d_gdir, d_gxch, ldf, st,
                                     c->d_Ddf, 2, false);
           else if (r.kind == KIND_TC)
-            rc = launch_quartets_tc(c, q, r.count, t1, t2, D, ldd, d_gdir, d_gxch, ldf, st,
-                                    c->d_Ddf, 2, r.n1, r.n2, false);
+            rc = launch_quartets_tc(c, q, r.count, t1, t2, D, ldd, d_gdir, d_gxch, ldf, st, 2,
+                                    r.n1, r.n2);
           else
             rc = launch_quartets_fp64(c, q, r.count, t1, t2, D, ldd, d_gdir, d_gxch, ldf, st, 2,
                                       nullptr);
@@ -4007,14 +4189,13 @@ int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
   bool byrun = c->prec == BG_PREC_AUTO || c->prec == BG_PREC_TC32;
   if (byrun) {
     int n = c->ndim;
-    if (!c->d_Ddf) CK(c, cudaMalloc(&c->d_Ddf, sizeof(float4) * (size_t)n * n));
-    k_dconv<<<1024, 256, 0, st>>>(D, ldd, n, c->d_Ddf);
-    CK(c, cudaGetLastError());
-    c->launches++;
     g_gaunt_dims = c->gaunt;
     if (!c->btuned && c->prec == BG_PREC_TC32) {
-      for (int k = 0; k < 2; ++k)
+      for (int k = 0; k < 2; ++k) {
         c->bruns[k] = uniform_runs(c->bseg[k], c->bsegkey[k], 0, k, KIND_TC, true);
+        if (regroup_list(c->d_bquart[k], c->bseg[k], c->bsegkey[k], c->bruns[k], 0, k, true, st))
+          return cuda_fail(c, cudaGetLastError(), "list regrouping");
+      }
       c->btuned = true;
     }
     if (!c->btuned) {
@@ -4043,13 +4224,16 @@ int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
         rc = tune_runs(c->bseg[k], c->bsegkey[k], 0, k, st, c->err_budget,
                        [&](int kind, long long start, long long m, int n1, int n2) {
           if (kind == KIND_TC)
-            return launch_breit_tc(c, q + 4 * start, m, 0, k, c->d_Ddf, bx, n, st, 2, n1, n2);
+            return launch_breit_tc(c, q + 4 * start, m, 0, k, D, ldd, bx, n, st, 2, n1, n2);
           return launch_breit(c, q + 4 * start, m, 0, k, D, ldd, bx, n, st, 2);
         }, zero, energy, c->bruns[k], true, &c->btune_rec);
       }
       cudaFree(bx);
       cudaFree(d_e);
       if (rc) return rc > 0 ? rc : cuda_fail(c, cudaGetLastError(), "Breit autotuning");
+      for (int k = 0; k < 2; ++k)
+        if (regroup_list(c->d_bquart[k], c->bseg[k], c->bsegkey[k], c->bruns[k], 0, k, true, st))
+          return cuda_fail(c, cudaGetLastError(), "list regrouping");
       c->btuned = true;
     }
   }
@@ -4058,7 +4242,7 @@ int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
       for (const Run &r : c->bruns[k]) {
         const int *q = c->d_bquart[k] + 4 * r.start;
         rc = r.kind == KIND_TC
-                 ? launch_breit_tc(c, q, r.count, 0, k, c->d_Ddf, d_bxch, ldf, st, 2, r.n1, r.n2)
+                 ? launch_breit_tc(c, q, r.count, 0, k, D, ldd, d_bxch, ldf, st, 2, r.n1, r.n2)
                  : launch_breit(c, q, r.count, 0, k, D, ldd, d_bxch, ldf, st, 2);
         if (rc) return rc;
       }
@@ -4176,6 +4360,7 @@ void bertha_gpu_free(bg_ctx *c) {
   cudaFree(c->d_Edf);
   cudaFree(c->d_Ef);
   cudaFree(c->d_Ddf);
+  cudaFree(c->d_qp);
   cudaFree(c->d_D);
   cudaFree(c->d_GD);
   cudaFree(c->d_GX);
@@ -4342,7 +4527,7 @@ int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
     int rc = batch_lists(b, ilev);
     if (rc) return rc;
   }
-  if (b->prec != BG_PREC_FP64) {
+  if (b->prec == BG_PREC_DF32 || b->prec == BG_PREC_AUTO) {
     if (!b->d_Ddf) BK(b, cudaMalloc(&b->d_Ddf, sizeof(float4) * std::max<long long>(b->span, 1)));
     k_dconv1<<<1024, 256, 0, st>>>((const double2 *)d_dent, b->span, b->d_Ddf);
     BK(b, cudaGetLastError());
@@ -4390,6 +4575,12 @@ int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
     cudaFree(gx);
     cudaFree(d_e);
     if (rc) return rc > 0 ? rc : batch_fail(b, cudaGetLastError(), "autotuning");
+    for (int t1 = 0; t1 < b->ncomp; ++t1)
+      for (int t2 = 0; t2 < b->ncomp; ++t2) {
+        int k = 2 * t1 + t2;
+        if (regroup_list(b->d_quart[k], b->seg[k], b->segkey[k], b->runs[k], t1, t2, false, st))
+          return batch_fail(b, cudaGetLastError(), "list regrouping");
+      }
     b->tuned = true;
   }
   if (b->prec == BG_PREC_TC32 && !b->tuned) {
@@ -4397,6 +4588,8 @@ int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
       for (int t2 = 0; t2 < b->ncomp; ++t2) {
         int k = 2 * t1 + t2;
         b->runs[k] = uniform_runs(b->seg[k], b->segkey[k], t1, t2, KIND_TC);
+        if (regroup_list(b->d_quart[k], b->seg[k], b->segkey[k], b->runs[k], t1, t2, false, st))
+          return batch_fail(b, cudaGetLastError(), "list regrouping");
       }
     b->tuned = true;
   }
@@ -4445,6 +4638,7 @@ void bertha_gpu_batch_free(bg_batch *b) {
   cudaFree(b->d_Edf);
   cudaFree(b->d_Ef);
   cudaFree(b->d_Ddf);
+  cudaFree(b->d_qp);
   cudaFree(b->d_inst);
   cudaFree(b->d_ndim);
   for (int k = 0; k < 4; ++k) cudaFree(b->d_quart[k]);

@@ -257,11 +257,12 @@ struct Args {
   const Shell *sh;
   const PairE *pe;
   const float2 *E;   // FP32 E copy (re, im), scaled like the double-float copy
-  const float4 *D;   // double-float density, n x n (batched: Inst placement)
+  const double2 *D;  // density as the caller holds it, leading dimension ldd (batched: Inst placement)
   double *GD, *GX;
   int ldd, ldf, nskp, isym, racah1;
   int sym;           // as QArgsDF
   const Inst *inst;
+  const double *qp;  // per-quartet records of k_qprep, one per list entry
   int tmem_cols, n1max, n2max, nbuf;
 };
 
@@ -270,10 +271,11 @@ struct ArgsB {
   const PairE *pe;        // kexp of each ordered pair (row prow of the first shell)
   const long long *offq;  // sigma-coupled E offsets [pair][LS/SL]
   const float2 *E;        // their FP32 copy, scaled by 2^(kexp lambda)
-  const float4 *D;        // double-float density (hi words used), n x n
+  const double2 *D;       // density as the caller holds it, leading dimension ldd
   double *BX;
   int ns, ldd, ldf, nskp, isym, racah1, gaunt;
   int dual;               // as BArgs
+  const double *qp;       // per-quartet records of k_qprep, one per list entry
   int tmem_cols, n1max, n2max, nbuf;
   int tri;                // the three Cartesian components' D1 side by side in TMEM
 };
@@ -331,71 +333,135 @@ __device__ __forceinline__ void sadd(float2 *p, float2 v) {
 }
 
 // ---- staging of one K chunk into the canonical K-major layout ----
+//
+// A staged operand is written in 16-byte pieces (4 consecutive K terms of one
+// row), piece p at float offset 4p, so that a warp stores four whole
+// 8-row x 4-term core matrices (512 contiguous bytes) and the shared-memory
+// banks take the stores without conflicts.  Piece p holds row prow(p) and
+// terms pk(p) .. pk(p)+3; the rows [8g, 8g+8) are the pieces [64g, 64g+64).
+__device__ __forceinline__ int prow(int p) { return ((p >> 6) << 3) | (p & 7); }
+__device__ __forceinline__ int pk(int p) { return ((p >> 3) & 7) << 2; }
+__device__ __forceinline__ int piece(int row, int k0) {
+  return ((row >> 3) << 6) | ((k0 >> 2) << 3) | (row & 7);
+}
+
+// hi and lo TF32 parts of four values into piece p of H and L.
+__device__ __forceinline__ void put4(float *H, float *L, int p, const float *v) {
+  float4 h, l;
+  tsplit(v[0], h.x, l.x);
+  tsplit(v[1], h.y, l.y);
+  tsplit(v[2], h.z, l.z);
+  tsplit(v[3], h.w, l.w);
+  reinterpret_cast<float4 *>(H)[p] = h;
+  reinterpret_cast<float4 *>(L)[p] = l;
+}
+
+// Zeroes rows [r0, r1) of a staged chunk.
+template <int NT>
+__device__ __forceinline__ void clear_rows(float *H, float *L, int r0, int r1, int tid) {
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int p = ((r0 >> 3) << 6) + tid; p < ((r1 + 7) >> 3) << 6; p += NT) {
+    int row = prow(p);
+    if (row >= r0 && row < r1) {
+      reinterpret_cast<float4 *>(H)[p] = z;
+      reinterpret_cast<float4 *>(L)[p] = z;
+    }
+  }
+}
 
 // A rows from E-coefficients: row (label, set, re/im) = 4 label + 2 set + ri
 // for ntl labels; src is label 0 set 0 term 0, rows of (label, set) rstride
-// apart; each term s scaled by 2^(kdiff lambda_s).  Rows from 4 ntl up to
-// the buffer's previous row count are cleared (the rest are zero already).
+// apart; each term s scaled by sc[lambda_s] (the exponent balancing's
+// power of two).  Rows from 4 ntl up to the buffer's previous row count are
+// cleared (the rest are zero already).
 template <int NT>
 __device__ __forceinline__ void stage_e_rows(float *Ah, float *Al, const float2 *src,
                                              long long rstride, int ntl, int kc, int nK,
-                                             int kdiff, const uint32_t *stuv, int &arows,
+                                             const float *sc, const uint32_t *stuv, int &arows,
                                              int tid) {
-  int nit = ntl * 2 * KC;
-  for (int b0 = 0; b0 < nit; b0 += 4 * NT) {
-    float2 ev[4];
+  const int rows = 4 * ntl, r8 = (rows + 7) & ~7;
+  const float *sf = reinterpret_cast<const float *>(src);
+  for (int p = tid; p < r8 * (KC / 4); p += NT) {
+    int row = prow(p), s0 = kc + pk(p);
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (row < rows) {
+      const float *e = sf + 2 * ((long long)(row >> 1) * rstride + s0) + (row & 1);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      int w = b0 + tid + j * NT;
-      int ls = w / KC, s = kc + (w % KC);
-      ev[j] = (w < nit && s < nK) ? src[(long long)ls * rstride + s] : make_float2(0.f, 0.f);
+      for (int j = 0; j < 4; ++j)
+        if (s0 + j < nK) v[j] = __ldg(e + 2 * j) * sc[tuvL(stuv[s0 + j])];
     }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      int w = b0 + tid + j * NT;
-      if (w >= nit) break;
-      int ls = w / KC, kk = w % KC, s = kc + kk;
-      float f = s < nK ? ldexpf(1.0f, kdiff * tuvL(stuv[s])) : 0.f;
-      int row = ls * 2;
-      float h, l;
-      tsplit(ev[j].x * f, h, l);
-      Ah[kmaj(row, kk)] = h; Al[kmaj(row, kk)] = l;
-      tsplit(ev[j].y * f, h, l);
-      Ah[kmaj(row + 1, kk)] = h; Al[kmaj(row + 1, kk)] = l;
-    }
+    put4(Ah, Al, p, v);
   }
-  int r = 4 * ntl;
-  for (int w = r * KC + tid; w < arows * KC; w += NT) {
-    int row = w / KC, kk = w % KC;
-    Ah[kmaj(row, kk)] = 0.f; Al[kmaj(row, kk)] = 0.f;
-  }
-  arows = r;
+  if (arows > r8) clear_rows<NT>(Ah, Al, r8, arows, tid);
+  arows = rows;
 }
 
-// B rows of a Hankel matrix: row q < n1, term s of the chunk: tab[(s+q) *
-// tstride + toff] (zero beyond nR rows or nK terms).
+// Hermite indices of (s + n) for the four terms s0 .. s0+3 (s0 a multiple
+// of 4) of one Hankel row n, from the table g_hx.
+__device__ __forceinline__ uint2 hx4(int n, int s0) {
+  return __ldg(reinterpret_cast<const uint2 *>(g_hx + n * NHS + s0));
+}
+
+// B rows of a Hankel matrix: row q < n1 (a multiple of 8), term s of the
+// chunk: tab[(s+q) * tstride + toff] (zero beyond nR rows or nK terms).
 template <int NT>
 __device__ __forceinline__ void stage_hankel(float *Bh, float *Bl, const float *tab, int tstride,
                                              int toff, int n1, int nR, int kc, int nK,
                                              const uint32_t *stuv, int tid) {
-  for (int w = tid; w < n1 * KC; w += NT) {
-    int n = w / KC, kk = w % KC, s = kc + kk;
-    float v = 0.f;
-    if (n < nR && s < nK) v = tab[hsum(stuv[s], stuv[n]) * tstride + toff];
-    float h, l;
-    tsplit(v, h, l);
-    Bh[kmaj(n, kk)] = h; Bl[kmaj(n, kk)] = l;
+  for (int p = tid; p < n1 * (KC / 4); p += NT) {
+    int n = prow(p), s0 = kc + pk(p);
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (n < nR) {
+      uint2 w = hx4(n, s0);
+      int ix[4] = {(int)(w.x & 0xFFFF), (int)(w.x >> 16), (int)(w.y & 0xFFFF), (int)(w.y >> 16)};
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (s0 + j < nK) v[j] = tab[ix[j] * tstride + toff];
+    }
+    put4(Bh, Bl, p, v);
+  }
+}
+
+// The Hankel rows of the Breit kernel-table entries (i, j) for components
+// i = ilo .. ilo+nb-1 (nb <= 3) at once, the table index of each element
+// found once: entry (i, j) of the 6 symmetric ones (i for i = j, else
+// i + j + 2) into the (i - ilo)-th B operand, hi at Bb + 2 (i - ilo) bstride
+// and lo bstride floats after it.
+template <int NT>
+__device__ __forceinline__ void stage_hankel_n(float *Bb, int bstride, int ilo, int nb, int cj,
+                                               const float *tab, int tstride, int n1, int nR,
+                                               int kc, int nK, const uint32_t *stuv, int tid) {
+  for (int p = tid; p < n1 * (KC / 4); p += NT) {
+    int n = prow(p), s0 = kc + pk(p);
+    int idx[4] = {-1, -1, -1, -1};
+    if (n < nR) {
+      uint2 w = hx4(n, s0);
+      int ix[4] = {(int)(w.x & 0xFFFF), (int)(w.x >> 16), (int)(w.y & 0xFFFF), (int)(w.y >> 16)};
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (s0 + j < nK) idx[j] = ix[j] * tstride;
+    }
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      if (b >= nb) break;
+      float v[4];
+      int ci = ilo + b, sw = ci == cj ? ci : ci + cj + 2;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = idx[j] >= 0 ? tab[idx[j] + sw] : 0.f;
+      float *H = Bb + 2 * b * bstride;
+      put4(H, H + bstride, p, v);
+    }
   }
 }
 
 // A rows of GEMM 2 from D1 in tensor memory (TMEM address ta of column kc at
 // lane 0): rows below `rows` only (D1's other rows are zero), each column q
-// times (-1)^|q| 2^(kdiff |q|); warps sharing a lane quarter split the 32
-// columns.
+// times sc[|q|] = (-1)^|q| 2^(kdiff |q|); warps sharing a lane quarter split
+// the 32 columns.
 template <int NT>
 __device__ __forceinline__ void stage_g(float *Ah, float *Al, uint32_t ta, int kc, int nR,
-                                        int rows, int kdiff, const uint32_t *stuv, int &arows,
-                                        int warp, int lane, int tid) {
+                                        int rows, const float *sc, const uint32_t *stuv,
+                                        int &arows, int warp, int lane, int tid) {
   constexpr int NQ = NT / 128, CW = KC / NQ;
   int quad = warp & 3, c0 = CW * (warp >> 2);
   int row = quad * 32 + lane;
@@ -405,59 +471,40 @@ __device__ __forceinline__ void stage_g(float *Ah, float *Al, uint32_t ta, int k
     if (CW == 16) tld16(a, v); else tld8(a, v);
     if (row < rows) {
 #pragma unroll
-      for (int j = 0; j < CW; ++j) {
-        int qq = kc + c0 + j;
-        float x = 0.f;
-        if (qq < nR) {
-          int L = tuvL(stuv[qq]);
-          x = v[j] * ldexpf((L & 1) ? -1.0f : 1.0f, kdiff * L);
+      for (int m = 0; m < CW / 4; ++m) {
+        float x[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          int qq = kc + c0 + 4 * m + j;
+          x[j] = qq < nR ? v[4 * m + j] * sc[tuvL(stuv[qq])] : 0.f;
         }
-        float h, l;
-        tsplit(x, h, l);
-        Ah[kmaj(row, c0 + j)] = h;
-        Al[kmaj(row, c0 + j)] = l;
+        put4(Ah, Al, piece(row, c0 + 4 * m), x);
       }
     }
   }
-  for (int w = rows * KC + tid; w < arows * KC; w += NT) {
-    int rw = w / KC, kk = w % KC;
-    Ah[kmaj(rw, kk)] = 0.f; Al[kmaj(rw, kk)] = 0.f;
-  }
+  if (arows > rows) clear_rows<NT>(Ah, Al, rows, arows, tid);
   arows = rows;
 }
 
 // B rows of GEMM 2 from the right pair's E-coefficients: row (label, set,
 // re/im) for nlR labels, rows of (label, set) rstride apart; zero rows up
-// to n2.
+// to n2 (a multiple of 8).
 template <int NT>
 __device__ __forceinline__ void stage_er(float *Bh, float *Bl, const float2 *src,
                                          long long rstride, int nlR, int n2, int kc, int nR,
                                          int tid) {
-  int nit = nlR * 2 * KC;
-  for (int b0 = 0; b0 < nit; b0 += 4 * NT) {
-    float2 ev[4];
+  const int rows = 4 * nlR;
+  const float *sf = reinterpret_cast<const float *>(src);
+  for (int p = tid; p < n2 * (KC / 4); p += NT) {
+    int row = prow(p), q0 = kc + pk(p);
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (row < rows) {
+      const float *e = sf + 2 * ((long long)(row >> 1) * rstride + q0) + (row & 1);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      int w = b0 + tid + j * NT;
-      int ls = w / KC, qq = kc + (w % KC);
-      ev[j] = (w < nit && qq < nR) ? src[(long long)ls * rstride + qq] : make_float2(0.f, 0.f);
+      for (int j = 0; j < 4; ++j)
+        if (q0 + j < nR) v[j] = __ldg(e + 2 * j);
     }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      int w = b0 + tid + j * NT;
-      if (w >= nit) break;
-      int ls = w / KC, kk = w % KC;
-      int row = ls * 2;
-      float h, l;
-      tsplit(ev[j].x, h, l);
-      Bh[kmaj(row, kk)] = h; Bl[kmaj(row, kk)] = l;
-      tsplit(ev[j].y, h, l);
-      Bh[kmaj(row + 1, kk)] = h; Bl[kmaj(row + 1, kk)] = l;
-    }
-  }
-  for (int w = 4 * nlR * KC + tid; w < n2 * KC; w += NT) {
-    int n = w / KC, kk = w % KC;
-    Bh[kmaj(n, kk)] = 0.f; Bl[kmaj(n, kk)] = 0.f;
+    put4(Bh, Bl, p, v);
   }
 }
 
@@ -495,32 +542,31 @@ __device__ __forceinline__ void load_slab(float *P, uint32_t tD2, int c0, int nc
 
 // FP64 R recursion (RMAKE's MD recursion, :31900) for one quartet into R/R2
 // (level by level, one barrier per level); returns the buffer holding
-// R^{(0)}.  F holds F_0..F_lam; g = (X, Y, Z, -2 alpha).
+// R^{(0)}.  G holds (-2 alpha)^n F_n for n = 0..lam (the k_qprep record),
+// (X, Y, Z) = P - Q, dn[i] = i.
 template <int NT>
-__device__ __forceinline__ double *r_recursion(double *R, double *R2, const double *F, int lam,
-                                               const double *g, const uint32_t *stuv, int tid) {
-  double X = g[0], Y = g[1], Z = g[2], m2a = g[3];
+__device__ __forceinline__ double *r_recursion(double *R, double *R2, const double *G, int lam,
+                                               double X, double Y, double Z, const double *dn,
+                                               const uint32_t *stuv, int tid) {
   double *cur = R, *nxt = R2;
   for (int n = lam; n >= 0; --n) {
     int cnt = ntuv(lam - n);
     for (int k = tid; k < cnt; k += NT) {
       double val;
       if (k == 0) {
-        double pw = 1.0;
-        for (int i = 0; i < n; ++i) pw *= m2a;
-        val = pw * F[n];
+        val = G[n];
       } else {
         uint32_t w = stuv[k];
         int t = w & 255, u = (w >> 8) & 255, v = (w >> 16) & 255;
         if (t > 0) {
           val = X * cur[hidx(t - 1, u, v)];
-          if (t > 1) val += double(t - 1) * cur[hidx(t - 2, u, v)];
+          if (t > 1) val += dn[t - 1] * cur[hidx(t - 2, u, v)];
         } else if (u > 0) {
           val = Y * cur[hidx(t, u - 1, v)];
-          if (u > 1) val += double(u - 1) * cur[hidx(t, u - 2, v)];
+          if (u > 1) val += dn[u - 1] * cur[hidx(t, u - 2, v)];
         } else {
           val = Z * cur[hidx(t, u, v - 1)];
-          if (v > 1) val += double(v - 1) * cur[hidx(t, u, v - 2)];
+          if (v > 1) val += dn[v - 1] * cur[hidx(t, u, v - 2)];
         }
       }
       nxt[k] = val;
@@ -553,15 +599,17 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   float *Rf = (float *)(base + LY.rf);
   float2 *Dsm = (float2 *)(base + LY.dsm);        // D(c,d), D(c,b), D(a,b), D(a,d)
   float2 *Acc = (float2 *)(base + LY.acc);        // J(a,b), K(a,d), J2(c,d), K2(c,b)
-  double *F = (double *)(base + LY.fb);
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
-  __shared__ double sgeo[8];
-  __shared__ int sk;
+  __shared__ double sqp[QPW];          // this quartet's k_qprep record
+  __shared__ double spre[MAXLAM + 1];  // PRE 2^(-k lambda)
+  __shared__ double sdn[MAXLAM + 1];   // sdn[i] = i
+  __shared__ float sEs[MAXDEGE + 1], sGs[MAXDEGE + 1];  // staging scales per lambda
   __shared__ uint32_t stuv[NTR];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nbuf = q.nbuf;
 
+  for (int i = tid; i <= MAXLAM; i += NT) sdn[i] = (double)i;
   for (int i = tid; i < NTR; i += NT)
     stuv[i] = (uint32_t)c_t[i] | ((uint32_t)c_u[i] << 8) | ((uint32_t)c_v[i] << 16) |
               ((uint32_t)(c_t[i] + c_u[i] + c_v[i]) << 24);
@@ -582,8 +630,12 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   Pipe pp = {mbar, {0u, 0u}, {false, false}};
   int arows[2] = {0, 0};  // rows of each A buffer that may be nonzero
   bool abort = false;
+  // the next quartet's record is loaded while this one is digested
+  double qnext = (tid < QPW && blockIdx.x < nq) ? q.qp[blockIdx.x * (long long)QPW + tid] : 0.0;
 
   for (long long qi = blockIdx.x; qi < nq && !abort; qi += gridDim.x) {
+    const double qcur = qnext;
+    if (tid < QPW && qi + gridDim.x < nq) qnext = q.qp[(qi + gridDim.x) * QPW + tid];
     int4 Q4 = quart[qi];
     const Shell &A = q.sh[Q4.x], &B = q.sh[Q4.y], &C = q.sh[Q4.z], &Dd = q.sh[Q4.w];
     int la = A.l, lb = B.l, lc = C.l, ld = Dd.l;
@@ -599,7 +651,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
       continue;
     }
     int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
-    const float4 *Dm = q.D;
+    const double2 *Dm = q.D;
     double *GDm = q.GD, *GXm = q.GX;
     size_t lddm = q.ldd, ldfm = q.ldf;
     int nskpm = q.nskp;
@@ -612,36 +664,22 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
       nskpm = I.nskp;
     }
     const PairE &pab_e = q.pe[A.prow + Q4.y], &pcd_e = q.pe[C.prow + Q4.w];
-    if (tid == 0) {
-      double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
-      double Px = (A.alpha * A.x + B.alpha * B.x) / p;
-      double Py = (A.alpha * A.y + B.alpha * B.y) / p;
-      double Pz = (A.alpha * A.z + B.alpha * B.z) / p;
-      double Qx = (C.alpha * C.x + Dd.alpha * Dd.x) / qq;
-      double Qy = (C.alpha * C.y + Dd.alpha * Dd.y) / qq;
-      double Qz = (C.alpha * C.z + Dd.alpha * Dd.z) / qq;
-      double aph = p * qq / (p + qq);
-      double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
-      double sg = swp ? -1.0 : 1.0;
-      sgeo[0] = sg * (Px - Qx); sgeo[1] = sg * (Py - Qy); sgeo[2] = sg * (Pz - Qz);
-      sgeo[3] = -2.0 * aph;
-      sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
-      sgeo[5] = T;
-      sk = half_floor_log2(2.0 * aph);
-    }
+    // the previous quartet's reads of sqp ended before its GEMMs' barriers
+    if (tid < QPW) sqp[tid] = qcur;
     // the previous quartet's TMEM reads and shared-memory use end here
     fence_before();
     __syncthreads();
     fence_after();
-    boys_block(sgeo[5], lam, F);
-    __syncthreads();
+    const int kq0 = (int)sqp[7];  // exponent-balancing shift k
+    if (tid <= lam) spre[tid] = ldexp(sqp[4], -kq0 * tid);
     {
-      const double *cur = r_recursion<NT>(R, R2, F, lam, sgeo, stuv, tid);
+      // R with P - Q in the orientation the contractions take
+      double sg = swp ? -1.0 : 1.0;
+      const double *cur = r_recursion<NT>(R, R2, sqp + 8, lam, sg * sqp[0], sg * sqp[1],
+                                          sg * sqp[2], sdn, stuv, tid);
       // PRE * R scaled by 2^(-k lambda) (exponent balancing), in FP32
-      double pre = sgeo[4];
-      int k = sk;
       for (int i = tid; i < ntuv(lam); i += NT)
-        Rf[i] = __double2float_rn(ldexp(cur[i] * pre, -k * tuvL(stuv[i])));
+        Rf[i] = __double2float_rn(cur[i] * spre[tuvL(stuv[i])]);
     }
     // roles
     const float2 *Eab = q.E + pab_e.off[t1];
@@ -654,7 +692,10 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
     int nl2L = swp ? nld : nlb, nl2R = swp ? nlb : nld;
     int lq[4] = {la, lb, lc, ld};
     int oab = t1 ? nskpm : 0, ocd = t2 ? nskpm : 0;
-    int kq0 = sk;
+    if (tid <= MAXDEGE) {
+      sEs[tid] = ldexpf(1.0f, (kq0 - kL) * tid);
+      sGs[tid] = ldexpf((tid & 1) ? -1.0f : 1.0f, (kq0 - kR) * tid);
+    }
     bool dual = q.sym && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
     // density blocks of this quartet: D(c,d), D(c,b), and for (cd|ab) D(a,b), D(a,d)
     {
@@ -668,8 +709,9 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
           int r = w / nc, c = w % nc;
           int fr = rs[blk]->fock[r >> 1][r & 1] + ro[blk];
           int fc = cs[blk]->fock[c >> 1][c & 1] + co[blk];
-          float4 v = Dm[(size_t)fr + lddm * fc];
-          Dsm[blk * MAXSP * MAXSP + r * MAXSP + c] = make_float2(v.x, v.z);
+          double2 v = Dm[(size_t)fr + lddm * fc];
+          Dsm[blk * MAXSP * MAXSP + r * MAXSP + c] =
+              make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
         }
       }
     }
@@ -689,7 +731,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
         fence_after();
         float *Ah = bufA(bsel), *Al = Ah + MROWS * KC;
         float *Bh = bufB(bsel), *Bl = Bh + bmax * KC;
-        stage_e_rows<NT>(Ah, Al, EL + (long long)l0 * 2 * nL, nL, ntl, kc, nL, kq0 - kL, stuv,
+        stage_e_rows<NT>(Ah, Al, EL + (long long)l0 * 2 * nL, nL, ntl, kc, nL, sEs, stuv,
                          arows[bsel], tid);
         stage_hankel<NT>(Bh, Bl, Rf, 1, 0, n1, nR, kc, nL, stuv, tid);
         fence_async_smem();
@@ -716,7 +758,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
         fence_after();
         float *Ah = bufA(bsel), *Al = Ah + MROWS * KC;
         float *Bh = bufB(bsel), *Bl = Bh + bmax * KC;
-        stage_g<NT>(Ah, Al, tD1 + (uint32_t)kc, kc, nR, rows, kq0 - kR, stuv, arows[bsel], warp,
+        stage_g<NT>(Ah, Al, tD1 + (uint32_t)kc, kc, nR, rows, sGs, stuv, arows[bsel], warp,
                     lane, tid);
         stage_er<NT>(Bh, Bl, ER, nR, nlR, n2, kc, nR, tid);
         fence_async_smem();
@@ -923,15 +965,17 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
   float *Wf = (float *)(base + LY.rf);
   float2 *Dsm = (float2 *)(base + LY.dsm);   // D(c,b), D(a,d)
   float2 *Acc = (float2 *)(base + LY.acc);   // K(a,d), K2(c,b)
-  double *F = (double *)(base + LY.fb);
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
-  __shared__ double sgeo[10];
-  __shared__ int sk;
+  __shared__ double sqp[QPW];          // this quartet's k_qprep record
+  __shared__ double s2k[MAXLAM + 1];   // 2^(-k lambda)
+  __shared__ double sdn[MAXLAM + 1];   // sdn[i] = i
+  __shared__ float sEs[MAXDEGE + 1], sGs[MAXDEGE + 1];  // staging scales per lambda
   __shared__ uint32_t stuv[NTR];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nbuf = q.nbuf;
 
+  for (int i = tid; i <= MAXLAM; i += NT) sdn[i] = (double)i;
   for (int i = tid; i < NTR; i += NT)
     stuv[i] = (uint32_t)c_t[i] | ((uint32_t)c_u[i] << 8) | ((uint32_t)c_v[i] << 16) |
               ((uint32_t)(c_t[i] + c_u[i] + c_v[i]) << 24);
@@ -952,8 +996,12 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
   Pipe pp = {mbar, {0u, 0u}, {false, false}};
   int arows[2] = {0, 0};
   bool abort = false;
+  // the next quartet's record is loaded while this one is digested
+  double qnext = (tid < QPW && blockIdx.x < nq) ? q.qp[blockIdx.x * (long long)QPW + tid] : 0.0;
 
   for (long long qi = blockIdx.x; qi < nq && !abort; qi += gridDim.x) {
+    const double qcur = qnext;
+    if (tid < QPW && qi + gridDim.x < nq) qnext = q.qp[(qi + gridDim.x) * QPW + tid];
     int4 Q4 = quart[qi];
     const Shell &A = q.sh[Q4.x], &B = q.sh[Q4.y], &C = q.sh[Q4.z], &Dd = q.sh[Q4.w];
     int la = A.l, lb = B.l, lc = C.l, ld = Dd.l;
@@ -970,60 +1018,45 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
     }
     int mcnt = ncntrs(A.cnt, B.cnt, C.cnt, Dd.cnt);
     bool dual = q.dual && (Q4.x != Q4.z || Q4.y != Q4.w || t1 != t2);
-    if (tid == 0) {
-      double p = A.alpha + B.alpha, qq = C.alpha + Dd.alpha;
-      double Px = (A.alpha * A.x + B.alpha * B.x) / p;
-      double Py = (A.alpha * A.y + B.alpha * B.y) / p;
-      double Pz = (A.alpha * A.z + B.alpha * B.z) / p;
-      double Qx = (C.alpha * C.x + Dd.alpha * Dd.x) / qq;
-      double Qy = (C.alpha * C.y + Dd.alpha * Dd.y) / qq;
-      double Qz = (C.alpha * C.z + Dd.alpha * Dd.z) / qq;
-      double aph = p * qq / (p + qq);
-      double T = aph * ((Qx - Px) * (Qx - Px) + (Qy - Py) * (Qy - Py) + (Qz - Pz) * (Qz - Pz));
-      // R and the kernel table for the left pair's centre minus the right's
-      double sg = swp ? -1.0 : 1.0;
-      sgeo[0] = sg * (Px - Qx); sgeo[1] = sg * (Py - Qy); sgeo[2] = sg * (Pz - Qz);
-      sgeo[3] = -2.0 * aph;
-      sgeo[4] = 2.0 * 17.493418327624863 / (sqrt(p + qq) * p * qq);
-      sgeo[5] = 0.5 / aph;
-      sgeo[6] = sg * (Qx - Px); sgeo[7] = sg * (Qy - Py); sgeo[8] = sg * (Qz - Pz);
-      sgeo[9] = T;
-      sk = half_floor_log2(2.0 * aph);
-    }
+    // the previous quartet's reads of sqp ended before its GEMMs' barriers
+    if (tid < QPW) sqp[tid] = qcur;
     fence_before();
     __syncthreads();
     fence_after();
-    boys_block(sgeo[9], lam, F);
-    __syncthreads();
+    const int kq0 = (int)sqp[7];  // exponent-balancing shift k
+    if (tid <= lamn) s2k[tid] = ldexp(1.0, -kq0 * tid);
     {
-      const double *cur = r_recursion<NT>(R, R2, F, lam, sgeo, stuv, tid);
+      // R and the kernel table for the left pair's centre minus the right's
+      double sg = swp ? -1.0 : 1.0;
+      const double *cur = r_recursion<NT>(R, R2, sqp + 8, lam, sg * sqp[0], sg * sqp[1],
+                                          sg * sqp[2], sdn, stuv, tid);
       // kernel table W_ij(N) = BFAC (delta_ij R_N - T_ij(N)) from PRE * R,
       // scaled by 2^(-k lambda_N), FP32 (6 symmetric entries per N)
-      double pre = sgeo[4], h2a = sgeo[5];
-      double pq[3] = {sgeo[6], sgeo[7], sgeo[8]};
+      double pre = sqp[4], h2a = sqp[6];
       double bfac = q.gaunt ? -1.0 : -0.5;
-      int k = sk;
       for (int w = tid; w < ntuv(lamn) * 6; w += NT) {
         int n = w / 6, e = w % 6;
         int i = e < 3 ? e : (e == 5 ? 1 : 0), j = e < 3 ? e : (e == 3 ? 1 : 2);
         uint32_t tw = stuv[n];
-        int N[3] = {(int)(tw & 255), (int)((tw >> 8) & 255), (int)((tw >> 16) & 255)};
+        int N0 = (int)(tw & 255), N1 = (int)((tw >> 8) & 255), N2 = (int)((tw >> 16) & 255);
         double rn = cur[n] * pre;
         double val;
         if (q.gaunt) {
           val = i == j ? -rn : 0.0;
         } else {
-          int a[3] = {N[0], N[1], N[2]};
-          a[i] += 1;
-          a[j] += 1;
-          double tt = cur[hidx(a[0], a[1], a[2])] * h2a;
-          a[j] -= 1;
-          tt -= cur[hidx(a[0], a[1], a[2])] * pq[j];
-          a[j] -= 1;
-          if (a[j] >= 0) tt += cur[hidx(a[0], a[1], a[2])] * double(N[j]);
+          // a = N + e_i + e_j, then a - e_j, then a - 2 e_j
+          int a0 = N0 + (i == 0) + (j == 0), a1 = N1 + (i == 1) + (j == 1);
+          int a2 = N2 + (i == 2) + (j == 2);
+          double tt = cur[hidx(a0, a1, a2)] * h2a;
+          a0 -= j == 0; a1 -= j == 1; a2 -= j == 2;
+          double pqj = -sg * sqp[j];  // (Q - P)_j in the orientation taken
+          tt -= cur[hidx(a0, a1, a2)] * pqj;
+          a0 -= j == 0; a1 -= j == 1; a2 -= j == 2;
+          int aj = j == 0 ? a0 : (j == 1 ? a1 : a2), Nj = j == 0 ? N0 : (j == 1 ? N1 : N2);
+          if (aj >= 0) tt += cur[hidx(a0, a1, a2)] * sdn[Nj];
           val = bfac * ((i == j ? rn : 0.0) - tt * pre);
         }
-        Wf[w] = __double2float_rn(ldexp(val, -k * tuvL(tw)));
+        Wf[w] = __double2float_rn(val * s2k[tuvL(tw)]);
       }
     }
     const PairE &pab_e = q.pe[A.prow + Q4.y], &pcd_e = q.pe[C.prow + Q4.w];
@@ -1039,7 +1072,10 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
     // Fock offsets: an LS pair has its first function large, second small
     int oa = t1 ? q.nskp : 0, ob = t1 ? 0 : q.nskp;
     int oc = t2 ? q.nskp : 0, od = t2 ? 0 : q.nskp;
-    int kq0 = sk;
+    if (tid <= MAXDEGE) {
+      sEs[tid] = ldexpf(1.0f, (kq0 - kL) * tid);
+      sGs[tid] = ldexpf((tid & 1) ? -1.0f : 1.0f, (kq0 - kR) * tid);
+    }
     {
       // D(c,b) and, for (cd|ab), D(a,d)
       int sizes[2][2] = {{2 * nlc, 2 * nlb}, {2 * nla, 2 * nld}};
@@ -1051,8 +1087,9 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
           int r = w / nc, c = w % nc;
           int fr = rs[blk]->fock[r >> 1][r & 1] + ro[blk];
           int fc = cs[blk]->fock[c >> 1][c & 1] + co[blk];
-          float4 v = q.D[(size_t)fr + (size_t)q.ldd * fc];
-          Dsm[blk * MAXSP * MAXSP + r * MAXSP + c] = make_float2(v.x, v.z);
+          double2 v = q.D[(size_t)fr + (size_t)q.ldd * fc];
+          Dsm[blk * MAXSP * MAXSP + r * MAXSP + c] =
+              make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
         }
       }
     }
@@ -1083,13 +1120,10 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
             fence_after();
             float *Ah = bufA(bsel), *Al = Ah + MROWS * KC;
             float *Bb = bufB(bsel);
-            stage_e_rows<NT>(Ah, Al, ELt + (long long)cj * nL, rsL, ntl, kc, nL, kq0 - kL, stuv,
+            stage_e_rows<NT>(Ah, Al, ELt + (long long)cj * nL, rsL, ntl, kc, nL, sEs, stuv,
                              arows[bsel], tid);
-            for (int ci = ilo; ci < ihi; ++ci) {
-              float *Bh = Bb + (ci - i0) * 2 * q.n1max * KC, *Bl = Bh + q.n1max * KC;
-              int sw = cj == ci ? ci : ci + cj + 2;  // symmetric table entry (i, j)
-              stage_hankel<NT>(Bh, Bl, Wf, 6, sw, n1, nR, kc, nL, stuv, tid);
-            }
+            stage_hankel_n<NT>(Bb + (ilo - i0) * 2 * q.n1max * KC, q.n1max * KC, ilo, ihi - ilo,
+                               cj, Wf, 6, n1, nR, kc, nL, stuv, tid);
             fence_async_smem();
             fence_before();
             __syncthreads();
@@ -1121,7 +1155,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
             fence_after();
             float *Ah = bufA(bsel), *Al = Ah + MROWS * KC;
             float *Bh = bufB(bsel), *Bl = Bh + q.n2max * KC;
-            stage_g<NT>(Ah, Al, tD1 + (uint32_t)kc, kc, nR, rows, kq0 - kR, stuv, arows[bsel],
+            stage_g<NT>(Ah, Al, tD1 + (uint32_t)kc, kc, nR, rows, sGs, stuv, arows[bsel],
                         warp, lane, tid);
             stage_er<NT>(Bh, Bl, ER + (long long)ci * nR, rsR, nlR, n2, kc, nR, tid);
             fence_async_smem();
