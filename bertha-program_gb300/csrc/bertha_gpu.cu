@@ -3166,13 +3166,23 @@ struct SegTune {
 };
 
 template <class Launch, class Zero, class Energy>
-int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, int t1, int t2,
-              cudaStream_t st, double budget, Launch &&launch, Zero &&zero, Energy &&energy,
-              std::vector<Run> &runs, bool breit = false, std::vector<TuneRow> *rec = nullptr) {
+int tune_runs(const int *list, const std::vector<long long> &seg, const std::vector<int> &key,
+              int t1, int t2, cudaStream_t st, double budget, Launch &&launch, Zero &&zero,
+              Energy &&energy, std::vector<Run> &runs, bool breit = false,
+              std::vector<TuneRow> *rec = nullptr) {
   runs.clear();
   if (seg.size() < 2) return 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -1;
+  // a segment above TUNE_SAMPLE quartets is timed and checked on an evenly
+  // strided sample of it (the list order within a segment follows the
+  // shells, so its first quartets are not representative)
+  int *samp = nullptr;
+  if (cudaMalloc(&samp, sizeof(int4) * TUNE_SAMPLE) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return -1;
+  }
   int rc = 0;
   std::vector<SegTune> tv;
   for (size_t i = 0; i + 1 < seg.size() && !rc; ++i) {
@@ -3182,15 +3192,25 @@ int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, in
     SegTune x = {seg[i], n, d.n1, d.n2, {0.f, 0.f, 0.f}, {0.0, 0.0, 0.0}, KIND_FP64};
     if (n >= TUNE_MIN) {
       long long m = std::min(n, TUNE_SAMPLE);
+      const int *q = list + 4 * seg[i];
+      if (m < n) {
+        long long stride = n / m;
+        if (cudaMemcpy2DAsync(samp, sizeof(int4), q, sizeof(int4) * stride, sizeof(int4), m,
+                              cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+          rc = -1;
+          break;
+        }
+        q = samp;
+      }
       double ej[3] = {0, 0, 0}, ek[3] = {0, 0, 0};
       for (int k = 0; k < 3 && !rc; ++k) {
         if (breit && k == KIND_DF32) continue;  // the Breit build has no split-precision kernel
         rc = zero();
-        if (!rc) rc = launch(k, seg[i], m, d.n1, d.n2);
+        if (!rc) rc = launch(k, q, m, d.n1, d.n2);
         if (!rc) rc = energy(ej[k], ek[k]);
         if (rc) break;
         cudaEventRecord(e0, st);
-        rc = launch(k, seg[i], m, d.n1, d.n2);
+        rc = launch(k, q, m, d.n1, d.n2);
         cudaEventRecord(e1, st);
         if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = -1;
         if (!rc) cudaEventElapsedTime(&x.t[k], e0, e1);
@@ -3203,6 +3223,8 @@ int tune_runs(const std::vector<long long> &seg, const std::vector<int> &key, in
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaStreamSynchronize(st);
+  cudaFree(samp);
   if (rc) return rc;
   // tensor-core switches by time saved per error, within the budget
   std::vector<int> cand;
@@ -3383,9 +3405,8 @@ int tune_ctx(bg_ctx *c, const double2 *d_D, int ldd, cudaStream_t st) {
       // the budget is shared by the component classes
       double budget = c->err_budget / (c->ncomp * c->ncomp);
       if (k == 0) c->tune_rec.clear();
-      rc = tune_runs(c->seg[k], c->segkey[k], t1, t2, st, budget,
-                     [&](int kind, long long start, long long m, int n1, int n2) {
-        const int *qq = q + 4 * start;
+      rc = tune_runs(q, c->seg[k], c->segkey[k], t1, t2, st, budget,
+                     [&](int kind, const int *qq, long long m, int n1, int n2) {
         if (kind == KIND_DF32)
           return launch_quartets_df(c, qq, m, t1, t2, d_D, ldd, gd, gx, n, st, c->d_Ddf, 2, false);
         if (kind == KIND_TC)
@@ -3511,15 +3532,13 @@ int batch_lists(bg_batch *b, int ilev) {
 }
 
 // One launch of the FP64, split-precision or tensor-core quartet kernel
-// (KIND_*) over entries [start, start + nq) of a batch's list of one
-// component class, both orders of each listed quartet digested; n1, n2 size
-// the tensor-core launch.
-int batch_launch(bg_batch *b, int t1, int t2, int kind, long long start, long long nq,
+// (KIND_*) over nq quartets of one component class of a batch (a stretch
+// of its list, or a tuning sample), both orders of each listed quartet
+// digested; n1, n2 size the tensor-core launch.
+int batch_launch(bg_batch *b, int t1, int t2, int kind, const int4 *quart, long long nq,
                  const double2 *d_D, double *d_GD, double *d_GX, cudaStream_t st, int n1 = 0,
                  int n2 = 0) {
-  int k = 2 * t1 + t2;
   if (nq <= 0) return 0;
-  const int4 *quart = (const int4 *)b->d_quart[k] + start;
   if (kind == KIND_DF32) {
     QArgsDF a;
     a.sh = b->d_sh; a.pe = b->d_pe; a.E = b->d_Edf; a.D = b->d_Ddf; a.Eci = b->d_Eci;
@@ -4221,11 +4240,11 @@ int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
       c->btune_rec.clear();
       for (int k = 0; k < 2 && !rc; ++k) {
         const int *q = c->d_bquart[k];
-        rc = tune_runs(c->bseg[k], c->bsegkey[k], 0, k, st, c->err_budget,
-                       [&](int kind, long long start, long long m, int n1, int n2) {
+        rc = tune_runs(q, c->bseg[k], c->bsegkey[k], 0, k, st, c->err_budget,
+                       [&](int kind, const int *qq, long long m, int n1, int n2) {
           if (kind == KIND_TC)
-            return launch_breit_tc(c, q + 4 * start, m, 0, k, D, ldd, bx, n, st, 2, n1, n2);
-          return launch_breit(c, q + 4 * start, m, 0, k, D, ldd, bx, n, st, 2);
+            return launch_breit_tc(c, qq, m, 0, k, D, ldd, bx, n, st, 2, n1, n2);
+          return launch_breit(c, qq, m, 0, k, D, ldd, bx, n, st, 2);
         }, zero, energy, c->bruns[k], true, &c->btune_rec);
       }
       cudaFree(bx);
@@ -4566,9 +4585,9 @@ int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
       for (int t2 = 0; t2 < b->ncomp && !rc; ++t2) {
         int k = 2 * t1 + t2;
         double budget = b->err_budget / (b->ncomp * b->ncomp);
-        rc = tune_runs(b->seg[k], b->segkey[k], t1, t2, st, budget,
-                       [&](int kind, long long start, long long m, int n1, int n2) {
-          return batch_launch(b, t1, t2, kind, start, m, D, gd, gx, st, n1, n2);
+        rc = tune_runs(b->d_quart[k], b->seg[k], b->segkey[k], t1, t2, st, budget,
+                       [&](int kind, const int *qq, long long m, int n1, int n2) {
+          return batch_launch(b, t1, t2, kind, (const int4 *)qq, m, D, gd, gx, st, n1, n2);
         }, zero, energy, b->runs[k]);
       }
     cudaFree(gd);
@@ -4598,13 +4617,13 @@ int bertha_gpu_batch_clmfast_device(bg_batch *b, const double *d_dent, int ilev,
       int k = 2 * t1 + t2, rc = 0;
       if (b->prec == BG_PREC_AUTO || b->prec == BG_PREC_TC32)
         for (const Run &r : b->runs[k]) {
-          rc = batch_launch(b, t1, t2, r.kind, r.start, r.count, D, d_gdir, d_gxch, st, r.n1,
-                            r.n2);
+          rc = batch_launch(b, t1, t2, r.kind, (const int4 *)b->d_quart[k] + r.start, r.count, D,
+                            d_gdir, d_gxch, st, r.n1, r.n2);
           if (rc) break;
         }
       else
-        rc = batch_launch(b, t1, t2, b->prec == BG_PREC_DF32 ? KIND_DF32 : KIND_FP64, 0,
-                          b->nquart[k], D, d_gdir, d_gxch, st);
+        rc = batch_launch(b, t1, t2, b->prec == BG_PREC_DF32 ? KIND_DF32 : KIND_FP64,
+                          (const int4 *)b->d_quart[k], b->nquart[k], D, d_gdir, d_gxch, st);
       if (rc) return rc;
     }
   k_herm_complete<<<dim3(gx, 16), 256, 0, st>>>((double2 *)d_gdir, 0, 0, b->d_inst, b->d_ndim,
