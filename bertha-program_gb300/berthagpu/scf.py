@@ -100,11 +100,16 @@ class DHFSCF:
         self.n = self.backend.n
 
     def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, mom=0, verbose=False,
-            guess=None, wfn_out=None, return_density=False, dtol=None):
+            guess=None, wfn_out=None, return_density=False, dtol=None, dc_first=None):
         """Iterate to |dE| < etol and, with dtol, until the largest element of
-        the DIIS error F P S - S P F (the orbital gradient; zero at a
-        stationary point) is below dtol too, so that a converged energy does
-        not depend on where a slowly drifting iteration happened to stop.
+        the DIIS error X^+ (F P S - S P F) X (the orbital gradient in the
+        orthonormal basis X of the overlap metric; zero at a stationary point)
+        is below dtol too, so that a converged energy does not depend on where
+        a slowly drifting iteration happened to stop.
+        dc_first: with a Breit Hamiltonian, iterate without the Breit term
+        until |dE| < dc_first, then add it (DIIS restarted): the Breit
+        interaction is a small correction, and the cheaper Dirac-Coulomb
+        iterations take the density most of the way.
         shift: LEVSHFT's virtual-space level shift
         SHLV in Eh (the H2O deck's stage-3 value 0.5), applied from the second
         iteration on; it moves the path, not the converged solution.
@@ -171,6 +176,9 @@ class DHFSCF:
         hist_F, hist_E = [], []
         energy, last = None, None
         iters, t_fock, t_lin = [], 0.0, 0.0
+        staged = bool(dc_first) and getattr(be, "breit", False)
+        if staged:
+            be.breit = False
         for it in range(1, max_iter + 1):
             ti = time.perf_counter()
             G = be.fock(D)
@@ -185,9 +193,10 @@ class DHFSCF:
                 # positive-energy virtuals of the last diagonalisation
                 A = S @ state["vir"]
                 F = F + shift * (A @ A.conj().T)
-            # DIIS on the commutator F P S - S P F, P = D^T
+            # DIIS on the commutator F P S - S P F, P = D^T, in the
+            # orthonormal basis
             P = D.T
-            err = F @ P @ S - S @ P @ F
+            err = X.conj().T @ (F @ P @ S - S @ P @ F) @ X
             hist_F.append(F)
             hist_E.append(err)
             if len(hist_F) > ndiis:
@@ -213,13 +222,24 @@ class DHFSCF:
             de = None if last is None else energy - last
             iters.append({"iter": it, "energy": energy, "de": de,
                           "err": float(err.abs().max().item()),
+                          "breit": bool(getattr(be, "breit", False)),
                           "s": time.perf_counter() - ti})
             if verbose:
                 print(iters[-1], flush=True)
+            if staged and not be.breit:
+                if last is not None and abs(de) < dc_first:
+                    # the Breit term from the next build on
+                    be.breit = True
+                    hist_F, hist_E = [], []
+                    energy = None
+                last = energy
+                continue
             if (last is not None and abs(de) < etol
                     and (dtol is None or iters[-1]["err"] < dtol)):
                 break
             last = energy
+        if staged:
+            be.breit = True
         if wfn_out:
             n = self.n
             e = eps.cpu().numpy().copy()
@@ -240,7 +260,8 @@ class DHFSCF:
         out = {"energy": energy, "enuc": enuc, "iterations": len(iters),
                "converged": bool(iters and iters[-1]["de"] is not None
                                  and abs(iters[-1]["de"]) < etol
-                                 and (dtol is None or iters[-1]["err"] < dtol)),
+                                 and (dtol is None or iters[-1]["err"] < dtol)
+                                 and (not staged or iters[-1]["breit"])),
                "gradient": iters[-1]["err"] if iters else None,
                "oneel_s": t_one, "fock_s": t_fock, "linalg_s": t_lin,
                "wall_s": t_one + t_fock + t_lin, "history": iters,
