@@ -13,6 +13,12 @@ all of them), the Fock build timed on the device in both precisions and,
 with --scf, the batched DHF SCF in both precisions:
 
   python -m berthagpu.run --atoms 96 [--zmax 86] [--scf]
+
+Quartets of the ERI microbenchmark's distribution digested through the
+class-segmented explicit-list entry point, optionally one angular class
+(l_a l_b l_c l_d) of one component class, device time per repeat:
+
+  python -m berthagpu.run --microbench 262144 --lclass 3333 --comp 1 1 --precision tc32
 """
 import argparse
 import json
@@ -33,6 +39,11 @@ def main(argv=None):
     g.add_argument("--case", choices=sorted(CASES))
     g.add_argument("--deck")
     g.add_argument("--atoms", type=int, help="batch of N seeded closed-shell atoms")
+    g.add_argument("--microbench", type=int,
+                   help="N quartets of the ERI microbenchmark's distribution")
+    p.add_argument("--lclass", help="--microbench: one angular class, e.g. 3333")
+    p.add_argument("--comp", type=int, nargs=2, default=None,
+                   help="--microbench: one component class t1 t2 (0 large, 1 small)")
     p.add_argument("--zmax", type=int, default=86, help="largest Z drawn for --atoms")
     p.add_argument("--scf-only", action="store_true",
                    help="--atoms: only the batched SCF, in --precision")
@@ -51,7 +62,7 @@ def main(argv=None):
     p.add_argument("--wfn-in", help="--scf: start from this .wfn file")
     p.add_argument("--wfn-out", help="--scf: write the final eigenvectors as a .wfn file")
     p.add_argument("--build", choices=["coulomb", "breit", "both"], default="coulomb")
-    p.add_argument("--precision", choices=["fp64", "df32", "auto"], default="fp64")
+    p.add_argument("--precision", choices=["fp64", "df32", "auto", "tc32"], default="fp64")
     p.add_argument("--ilev", type=int, default=3)
     p.add_argument("--screen", type=float, default=0.0)
     p.add_argument("--repeat", type=int, default=1)
@@ -61,6 +72,9 @@ def main(argv=None):
     a = p.parse_args(argv)
     if a.atoms:
         print(json.dumps(atoms_main(a)), flush=True)
+        return
+    if a.microbench:
+        print(json.dumps(microbench_main(a)), flush=True)
         return
     b = CASES[a.case]() if a.case else deck.read_deck(a.deck)
     if a.build != "coulomb" and b.hmlt < deck.HMLT["DHFR"]:
@@ -98,6 +112,55 @@ def main(argv=None):
         out["energy_bx_eh"] = float(0.5 * np.sum(dent * bx).real)
     fb.close()
     print(json.dumps(out), flush=True)
+
+
+def microbench_main(a):
+    """Explicit lists of the ERI microbenchmark (workloads.microbench_*),
+    grouped by angular class, digested with bertha_gpu_quartets_segments;
+    device time of each repeat by CUDA events."""
+    import torch
+
+    from . import workloads
+    b = workloads.microbench_pool(seed=a.seed)
+    raw = workloads.microbench_quartets(b, a.microbench, seed=a.seed)
+    dent = deck.density(b, seed=a.seed)
+    fb = FockBuilder(b)
+    fb.set_precision(a.precision)
+    n = fb.ndim
+    D = torch.from_numpy(np.ascontiguousarray(dent.T).view(np.float64).reshape(n, 2 * n)).cuda()
+    GD = torch.zeros(n, 2 * n, dtype=torch.float64, device="cuda")
+    GX = torch.zeros_like(GD)
+    jobs = []
+    for cls, q in raw.items():
+        if a.comp and tuple(cls) != tuple(a.comp):
+            continue
+        qs, seg, lcl = workloads.group_by_class(b, q)
+        keep = [i for i in range(len(seg) - 1)
+                if not a.lclass or "".join(str(int(x)) for x in lcl[i]) == a.lclass]
+        if not keep:
+            continue
+        dq = torch.from_numpy(qs).cuda()
+        jobs.append((cls, dq, seg, lcl, keep))
+    st = torch.cuda.current_stream()
+    times, nq = [], 0
+    for r in range(a.repeat):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for cls, dq, seg, lcl, keep in jobs:
+            for i in keep:
+                fb.quartets_segments(dq[int(seg[i]):].data_ptr(), seg[i:i + 2] - seg[i],
+                                     lcl[i:i + 1], cls[0], cls[1], D.data_ptr(), GD.data_ptr(),
+                                     GX.data_ptr(), n, st.cuda_stream)
+                if r == 0:
+                    nq += int(seg[i + 1] - seg[i])
+        e1.record(st)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    from . import _lib
+    fb.close()
+    return {"microbench": a.microbench, "lclass": a.lclass, "comp": a.comp,
+            "precision": a.precision, "quartets": nq, "device_s": times,
+            "quartets_per_s": nq / min(times), "device_status": _lib.device_status()}
 
 
 def scf_main(a, b):

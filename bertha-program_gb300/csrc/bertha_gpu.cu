@@ -4240,7 +4240,8 @@ int bertha_gpu_brtfast_device(bg_ctx *c, const double *d_dent, int ldd, int ilev
       c->btune_rec.clear();
       for (int k = 0; k < 2 && !rc; ++k) {
         const int *q = c->d_bquart[k];
-        rc = tune_runs(q, c->bseg[k], c->bsegkey[k], 0, k, st, c->err_budget,
+        // the budget is shared by the two component classes
+        rc = tune_runs(q, c->bseg[k], c->bsegkey[k], 0, k, st, 0.5 * c->err_budget,
                        [&](int kind, const int *qq, long long m, int n1, int n2) {
           if (kind == KIND_TC)
             return launch_breit_tc(c, qq, m, 0, k, D, ldd, bx, n, st, 2, n1, n2);

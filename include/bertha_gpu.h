@@ -103,8 +103,9 @@ int bertha_gpu_auto_stats(const bg_ctx *ctx, long long *nq_fp64, long long *nq_d
 int bertha_gpu_kernel_stats(const bg_ctx *ctx, long long nq[3], int *nruns);
 
 /* Energy error (Eh) the BG_PREC_AUTO tuner may spend on tensor-core classes
- * per Coulomb build (shared equally by the component classes) and, apart,
- * per Breit build (default 1e-7 each; 0 keeps every class FP64-accurate).
+ * per Coulomb build and, apart, per Breit build (default 1e-7 each, shared
+ * equally by each build's component classes; 0 keeps every class
+ * FP64-accurate).
  * Within a class, quartets are grouped by the decade of their Schwarz bound
  * Q_ab Q_cd, so that the small-magnitude part of a class can take the
  * tensor cores while its large part stays FP64.  Changing it retunes. */
@@ -117,7 +118,9 @@ int bertha_gpu_set_error_budget(bg_ctx *ctx, double eh);
  * ((l_a*4 + l_b)*4 + l_c)*4 + l_d, quartets, chosen kernel (0 FP64,
  * 1 split, 2 tensor cores); vals[6i..6i+5] = sample time (ms) of the three
  * kernels (0 when not run) and their estimated energy errors (Eh).  At most
- * cap rows are written; *nrows gets the record's length. */
+ * cap rows are written; *nrows gets the record's length.  After tuning the
+ * library reorders its lists by chosen kernel, so the record is in tuning
+ * order, not list order. */
 int bertha_gpu_tuning_record(const bg_ctx *ctx, int breit, int cap, int *info, double *vals,
                              int *nrows);
 

@@ -1,0 +1,54 @@
+"""The one-centre Coulomb matrices by the reference's default route (Racah
+algebra and beta-function radial integrals, COULOMB1) against the MD
+one-centre quartets of the oracle (RACAH1 off, the route the GPU library
+uses for one-centre terms).  The two are independent algorithms for the
+same integrals: their agreement pins the MD one-centre path to the
+reference's own algorithm."""
+import numpy as np
+import pytest
+
+from berthagpu import deck, wfn
+from oracle import oracle as orc
+from oracle import racah1
+
+TOL = 1e-12
+
+
+def _atom(shells, seed):
+    b = deck.make_basis([((0.0, 0.0, 0.0), shells)], hmlt="DHFR", isym=0)
+    d = deck.density(b, seed=seed)
+    lrge, _ = wfn.fock_layout(b)
+    rd, rx = racah1.coulomb1(b, d, lrge)
+    md, mx = orc.clmfast(b, d, 3, racah1=False)
+    scale = max(np.abs(md).max(), np.abs(mx).max())
+    return np.abs(rd - md).max() / scale, np.abs(rx - mx).max() / scale
+
+
+def test_sym3j_against_sympy():
+    wigner = pytest.importorskip("sympy.physics.wigner")
+    from sympy import Rational
+    for ja in (1, 3, 5, 7):
+        for jb in (1, 3, 5):
+            for l in range(0, 5):
+                for ma in range(-ja, ja + 1, 2):
+                    for mb in range(-jb, jb + 1, 2):
+                        for m in range(-l, l + 1):
+                            ref = float(wigner.wigner_3j(Rational(ja, 2), l, Rational(jb, 2),
+                                                         Rational(ma, 2), m, Rational(mb, 2)))
+                            assert abs(racah1.sym3j(ja, l, jb, ma, m, mb) - ref) < 1e-14
+
+
+@pytest.mark.parametrize("case,shells", [
+    ("Ne-like s,p", {0: [0.25, 1.9, 14.0, 110.0], 1: [0.4, 3.1, 25.0]}),
+    ("Ar-like s,p,d", {0: [0.2, 2.0, 30.0], 1: [0.35, 4.0], 2: [0.9, 5.5]}),
+    ("s,p,d,f", {0: [0.3, 9.0], 1: [0.6], 2: [1.2], 3: [1.8]}),
+])
+def test_racah_matches_md_one_centre(case, shells):
+    ej, ek = _atom(shells, seed=len(case))
+    assert ej <= TOL and ek <= TOL, (case, ej, ek)
+
+
+def test_racah_wide_exponent_range():
+    """Exponent ratios of 1e4 within one shell (core and valence)."""
+    ej, ek = _atom({0: [0.05, 1.0, 40.0, 600.0], 1: [0.1, 8.0]}, seed=11)
+    assert ej <= TOL and ek <= TOL, (ej, ek)
