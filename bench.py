@@ -415,13 +415,15 @@ def tlf_builds(torch):
     bs = deck.tlf_small_basis()
     scf = {"case": "TlF, Tl 7s6p4d3f / F 4s3p1d, DHFB", "ndim": bs.ndim, "nocc": 90,
            "guess": "bare nucleus, maximum overlap from iteration 3",
-           "etol_eh": 1e-10, "density_change_tol": 1e-6}
+           "etol_eh": 1e-10, "density_change_tol": 1e-4}
     dens = {}
     for prec in ("fp64", "auto"):
         s_ = DHFSCF(bs, nocc=90, precision=prec, screen=1e-12, torch=torch)
         if prec == "auto":
             s_.backend.fb.set_error_budget(TLF_BUDGET)
-        r = s_.run(max_iter=200, etol=1e-10, dtol=1e-6, mom=3, return_density=True)
+        # (the energy settles to 1e-10 Eh while the density keeps moving at
+        # a few 1e-5 along near-degenerate rotations)
+        r = s_.run(max_iter=150, etol=1e-10, dtol=1e-4, mom=3, return_density=True)
         dens[prec] = r["density"]
         scf[prec] = {k: r[k] for k in ("energy", "iterations", "converged", "density_change",
                                        "commutator", "wall_s", "fock_s")}
