@@ -214,7 +214,7 @@ __host__ __device__ inline Layout layout(int bbytes, int nbuf, int rfbytes, int 
   L.rf = rup(L.bbuf + breg, 128);
   L.dsm = L.rf + rup(rfbytes, 128);
   L.acc = L.dsm + nblk * MAXSP * MAXSP * 8;
-  L.fb = L.acc + nblk * MAXSP * MAXSP * 8;
+  L.fb = L.acc + nblk * MAXSP * MAXSP * 16;  // FP64 accumulators
   L.total = L.fb + (MAXLAM + 4) * 8 + 128;  // + alignment slack
   return L;
 }
@@ -327,9 +327,14 @@ __device__ __forceinline__ void cmac(float2 &acc, float2 u, float2 d) {
   acc.y = fmaf(u.x, d.y, fmaf(u.y, d.x, acc.y));
 }
 
-__device__ __forceinline__ void sadd(float2 *p, float2 v) {
-  atomicAdd(&p->x, v.x);
-  atomicAdd(&p->y, v.y);
+// A work item's FP32 contribution into a shared FP64 accumulator: the
+// accumulation order of the items is not fixed, and in FP64 its rounding
+// stays at the level of the global FP64 sums (FP32 accumulators would make
+// a build's result vary by ~1e-7 between identical calls, enough to keep
+// an SCF from converging to 1e-9 Eh).
+__device__ __forceinline__ void sadd(double2 *p, float2 v) {
+  atomicAdd(&p->x, (double)v.x);
+  atomicAdd(&p->y, (double)v.y);
 }
 
 // ---- staging of one K chunk into the canonical K-major layout ----
@@ -598,7 +603,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   double *R2 = R + NTR;
   float *Rf = (float *)(base + LY.rf);
   float2 *Dsm = (float2 *)(base + LY.dsm);        // D(c,d), D(c,b), D(a,b), D(a,d)
-  float2 *Acc = (float2 *)(base + LY.acc);        // J(a,b), K(a,d), J2(c,d), K2(c,b)
+  double2 *Acc = (double2 *)(base + LY.acc);      // J(a,b), K(a,d), J2(c,d), K2(c,b)
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
   __shared__ double sqp[QPW];          // this quartet's k_qprep record
@@ -715,7 +720,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
         }
       }
     }
-    for (int i = tid; i < 4 * MAXSP * MAXSP; i += NT) Acc[i] = make_float2(0.f, 0.f);
+    for (int i = tid; i < 4 * MAXSP * MAXSP; i += NT) Acc[i] = make_double2(0.0, 0.0);
     __syncthreads();  // R (FP64) is dead: the B buffers may overwrite it
 
     const uint32_t tD1 = tmem, tD2 = tmem + (uint32_t)n1;
@@ -807,8 +812,8 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
           float sl = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
           const float2 *Dcd = Dsm, *Dcb = Dsm + MAXSP * MAXSP;
           const float2 *Dab = Dsm + 2 * MAXSP * MAXSP, *Dad = Dsm + 3 * MAXSP * MAXSP;
-          float2 *Jl = Acc, *Kl = Acc + MAXSP * MAXSP, *J2 = Acc + 2 * MAXSP * MAXSP,
-                 *K2 = Acc + 3 * MAXSP * MAXSP;
+          double2 *Jl = Acc, *Kl = Acc + MAXSP * MAXSP, *J2 = Acc + 2 * MAXSP * MAXSP,
+                  *K2 = Acc + 3 * MAXSP * MAXSP;
           float2 r16[16];
           combos16(sv, sl, slr, r16);
           // (ab|cd) m-sign combination from the (left|right) one; every index
@@ -876,8 +881,8 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
                 jv = fmaf(TCV(s, s, t, t).x, Dcd[(ic * 2 + t) * MAXSP + id * 2 + t].x, jv);
                 kv = fmaf(TCV(s, t, t, s).x, Dcb[(ic * 2 + t) * MAXSP + ib * 2 + t].x, kv);
               }
-              atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, jv);
-              atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
+              atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, (double)jv);
+              atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, (double)kv);
             }
             if (dual) {
 #pragma unroll
@@ -888,8 +893,8 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
                   jv = fmaf(TCV(t, t, s, s).x, Dab[(ia * 2 + t) * MAXSP + ib * 2 + t].x, jv);
                   kv = fmaf(TCV(t, s, s, t).x, Dad[(ia * 2 + t) * MAXSP + id * 2 + t].x, kv);
                 }
-                atomicAdd(&J2[(ic * 2 + s) * MAXSP + id * 2 + s].x, jv);
-                atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
+                atomicAdd(&J2[(ic * 2 + s) * MAXSP + id * 2 + s].x, (double)jv);
+                atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, (double)kv);
               }
             }
           }
@@ -912,13 +917,13 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
       double *G = (f == 0 || f == 2) ? GDm : GXm;
       for (int w = tid; w < nr * nc; w += NT) {
         int a = w / nc, b = w % nc;
-        float2 v = Acc[f * MAXSP * MAXSP + a * MAXSP + b];
-        if (v.x == 0.f && v.y == 0.f) continue;
+        double2 v = Acc[f * MAXSP * MAXSP + a * MAXSP + b];
+        if (v.x == 0.0 && v.y == 0.0) continue;
         int fa = sh4[ra]->fock[a >> 1][a & 1] + off4[ra];
         int fb = sh4[ca]->fock[b >> 1][b & 1] + off4[ca];
         double *dst = G + 2 * ((size_t)fa + ldfm * fb);
-        atomicAdd(dst, wq * (double)v.x);
-        atomicAdd(dst + 1, wq * (double)v.y);
+        atomicAdd(dst, wq * v.x);
+        atomicAdd(dst + 1, wq * v.y);
       }
     }
   }
@@ -964,7 +969,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
   double *R2 = R + NTR;
   float *Wf = (float *)(base + LY.rf);
   float2 *Dsm = (float2 *)(base + LY.dsm);   // D(c,b), D(a,d)
-  float2 *Acc = (float2 *)(base + LY.acc);   // K(a,d), K2(c,b)
+  double2 *Acc = (double2 *)(base + LY.acc); // K(a,d), K2(c,b)
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
   __shared__ double sqp[QPW];          // this quartet's k_qprep record
@@ -1093,7 +1098,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
         }
       }
     }
-    for (int i = tid; i < 2 * MAXSP * MAXSP; i += NT) Acc[i] = make_float2(0.f, 0.f);
+    for (int i = tid; i < 2 * MAXSP * MAXSP; i += NT) Acc[i] = make_double2(0.0, 0.0);
     __syncthreads();
 
     const int nslot = q.tri ? 3 : 1;  // D1 accumulators side by side
@@ -1206,7 +1211,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
           double pl = swp ? pcd : pab, pr = swp ? pab : pcd;
           float sl = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
           const float2 *Dcb = Dsm, *Dad = Dsm + MAXSP * MAXSP;
-          float2 *Kl = Acc, *K2 = Acc + MAXSP * MAXSP;
+          double2 *Kl = Acc, *K2 = Acc + MAXSP * MAXSP;
           float2 r16[16];
           combos16(sv, sl, slr, r16);
 #define TCV(sa, sb, sc, sd) (swp ? r16[8 * (sc) + 4 * (sd) + 2 * (sa) + (sb)] \
@@ -1246,7 +1251,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
 #pragma unroll
               for (int t = 0; t < 2; ++t)
                 kv = fmaf(TCV(s, t, t, s).x, Dcb[(ic * 2 + t) * MAXSP + ib * 2 + t].x, kv);
-              atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, kv);
+              atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, (double)kv);
             }
             if (dual) {
 #pragma unroll
@@ -1255,7 +1260,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
 #pragma unroll
                 for (int t = 0; t < 2; ++t)
                   kv = fmaf(TCV(t, s, s, t).x, Dad[(ia * 2 + t) * MAXSP + id * 2 + t].x, kv);
-                atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, kv);
+                atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, (double)kv);
               }
             }
           }
@@ -1270,22 +1275,22 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
     const double wq = (q.dual == 2 && t2 == 1 && Q4.x == Q4.w && Q4.y == Q4.z) ? 0.5 : 1.0;
     for (int w = tid; w < 2 * nla * 2 * nld; w += NT) {
       int a = w / (2 * nld), d = w % (2 * nld);
-      float2 v = Acc[a * MAXSP + d];
-      if (v.x == 0.f && v.y == 0.f) continue;
+      double2 v = Acc[a * MAXSP + d];
+      if (v.x == 0.0 && v.y == 0.0) continue;
       int fa = A.fock[a >> 1][a & 1] + oa, fdd = Dd.fock[d >> 1][d & 1] + od;
       double *dst = q.BX + 2 * ((size_t)fa + (size_t)q.ldf * fdd);
-      atomicAdd(dst, wq * (double)v.x);
-      atomicAdd(dst + 1, wq * (double)v.y);
+      atomicAdd(dst, wq * v.x);
+      atomicAdd(dst + 1, wq * v.y);
     }
     if (dual)
       for (int w = tid; w < 2 * nlc * 2 * nlb; w += NT) {
         int cc = w / (2 * nlb), b = w % (2 * nlb);
-        float2 v = Acc[MAXSP * MAXSP + cc * MAXSP + b];
-        if (v.x == 0.f && v.y == 0.f) continue;
+        double2 v = Acc[MAXSP * MAXSP + cc * MAXSP + b];
+        if (v.x == 0.0 && v.y == 0.0) continue;
         int fcc = C.fock[cc >> 1][cc & 1] + oc, fbb = B.fock[b >> 1][b & 1] + ob;
         double *dst = q.BX + 2 * ((size_t)fcc + (size_t)q.ldf * fbb);
-        atomicAdd(dst, wq * (double)v.x);
-        atomicAdd(dst + 1, wq * (double)v.y);
+        atomicAdd(dst, wq * v.x);
+        atomicAdd(dst + 1, wq * v.y);
       }
   }
   if (abort && tid == 0) atomicOr(&g_tc_status, 1);
