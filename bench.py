@@ -198,9 +198,12 @@ class ClockSampler:
 TRAFFIC_BYTES_PER_LAUNCH = 10.749e9
 
 
-# DRAM bytes per k_quartet_tc launch of this workload (dram__bytes_read.sum
-# + dram__bytes_write.sum of an ncu capture); None until captured.
-TC_TRAFFIC_BYTES_PER_STEP = None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# k_quartet_tc launches of one 2^20-quartet step of this workload's
+# distribution, from a one-pass ncu launch list of the run module's
+# microbenchmark (profiles/k_quartet_tc_eri_microbench_launches.md: 42.19 GB
+# over the step's launches).
+TC_TRAFFIC_BYTES_PER_STEP = 42.19e9
 
 
 def read_traffic():
@@ -803,8 +806,8 @@ def run_gpu(args):
                     "peak_source": "cuBLAS TF32 GEMM 8192^3 measured in this run "
                                    "(MEASURED_PEAKS.json has no TF32 entry)",
                     "flops_per_step": 3.0 * tot_cflops,
-                    "traffic": (TC_TRAFFIC_BYTES_PER_STEP / len(dq)
-                                if TC_TRAFFIC_BYTES_PER_STEP else None),
+                    "traffic": TC_TRAFFIC_BYTES_PER_STEP,
+                    "traffic_per": "step (all k_quartet_tc launches of one step, as achieved)",
                     "fp64_kernel": fp64_roof}
     else:
         roofline = dict(fp64_roof)
