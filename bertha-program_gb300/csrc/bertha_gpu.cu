@@ -21,6 +21,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "bertha_gpu.h"
@@ -2366,7 +2367,9 @@ constexpr size_t SM_SMEM = 233472;  // 228 KB of shared memory per SM
 constexpr size_t TC_SMEM_MAX = 232448;  // 227 KB, the per-CTA opt-in limit
 size_t g_tc_smem_max = 122880;  // dynamic shared memory the tensor-core kernels may ask for
 
-TcGeom tc_geom(int n1, int n2, bool breit = false) {
+// f64acc: the Coulomb kernel's shared J/K accumulators in FP64 (Fock
+// builds) or FP32 (explicit lists); the Breit kernel's are FP64.
+TcGeom tc_geom(int n1, int n2, bool breit = false, bool f64acc = true) {
   TcGeom g;
   g.tri = breit && 3 * n1 + n2 <= 512 ? 1 : 0;
   int need = (g.tri ? 3 * n1 : n1) + n2, cols = 32;
@@ -2374,7 +2377,7 @@ TcGeom tc_geom(int n1, int n2, bool breit = false) {
   g.cols = cols;
   auto total = [&](int nb) {
     return breit ? (size_t)tcq::layout_b(n1, n2, nb, g.tri).total
-                 : (size_t)tcq::layout_c(n1, n2, nb).total;
+                 : (size_t)tcq::layout_c(n1, n2, nb, f64acc).total;
   };
   size_t s = total(1);
   int ctas = std::min(2, 512 / cols);
@@ -2583,7 +2586,10 @@ const char *device_setup(int dev) {
   int optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return "shared-memory opt-in query failed";
-  const void *tck[4] = {(const void *)k_quartet_tc<256>, (const void *)k_quartet_tc<512>,
+  const void *tck[6] = {(const void *)k_quartet_tc<256, true>,
+                        (const void *)k_quartet_tc<512, true>,
+                        (const void *)k_quartet_tc<256, false>,
+                        (const void *)k_quartet_tc<512, false>,
                         (const void *)k_breit_tc<256>, (const void *)k_breit_tc<512>};
   size_t stat = 0;
   for (const void *f : tck) {
@@ -2806,7 +2812,10 @@ int launch_quartets_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
                        cudaStream_t st, int sym, int n1, int n2) {
   if (nq <= 0) return 0;
   if (!c->d_qp) CK(c, cudaMalloc(&c->d_qp, sizeof(double) * QPW * QP_CHUNK));
-  TcGeom g = tc_geom(n1, n2);
+  // explicit lists (sym 0) are digested once: FP32 shared accumulators;
+  // Fock builds (sym 2) accumulate in FP64 so that repeated builds agree
+  const bool f64 = sym != 0;
+  TcGeom g = tc_geom(n1, n2, false, f64);
   tcq::Args a;
   a.sh = c->d_sh; a.pe = c->d_pe; a.E = c->d_Ef; a.D = d_D;
   a.GD = d_GD; a.GX = d_GX; a.ldd = ldd; a.ldf = ldf; a.nskp = c->nskp;
@@ -2818,10 +2827,14 @@ int launch_quartets_tc(bg_ctx *c, const int *d_q, long long nq, int t1, int t2,
     k_qprep<<<(unsigned)std::min<long long>((m + 127) / 128, 152LL * 16), 128, 0, st>>>(
         c->d_sh, qq, m, 2 * t1 + 2 * t2, c->d_qp);
     long long grid = std::min<long long>(m, 152LL * g.ctas_per_sm);
-    if (g.nt == 512)
-      k_quartet_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, qq, m, t1, t2);
+    if (g.nt == 512 && f64)
+      k_quartet_tc<512, true><<<(unsigned)grid, 512, g.smem, st>>>(a, qq, m, t1, t2);
+    else if (g.nt == 512)
+      k_quartet_tc<512, false><<<(unsigned)grid, 512, g.smem, st>>>(a, qq, m, t1, t2);
+    else if (f64)
+      k_quartet_tc<256, true><<<(unsigned)grid, 256, g.smem, st>>>(a, qq, m, t1, t2);
     else
-      k_quartet_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, qq, m, t1, t2);
+      k_quartet_tc<256, false><<<(unsigned)grid, 256, g.smem, st>>>(a, qq, m, t1, t2);
     CK(c, cudaGetLastError());
     c->launches += 2;
   }
@@ -3560,9 +3573,9 @@ int batch_launch(bg_batch *b, int t1, int t2, int kind, const int4 *quart, long 
           b->d_sh, quart + s0, m, 2 * t1 + 2 * t2, b->d_qp);
       long long grid = std::min<long long>(m, 152LL * g.ctas_per_sm);
       if (g.nt == 512)
-        k_quartet_tc<512><<<(unsigned)grid, 512, g.smem, st>>>(a, quart + s0, m, t1, t2);
+        k_quartet_tc<512, true><<<(unsigned)grid, 512, g.smem, st>>>(a, quart + s0, m, t1, t2);
       else
-        k_quartet_tc<256><<<(unsigned)grid, 256, g.smem, st>>>(a, quart + s0, m, t1, t2);
+        k_quartet_tc<256, true><<<(unsigned)grid, 256, g.smem, st>>>(a, quart + s0, m, t1, t2);
       b->launches += 2;
     }
     b->launches--;  // counted once more below

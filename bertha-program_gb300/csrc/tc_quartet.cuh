@@ -203,7 +203,8 @@ constexpr int ABYTES = 2 * MROWS * KC * 4;    // one A staging buffer (hi and lo
 struct Layout {
   int abuf, bbuf, bsz, rf, dsm, acc, fb, total;
 };
-__host__ __device__ inline Layout layout(int bbytes, int nbuf, int rfbytes, int nblk) {
+__host__ __device__ inline Layout layout(int bbytes, int nbuf, int rfbytes, int nblk,
+                                          int accb) {
   Layout L;
   L.abuf = 0;
   L.bsz = rup(bbytes, 128);
@@ -214,7 +215,7 @@ __host__ __device__ inline Layout layout(int bbytes, int nbuf, int rfbytes, int 
   L.rf = rup(L.bbuf + breg, 128);
   L.dsm = L.rf + rup(rfbytes, 128);
   L.acc = L.dsm + nblk * MAXSP * MAXSP * 8;
-  L.fb = L.acc + nblk * MAXSP * MAXSP * 16;  // FP64 accumulators
+  L.fb = L.acc + nblk * MAXSP * MAXSP * accb;  // accb: 8 (FP32) or 16 (FP64) per element
   L.total = L.fb + (MAXLAM + 4) * 8 + 128;  // + alignment slack
   return L;
 }
@@ -229,11 +230,11 @@ __host__ __device__ inline int bbytes_b(int n1, int n2, int tri) {
   int b1 = (tri ? 3 : 1) * 2 * n1 * KC * 4, b2 = 2 * n2 * KC * 4;
   return b1 > b2 ? b1 : b2;
 }
-__host__ __device__ inline Layout layout_c(int n1, int n2, int nbuf) {
-  return layout(bbytes_c(n1, n2), nbuf, NTR * 4, 4);
+__host__ __device__ inline Layout layout_c(int n1, int n2, int nbuf, bool f64acc) {
+  return layout(bbytes_c(n1, n2), nbuf, NTR * 4, 4, f64acc ? 16 : 8);
 }
 __host__ __device__ inline Layout layout_b(int n1, int n2, int nbuf, int tri) {
-  return layout(bbytes_b(n1, n2, tri), nbuf, NWT * 6 * 4, 2);
+  return layout(bbytes_b(n1, n2, tri), nbuf, NWT * 6 * 4, 2, 16);
 }
 
 // MMA completion tracking of up to two staging buffers: one mbarrier per
@@ -335,6 +336,11 @@ __device__ __forceinline__ void cmac(float2 &acc, float2 u, float2 d) {
 __device__ __forceinline__ void sadd(double2 *p, float2 v) {
   atomicAdd(&p->x, (double)v.x);
   atomicAdd(&p->y, (double)v.y);
+}
+// The same into an FP32 accumulator (one-shot explicit-list digestion).
+__device__ __forceinline__ void sadd(float2 *p, float2 v) {
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
 }
 
 // ---- staging of one K chunk into the canonical K-major layout ----
@@ -587,14 +593,18 @@ __device__ __forceinline__ double *r_recursion(double *R, double *R2, const doub
 // ---------------------------------------------------------------------------
 // Coulomb kernel
 // ---------------------------------------------------------------------------
-template <int NT>
+template <int NT, bool F64ACC>
 __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : 2)
 k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   using namespace tcq;
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char *base =
       (unsigned char *)(((uintptr_t)tc_smem_raw + 127) & ~(uintptr_t)127);
-  const Layout LY = layout_c(q.n1max, q.n2max, q.nbuf);
+  // shared J/K accumulators: FP64 in Fock builds (repeated builds agree to
+  // FP64 rounding, which an SCF needs), FP32 for one-shot explicit lists
+  using Acc2 = typename std::conditional<F64ACC, double2, float2>::type;
+  using AccS = typename std::conditional<F64ACC, double, float>::type;
+  const Layout LY = layout_c(q.n1max, q.n2max, q.nbuf, F64ACC);
   const int bmax = q.n1max > q.n2max ? q.n1max : q.n2max;
   auto bufA = [&](int b) { return (float *)(base + LY.abuf + b * ABYTES); };
   auto bufB = [&](int b) { return (float *)(base + LY.bbuf + b * LY.bsz); };
@@ -603,7 +613,7 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
   double *R2 = R + NTR;
   float *Rf = (float *)(base + LY.rf);
   float2 *Dsm = (float2 *)(base + LY.dsm);        // D(c,d), D(c,b), D(a,b), D(a,d)
-  double2 *Acc = (double2 *)(base + LY.acc);      // J(a,b), K(a,d), J2(c,d), K2(c,b)
+  Acc2 *Acc = (Acc2 *)(base + LY.acc);            // J(a,b), K(a,d), J2(c,d), K2(c,b)
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
   __shared__ double sqp[QPW];          // this quartet's k_qprep record
@@ -720,7 +730,10 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
         }
       }
     }
-    for (int i = tid; i < 4 * MAXSP * MAXSP; i += NT) Acc[i] = make_double2(0.0, 0.0);
+    for (int i = tid; i < 4 * MAXSP * MAXSP; i += NT) {
+      Acc[i].x = AccS(0);
+      Acc[i].y = AccS(0);
+    }
     __syncthreads();  // R (FP64) is dead: the B buffers may overwrite it
 
     const uint32_t tD1 = tmem, tD2 = tmem + (uint32_t)n1;
@@ -812,8 +825,8 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
           float sl = pl < 0 ? -1.f : 1.f, slr = (pl * pr) < 0 ? -1.f : 1.f;
           const float2 *Dcd = Dsm, *Dcb = Dsm + MAXSP * MAXSP;
           const float2 *Dab = Dsm + 2 * MAXSP * MAXSP, *Dad = Dsm + 3 * MAXSP * MAXSP;
-          double2 *Jl = Acc, *Kl = Acc + MAXSP * MAXSP, *J2 = Acc + 2 * MAXSP * MAXSP,
-                  *K2 = Acc + 3 * MAXSP * MAXSP;
+          Acc2 *Jl = Acc, *Kl = Acc + MAXSP * MAXSP, *J2 = Acc + 2 * MAXSP * MAXSP,
+               *K2 = Acc + 3 * MAXSP * MAXSP;
           float2 r16[16];
           combos16(sv, sl, slr, r16);
           // (ab|cd) m-sign combination from the (left|right) one; every index
@@ -881,8 +894,8 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
                 jv = fmaf(TCV(s, s, t, t).x, Dcd[(ic * 2 + t) * MAXSP + id * 2 + t].x, jv);
                 kv = fmaf(TCV(s, t, t, s).x, Dcb[(ic * 2 + t) * MAXSP + ib * 2 + t].x, kv);
               }
-              atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, (double)jv);
-              atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, (double)kv);
+              atomicAdd(&Jl[(ia * 2 + s) * MAXSP + ib * 2 + s].x, (AccS)jv);
+              atomicAdd(&Kl[(ia * 2 + s) * MAXSP + id * 2 + s].x, (AccS)kv);
             }
             if (dual) {
 #pragma unroll
@@ -893,8 +906,8 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
                   jv = fmaf(TCV(t, t, s, s).x, Dab[(ia * 2 + t) * MAXSP + ib * 2 + t].x, jv);
                   kv = fmaf(TCV(t, s, s, t).x, Dad[(ia * 2 + t) * MAXSP + id * 2 + t].x, kv);
                 }
-                atomicAdd(&J2[(ic * 2 + s) * MAXSP + id * 2 + s].x, (double)jv);
-                atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, (double)kv);
+                atomicAdd(&J2[(ic * 2 + s) * MAXSP + id * 2 + s].x, (AccS)jv);
+                atomicAdd(&K2[(ic * 2 + s) * MAXSP + ib * 2 + s].x, (AccS)kv);
               }
             }
           }
@@ -917,13 +930,13 @@ k_quartet_tc(tcq::Args q, const int4 *quart, long long nq, int t1, int t2) {
       double *G = (f == 0 || f == 2) ? GDm : GXm;
       for (int w = tid; w < nr * nc; w += NT) {
         int a = w / nc, b = w % nc;
-        double2 v = Acc[f * MAXSP * MAXSP + a * MAXSP + b];
-        if (v.x == 0.0 && v.y == 0.0) continue;
+        Acc2 v = Acc[f * MAXSP * MAXSP + a * MAXSP + b];
+        if (v.x == AccS(0) && v.y == AccS(0)) continue;
         int fa = sh4[ra]->fock[a >> 1][a & 1] + off4[ra];
         int fb = sh4[ca]->fock[b >> 1][b & 1] + off4[ca];
         double *dst = G + 2 * ((size_t)fa + ldfm * fb);
-        atomicAdd(dst, wq * v.x);
-        atomicAdd(dst + 1, wq * v.y);
+        atomicAdd(dst, wq * (double)v.x);
+        atomicAdd(dst + 1, wq * (double)v.y);
       }
     }
   }
