@@ -445,7 +445,7 @@ __device__ inline int ncntrs(int a, int b, int c, int d) {
 
 // CLMFAST label-level selection rules (bertha-scf.f:11843-11939)
 __device__ bool label_ok(int isym, int racah1, int mcnt, const int *kq, const int *mq,
-                         const int *lq) {
+                         const int *lq, bool breit = false) {
   int jq[4];
   for (int i = 0; i < 4; ++i) jq[i] = 2 * abs(kq[i]) - 1;
   bool onec = (mcnt == 1 && !racah1);
@@ -453,9 +453,15 @@ __device__ bool label_ok(int isym, int racah1, int mcnt, const int *kq, const in
     int nui = max(abs(jq[0] - jq[1]) / 2, abs(jq[2] - jq[3]) / 2);
     int nuf = min((jq[0] + jq[1]) / 2, (jq[2] + jq[3]) / 2);
     if (nui > nuf) return false;
+    // a tensor order nu coupling both pairs: both l_a + l_b + nu and
+    // l_c + l_d + nu even (CLMFAST :11914-11939); for the Breit
+    // interaction also both odd with nu > 0, its magnetic terms (BRTFAST's
+    // ISELK, :17443-17456)
     bool selk = false;
-    for (int nu = nui; nu <= nuf; ++nu)
-      if (((lq[0] + lq[1] + nu) & 1) == 0 && ((lq[2] + lq[3] + nu) & 1) == 0) selk = true;
+    for (int nu = nui; nu <= nuf; ++nu) {
+      int pab = (lq[0] + lq[1] + nu) & 1, pcd = (lq[2] + lq[3] + nu) & 1;
+      if ((pab == 0 && pcd == 0) || (breit && pab == 1 && pcd == 1 && nu != 0)) selk = true;
+    }
     if (!selk) return false;
   }
   if (isym == 1 || isym == 2) {
@@ -1329,7 +1335,7 @@ k_breit(BArgs q, const int4 *quart, long long nq, int t1, int t2) {
         label_of(lc, ic, kq[2], mm[2]);
         label_of(ld, id, kq[3], mm[3]);
         for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
-        if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
+        if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq, true)) continue;
         double pab = -pair_phase(kq[0], mm[0], kq[1], mm[1]);
         double pcd = -pair_phase(kq[2], mm[2], kq[3], mm[3]);
         double pl = swp ? pcd : pab, pr = swp ? pab : pcd;

@@ -1215,7 +1215,7 @@ k_breit_tc(tcq::ArgsB q, const int4 *quart, long long nq, int t1, int t2) {
           label_of(lc, ic, kq[2], mm[2]);
           label_of(ld, id, kq[3], mm[3]);
           for (int i = 0; i < 4; ++i) mq[i] = 2 * mm[i] - 1;
-          if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq)) continue;
+          if (!label_ok(q.isym, q.racah1, mcnt, kq, mq, lq, true)) continue;
           float2 sv[8];
           products8(P + (lab * 4) * PSTR + (lr - r0) * 4, sv);
           // Breit phases: the Coulomb pair phases negated (BRTFAST :17528-17533)

@@ -610,8 +610,10 @@ inline double phase_pair(int kqa, int ma, int kqb, int mb) {
 }
 
 // Selection rules of CLMFAST for one label quartet (bertha-scf.f:11914-11939
-// and 11843-11890).  Returns false if the quartet is skipped.
-bool label_rules(const Opts &o, int mcnt, const Label *lab, const int *lq) {
+// and 11843-11890); with breit, those of BRTFAST (:17432-17486), whose
+// tensor-order rule also keeps both parities odd with nu > 0 (the magnetic
+// terms).  Returns false if the quartet is skipped.
+bool label_rules(const Opts &o, int mcnt, const Label *lab, const int *lq, bool breit = false) {
   int mq[4], jq[4];
   for (int i = 0; i < 4; ++i) {
     mq[i] = 2 * lab[i].ma - 1;
@@ -622,9 +624,10 @@ bool label_rules(const Opts &o, int mcnt, const Label *lab, const int *lq) {
     int nuf = std::min((jq[0] + jq[1]) / 2, (jq[2] + jq[3]) / 2);
     if (nui > nuf) return false;
     bool selk = false;
-    for (int nu = nui; nu <= nuf; ++nu)
-      if ((lq[0] + lq[1] + nu) % 2 == 0 && (lq[2] + lq[3] + nu) % 2 == 0)
-        selk = true;
+    for (int nu = nui; nu <= nuf; ++nu) {
+      int pab = (lq[0] + lq[1] + nu) % 2, pcd = (lq[2] + lq[3] + nu) % 2;
+      if ((pab == 0 && pcd == 0) || (breit && pab == 1 && pcd == 1 && nu != 0)) selk = true;
+    }
     if (!selk) return false;
   }
   if (o.isym == 1 || o.isym == 2) {
@@ -1011,7 +1014,7 @@ void breit_full(const Basis &b, const Opts &o, bool gaunt, const Mat &D, Mat &BX
               for (int id = 0; id < Ecd.nlab_b; ++id) {
                 const Label &LC = Ecd.la[ic], &LD = Ecd.lb[id];
                 Label quad[4] = {LA, LB, LC, LD};
-                if (!label_rules(o, mcnt, quad, lq)) continue;
+                if (!label_rules(o, mcnt, quad, lq, true)) continue;
                 double pab = phase_breit(LA.kq, LA.ma, LB.kq, LB.ma);
                 double pcd = phase_breit(LC.kq, LC.ma, LD.kq, LD.ma);
                 Eri16 rr;

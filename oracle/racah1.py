@@ -318,3 +318,260 @@ def coulomb1(basis, dent, lrge):
                                     gx[S["a"], L["d"]] += np.einsum("abcd,cb->ad", XSL,
                                                                     dent[L["c"], S["b"]])
     return gd, gx
+
+
+# ---------------------------------------------------------------------------
+# One-centre Breit (Gaunt plus gauge) exchange matrix by the Racah route:
+# BREIT1 (bertha-scf.f:26014) with TNSBRT1 (:28691), ANGBRT1 (:28813),
+# BRCOEF1 (the coefficients of Grant and Pyper's table 2), BTABRT1 (:28354),
+# RKBRT1 (:28525) and the closed-shell exchange digestion of BRTMT1G
+# (:27462): BXCH from (AD|CB).
+# ---------------------------------------------------------------------------
+
+def tnsbrt1(lqn):
+    """Tensor orders of the Breit interaction for an LQN block: NU where
+    both LA+LB+NU and LC+LD+NU are odd (NU > 0), NU-1 and NU+1 where both
+    are even (NU-1 only for NU > 0); an ordered list without repeats."""
+    if (lqn[0] + lqn[1]) % 2 != (lqn[2] + lqn[3]) % 2:
+        return []
+    nui = max(abs(lqn[0] - lqn[1]), abs(lqn[2] - lqn[3]))
+    nuf = min(lqn[0] + lqn[1], lqn[2] + lqn[3])
+    if nui > nuf:
+        return []
+    out = []
+    for nu in range(nui, nuf + 1):
+        pab, pcd = (lqn[0] + lqn[1] + nu) % 2, (lqn[2] + lqn[3] + nu) % 2
+        if pab == 1 and pcd == 1 and nu != 0:
+            vals = [nu]
+        elif pab == 0 and pcd == 0:
+            vals = ([nu - 1] if nu > 0 else []) + [nu + 1]
+        else:
+            vals = []
+        for v in vals:
+            if v not in out:
+                out.append(v)
+    return sorted(out)
+
+
+def brcoef1(kqn, nu):
+    """SCOEFF[i][0] (order NU-1) and SCOEFF[i][1] (order NU+1) for the eight
+    component integrals LSLS, SLSL, LSSL, SLLS (upper, lower) (BRCOEF1)."""
+    kca, kdb = kqn[1] - kqn[0], kqn[3] - kqn[2]
+    s = [[0.0, 0.0] for _ in range(8)]
+    if nu >= 1:
+        b1 = nu * (nu + 1) / (2 * nu * (2 * nu - 1))
+        c1 = (nu - 2) / (2 * nu * (2 * nu - 1))
+        s[0][0] = (nu + kca) * (b1 - c1 * kdb)
+        s[1][0] = (nu + kdb) * (b1 - c1 * kca)
+        s[2][0] = (nu - kca) * (b1 + c1 * kdb)
+        s[3][0] = (nu - kdb) * (b1 + c1 * kca)
+        s[4][0] = -(nu + kca) * (b1 + c1 * kdb)
+        s[5][0] = -(nu - kdb) * (b1 - c1 * kca)
+        s[6][0] = -(nu - kca) * (b1 - c1 * kdb)
+        s[7][0] = -(nu + kdb) * (b1 + c1 * kca)
+    if nu >= 0:
+        b2 = nu * (nu + 1) / ((2 * nu + 2) * (2 * nu + 3))
+        c2 = (nu + 3) / ((2 * nu + 2) * (2 * nu + 3))
+        s[0][1] = -(nu + 1 - kdb) * (b2 + c2 * kca)
+        s[1][1] = -(nu + 1 - kca) * (b2 + c2 * kdb)
+        s[2][1] = -(nu + 1 + kdb) * (b2 - c2 * kca)
+        s[3][1] = -(nu + 1 + kca) * (b2 - c2 * kdb)
+        s[4][1] = (nu + 1 + kdb) * (b2 + c2 * kca)
+        s[5][1] = (nu + 1 - kca) * (b2 - c2 * kdb)
+        s[6][1] = (nu + 1 - kdb) * (b2 - c2 * kca)
+        s[7][1] = (nu + 1 + kca) * (b2 + c2 * kdb)
+    return s
+
+
+def angbrt1(kqn, lqn, nus):
+    """Breit angular coefficients BCOF[lten][imu] as dicts over the signed
+    twice-m values (ma, mb, mc, md), and the flags of the orders used by
+    this KQN block (ANGBRT1)."""
+    jq = [2 * abs(k) - 1 for k in kqn]
+    nuit = max(abs(jq[0] - jq[1]) // 2, abs(jq[2] - jq[3]) // 2)
+    nuft = min((jq[0] + jq[1]) // 2, (jq[2] + jq[3]) // 2)
+    if nuit > nuft:
+        return None
+    if (lqn[0] + lqn[1]) % 2 != (lqn[2] + lqn[3]) % 2:
+        return None
+    mss = [[s * (2 * m - 1) for m in range(1, abs(k) + 1) for s in (-1, 1)] for k in kqn]
+    inu = [False] * len(nus)
+    bcof = [[{} for _ in range(8)] for _ in nus]
+    used = False
+
+    def add(lt, coef):
+        # BCOF(lt, imu, ...) += AJJN * coef[imu]
+        for imu in range(8):
+            c = coef[imu]
+            if c == 0.0:
+                continue
+            d = bcof[lt][imu]
+            for key, v in ajjn.items():
+                d[key] = d.get(key, 0.0) + v * c
+    for nu in range(nuit, nuft + 1):
+        pab, pcd = (lqn[0] + lqn[1] + nu) % 2, (lqn[2] + lqn[3] + nu) % 2
+        if not ((pab == 1 and pcd == 1 and nu != 0) or (pab == 0 and pcd == 0)):
+            continue
+        ajjn = {}
+        for ma in mss[0]:
+            for mb in mss[1]:
+                dab = dk(jq[0], ma, jq[1], mb, nu)
+                for mc in mss[2]:
+                    for md in mss[3]:
+                        ajjn[(ma, mb, mc, md)] = dab * dk(jq[3], md, jq[2], mc, nu)
+        used = True
+        if pab == 1:
+            lt = nus.index(nu)
+            inu[lt] = True
+            rc = -(kqn[0] + kqn[1]) * (kqn[2] + kqn[3]) / (nu * (nu + 1))
+            add(lt, [rc] * 8)
+        else:
+            sc = brcoef1(kqn, nu)
+            if nu > 0:
+                lt = nus.index(nu - 1)
+                inu[lt] = True
+                add(lt, [sc[i][0] for i in range(8)])
+            lt = nus.index(nu + 1)
+            inu[lt] = True
+            add(lt, [sc[i][1] for i in range(8)])
+    if not used:
+        return None
+    return inu, bcof
+
+
+def rk_breit_block(kqn, lqn, nus, inu, exps):
+    """RKBRT1 (with IJSET1, KLSET1, BTABRT1): radial Breit integrals
+    RJ[comp][lten] = (upper, lower) arrays [na, nb, nc, nd] for the
+    component integrals LSLS, SLSL, LSSL, SLLS, normalised."""
+    ea, eb, ec, ed = (np.asarray(e, dtype=float) for e in exps)
+    shp = (len(ea), len(eb), len(ec), len(ed))
+    EI = ea[:, None, None, None] * np.ones(shp)
+    EJ = eb[None, :, None, None] * np.ones(shp)
+    EK = ec[None, None, :, None] * np.ones(shp)
+    EL = ed[None, None, None, :] * np.ones(shp)
+    tij0, tkl0 = EI + EJ, EK + EL
+    xj = (tij0 / (tij0 + tkl0), tkl0 / (tij0 + tkl0))
+    nui, nuf = nus[0], nus[-1]
+    nunum = len(nus)
+    nvals = (nuf - nui) // 2 + 2
+    bdu, bdl = {}, {}
+    for nx in range(1, nvals + 1):
+        iaa = (lqn[0] + lqn[1] + nui + 2 * nx, lqn[2] + lqn[3] + nui + 2 * nx)
+        for ny in range(1, nvals + 1):
+            ibb = (lqn[2] + lqn[3] - nuf + 2 * ny - 1, lqn[0] + lqn[1] - nuf + 2 * ny - 1)
+            bdu[(nx, ny)] = _beta(xj[0], (iaa[0] - 1) // 2, ibb[0] // 2)
+            bdl[(nx, ny)] = _beta(xj[1], (iaa[1] - 1) // 2, ibb[1] // 2)
+
+    def eij(p):
+        return np.sqrt(tij0) ** (-(lqn[0] + lqn[1] + p))
+
+    def ekl(p):
+        return np.sqrt(tkl0) ** (-(lqn[2] + lqn[3] + p))
+    lsum = sum(lqn)
+    C3, C5, C7 = (0.25 * gamhlf(lsum + k) for k in (3, 5, 7))
+    ti, tj, tk, tl = (float(lqn[n] + kqn[n] + 1) for n in range(4))
+    out = {c: [None] * nunum for c in ("LSLS", "SLSL", "LSSL", "SLLS")}
+    for lt in range(nunum):
+        if not inu[lt]:
+            continue
+        L, nten, nu = lt + 1, nunum - (lt + 1), nus[lt]
+        B21L = eij(-nu + 1) * ekl(nu + 2) * bdl[(L, nten + 1)]
+        B21U = eij(nu + 2) * ekl(-nu + 1) * bdu[(L, nten + 1)]
+        B23L = eij(-nu + 3) * ekl(nu + 2) * bdl[(L, nten + 2)]
+        B41U = eij(nu + 4) * ekl(-nu + 1) * bdu[(L + 1, nten + 1)]
+        B41L = eij(-nu + 1) * ekl(nu + 4) * bdl[(L + 1, nten + 1)]
+        B23U = eij(nu + 2) * ekl(-nu + 3) * bdu[(L, nten + 2)]
+        B43L = eij(-nu + 3) * ekl(nu + 4) * bdl[(L + 1, nten + 2)]
+        B43U = eij(nu + 4) * ekl(-nu + 3) * bdu[(L + 1, nten + 2)]
+
+        def pair(E1, E2, T1, T2):
+            # (4 E1 E2 C7 B43 - 2 T2 E1 C5 B41 - 2 T1 E2 C5 B23 + T1 T2 C3 B21),
+            # upper; the lower form swaps B41 and B23
+            up = (4 * E1 * E2 * C7 * B43U - 2 * T2 * E1 * C5 * B41U
+                  - 2 * T1 * E2 * C5 * B23U + T1 * T2 * C3 * B21U)
+            lo = (4 * E1 * E2 * C7 * B43L - 2 * T2 * E1 * C5 * B23L
+                  - 2 * T1 * E2 * C5 * B41L + T1 * T2 * C3 * B21L)
+            return up, lo
+        out["LSLS"][lt] = pair(EJ, EL, tj, tl)
+        out["SLSL"][lt] = pair(EI, EK, ti, tk)
+        out["LSSL"][lt] = pair(EJ, EK, tj, tk)
+        out["SLLS"][lt] = pair(EI, EL, ti, tl)
+    nla, nsa = _norms(lqn[0], ea)
+    nlb, nsb = _norms(lqn[1], eb)
+    nlc, nsc = _norms(lqn[2], ec)
+    nld, nsd = _norms(lqn[3], ed)
+    N = {"L": (nla, nlb, nlc, nld), "S": (nsa, nsb, nsc, nsd)}
+    for comp in out:
+        f = (N[comp[0]][0][:, None, None, None] * N[comp[1]][1][None, :, None, None]
+             * N[comp[2]][2][None, None, :, None] * N[comp[3]][3][None, None, None, :])
+        out[comp] = [None if x is None else (x[0] * f, x[1] * f) for x in out[comp]]
+    return out
+
+
+def breit1(basis, dent, lrge):
+    """BXCH (full NDIM x NDIM) of a one-centre basis (centre 0) for the
+    density DENT by BREIT1's Racah route (Gaunt plus gauge term)."""
+    n = dent.shape[0]
+    nskp = n // 2
+    bx = np.zeros((n, n), dtype=complex)
+    lmax = int(basis.lmax[0])
+    kas = list(range(1, 2 * lmax + 2))
+    exps = {l: np.asarray(basis.ex[0, l, :int(basis.nfn[0, l])], dtype=float)
+            for l in range(lmax + 1)}
+
+    def lv(k):
+        return k if k > 0 else -k - 1
+
+    def rng(ka, m2, comp):
+        k = kappa_of(ka)
+        o = int(lrge[0, ka, abs(m2) - 1 + (1 if m2 > 0 else 0)])
+        if comp == "S":
+            o += nskp
+        return slice(o, o + len(exps[lv(k)]))
+    icomp = {"LSLS": 0, "SLSL": 2, "LSSL": 4, "SLLS": 6}
+    for ka in kas:
+        for kb in kas:
+            for kc in kas:
+                for kd in kas:
+                    kqn = [kappa_of(k) for k in (ka, kb, kc, kd)]
+                    lqn = [lv(k) for k in kqn]
+                    nus = tnsbrt1(lqn)
+                    if not nus:
+                        continue
+                    ang = angbrt1(kqn, lqn, nus)
+                    if ang is None:
+                        continue
+                    inu, bcof = ang
+                    rj = rk_breit_block(kqn, lqn, nus, inu, [exps[l] for l in lqn])
+                    ms = [[s * (2 * m - 1) for m in range(1, abs(k) + 1) for s in (-1, 1)]
+                          for k in kqn]
+                    for ma in ms[0]:
+                        for mb in ms[1]:
+                            for mc in ms[2]:
+                                for md in ms[3]:
+                                    if ma - md != mb - mc:
+                                        continue
+                                    key = (ma, mb, mc, md)
+                                    X = {}
+                                    for comp, i0 in icomp.items():
+                                        acc = 0.0
+                                        for lt in range(len(nus)):
+                                            if not inu[lt]:
+                                                continue
+                                            fu = bcof[lt][i0].get(key, 0.0)
+                                            fl = bcof[lt][i0 + 1].get(key, 0.0)
+                                            angsum = sum(abs(bcof[lt][i].get(key, 0.0))
+                                                         for i in range(8))
+                                            if angsum <= SENS:
+                                                continue
+                                            up, lo = rj[comp][lt]
+                                            acc = acc + fu * up + fl * lo
+                                        X[comp] = acc
+                                    for comp, x in X.items():
+                                        if np.isscalar(x):
+                                            continue
+                                        ta, tb, tc, td = comp
+                                        # BXCH: (AD|CB), K(a, d) += (ab|cd) D(c, b)
+                                        bx[rng(ka, ma, ta), rng(kd, md, td)] += np.einsum(
+                                            "abcd,cb->ad", x, dent[rng(kc, mc, tc), rng(kb, mb, tb)])
+    return bx

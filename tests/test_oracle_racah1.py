@@ -52,3 +52,39 @@ def test_racah_wide_exponent_range():
     """Exponent ratios of 1e4 within one shell (core and valence)."""
     ej, ek = _atom({0: [0.05, 1.0, 40.0, 600.0], 1: [0.1, 8.0]}, seed=11)
     assert ej <= TOL and ek <= TOL, (ej, ek)
+
+
+@pytest.mark.parametrize("shells", [
+    {0: [0.5]},
+    {0: [0.25, 1.9, 14.0], 1: [0.4, 3.1]},
+    {0: [0.2, 30.0], 1: [0.35, 4.0, 40.0]},
+])
+def test_racah_breit_matches_md_one_centre(shells):
+    """BREIT1's Racah route (Gaunt plus gauge, Grant and Pyper's
+    coefficients) against the MD one-centre Breit quartets, s and p shells.
+    (From d shells on, BREIT1 limits the tensor orders by the triangle of
+    the large components' l and leaves out terms such as (ss|sd) that the
+    MD route, like BRTFAST's own RACAH1-off path, includes.)"""
+    b = deck.make_basis([((0.0, 0.0, 0.0), shells)], hmlt="DHFB", isym=0)
+    d = deck.density(b, seed=9)
+    lrge, _ = wfn.fock_layout(b)
+    rb = racah1.breit1(b, d, lrge)
+    mb = orc.brtfast(b, d, 3, racah1=False)
+    assert np.abs(rb - mb).max() <= TOL * np.abs(mb).max()
+
+
+def test_breit_one_centre_keeps_magnetic_terms():
+    """BRTFAST's one-centre selection (RACAH1 off) keeps tensor orders with
+    l_a + l_b + nu and l_c + l_d + nu both odd: the p1/2-p3/2 exchange of a
+    p1/2 density is nonzero for the Breit interaction (and zero for the
+    Coulomb one, where only even orders couple)."""
+    b = deck.make_basis([((0.0, 0.0, 0.0), {0: [0.5], 1: [0.8]})], hmlt="DHFB", isym=0)
+    lrge, labels = wfn.fock_layout(b)
+    kap = np.concatenate([labels[:, 1], labels[:, 1]])
+    d0 = deck.density(b, seed=3)
+    p12 = kap == 1
+    d = np.where(p12[:, None] & p12[None, :], d0, 0)
+    bx = orc.brtfast(b, d, 3, racah1=False)
+    blk = np.ix_(kap == 1, kap == -2)
+    assert np.abs(bx[blk]).max() > 1e-3
+    assert np.abs(bx[blk] - racah1.breit1(b, d, lrge)[blk]).max() < 1e-12
