@@ -131,7 +131,10 @@ def read_deck(path):
     """Read a BERTHA .inp deck (CARDIN, bertha-scf.f:150-611) into a Basis.
 
     Supports the OPTIMISED, GEOMETRIC and EVENTEMPR basis types.  Returns
-    (basis, meta) where meta holds the remaining scalar fields.
+    (basis, meta) where meta holds the remaining fields: the calculation
+    tree, NCLS (closed-shell spinors), the starting stage ILEV, READIN, the
+    level shifts SHLEV(1..3) and each centre's electron count IQNC (the
+    atomic configuration's, :313-314).
     """
     with open(path) as f:
         lines = [ln for ln in f.read().splitlines() if ln.strip()]
@@ -147,7 +150,7 @@ def read_deck(path):
         raise ValueError(f"unknown HMLT {hmlt}")
     rec(); readin = rec()[0].upper().startswith(".T")
     rec(); ncnt = int(rec()[0])
-    centres, znuc, anuc = [], [], []
+    centres, znuc, anuc, nelec = [], [], [], []
     for _ in range(ncnt):
         rec(); rec()
         pos = [_num(t) for t in rec()[:3]]
@@ -157,6 +160,7 @@ def read_deck(path):
         rec(); bt = rec()
         btyp, lmax = bt[0], int(bt[1])
         rec(); cnf = rec()
+        nelec.append(int(_num(cnf[1])) if len(cnf) > 1 else int(round(znuc[-1])))
         if cnf[0] == "MANUAL":
             rec()
             for _l in range(lmax + 1):
@@ -179,7 +183,7 @@ def read_deck(path):
         centres.append((pos, exps))
     rec(); shl = rec()
     ncls = int(shl[0])
-    rec(); rec()
+    rec(); shifts = tuple(_num(t) for t in rec()[:3])
     rec(); ilev = int(rec()[0])
     basis = make_basis(centres, hmlt=hmlt, name=molcl)
     basis.znuc, basis.anuc = tuple(znuc), tuple(anuc)
@@ -187,7 +191,8 @@ def read_deck(path):
         ilev = 1
     if ncnt == 1 or readin:
         ilev = 3
-    return basis, {"tree": tree, "ncls": ncls, "ilev": ilev, "readin": readin}
+    return basis, {"tree": tree, "ncls": ncls, "ilev": ilev, "readin": readin,
+                   "shifts": shifts, "nelec": tuple(nelec)}
 
 
 # ---------------------------------------------------------------------------

@@ -59,6 +59,13 @@ def main(argv=None):
     p.add_argument("--max-iter", type=int, default=80, help="--scf: iteration limit")
     p.add_argument("--guess", choices=["bare", "atomic"], default="bare",
                    help="--scf: bare-nucleus start or superposed atomic densities")
+    p.add_argument("--staged", action="store_true",
+                   help="--scf: HFSCF's integral inclusion stages from ILEV 1 (a deck's "
+                        "starting stage and level shifts when given)")
+    p.add_argument("--stage-iter", type=int, default=15,
+                   help="--staged: iteration limit of each stage before the last")
+    p.add_argument("--dtol", type=float, default=None,
+                   help="--scf: largest density-matrix change for convergence")
     p.add_argument("--wfn-in", help="--scf: start from this .wfn file")
     p.add_argument("--wfn-out", help="--scf: write the final eigenvectors as a .wfn file")
     p.add_argument("--build", choices=["coulomb", "breit", "both"], default="coulomb")
@@ -69,6 +76,7 @@ def main(argv=None):
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--no-racah1", action="store_true")
     p.add_argument("--gaunt", action="store_true")
+    p.add_argument("--verbose", action="store_true", help="--scf: print every iteration")
     a = p.parse_args(argv)
     if a.atoms:
         print(json.dumps(atoms_main(a)), flush=True)
@@ -76,11 +84,15 @@ def main(argv=None):
     if a.microbench:
         print(json.dumps(microbench_main(a)), flush=True)
         return
-    b = CASES[a.case]() if a.case else deck.read_deck(a.deck)
+    meta = {}
+    if a.case:
+        b = CASES[a.case]()
+    else:
+        b, meta = deck.read_deck(a.deck)
     if a.build != "coulomb" and b.hmlt < deck.HMLT["DHFR"]:
         b = dataclasses_replace(b, deck.HMLT["DHFB"])
     if a.scf:
-        print(json.dumps(scf_main(a, b)), flush=True)
+        print(json.dumps(scf_main(a, b, meta)), flush=True)
         return
     dent = deck.density(b, seed=a.seed, real=b.isym != 0)
     out = {"case": a.case or a.deck, "ndim": b.ndim, "shells": len(b.shells()),
@@ -163,11 +175,29 @@ def microbench_main(a):
             "quartets_per_s": nq / min(times), "device_status": _lib.device_status()}
 
 
-def scf_main(a, b):
+def stage_plan(meta, shift, stage_iter):
+    """HFSCF's stages before the last (:6038-6098) as DHFSCF.run's `stages`:
+    from the deck's starting stage (ILEV, :519-536) up to stage 2, each with
+    its level shift SHLEV and HFSCF's energy tolerance (ENRGLV1 = 1e-8,
+    ENRGLV2 = 5e-11, :5167-5168), and the shift of stage 3."""
+    shifts = meta.get("shifts") or (shift, shift, shift)
+    tols = {1: 1e-8, 2: 5e-11}
+    start = int(meta.get("ilev", 1))
+    plan = [(lv, shifts[lv - 1], tols[lv], stage_iter) for lv in (1, 2) if lv >= start]
+    return plan, shifts[2]
+
+
+def scf_main(a, b, meta=None):
     """Closed-shell DHF SCF of one molecule on the GPU (every step on the
-    device), FP64 or mixed precision as --precision says."""
+    device), FP64 or mixed precision as --precision says.  With a deck:
+    NCLS occupied spinors, its atoms' electron counts for the atomic start
+    and, with --staged, its stages and level shifts."""
     from .scf import DHFSCF
-    nocc = a.nocc or int(round(sum(b.znuc)))
+    meta = meta or {}
+    nocc = a.nocc or int(meta.get("ncls") or round(sum(b.znuc)))
+    stages, shift = None, a.shift
+    if a.staged:
+        stages, shift = stage_plan(meta, a.shift, a.stage_iter)
     s = DHFSCF(b, nocc, precision=a.precision, screen=a.screen or 1e-12,
                breit=False if a.no_breit else None, racah1=False)
     guess = None
@@ -177,10 +207,10 @@ def scf_main(a, b):
         guess = wfn.read_wfn(a.wfn_in, b.ndim)
     elif a.guess == "atomic":
         from .scf import atomic_guess
-        guess = atomic_guess(b)
+        guess = atomic_guess(b, nelec=meta.get("nelec"))
     t_guess = time.perf_counter() - t0
-    r = s.run(etol=a.etol, max_iter=a.max_iter, ndiis=a.ndiis, shift=a.shift, mom=a.mom,
-              guess=guess, wfn_out=a.wfn_out)
+    r = s.run(etol=a.etol, max_iter=a.max_iter, ndiis=a.ndiis, shift=shift, mom=a.mom,
+              guess=guess, wfn_out=a.wfn_out, dtol=a.dtol, stages=stages, verbose=a.verbose)
     r["guess"] = "wfn" if a.wfn_in else a.guess
     r["guess_s"] = t_guess
     s.close()
@@ -188,8 +218,9 @@ def scf_main(a, b):
     r["orbital_energies"] = r["orbital_energies"][-4:]
     r.update({"case": a.case or a.deck, "ndim": b.ndim, "nocc": nocc,
               "precision": a.precision, "breit": not a.no_breit and b.hmlt >= deck.HMLT["DHFB"],
-              "screen": a.screen or 1e-12, "shift": a.shift, "mom": a.mom, "ndiis": a.ndiis,
-              "iter_s": [h["s"] for h in hist],
+              "screen": a.screen or 1e-12, "shift": shift, "mom": a.mom, "ndiis": a.ndiis,
+              "stages": stages, "iter_s": [h["s"] for h in hist],
+              "ilev": [h["ilev"] for h in hist],
               "energies": [h["energy"] for h in hist]})
     return r
 

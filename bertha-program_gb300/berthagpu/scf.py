@@ -11,9 +11,10 @@ F C = S C E (ZHEGV, :5557) and DENSTY (:3580, D_ij = sum_occ conj(C_i) C_j
 over the lowest NOCC positive-energy states).  Everything stays on the
 device: the Fock build through the library's device entry points, the
 linear algebra (eigensolver, DIIS) through torch on the same stream, FP64.
-The reference's stage progression (ILEV 1..3), level shifting and damping
-only change the path to convergence; this driver starts from the
-bare-nucleus guess and runs every iteration at stage 3.
+The reference's stage progression (ILEV 1..3 with a level shift per
+stage, :6038-6110) is available as `stages`; without it every iteration
+runs at stage 3.  Stages, level shifts and the start only change the path
+to convergence, not the converged solution.
 """
 import time
 
@@ -50,6 +51,7 @@ class GPUBackend:
         self.fb.set_screening(screen)
         self.n = self.fb.ndim
         self.device = "cuda"
+        self.ilev = 3  # integral inclusion level of the Coulomb builds
         self.bufs = [self._mat() for _ in range(4)]
 
     def _mat(self):
@@ -71,7 +73,8 @@ class GPUBackend:
         bd, bj, bk, bb = self.bufs
         sp = self._stream()
         bd.copy_(D.T)
-        self.fb.clmfast_device(bd.data_ptr(), bj.data_ptr(), bk.data_ptr(), 3, self.n, sp)
+        self.fb.clmfast_device(bd.data_ptr(), bj.data_ptr(), bk.data_ptr(), self.ilev, self.n,
+                               sp)
         G = (bj - bk).T
         if self.breit:
             self.fb.brtfast_device(bd.data_ptr(), bb.data_ptr(), 3, self.n, sp)
@@ -100,7 +103,8 @@ class DHFSCF:
         self.n = self.backend.n
 
     def run(self, max_iter=60, etol=1e-9, ndiis=8, shift=0.5, mom=0, verbose=False,
-            guess=None, wfn_out=None, return_density=False, dtol=None, dc_first=None):
+            guess=None, wfn_out=None, return_density=False, dtol=None, dc_first=None,
+            stages=None):
         """Iterate to |dE| < etol and, with dtol, until the largest change of
         a density-matrix element between iterations is below dtol too, so
         that a converged energy does not depend on where a slowly drifting
@@ -125,7 +129,16 @@ class DHFSCF:
         its occupied states) or "atomic" (superposed atomic densities, see
         atomic_guess).  wfn_out: write the last eigenvalues and eigenvectors
         as a `.wfn` file (virtual eigenvalues without the level shift, as
-        HFSCF writes them)."""
+        HFSCF writes them).
+        stages: HFSCF's integral inclusion levels before the last one, as
+        (ilev, shift, tol, max_iter) tuples, e.g. ((1, 3.0, 1e-8, 12),
+        (2, 1.0, 5e-11, 15)): iterate with the Coulomb build at ILEV ilev
+        and level shift `shift` until the weighted energy difference
+        |dE| / (|E| + 1) falls below tol (HFSCF's ENRGLV1 = 1e-8 and
+        ENRGLV2 = 5e-11, :5167-5168) or the stage has run max_iter
+        iterations, then move to the next stage with a fresh DIIS subspace;
+        the last stage is ILEV 3 with `shift`, where the convergence tests
+        apply."""
         t = self.torch
         be = self.backend
         dev = be.device
@@ -182,6 +195,14 @@ class DHFSCF:
         staged = bool(dc_first) and getattr(be, "breit", False)
         if staged:
             be.breit = False
+        plan = [tuple(st) for st in (stages or ())]
+        si, n_stage = 0, 0
+
+        def enter_stage():
+            be.ilev = plan[si][0] if si < len(plan) else 3
+            return plan[si][1] if si < len(plan) else shift
+
+        cur_shift = enter_stage()
         for it in range(1, max_iter + 1):
             ti = time.perf_counter()
             G = be.fock(D)
@@ -191,11 +212,11 @@ class DHFSCF:
             F = H1 + G
             # ENRGIES on the density that built F
             energy = enuc + float(t.sum(D * (H1 + 0.5 * G)).real.item())
-            if shift and it > 1:
+            if cur_shift and it > 1 and "vir" in state:
                 # LEVSHFT (:3641): F += SHLV sum_vir (S c_v)(S c_v)^+ over the
                 # positive-energy virtuals of the last diagonalisation
                 A = S @ state["vir"]
-                F = F + shift * (A @ A.conj().T)
+                F = F + cur_shift * (A @ A.conj().T)
             # DIIS on the commutator F P S - S P F, P = D^T
             P = D.T
             err = F @ P @ S - S @ P @ F
@@ -227,9 +248,23 @@ class DHFSCF:
             iters.append({"iter": it, "energy": energy, "de": de, "ddens": ddens,
                           "err": float(err.abs().max().item()),
                           "breit": bool(getattr(be, "breit", False)),
+                          "ilev": int(getattr(be, "ilev", 3)), "shift": cur_shift,
                           "s": time.perf_counter() - ti})
             if verbose:
                 print(iters[-1], flush=True)
+            if si < len(plan):
+                # HFSCF's stage test (:6038-6098) on the weighted energy
+                # difference
+                n_stage += 1
+                if ((de is not None and abs(de) / (abs(energy) + 1.0) < plan[si][2])
+                        or n_stage >= plan[si][3]):
+                    si, n_stage = si + 1, 0
+                    cur_shift = enter_stage()
+                    hist_F, hist_E = [], []
+                    last = None
+                else:
+                    last = energy
+                continue
             if staged and not be.breit:
                 if last is not None and abs(de) < dc_first:
                     # the Breit term from the next build on
@@ -244,16 +279,18 @@ class DHFSCF:
             last = energy
         if staged:
             be.breit = True
+        final_stage = si >= len(plan)
+        be.ilev = 3
         if wfn_out:
             n = self.n
             e = eps.cpu().numpy().copy()
             Cn = C.cpu().numpy()
-            if shift and len(iters) > 1:
+            if cur_shift and len(iters) > 1:
                 vir = np.ones(len(e), bool)
                 vir[:nneg] = False
                 occ_e = sorted(e[nneg:])[:self.nocc]
                 vir &= ~np.isin(e, occ_e)
-                e[vir] -= shift
+                e[vir] -= cur_shift
             # the orthogonaliser may drop near-singular directions: pad to
             # NDIM records with zero vectors
             eign = np.zeros(n)
@@ -265,7 +302,8 @@ class DHFSCF:
                "converged": bool(iters and iters[-1]["de"] is not None
                                  and abs(iters[-1]["de"]) < etol
                                  and (dtol is None or iters[-1]["ddens"] < dtol)
-                                 and (not staged or iters[-1]["breit"])),
+                                 and (not staged or iters[-1]["breit"])
+                                 and final_stage),
                "density_change": iters[-1]["ddens"] if iters else None,
                "commutator": iters[-1]["err"] if iters else None,
                "oneel_s": t_one, "fock_s": t_fock, "linalg_s": t_lin,
@@ -291,7 +329,7 @@ class DHFSCF:
         self.backend.close()
 
 
-def atomic_guess(basis, torch=None, backend_factory=None, max_iter=25, etol=1e-6):
+def atomic_guess(basis, torch=None, backend_factory=None, max_iter=25, etol=1e-6, nelec=None):
     """Starting density of a molecule from SCFs of its atoms (the role of the
     atomic wavefunctions the reference reads from bertha-atomic): for every
     centre, a Dirac-Coulomb SCF of the centre's own basis functions with
@@ -300,7 +338,8 @@ def atomic_guess(basis, torch=None, backend_factory=None, max_iter=25, etol=1e-6
     on the centre's rows and columns of the molecular layout (FOCKIND).
     Centres with the same charge and exponents share one atomic SCF.
     backend_factory(atom) makes the Fock-build backend of an atom (default:
-    the GPU library)."""
+    the GPU library).  nelec: electrons per centre instead of Z (the
+    electron counts of a deck's atomic configurations, e.g. an ion's)."""
     if torch is None:
         import torch as _t
         torch = _t
@@ -312,10 +351,11 @@ def atomic_guess(basis, torch=None, backend_factory=None, max_iter=25, etol=1e-6
             dens.append(None)
             continue
         atom = wfn.atom_of_centre(basis, c, hmlt=hm)
-        key = (z, atom.ex.tobytes(), atom.nfn.tobytes())
+        ne = z if nelec is None else int(nelec[c])
+        key = (z, ne, atom.ex.tobytes(), atom.nfn.tobytes())
         if key not in cache:
             be = backend_factory(atom) if backend_factory else None
-            s = DHFSCF(atom, nocc=z, screen=1e-12, racah1=False, torch=torch, backend=be)
+            s = DHFSCF(atom, nocc=ne, screen=1e-12, racah1=False, torch=torch, backend=be)
             r = s.run(max_iter=max_iter, etol=etol, mom=2, return_density=True)
             s.close()
             cache[key] = r["density"].cpu().numpy()

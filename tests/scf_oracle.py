@@ -16,6 +16,7 @@ class OracleBackend:
         self.racah1 = racah1
         self.breit = breit
         self.n = basis.ndim
+        self.ilev = 3
 
     def oneel(self):
         b = self.basis
@@ -24,7 +25,7 @@ class OracleBackend:
 
     def fock(self, D):
         d = np.asfortranarray(D.numpy())
-        gd, gx = orc.clmfast(self.basis, d, 3, racah1=self.racah1)
+        gd, gx = orc.clmfast(self.basis, d, self.ilev, racah1=self.racah1)
         g = gd - gx
         if self.breit:
             g = g - orc.brtfast(self.basis, d, 3, racah1=self.racah1)

@@ -103,6 +103,7 @@ AUFBAU,9
     assert np.allclose(b.ex[0, 1, :2], [0.2, 0.6])
     assert np.allclose(b.ex[1, 0, :2], [15.0, 0.3])
     assert meta["ilev"] == 1 and meta["ncls"] == 10
+    assert meta["shifts"] == (1.0, 1.0, 0.5) and meta["nelec"] == (1, 9)
     assert b.ndim == 4 * (3 + 3 * 2) + 4 * 2
 
 

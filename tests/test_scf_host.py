@@ -41,3 +41,28 @@ def test_helium_maximum_overlap_and_wfn(tmp_path):
     r2 = scf.run(max_iter=30, etol=1e-10, guess=(eign, coef))
     assert r2["converged"] and r2["iterations"] <= 3
     assert abs(r2["energy"] - r["energy"]) < 1e-9
+
+
+def test_staged_inclusion_reaches_the_same_solution():
+    """HFSCF's integral inclusion stages (ILEV 1 with a 3 Eh level shift,
+    ILEV 2 with 1 Eh, then ILEV 3) change the path, not the converged
+    Dirac-Coulomb energy: H2 at 1.4 bohr, staged and unstaged."""
+    h = {0: deck.geometric(0.08, 3.0, 6), 1: [0.6]}
+    h2 = deck.make_basis([((0.0, 0.0, 0.0), h), ((0.0, 0.0, 1.4), h)], hmlt="DHFR")
+    h2.znuc, h2.anuc = (1.0, 1.0), (1.0, 1.0)
+    out = {}
+    for staged in (False, True):
+        scf = DHFSCF(h2, nocc=2, torch=torch, backend=OracleBackend(h2, racah1=False))
+        r = scf.run(max_iter=60, etol=1e-11, dtol=1e-8, shift=0.0,
+                    stages=((1, 3.0, 1e-8, 12), (2, 1.0, 5e-11, 15)) if staged else None)
+        assert r["converged"], (staged, r["history"][-3:])
+        out[staged] = r
+    levels = [h["ilev"] for h in out[True]["history"]]
+    assert levels[0] == 1 and 2 in levels and levels[-1] == 3
+    assert levels == sorted(levels)
+    assert all(h["ilev"] == 3 for h in out[False]["history"])
+    assert abs(out[True]["energy"] - out[False]["energy"]) < 1e-9
+    # stage 1 leaves out the two-centre (LL|SS), (SS|LL) and (SS|SS) terms:
+    # its energies differ from the full Hamiltonian's
+    e1 = [h["energy"] for h in out[True]["history"] if h["ilev"] == 1][-1]
+    assert abs(e1 - out[False]["energy"]) > 1e-7

@@ -1,0 +1,90 @@
+"""The reference's own recorded Dirac-Coulomb SCF of YbF+ (R = 3.88 bohr,
+NDIM 1052, Yb 26s26p15d8f / F 10s6p with exponents up to 1.6e9, Gaussian
+nuclei) as a golden result for the whole Fock-build chain: basis and
+kinetic balance, one-electron matrices, the two-electron Coulomb terms
+(the one-centre ones by the MD route where the reference used its Racah
+route) and the closed-shell SCF.  The fixture `golden/ybf_plus_388.json`
+holds the deck's data and the energies the reference printed at every
+iteration (written by `golden/make_ybf_golden.py` from the deck and the
+log of its run).
+
+The reference's run stopped with its last three stage-3 energies spread
+over 4.4e-3 Eh (-14167.0575 to -14167.0618), so its total energy is known
+to a few mEh, not to its printed digits; the test bounds follow from that
+spread.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from berthagpu import deck
+from berthagpu.scf import CLIGHT, nuclear_repulsion
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ybf_plus_388.json")
+
+
+def _gold():
+    with open(GOLD) as f:
+        return json.load(f)
+
+
+def _basis(g):
+    cents = [(c["xyz"], {int(l): e for l, e in c["exponents"].items()}) for c in g["centres"]]
+    b = deck.make_basis(cents, hmlt=g["hamiltonian_of_scf"], name="YbFplus_388")
+    b.znuc = tuple(c["z"] for c in g["centres"])
+    b.anuc = tuple(c["mass"] for c in g["centres"])
+    return b
+
+
+def test_fixture_basis_and_nuclei():
+    """The fixture's basis gives the reference's Fock-matrix dimension, its
+    geometry the printed nucleus-nucleus energy, and its energy terms add
+    up to each printed total (ENRGIES' sum)."""
+    g = _gold()
+    b = _basis(g)
+    assert b.ndim == g["ndim"] == 1052
+    assert abs(g["speed_of_light"] - CLIGHT) < 1e-10
+    for it in g["iterations"]:
+        assert abs(nuclear_repulsion(b) - it["enuc"]) < 1e-9
+        tot = it["enuc"] + it["enuc_el"] + it["ekin"] + it["gdir"] - it["gxch"]
+        assert abs(tot - it["total"]) < 1e-8
+    stage3 = [it["total"] for it in g["iterations"] if it["ilev"] == 3]
+    assert len(stage3) == 3 and max(stage3) - min(stage3) < 5e-3
+
+
+@pytest.mark.gpu
+def test_ybf_dirac_coulomb_scf_matches_reference():
+    """FP64 SCF on the GPU from the deck's atomic configurations (Yb 68 and
+    F 10 electrons), through HFSCF's stages with the deck's level shifts
+    (3, 1, 0 Eh), compared with the reference's last stage-3 iteration."""
+    import torch
+
+    from berthagpu.scf import DHFSCF, atomic_guess
+    g = _gold()
+    b = _basis(g)
+    nelec = [c["nelec"] for c in g["centres"]]
+    guess = atomic_guess(b, torch=torch, nelec=nelec)
+    scf = DHFSCF(b, nocc=g["ncls"], precision="fp64", screen=1e-12, racah1=False, torch=torch)
+    sh = g["shifts"]
+    r = scf.run(max_iter=50, etol=1e-7, shift=sh[2], guess=guess, verbose=True,
+                stages=((1, sh[0], 1e-8, 12), (2, sh[1], 5e-11, 15)))
+    scf.close()
+    last = g["iterations"][-1]
+    ref_eps = np.sort([s["energy"] for s in g["spinors_last"]])[:g["ncls"]]
+    eps = np.asarray(r["orbital_energies"])
+    hist = r["history"]
+    print(json.dumps({"energy": r["energy"], "iterations": r["iterations"],
+                      "converged": r["converged"], "last_de": hist[-1]["de"],
+                      "ddens": hist[-1]["ddens"], "fock_s": r["fock_s"],
+                      "linalg_s": r["linalg_s"],
+                      "delta_total": r["energy"] - last["total"],
+                      "delta_spinors_max": float(np.abs(eps - ref_eps).max()),
+                      "delta_spinors": (eps - ref_eps).tolist(),
+                      "ilev": [h["ilev"] for h in hist],
+                      "energies": [h["energy"] for h in hist]}), flush=True)
+    assert hist[-1]["ilev"] == 3
+    assert abs(hist[-1]["de"]) < 1e-5
+    assert abs(r["energy"] - last["total"]) < 1e-2
+    assert np.abs(eps - ref_eps).max() < 1e-2
