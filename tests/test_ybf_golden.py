@@ -9,9 +9,13 @@ iteration (written by `golden/make_ybf_golden.py` from the deck and the
 log of its run).
 
 The reference's run stopped with its last three stage-3 energies spread
-over 4.4e-3 Eh (-14167.0575 to -14167.0618), so its total energy is known
-to a few mEh, not to its printed digits; the test bounds follow from that
-spread.
+over 4.4e-3 Eh (-14167.0575 to -14167.0618) and its occupied spinor
+energies still moving by up to 5.0e-5 Eh per iteration, so its results
+are known to those amounts, not to their printed digits; the test bounds
+follow from them.  (Measured on a GB300: the GPU SCF ends at
+-14167.060155 Eh, inside the band and 1.7e-3 Eh above the last printed
+total, with all 78 occupied spinor energies within 1.3e-5 Eh of the
+reference's.)
 """
 import json
 import os
@@ -84,7 +88,11 @@ def test_ybf_dirac_coulomb_scf_matches_reference():
                       "delta_spinors": (eps - ref_eps).tolist(),
                       "ilev": [h["ilev"] for h in hist],
                       "energies": [h["energy"] for h in hist]}), flush=True)
-    assert hist[-1]["ilev"] == 3
-    assert abs(hist[-1]["de"]) < 1e-5
-    assert abs(r["energy"] - last["total"]) < 1e-2
-    assert np.abs(eps - ref_eps).max() < 1e-2
+    assert r["converged"] and hist[-1]["ilev"] == 3
+    stage3 = [it["total"] for it in g["iterations"] if it["ilev"] == 3]
+    assert min(stage3) - 1e-3 <= r["energy"] <= max(stage3) + 1e-3
+    # the reference's own last-iteration change of its spinor energies
+    prev_eps = np.sort([s["energy"] for s in g["spinors_previous"]])[:g["ncls"]]
+    drift = np.abs(ref_eps - prev_eps).max()
+    assert drift < 6e-5
+    assert np.abs(eps - ref_eps).max() < drift
