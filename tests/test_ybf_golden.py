@@ -96,3 +96,18 @@ def test_ybf_dirac_coulomb_scf_matches_reference():
     drift = np.abs(ref_eps - prev_eps).max()
     assert drift < 6e-5
     assert np.abs(eps - ref_eps).max() < drift
+
+
+def test_stage_plan_follows_the_deck():
+    """The run module's HFSCF stage plan: from the deck's starting stage,
+    its level shifts and HFSCF's stage tolerances; stage 3's shift is the
+    last one."""
+    from berthagpu.run import stage_plan
+    plan, last = stage_plan({"ilev": 1, "shifts": (3.0, 1.0, 0.0)}, 0.5, 12)
+    assert plan == [(1, 3.0, 1e-8, 12), (2, 1.0, 5e-11, 12)] and last == 0.0
+    plan, last = stage_plan({"ilev": 2, "shifts": (3.0, 1.0, 0.25)}, 0.5, 9)
+    assert plan == [(2, 1.0, 5e-11, 9)] and last == 0.25
+    plan, last = stage_plan({"ilev": 3, "shifts": (3.0, 1.0, 0.0)}, 0.5, 9)
+    assert plan == [] and last == 0.0
+    plan, last = stage_plan({}, 0.5, 9)
+    assert [p[0] for p in plan] == [1, 2] and last == 0.5
