@@ -685,6 +685,14 @@ void fock_full(const Basis &b, const Opts &o, const Mat &D, Mat &GD, Mat &GX) {
   if (o.hmlt == 0) tcomp = {0};
   else tcomp = {1, 0};  // SS then LL, as ITSTRT=4, ITSKIP=-3
   const Cart &C = cart();
+  // OpenMP inside each class: every thread digests into its own matrices,
+  // summed in thread order at the end (the serial result up to rounding)
+  int nthr = 1;
+#ifdef _OPENMP
+  nthr = omp_get_max_threads();
+#endif
+  const size_t nn = (size_t)b.ndim * b.ndim;
+  std::vector<std::vector<cplx>> accd(nthr), accx(nthr);
   for (int ca = 0; ca < b.ncnt; ++ca)
   for (int cb = 0; cb < b.ncnt; ++cb)
   for (int cc = 0; cc < b.ncnt; ++cc)
@@ -711,8 +719,11 @@ void fock_full(const Basis &b, const Opts &o, const Mat &D, Mat &GD, Mat &GX) {
         std::vector<double> R((size_t)nij * nkl * ntuv(lam));
         const double *A = &b.xyz[3 * ca], *B = &b.xyz[3 * cb];
         const double *Cc = &b.xyz[3 * cc], *Dd = &b.xyz[3 * cd];
-        for (int i = 0; i < Eab.na; ++i)
-        for (int j = 0; j < Eab.nb; ++j) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic)
+#endif
+        for (int ijr = 0; ijr < nij; ++ijr) {
+          int i = ijr / Eab.nb, j = ijr % Eab.nb;
           double ei = b.ex[ca][lA][i], ej = b.ex[cb][lB][j], eij = ei + ej;
           double P[3];
           for (int x = 0; x < 3; ++x) P[x] = (A[x] * ei + B[x] * ej) / eij;
@@ -730,14 +741,31 @@ void fock_full(const Basis &b, const Opts &o, const Mat &D, Mat &GD, Mat &GX) {
             for (int n = 0; n < ntuv(lam); ++n) r[n] *= pre;
           }
         }
-        std::vector<cplx> g11((size_t)nkl * ncd), g21((size_t)nkl * ncd);
         int offab = t1 ? b.nskp : 0, offcd = t2 ? b.nskp : 0;
-        for (int ia = 0; ia < Eab.nlab_a; ++ia)
-        for (int ib = 0; ib < Eab.nlab_b; ++ib) {
+        const long long nwork = (long long)Eab.nlab_a * Eab.nlab_b * nij;
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+        {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        if (accd[tid].empty()) {
+          accd[tid].assign(nn, cplx(0));
+          accx[tid].assign(nn, cplx(0));
+        }
+        Mat TD{accd[tid].data(), b.ndim}, TX{accx[tid].data(), b.ndim};
+        std::vector<cplx> g11((size_t)nkl * ncd), g21((size_t)nkl * ncd);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic)
+#endif
+        for (long long w = 0; w < nwork; ++w) {
+          int ij = (int)(w % nij), iab = (int)(w / nij);
+          int ia = iab / Eab.nlab_b, ib = iab % Eab.nlab_b;
+          int i = ij / Eab.nb, j = ij % Eab.nb;
           const Label &LA = Eab.la[ia], &LB = Eab.lb[ib];
-          for (int i = 0; i < Eab.na; ++i)
-          for (int j = 0; j < Eab.nb; ++j) {
-            int ij = i * Eab.nb + j;
+          {
             const cplx *e11 = Eab.at(ia, ib, 0, ij), *e21 = Eab.at(ia, ib, 1, ij);
             // first contraction G(kl, t'u'v') for all kl
             for (int kl = 0; kl < nkl; ++kl) {
@@ -776,13 +804,22 @@ void fock_full(const Basis &b, const Opts &o, const Mat &D, Mat &GD, Mat &GX) {
                              b.lrge[cc][LC.ka][2 * LC.ma - 1] + offcd + k};
                 int nd[2] = {b.lrge[cd][LD.ka][2 * LD.ma - 2] + offcd + l,
                              b.lrge[cd][LD.ka][2 * LD.ma - 1] + offcd + l};
-                digest(rr, na, nb, nc, nd, D, GD, GX, o.isym);
+                digest(rr, na, nb, nc, nd, D, TD, TX, o.isym);
               }
             }
           }
         }
+        }  // omp parallel
       }
     }
+  }
+  for (int t = 0; t < nthr; ++t) {
+    if (accd[t].empty()) continue;
+    for (int j = 0; j < b.ndim; ++j)
+      for (int i = 0; i < b.ndim; ++i) {
+        GD(i, j) += accd[t][i + (size_t)b.ndim * j];
+        GX(i, j) += accx[t][i + (size_t)b.ndim * j];
+      }
   }
 }
 

@@ -52,7 +52,7 @@ def _worker(rank, world, port, out):
 
 def test_two_rank_replicas():
     world = 2
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of a threaded process
     out = mgr.dict()
     mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
     for r in range(world):
