@@ -98,3 +98,33 @@ def test_atomic_guess_scf_on_oracle_backend():
     r1 = scf.run(max_iter=40, etol=1e-10, guess=D0)
     assert r0["converged"] and r1["converged"]
     assert abs(r0["energy"] - r1["energy"]) < 1e-8
+
+
+def test_atomic_guess_energy_of_distant_ions():
+    """Two atoms 30 bohr apart with s, p, d (and f) functions, one of them
+    an ion (the deck's electron count): the molecule's energy at the
+    superposed atomic densities is the sum of the atoms' SCF energies plus
+    the ions' Coulomb energy, which checks the placement of every (kappa, m)
+    block of both centres."""
+    A = {0: deck.geometric(0.3, 2.5, 6), 1: deck.geometric(0.5, 2.5, 3), 2: [1.2]}
+    B = {0: deck.geometric(0.2, 2.5, 6), 1: deck.geometric(0.4, 2.5, 3), 2: [0.9], 3: [1.5]}
+    R = np.array([0.3, 0.4, 30.0])
+    b = deck.make_basis([((0, 0, 0), A), (tuple(R), B)], hmlt="DHFR")
+    b.znuc, b.anuc = (10.0, 12.0), (20.0, 24.0)
+    nelec = (10, 10)  # neon-like atom and a doubly charged magnesium-like ion
+    factory = lambda atom: OracleBackend(atom, racah1=False)  # noqa: E731
+    e_atoms = []
+    for c in range(2):
+        atom = wfn.atom_of_centre(b, c, hmlt="DHFR")
+        r = DHFSCF(atom, nocc=nelec[c], torch=torch, backend=factory(atom)).run(
+            max_iter=40, etol=1e-10, mom=2)
+        assert r["converged"]
+        e_atoms.append(r["energy"])
+    D0 = atomic_guess(b, torch=torch, backend_factory=factory, max_iter=40, etol=1e-10,
+                      nelec=nelec)
+    S = factory(b).oneel()[0].numpy()
+    assert abs(np.sum(D0 * S).real - sum(nelec)) < 1e-8  # ENRGIES' sum with the overlap
+    e = DHFSCF(b, nocc=20, torch=torch, backend=factory(b)).energy_at(torch.as_tensor(D0))
+    # the neutral atom sees the ion's charge only through its own tails:
+    # the remaining interaction is far below the checked bound
+    assert abs(e - sum(e_atoms)) < 1e-6, (e, sum(e_atoms))
