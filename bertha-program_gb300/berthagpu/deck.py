@@ -132,9 +132,10 @@ def read_deck(path):
 
     Supports the OPTIMISED, GEOMETRIC and EVENTEMPR basis types.  Returns
     (basis, meta) where meta holds the remaining fields: the calculation
-    tree, NCLS (closed-shell spinors), the starting stage ILEV, READIN, the
-    level shifts SHLEV(1..3) and each centre's electron count IQNC (the
-    atomic configuration's, :313-314).
+    tree, NCLS (closed-shell spinors), the open-shell details of an
+    open-shell deck (NOPN, NOELEC, ACFF, BCFF, IOPN; None when closed), the
+    starting stage ILEV, READIN, the level shifts SHLEV(1..3) and each
+    centre's electron count IQNC (the atomic configuration's, :313-314).
     """
     with open(path) as f:
         lines = [ln for ln in f.read().splitlines() if ln.strip()]
@@ -183,7 +184,20 @@ def read_deck(path):
         centres.append((pos, exps))
     rec(); shl = rec()
     ncls = int(shl[0])
-    rec(); shifts = tuple(_num(t) for t in rec()[:3])
+    nopn = int(shl[1]) if len(shl) > 1 else 0
+    noelec = int(shl[2]) if len(shl) > 2 else 0
+    open_shell = None
+    title = rec()
+    if nopn > 0:
+        open_shell = {"nopn": nopn, "noelec": noelec, "acff": None, "bcff": None, "iopn": None}
+        if "LEVEL SHIFT" not in " ".join(title).upper():
+            # ACFF, BCFF and the open-shell orbitals IOPN (:486-489); older
+            # decks go straight on to the level shifts
+            t = rec()
+            open_shell.update(acff=_num(t[0]), bcff=_num(t[1]),
+                              iopn=[int(_num(x)) for x in t[2:2 + nopn]])
+            title = rec()
+    shifts = tuple(_num(t) for t in rec()[:3])
     rec(); ilev = int(rec()[0])
     basis = make_basis(centres, hmlt=hmlt, name=molcl)
     basis.znuc, basis.anuc = tuple(znuc), tuple(anuc)
@@ -191,8 +205,8 @@ def read_deck(path):
         ilev = 1
     if ncnt == 1 or readin:
         ilev = 3
-    return basis, {"tree": tree, "ncls": ncls, "ilev": ilev, "readin": readin,
-                   "shifts": shifts, "nelec": tuple(nelec)}
+    return basis, {"tree": tree, "ncls": ncls, "open_shell": open_shell, "ilev": ilev,
+                   "readin": readin, "shifts": shifts, "nelec": tuple(nelec)}
 
 
 # ---------------------------------------------------------------------------

@@ -194,6 +194,9 @@ def scf_main(a, b, meta=None):
     and, with --staged, its stages and level shifts."""
     from .scf import DHFSCF
     meta = meta or {}
+    if meta.get("open_shell"):
+        raise SystemExit("open-shell decks (NOPN > 0) need QDIR/QXCH, which are not built; "
+                         "the SCF driver is closed-shell")
     nocc = a.nocc or int(meta.get("ncls") or round(sum(b.znuc)))
     stages, shift = None, a.shift
     if a.staged:

@@ -107,6 +107,50 @@ AUFBAU,9
     assert b.ndim == 4 * (3 + 3 * 2) + 4 * 2
 
 
+def test_deck_reader_open_shell(tmp_path):
+    """NOPN > 0: ACFF, BCFF and IOPN follow (:486-489), or, in older
+    decks, the level shifts follow directly."""
+    head = """'OUTPUT STRING'
+Cs
+'TREE'
+HFSCF
+'HAMILTONIAN'
+DHFR
+'CONTINUING'
+.FALSE.
+'NUMBER OF ATOMIC CENTRES'
+1
+'CENTER 1'
+'CARTESIAN COORDINATES'
+0.0,0.0,0.0
+'NUCLEUS'
+GAUSS,55,132.9
+'ATOMIC BASIS: TYPE AND LMAX'
+GEOMETRIC,1
+'ELECTRON CONFIGURATION'
+AUFBAU,55
+'BASIS SET EXPONENTS'
+0.01 2.1 30
+0.01 2.1 20
+'NUMBER OF CLOSED- AND OPEN-SHELL ORBITALS AND OPEN-SHELL ELECTRONS'
+54,2,1
+"""
+    tail = """'LEVEL SHIFT PARAMETER FOR EACH INTEGRAL INCLUSION LEVEL'
+0.3,0.3,0.2
+'STARTING STAGE'
+1
+"""
+    new = head + "'SPECIFY OPEN-SHELL INFORMATION'\n0.0D0,-2.0D0,55,56\n" + tail
+    for text, iopn in ((new, [55, 56]), (head + tail, None)):
+        p = tmp_path / "cs.inp"
+        p.write_text(text)
+        b, meta = deck.read_deck(str(p))
+        assert meta["ncls"] == 54 and meta["shifts"] == (0.3, 0.3, 0.2)
+        o = meta["open_shell"]
+        assert o["nopn"] == 2 and o["noelec"] == 1 and o["iopn"] == iopn
+        assert b.nfn[0, 0] == 30 and abs(b.ex[0, 0, 29] - 0.01 * 2.1 ** 29) < 1e-6
+
+
 def test_missing_library_fails_loudly(monkeypatch):
     monkeypatch.setattr(_lib, "_L", None)
     monkeypatch.setattr(_lib, "LIB", "/nonexistent/libberthagpu.so")
