@@ -218,7 +218,9 @@ int bertha_gpu_oneel_device(bg_ctx *ctx, const double *znuc, const double *xi,
 
 /* Fock-build digestion over an explicit list of ordered shell quartets
  * (device array, 4 ints each: shell a, b, c, d as numbered by
- * bertha_gpu_shells) with component classes t1 (ab) and t2 (cd), 0 = LL and
+ * bertha_gpu_shells, each in [0, nshell); the device list is not checked,
+ * so an index outside that range reads past the shell tables) with
+ * component classes t1 (ab) and t2 (cd), 0 = LL and
  * 1 = SS.  Adds, without zeroing, J(a,b) += (ab|cd) D(c,d) and
  * K(a,d) += (ab|cd) D(c,b) over every spinor label and m-sign of each
  * quartet: batch types 1 and 5 of CLMMTG/CLMMTZ (bertha-scf.f:13841). */
