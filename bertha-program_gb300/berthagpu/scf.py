@@ -77,7 +77,8 @@ class GPUBackend:
                                sp)
         G = (bj - bk).T
         if self.breit:
-            self.fb.brtfast_device(bd.data_ptr(), bb.data_ptr(), 3, self.n, sp)
+            # multi-centre Breit quartets from ILEV 3 on, as BRTFAST (:17231)
+            self.fb.brtfast_device(bd.data_ptr(), bb.data_ptr(), self.ilev, self.n, sp)
             G = G - bb.T
         return G
 

@@ -28,7 +28,7 @@ class OracleBackend:
         gd, gx = orc.clmfast(self.basis, d, self.ilev, racah1=self.racah1)
         g = gd - gx
         if self.breit:
-            g = g - orc.brtfast(self.basis, d, 3, racah1=self.racah1)
+            g = g - orc.brtfast(self.basis, d, self.ilev, racah1=self.racah1)
         return torch.from_numpy(np.ascontiguousarray(g))
 
     def sync(self):

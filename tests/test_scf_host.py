@@ -43,16 +43,20 @@ def test_helium_maximum_overlap_and_wfn(tmp_path):
     assert abs(r2["energy"] - r["energy"]) < 1e-9
 
 
-def test_staged_inclusion_reaches_the_same_solution():
+@pytest.mark.parametrize("hmlt", ["DHFR", "DHFB"])
+def test_staged_inclusion_reaches_the_same_solution(hmlt):
     """HFSCF's integral inclusion stages (ILEV 1 with a 3 Eh level shift,
-    ILEV 2 with 1 Eh, then ILEV 3) change the path, not the converged
-    Dirac-Coulomb energy: H2 at 1.4 bohr, staged and unstaged."""
+    ILEV 2 with 1 Eh, then ILEV 3; multi-centre Breit terms from ILEV 3 on)
+    change the path, not the converged energy: H2 at 1.4 bohr, staged and
+    unstaged, Dirac-Coulomb and Dirac-Coulomb-Breit."""
     h = {0: deck.geometric(0.08, 3.0, 6), 1: [0.6]}
-    h2 = deck.make_basis([((0.0, 0.0, 0.0), h), ((0.0, 0.0, 1.4), h)], hmlt="DHFR")
+    h2 = deck.make_basis([((0.0, 0.0, 0.0), h), ((0.0, 0.0, 1.4), h)], hmlt=hmlt)
     h2.znuc, h2.anuc = (1.0, 1.0), (1.0, 1.0)
+    breit = hmlt == "DHFB"
     out = {}
     for staged in (False, True):
-        scf = DHFSCF(h2, nocc=2, torch=torch, backend=OracleBackend(h2, racah1=False))
+        scf = DHFSCF(h2, nocc=2, torch=torch,
+                     backend=OracleBackend(h2, racah1=False, breit=breit))
         r = scf.run(max_iter=60, etol=1e-11, dtol=1e-8, shift=0.0,
                     stages=((1, 3.0, 1e-8, 12), (2, 1.0, 5e-11, 15)) if staged else None)
         assert r["converged"], (staged, r["history"][-3:])
