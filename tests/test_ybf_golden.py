@@ -111,3 +111,37 @@ def test_stage_plan_follows_the_deck():
     assert plan == [] and last == 0.0
     plan, last = stage_plan({}, 0.5, 9)
     assert [p[0] for p in plan] == [1, 2] and last == 0.5
+
+
+def test_log_parser_reads_iterations_and_spinors():
+    """The fixture script's parser on a two-iteration excerpt in the log's
+    layout: iteration headers, spinor table rows, ENRGIES' terms and the
+    inclusion level."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_ybf_golden import parse_log
+    block = """
+                           Iteration number  {it}
+ ========================================================================
+ Orb.  Centre    Term sym.   m_j              Energy (au)      Population
+ ------------------------------------------------------------------------
+   1   1 (Yb)     1s_1/2    -1/2       -2268.0932706{d}      0.99999999
+   2   2 (F )     2p_3/2     3/2          -0.7287{d}      0.50165025
+ ========================================================================
+ Nucleus-nucleus             (N)                         162.371134020619
+ Electron-nucleus            (V)                      -49659.30514789204{d}
+ Electron kinetic            (T)                       29887.61797559624{d}
+ Coulomb direct (closed)     (GD)                       5738.70418349756{d}
+ Coulomb exchange (closed)   (GX)                        298.44982271876{d}
+ Molecule total                                       -14169.06167749638{d}
+ Iteration number                                                      {it}
+ Integral inclusion level                                               {lv}
+"""
+    text = block.format(it=1, d=1, lv=1) + block.format(it=12, d=2, lv=3)
+    its = parse_log(text)
+    assert [i["iter"] for i in its] == [1, 12] and [i["ilev"] for i in its] == [1, 3]
+    assert its[1]["terms"]["total"] == -14169.061677496382
+    assert its[0]["terms"]["gxch"] == 298.449822718761
+    sp = its[1]["spinors"]
+    assert len(sp) == 2 and sp[0]["term"] == "1s_1/2" and sp[1]["centre"] == 2
+    assert sp[1]["energy"] == -0.72872 and sp[1]["mj"] == "3/2"
