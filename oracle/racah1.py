@@ -231,11 +231,12 @@ def kappa_of(ka):
     return ka // 2 if ka % 2 == 0 else -(ka // 2) - 1
 
 
-def coulomb1(basis, dent, lrge):
+def coulomb1(basis, dent, lrge, pairs=None):
     """GDIR and GXCH (full NDIM x NDIM) of a one-centre basis (centre 0)
     for the density DENT, by COULOMB1's Racah route; lrge[0, KA, slot] is
     the first large-component Fock index of the (KA, m) block, slot =
-    2|m| - 1 + (m > 0) - 1 (FOCKIND)."""
+    2|m| - 1 + (m > 0) - 1 (FOCKIND).  pairs: only these (KA, KB) blocks
+    (the contributions of disjoint sets of pairs add up to the whole)."""
     n = dent.shape[0]
     nskp = n // 2
     gd = np.zeros((n, n), dtype=complex)
@@ -258,6 +259,8 @@ def coulomb1(basis, dent, lrge):
 
     for ka in kas:
         for kb in kas:
+            if pairs is not None and (ka, kb) not in pairs:
+                continue
             for kc in kas:
                 for kd in kas:
                     kqn = [kappa_of(k) for k in (ka, kb, kc, kd)]

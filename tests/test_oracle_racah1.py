@@ -88,3 +88,38 @@ def test_breit_one_centre_keeps_magnetic_terms():
     blk = np.ix_(kap == 1, kap == -2)
     assert np.abs(bx[blk]).max() > 1e-3
     assert np.abs(bx[blk] - racah1.breit1(b, d, lrge)[blk]).max() < 1e-12
+
+
+def test_reference_default_route_equals_md_route_on_a_molecule():
+    """A diatomic by the reference's default route (CLMFAST with RACAH1 on
+    for the multi-centre terms, COULOMB1 on each centre, as HFSCF calls them
+    at :5401-5421) and by the MD route throughout (RACAH1 off, the GPU
+    library's route): the same two-electron Fock matrix, on densities with
+    the molecule's symmetry (superposed atomic densities and the SCF's
+    first iterations).  (CLMFAST's real digestion for linear molecules
+    assumes that symmetry; COULOMB1's digestion does not, so the bound
+    allows for the eigensolver's rounding-level breaking of it.)"""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    import torch
+
+    from berthagpu.scf import DHFSCF, atomic_guess
+    from scf_oracle import OracleBackend, ReferenceRouteBackend
+    # closed-shell atoms in these functions, so that the atomic densities
+    # are spherical (a partly filled degenerate shell would break the
+    # symmetry the real digestion assumes)
+    A = {0: deck.geometric(0.3, 2.5, 4), 1: deck.geometric(0.5, 2.5, 2), 2: [1.2]}
+    B = {0: deck.geometric(0.2, 2.5, 4), 1: deck.geometric(0.4, 2.5, 2), 2: [0.9], 3: [1.5]}
+    b = deck.make_basis([((0, 0, 0), A), ((0, 0, 2.1), B)], hmlt="DHFR")
+    b.znuc, b.anuc = (10.0, 12.0), (20.0, 24.0)
+    md = lambda a: OracleBackend(a, racah1=False)  # noqa: E731
+    D0 = torch.as_tensor(atomic_guess(b, torch=torch, backend_factory=md, max_iter=40,
+                                      etol=1e-10))
+    r = DHFSCF(b, nocc=22, torch=torch, backend=md(b)).run(max_iter=3, guess=D0,
+                                                            return_density=True)
+    with ProcessPoolExecutor(max_workers=2, mp_context=mp.get_context("spawn")) as pool:
+        for D in (D0, r["density"]):
+            g_ref = ReferenceRouteBackend(b, pool, torch).fock(D).numpy()
+            g_md = md(b).fock(D).numpy()
+            assert np.abs(g_ref - g_md).max() <= 1e-10 * np.abs(g_md).max()
