@@ -6,11 +6,12 @@ calls them (bertha-scf.f:5401-5421).  The SCF path is the one of
 tests/test_ybf_golden.py: atomic start from the deck's configurations,
 HFSCF's stages with the deck's level shifts.
 
-CPU only and slow (about two hours on 8 cores: a stage-3 multi-centre
-build alone takes about 8 minutes).  Writes ybf_plus_388_oracle.json
-beside this file: the energy, the iterations and the occupied spinor
-energies, which tests/test_ybf_golden.py compares with the reference's
-log.
+CPU only and slow: on 8 cores the atomic start takes about 30 minutes
+and a stage-3 build 6-7 minutes, and 32 iterations took 3.1 hours with
+stage 3 still oscillating at the mEh level, as the reference's own stage
+3 did.  Prints every iteration; at the end writes ybf_plus_388_oracle.json
+beside this file (the energy, the iterations and the occupied spinor
+energies).
 
   python tests/golden/run_ybf_oracle_scf.py
 """
