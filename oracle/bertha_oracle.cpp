@@ -3,13 +3,19 @@
 // tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use it,
 // as the checker; the GPU library never links or calls it.
 //
-// Parity status: the reference ships no golden vectors and no Fortran
-// compiler exists on this machine, so parity of this restatement is UNPINNED
-// against reference outputs.  It is checked instead against independent
-// mathematics (tests/test_oracle_pins.py): Boys values against mpmath, the
-// Hermite E-coefficients against direct evaluation of the spinor overlap
-// densities, the time-reversal phase relations the reference relies on, and
-// closed forms for (ss|ss).
+// Parity status: the reference ships no golden vectors, and its Fortran
+// cannot be compiled on this machine.  Its one recorded run, the YbF+
+// Dirac-Coulomb SCF log, is the fixture tests/golden/ybf_plus_388.json.  The
+// GPU SCF reproduces that log (tests/test_ybf_golden.py), and the GPU
+// build matches this restatement to 1e-11 in the parity tests.  An SCF of
+// the deck by this restatement's RACAH1-on route reaches the log's stage-3
+// band (tests/golden/run_ybf_oracle_scf.py).  It is checked further against
+// independent mathematics (tests/test_oracle_pins.py): Boys values against
+// mpmath, the Hermite E-coefficients against direct evaluation of the
+// spinor overlap densities, the time-reversal phase relations the reference
+// relies on, and closed forms for (ss|ss).  It is also checked against the
+// reference's one-centre Racah route (oracle/racah1.py,
+// tests/test_oracle_racah1.py).
 //
 // Routines restated (bertha-scf.f line numbers):
 //   FUNFM  32465-32619   Boys function, four regimes
